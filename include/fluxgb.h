@@ -1,0 +1,232 @@
+/*
+ * fluxgb — C ABI of the GB300 (sm_103a) radiosity / thermal hot path.
+ *
+ * Conventions
+ *   - Every function returns an fgb_status (0 = FGB_OK). On failure the
+ *     message is available from fgb_last_error() on the same host thread.
+ *   - All array arguments are DEVICE pointers (allocated by the caller, e.g.
+ *     as torch tensors or with cudaMalloc), C-contiguous, with the element
+ *     type in the function name.  Sizes are plain integers.
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default
+ *     stream).  Calls are asynchronous with respect to the host unless the
+ *     comment says otherwise; device-side error flags are OR-ed into a
+ *     caller-provided `unsigned* flags` word (FGB_FLAG_*) that the caller
+ *     reads after synchronising.
+ *   - No torch or C++ types cross this boundary.
+ *
+ * Each declaration names the reference interface it replaces
+ * (paths inside the fluxpy source tree, file:line).
+ */
+#ifndef FLUXGB_H
+#define FLUXGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+enum fgb_status {
+  FGB_OK = 0,
+  FGB_BAD_ARG = 1,        /* invalid size / argument (reference: ValueError) */
+  FGB_NONFINITE = 2,      /* non-finite input or output (RuntimeError)       */
+  FGB_NEGATIVE = 3,       /* negative flux / temperature (RuntimeError)      */
+  FGB_ZERO_PIVOT = 4,     /* tridiagonal zero pivot (tridag.c:14-26 exit(1)) */
+  FGB_NO_CONVERGENCE = 5, /* iteration cap reached (solve.py has no cap)     */
+  FGB_DEVICE_TIMEOUT = 6, /* a bounded device-side wait gave up              */
+  FGB_CUDA_ERR = 7,       /* CUDA runtime error                              */
+  FGB_NO_MEMORY = 8,      /* device allocation failed                        */
+  FGB_TOO_LARGE = 9       /* request exceeds a documented fixed capacity     */
+};
+
+/* device-side flag bits (OR-ed into *flags) */
+#define FGB_FLAG_NONFINITE_IN   (1u << 0)
+#define FGB_FLAG_NEGATIVE_IN    (1u << 1)
+#define FGB_FLAG_NONFINITE_OUT  (1u << 2)
+#define FGB_FLAG_NEGATIVE_OUT   (1u << 3)
+#define FGB_FLAG_ZERO_PIVOT     (1u << 4)
+#define FGB_FLAG_PREDCORR_MAX   (1u << 5) /* conductionQ.c:173 warning      */
+#define FGB_FLAG_STACK_OVERFLOW (1u << 6) /* BVH traversal stack exhausted  */
+#define FGB_FLAG_INDEX_RANGE    (1u << 7)
+#define FGB_FLAG_RANK_CAP       (1u << 8) /* ACA reached its rank cap       */
+
+/* Message of the last failed call on this host thread ("" if none). */
+const char* fgb_last_error(void);
+/* Library version string. */
+const char* fgb_version(void);
+
+/* ------------------------------------------------ 1-D conduction (a14) */
+/*
+ * One Crank-Nicolson step of the radiative-flux boundary problem for every
+ * facet.  Replaces the per-facet loop over
+ *   void conductionQ(int nz, double z[], double dt, double Qn, double Qnp1,
+ *                    double T[], double ti[], double rhoc[], double emiss,
+ *                    double Fgeotherm, double *Fsurf)
+ * (src/flux/pcc/thrmlLib.h:3-4, src/flux/pcc/conductionQ.c:10) as driven by
+ * PccThermalModel1D.step (src/flux/thermal.pyx:249-261).
+ *   z[0..nz], ti[0..nz], rhoc[0..nz]  per-layer, shared by all facets
+ *   Qn, Qnp1, emiss, Fgeotherm, Fsurf[num_faces]
+ *   T_in, T_out[num_faces * (nz+1)]   row-major; may alias (in place)
+ */
+int fgb_conduction_q_f64(int num_faces, int nz, const double* z, double dt,
+                         const double* Qn, const double* Qnp1, const double* T_in,
+                         double* T_out, const double* ti, const double* rhoc,
+                         const double* emiss, const double* Fgeotherm, double* Fsurf,
+                         unsigned* flags, void* stream);
+/* Same in FP32 (same algorithm; used by the FP32 time-stepping driver). */
+int fgb_conduction_q_f32(int num_faces, int nz, const float* z, float dt, const float* Qn,
+                         const float* Qnp1, const float* T_in, float* T_out,
+                         const float* ti, const float* rhoc, const float* emiss,
+                         const float* Fgeotherm, float* Fsurf, unsigned* flags,
+                         void* stream);
+/*
+ * Prescribed-surface-temperature step.  Replaces the per-facet loop over
+ *   void conductionT(int nz, double z[], double dt, double T[], double Tsurf,
+ *                    double Tsurfp1, double ti[], double rhoc[],
+ *                    double Fgeotherm, double *Fsurf)
+ * (src/flux/pcc/thrmlLib.h:6-8, conductionT.c:4; thermal.pyx:275-286).
+ */
+int fgb_conduction_t_f64(int num_faces, int nz, const double* z, double dt,
+                         const double* Tsurf, const double* Tsurfp1, const double* T_in,
+                         double* T_out, const double* ti, const double* rhoc,
+                         const double* Fgeotherm, double* Fsurf, unsigned* flags,
+                         void* stream);
+
+
+/* ---------------------------------------------- facet geometry (a1) */
+/*
+ * Centroids P (nf x 3), unit normals N (nf x 3) and areas A (nf) of a mesh
+ * with vertices V (nv x 3) and faces F (nf x 3, int64), bit-identical to
+ * numpy's get_centroids / get_surface_normals_and_face_areas
+ * (src/flux/shape.py:16-45) as called by TrimeshShapeModel.__init__
+ * (shape.py:92-106).  Any of P, N, A may be NULL.
+ */
+int fgb_facet_geometry_f64(const double* V, long long nv, const long long* F, long long nf,
+                           double* P, double* N, double* A, unsigned* flags, void* stream);
+int fgb_facet_geometry_f32(const float* V, long long nv, const long long* F, long long nf,
+                           float* P, float* N, float* A, unsigned* flags, void* stream);
+
+/* ------------------------------------------------------- LBVH (a2) */
+/*
+ * Build a linear BVH over the triangles (FP32 vertices as Embree stores
+ * them; keep_f64 also keeps FP64 vertices for CGAL semantics).  Replaces
+ * EmbreeTrimeshShapeModel._make_scene (src/flux/shape.py:296-344) and
+ *   void cgal_aabb_init_from_trimesh(cgal_aabb *aabb, size_t num_points,
+ *        double (*points)[3], size_t num_faces, size_t (*faces)[3])
+ * (src/flux/cgal/aabb_wrapper.h:8-10).  *out_bvh receives an opaque handle
+ * owned by the library (device memory), released by fgb_bvh_free
+ * (cgal_aabb_dealloc, aabb_wrapper.h:11).  Synchronous allocation; the build
+ * itself runs on `stream`.
+ */
+int fgb_bvh_build_f64(const double* V, long long nv, const long long* F, long long nf,
+                      int keep_f64, void** out_bvh, unsigned* flags, void* stream);
+int fgb_bvh_build_f32(const float* V, long long nv, const long long* F, long long nf,
+                      int keep_f64, void** out_bvh, unsigned* flags, void* stream);
+int fgb_bvh_free(void* bvh);
+int fgb_bvh_info(const void* bvh, long long* num_prims, long long* bytes);
+
+/* ------------------------------------------- ray queries (a3, a4) */
+/* semantics: 0 = Embree backend (shape.py:349-421), 1 = CGAL backend
+ * (aabb_wrapper.cpp:64-108). */
+/*
+ * Pair visibility.  paired == 0: vis[p*n+q] for (I[p], J[q]) (m x n), as
+ * TrimeshShapeModel.get_visibility / _get_visibility (shape.py:138-163,
+ * 272-281, 349-398) and
+ *   bool cgal_aabb_test_face_to_face_vis(cgal_aabb const *aabb, size_t i, size_t j)
+ * (aabb_wrapper.h:12).  paired != 0: vis[k] for (I[k], J[k]).  near_edge
+ * (optional) flags rays that passed within 1e-6 (relative) of an edge.
+ */
+int fgb_visibility_f64(const void* bvh, const double* P, long long num_faces, const long long* I,
+                       long long m, const long long* J, long long n, int paired, int semantics,
+                       unsigned char* vis, unsigned char* near_edge, unsigned* flags, void* stream);
+int fgb_visibility_f32(const void* bvh, const float* P, long long num_faces, const long long* I,
+                       long long m, const long long* J, long long n, int paired, int semantics,
+                       unsigned char* vis, unsigned char* near_edge, unsigned* flags, void* stream);
+/*
+ * Sun occlusion of facets I along directions D.  per_facet == 0: D holds
+ * ndirs directions and occluded[p*ndirs+k] is written; per_facet != 0: D is
+ * m x 3, one direction per facet.  Replaces TrimeshShapeModel.is_occluded
+ * (shape.py:181-188, 283-292, 400-421) and
+ *   bool cgal_aabb_ray_from_centroid_is_occluded(cgal_aabb const *aabb, size_t i, double d[3])
+ * (aabb_wrapper.h:13-14).
+ */
+int fgb_occluded_f64(const void* bvh, const double* P, const double* N, long long num_faces,
+                     const long long* I, long long m, const double* D, long long ndirs,
+                     int per_facet, int semantics, unsigned char* occluded, unsigned* flags,
+                     void* stream);
+int fgb_occluded_f32(const void* bvh, const float* P, const float* N, long long num_faces,
+                     const long long* I, long long m, const float* D, long long ndirs,
+                     int per_facet, int semantics, unsigned char* occluded, unsigned* flags,
+                     void* stream);
+/*
+ * Direct irradiance for K sun directions: E[i*K+k] = F0[k] max(0, N_i.d_k)
+ * if facet i sees the sun along d_k, else 0 — get_direct_irradiance
+ * (shape.py:190-226) for every column at once.
+ */
+int fgb_direct_irradiance_f64(const void* bvh, const double* P, const double* N,
+                              long long num_faces, const double* D, long long K, const double* F0,
+                              int semantics, double* E, unsigned* flags, void* stream);
+int fgb_direct_irradiance_f64_to_f32(const void* bvh, const double* P, const double* N,
+                                     long long num_faces, const double* D, long long K,
+                                     const double* F0, int semantics, float* E, unsigned* flags,
+                                     void* stream);
+int fgb_direct_irradiance_f32(const void* bvh, const float* P, const float* N, long long num_faces,
+                              const float* D, long long K, const float* F0, int semantics,
+                              float* E, unsigned* flags, void* stream);
+/*
+ * First intersection of FP64 rays (X[p], D[p]): hit[p] = facet id or -1,
+ * xt[p] = hit point.  Replaces
+ *   bool cgal_aabb_intersect1(cgal_aabb const *aabb, double const x[3],
+ *        double const d[3], size_t *i, double xt[3])
+ * (aabb_wrapper.h:15-16; CgalTrimeshShapeModel._intersect1, shape.py:269).
+ * Needs a BVH built with keep_f64.
+ */
+int fgb_intersect1_f64(const void* bvh, const double* X, const double* D, long long m,
+                       long long* hit, double* xt, unsigned* flags, void* stream);
+
+/* --------------------------------------- form-factor pair kernel (a5) */
+/*
+ * Two-pass CSR assembly of form factors for a list of tiles (tile t: rows
+ * I[row0[t] .. +nrows[t]), columns J[col0[t] .. +ncols[t])).  Replaces the
+ * row loop of get_form_factor_matrix (src/flux/form_factors.py:11-72).
+ *   word_off[T+1]: exclusive prefix of nrows*ceil(ncols/32); row_off[T+1]:
+ *   exclusive prefix of nrows.
+ * fgb_ff_count_*: bits[total_words] (visible-and-kept bitmask),
+ *   row_counts[total_rows] (must be zeroed), stats[0] += kept pairs,
+ *   stats[1] += near-edge pairs.
+ * The caller scans row_counts into indptr[total_rows+1] (int64), then
+ * fgb_ff_fill_* writes indices (column position within the tile, int32) and
+ * data.
+ */
+int fgb_ff_count_f64(const void* bvh, const double* P, const double* N, const double* A,
+                     const long long* I, const long long* J, const long long* row0,
+                     const long long* nrows, const long long* col0, const long long* ncols,
+                     const long long* word_off, const long long* row_off, long long num_tiles,
+                     long long total_words, double eps, int semantics, unsigned* bits,
+                     int* row_counts, unsigned long long* stats, unsigned* flags, void* stream);
+int fgb_ff_count_f32(const void* bvh, const float* P, const float* N, const float* A,
+                     const long long* I, const long long* J, const long long* row0,
+                     const long long* nrows, const long long* col0, const long long* ncols,
+                     const long long* word_off, const long long* row_off, long long num_tiles,
+                     long long total_words, float eps, int semantics, unsigned* bits,
+                     int* row_counts, unsigned long long* stats, unsigned* flags, void* stream);
+int fgb_ff_fill_f64(const double* P, const double* N, const double* A, const long long* I,
+                    const long long* J, const long long* row0, const long long* nrows,
+                    const long long* col0, const long long* ncols, const long long* word_off,
+                    const long long* row_off, long long num_tiles, long long total_rows,
+                    const unsigned* bits, const long long* indptr, int* indices, double* data,
+                    void* stream);
+int fgb_ff_fill_f32(const float* P, const float* N, const float* A, const long long* I,
+                    const long long* J, const long long* row0, const long long* nrows,
+                    const long long* col0, const long long* ncols, const long long* word_off,
+                    const long long* row_off, long long num_tiles, long long total_rows,
+                    const unsigned* bits, const long long* indptr, int* indices, float* data,
+                    void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FLUXGB_H */

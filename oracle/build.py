@@ -1,0 +1,67 @@
+"""Build the checker libraries (test infrastructure, never the product).
+
+* ``oracle/liboracle.so``: the C restatements in ``oracle/*.c``.
+* ``oracle/_ref/libpcc_ref.so``: the reference's own conduction sources
+  (``src/flux/pcc/{conductionQ,conductionT,tridag}.c``) compiled directly
+  with gcc from where they lie in the reference tree, when that tree is
+  present (it is not on GPU machines, which then use ``liboracle.so``).
+
+Both are compiled with ``-ffp-contract=off`` so that results do not depend on
+FMA contraction (gcc contracts by default on aarch64).
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+from pathlib import Path
+
+ORACLE_DIR = Path(__file__).resolve().parent
+REF_DIR = ORACLE_DIR / "_ref"
+ORACLE_LIB = ORACLE_DIR / "liboracle.so"
+REF_PCC_LIB = REF_DIR / "libpcc_ref.so"
+REFERENCE_ROOT = Path(os.environ.get("FLUXPY_REFERENCE", "/root/reference"))
+REF_PCC_SOURCES = ["conductionQ.c", "conductionT.c", "tridag.c"]
+
+CFLAGS = ["-O2", "-fPIC", "-shared", "-std=gnu11", "-ffp-contract=off", "-fno-fast-math"]
+
+
+def _newer(target: Path, deps) -> bool:
+    if not target.exists():
+        return True
+    t = target.stat().st_mtime
+    return any(Path(d).stat().st_mtime > t for d in deps)
+
+
+def _cc(srcs, out: Path, extra=()) -> None:
+    cmd = ["gcc", *CFLAGS, *extra, *map(str, srcs), "-o", str(out), "-lm", "-fopenmp"]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"gcc failed:\n{' '.join(cmd)}\n{res.stderr}")
+
+
+def build_oracle() -> Path:
+    srcs = sorted(ORACLE_DIR.glob("*.c"))
+    if _newer(ORACLE_LIB, srcs):
+        _cc(srcs, ORACLE_LIB)
+    return ORACLE_LIB
+
+
+def build_ref() -> Path | None:
+    pcc = REFERENCE_ROOT / "src" / "flux" / "pcc"
+    srcs = [pcc / s for s in REF_PCC_SOURCES]
+    if not all(s.exists() for s in srcs):
+        return None
+    REF_DIR.mkdir(exist_ok=True)
+    if _newer(REF_PCC_LIB, srcs):
+        _cc(srcs, REF_PCC_LIB, extra=["-I", str(pcc)])
+    return REF_PCC_LIB
+
+
+def build() -> None:
+    build_oracle()
+    build_ref()
+
+
+if __name__ == "__main__":
+    build()
+    print(ORACLE_LIB, REF_PCC_LIB if REF_PCC_LIB.exists() else "(no reference tree)")

@@ -1,0 +1,177 @@
+"""Generate the golden fixtures under tests/golden/ from the reference tree.
+
+Run in a container that has the fluxpy reference checked out (read-only) at
+$FLUXPY_REFERENCE (default /root/reference):
+
+    python tests/golden/make_golden.py [section ...]
+
+Sections:
+  pcc      the reference's PCC golden files
+           (tests/data/thermal/pcc_thermal_model_1d/{Tsurface,Tprofile}_conductionQ,
+           written by the reference's own PCC code) parsed into
+           pcc_conductionQ.npz.
+  spheres  the reference's sphere meshes (tests/data/icosa_sphere*.npz,
+           used by tests/test_shape.py / test_form_factors.py there) copied
+           as V/F arrays into spheres.npz.
+  ffref    form-factor matrices and steady-state solves computed by the
+           reference's Python code (src/flux/form_factors.py,
+           compressed_form_factors.py, solve.py, model.py), imported from the
+           reference tree with the runtime shims its code needs under numpy 2
+           and scipy 1.18, with visibility from the oracle's CPU ray caster
+           plugged into the reference's backend seam
+           (TrimeshShapeModel._get_visibility / _is_occluded).
+The GPU machines have no reference tree; the tests read only these files.
+"""
+from __future__ import annotations
+
+import csv
+import os
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+REF = Path(os.environ.get("FLUXPY_REFERENCE", "/root/reference"))
+
+
+def make_pcc():
+    d = REF / "tests" / "data" / "thermal" / "pcc_thermal_model_1d"
+    out = []
+    for name in ("Tprofile_conductionQ", "Tsurface_conductionQ"):
+        rows = []
+        with open(d / name) as f:
+            for row in csv.reader(f, delimiter=" ", quoting=csv.QUOTE_NONNUMERIC):
+                rows.append([x for x in row if x != ""])
+        out.append(np.array(rows, dtype=np.float64))
+    np.savez_compressed(HERE / "pcc_conductionQ.npz", Tprofile=out[0], Tsurface=out[1])
+    print("pcc:", out[0].shape, out[1].shape)
+
+
+def make_spheres():
+    arrs = {}
+    for name in ("icosa_sphere", "icosa_sphere_5"):
+        z = np.load(REF / "tests" / "data" / f"{name}.npz")
+        arrs[f"{name}_V"] = z["V"]
+        arrs[f"{name}_F"] = z["F"]
+    np.savez_compressed(HERE / "spheres.npz", **arrs)
+    print("spheres:", {k: v.shape for k, v in arrs.items()})
+
+
+def import_reference():
+    """Import the reference package from its source tree with the runtime
+    shims its code needs here (numpy 2.x, scipy 1.18): the removed
+    np.product alias, the cached_property package (stdlib equivalent), and
+    the LinearOperator attributes that scipy now expects from subclasses that
+    never call LinearOperator.__init__.  flux.thermal (Cython) is not built:
+    a placeholder module satisfies flux.model's import."""
+    import functools
+    import types
+
+    import scipy.sparse.linalg as sla
+    np.product = np.prod
+    sys.modules.setdefault("cached_property",
+                           types.SimpleNamespace(cached_property=functools.cached_property))
+    try:
+        import scipy._external.array_api_compat.numpy as npc
+        sla.LinearOperator._xp = npc
+    except Exception:
+        pass
+    sla.LinearOperator.ndim = 2
+    thermal = types.ModuleType("flux.thermal")
+    thermal.PccThermalModel1D = None
+    sys.modules["flux.thermal"] = thermal
+    sys.path.insert(0, str(REF / "src"))
+    import flux.compressed_form_factors as cff
+    import flux.form_factors as ff
+    import flux.model as model
+    import flux.shape as shape
+    import flux.solve as solve
+    return shape, ff, cff, solve, model
+
+
+def oracle_shape_class(shape_mod, sem):
+    """A reference TrimeshShapeModel whose ray queries come from the oracle's
+    CPU ray caster (plugged into the reference's backend seam)."""
+    sys.path.insert(0, str(HERE.parent.parent))
+    from oracle import vis
+
+    class OracleShape(shape_mod.TrimeshShapeModel):
+        def _make_scene(self):
+            self._scene = vis.Scene(self.V, self.F)
+
+        def _get_visibility(self, I, J):
+            return self._scene.visibility(self.P, np.asarray(I, np.int64), np.asarray(J, np.int64),
+                                          sem=sem)
+
+        def _is_occluded(self, I, D):
+            return self._scene.occluded(self.P, self.N, np.asarray(I, np.int64), D, sem=sem)
+
+    return OracleShape
+
+
+def make_ffref():
+    """Reference Python form factors, compressed matrices and solves."""
+    shape, ff, cff, solve, model = import_reference()
+    sys.path.insert(0, str(HERE.parent.parent))
+    from fluxpy_gb300 import terrain
+    out = {}
+    Shape = oracle_shape_class(shape, 0)
+    # (1) inward sphere, all pairs visible (tests/test_form_factors.py:18-38)
+    z = np.load(REF / "tests" / "data" / "icosa_sphere_5.npz")
+    V, F = z["V"], z["F"]
+    sm = Shape(V, F)
+    sm.N[(sm.P * sm.N).sum(1) > 0] *= -1
+    A = ff.get_form_factor_matrix(sm)
+    S = A[0::4]  # every 4th row keeps the fixture small
+    out.update(sphere_V=V, sphere_F=F, sphere_N=sm.N, sphere_data=S.data,
+               sphere_indices=S.indices, sphere_indptr=S.indptr, sphere_nnz=A.nnz)
+    # (2) the spherical crater with occlusion, Embree semantics
+    V, F = terrain.spherical_crater()
+    sm = Shape(V, F)
+    A = ff.get_form_factor_matrix(sm)
+    S = A[0::16]  # every 16th row keeps the fixture small
+    out.update(crater_V=V, crater_F=F, crater_data=S.data, crater_indices=S.indices,
+               crater_indptr=S.indptr, crater_nnz=A.nnz, crater_rowsum=np.asarray(A.sum(1)).ravel())
+    # (3) solves on the crater (rho 0.12, emissivity 0.95, F0 1365, sun at
+    # 10 degrees elevation, azimuth 0), reference Jacobi
+    e0 = np.deg2rad(10.0)
+    dsun = np.array([np.cos(e0), 0.0, np.sin(e0)])
+    E = sm.get_direct_irradiance(1365.0, dsun)
+    B, niter = solve.solve_radiosity(A, E, 0.12, "right", "jacobi")
+    T = model.compute_steady_state_temp(A, E, 0.12, 0.95)
+    out.update(crater_E=E, crater_B=B, crater_niter=niter, crater_T=T)
+    # multi-column visible solve (E.ndim == 2 path of compute_steady_state_temp)
+    dirs = terrain.sun_directions([10.0, 20.0, 5.0], [0.0, 90.0, 200.0])
+    E2 = np.column_stack([sm.get_direct_irradiance(1365.0, d) for d in dirs])
+    B2, niter2 = solve.solve_radiosity(A, E2, 0.12, "right", "jacobi")
+    T2 = model.compute_steady_state_temp(A, E2, 0.12, 0.95)
+    out.update(crater_E2=E2, crater_B2=B2, crater_niter2=niter2, crater_T2=T2)
+    # (4) compressed matrices at tol=0 (tests/test_compressed_form_factors.py)
+    rng = np.random.default_rng(7)
+    zs = np.load(REF / "tests" / "data" / "icosa_sphere.npz")
+    Vs = zs["V"] * rng.random(3)
+    sms = Shape(Vs, zs["F"])
+    sms.N[(sms.P * sms.N).sum(1) > 0] *= -1
+    C = cff.CompressedFormFactorMatrix(sms, tol=0, max_depth=1, force_max_depth=True,
+                                       RootBlock=cff.FormFactorOctreeBlock)
+    x = rng.standard_normal(sms.num_faces)
+    out.update(octsphere_V=Vs, octsphere_F=zs["F"], octsphere_N=sms.N, octsphere_x=x,
+               octsphere_y=C @ x,
+               octsphere_types=np.array([type(b).__name__ for b in C._root._blocks.ravel()]),
+               octsphere_rows=np.array([len(r) for r in C._root._row_block_inds]))
+    for depth in (1, 2, 3):
+        Cq = cff.CompressedFormFactorMatrix(sm, tol=0, max_depth=depth, force_max_depth=False,
+                                            RootBlock=cff.FormFactorQuadtreeBlock, min_size=4096)
+        out[f"crater_quad{depth}_y"] = Cq @ E
+        out[f"crater_quad{depth}_depth"] = Cq.depth
+    np.savez_compressed(HERE / "ffref.npz", **out)
+    print("ffref:", {k: getattr(v, "shape", v) for k, v in out.items()})
+
+
+SECTIONS = {"pcc": make_pcc, "spheres": make_spheres, "ffref": make_ffref}
+
+if __name__ == "__main__":
+    todo = sys.argv[1:] or list(SECTIONS)
+    for s in todo:
+        SECTIONS[s]()

@@ -73,6 +73,25 @@ SIGNATURES: dict[str, list] = {
     "fgb_ff_count_f32": [P, P, P, P, P, P, P, P, P, P, P, P, I64, I64, F32, I32, P, P, P, U32P, P],
     "fgb_ff_fill_f64": [P, P, P, P, P, P, P, P, P, P, P, I64, I64, P, P, P, P, P],
     "fgb_ff_fill_f32": [P, P, P, P, P, P, P, P, P, P, P, I64, I64, P, P, P, P, P],
+    # compression (a6-a8)
+    "fgb_aca_scratch_floats": [I32, I64, I64, P],
+    "fgb_aca_f64": [P, P, P, P, P, I64, P, P, P, P, I64, I64, F64, I32, F32, I32, I32, P, I32,
+                    P, I64, P, P, P, P, U32P, P],
+    # block matvec (a9)
+    "fgb_matvec_f32": [P, P, P, P, P, P, P, F32, I32, P],
+    "fgb_matvec_f64": [P, P, P, P, P, P, P, F64, I32, P],
+    "fgb_matmat_f32": [P, P, P, P, P, P, I32, P, F32, I32, P],
+    "fgb_matmat_bf16": [P, P, P, P, P, P, P, I32, P, F32, I32, P],
+    # solve (a10-a12)
+    "fgb_scale_rows_f32": [P, P, F32, P, I64, I32, P],
+    "fgb_scale_rows_bf16": [P, P, F32, P, I64, I32, P],
+    "fgb_colmax_absdiff": [P, P, I64, I32, P, P],
+    "fgb_residual": [P, P, P, P, I64, I32, P, P],
+    "fgb_axpy_cols": [P, P, P, I64, I32, P],
+    "fgb_gather_rows_f32": [P, P, P, I64, I32, P],
+    "fgb_gather_rows_f64": [P, P, P, I64, I32, P],
+    "fgb_csr_spmm_f64": [P, P, P, I64, P, I32, P, P, F64, P],
+    "fgb_csr_spmm_f32": [P, P, P, I64, P, I32, P, P, F32, P],
 }
 _RESTYPES = {"fgb_last_error": C.c_char_p, "fgb_version": C.c_char_p}
 

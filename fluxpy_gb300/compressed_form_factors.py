@@ -1,0 +1,1312 @@
+"""Hierarchical compressed form-factor matrix on the GPU: drop-in for
+``flux.compressed_form_factors``.
+
+Structure (src/flux/compressed_form_factors.py:285-386, 512-698): rows and
+columns are split recursively into octants (``FormFactorOctreeBlock``) or
+quadrants (``FormFactorQuadtreeBlock``, the default root) about the midpoint
+of their bounding box, ``<=`` going to the low side (src/flux/octree.py:5-18,
+quadtree.py:5-18); every block of that tree is a leaf (zero / dense / sparse
+/ low-rank) or is subdivided again.
+
+What differs from the reference, by design:
+  * the reference assembles the full sparse matrix of every root block and
+    picks, per block, the smallest of {CSR, ARPACK SVD, children}; here a
+    block is low-rank when its two clusters are well separated
+    (min(diam) <= eta * dist) and its adaptive cross approximation
+    (libfluxgb ``fgb_aca_f64``, relative Frobenius tolerance ``tol``)
+    converges under its rank cap; blocks below ``min_size`` entries, at
+    ``max_depth``, or between leaf clusters are evaluated exactly by the
+    fused pair kernel (``fgb_ff_count/fill``).  Only O(N log N) entries and
+    rays are evaluated, not N^2.
+  * the leaves live on the device in one flat layout (libfluxgb matvec.cu):
+    the Python block tree (``_root._blocks`` etc.) is materialised lazily
+    from it for introspection, with the reference's block classes and the
+    reference's dense-vs-CSR choice by bytes and all-dense / all-sparse
+    collapsing.
+  * storage precision: ``dtype`` (default: the shape model's dtype, so FP64
+    shape models reproduce the reference's FP64 products); FP32 and BF16
+    copies are made for the fast paths.
+
+Products: ``F @ x`` with numpy input returns numpy (the reference's
+LinearOperator behaviour); with a CUDA tensor it stays on the device.
+"""
+from __future__ import annotations
+
+import copy
+import ctypes as C
+import itertools as it
+import pickle
+
+import numpy as np
+import scipy.sparse
+import scipy.sparse.linalg
+import torch
+
+from . import _lib, config
+from .form_factors import ff_tiles
+
+
+# ------------------------------------------------------------------ tree --
+class ClusterTree:
+    """Recursive 2^d-ary partition of the facet centroids.
+
+    ``perm`` lists facet ids in cluster order: every node is the contiguous
+    range perm[start:start+size], grouped by its descendants.  The
+    reference's index list of a node (its np.where order) is the same set in
+    ascending id order (``ref_indices``).  Children are always 2^d (some
+    possibly empty), ordered as itertools.product([le, gt], repeat=d).
+    """
+
+    def __init__(self, P, ndim, leaf_size=64, max_levels=64):
+        X = np.ascontiguousarray(P[:, :ndim], dtype=np.float64)
+        N = X.shape[0]
+        nch = 1 << ndim
+        self.ndim = ndim
+        self.nch = nch
+        perm = np.arange(N, dtype=np.int64)
+        start = [0]
+        size = [N]
+        level = [0]
+        children = [None]
+        lo_list = [X.min(0) if N else np.zeros(ndim)]
+        hi_list = [X.max(0) if N else np.zeros(ndim)]
+        frontier = np.array([0], dtype=np.int64) if N > leaf_size else np.zeros(0, np.int64)
+        lev = 0
+        while frontier.size and lev < max_levels:
+            starts = np.array([start[f] for f in frontier], dtype=np.int64)
+            sizes = np.array([size[f] for f in frontier], dtype=np.int64)
+            idx = np.concatenate([perm[s:s + n] for s, n in zip(starts, sizes)])
+            seg = np.repeat(np.arange(frontier.size), sizes)
+            pts = X[idx]
+            offs = np.concatenate([[0], np.cumsum(sizes)[:-1]])
+            lo = np.minimum.reduceat(pts, offs, axis=0)
+            hi = np.maximum.reduceat(pts, offs, axis=0)
+            mid = (lo + hi) / 2
+            code = np.zeros(idx.size, dtype=np.int64)
+            for a in range(ndim):
+                code |= (pts[:, a] > mid[seg, a]).astype(np.int64) << (ndim - 1 - a)
+            order = np.lexsort((np.arange(idx.size), code, seg))
+            new_idx = idx[order]
+            counts = np.bincount(seg * nch + code, minlength=frontier.size * nch).reshape(-1, nch)
+            new_frontier = []
+            pos = 0
+            for q, f in enumerate(frontier):
+                s0 = starts[q]
+                perm[s0:s0 + sizes[q]] = new_idx[pos:pos + sizes[q]]
+                pos += sizes[q]
+                ch = []
+                cs = s0
+                for c in range(nch):
+                    cid = len(start)
+                    n_c = int(counts[q, c])
+                    start.append(int(cs))
+                    size.append(n_c)
+                    level.append(lev + 1)
+                    children.append(None)
+                    if n_c:
+                        seg_pts = X[perm[cs:cs + n_c]]
+                        lo_list.append(seg_pts.min(0))
+                        hi_list.append(seg_pts.max(0))
+                    else:
+                        lo_list.append(np.full(ndim, np.nan))
+                        hi_list.append(np.full(ndim, np.nan))
+                    ch.append(cid)
+                    if n_c > leaf_size and not np.all(seg_pts.min(0) == seg_pts.max(0)):
+                        new_frontier.append(cid)
+                    cs += n_c
+                children[f] = ch
+            frontier = np.array(new_frontier, dtype=np.int64)
+            lev += 1
+        self.perm = perm
+        self.start = np.array(start, dtype=np.int64)
+        self.size = np.array(size, dtype=np.int64)
+        self.level = np.array(level, dtype=np.int64)
+        self.children = children
+        self.lo = np.array(lo_list)
+        self.hi = np.array(hi_list)
+        self.num_nodes = len(start)
+
+    def indices(self, node):
+        s = self.start[node]
+        return self.perm[s:s + self.size[node]]
+
+    def ref_indices(self, node):
+        return np.sort(self.indices(node))
+
+
+def _bbox3(P, tree):
+    """3-D bounding boxes of every node (for admissibility)."""
+    lo = np.full((tree.num_nodes, 3), np.nan)
+    hi = np.full((tree.num_nodes, 3), np.nan)
+    Pp = P[tree.perm]
+    nz = np.where(tree.size > 0)[0]
+    for node in nz:
+        s, n = tree.start[node], tree.size[node]
+        seg = Pp[s:s + n]
+        lo[node] = seg.min(0)
+        hi[node] = seg.max(0)
+    return lo, hi
+
+
+# ------------------------------------------------------------- builder --
+LEAF_ZERO, LEAF_DENSE, LEAF_SPARSE, LEAF_LOWRANK, NODE = 0, 1, 2, 3, 4
+
+
+class _Plan:
+    """The block tree as flat arrays: one record per block (leaf or node)."""
+
+    def __init__(self):
+        self.rows = []      # row cluster node id
+        self.cols = []      # col cluster node id
+        self.parent = []    # parent block id (-1 for root)
+        self.kind = []      # LEAF_* or NODE
+        self.child0 = []    # first child block id (NODE)
+
+
+class _DeviceOperator:
+    """Flat device layout consumed by libfluxgb's matvec kernels."""
+
+    def __init__(self, dev):
+        self.dev = dev
+
+
+class fgb_op_desc(C.Structure):
+    _fields_ = [
+        ("r0", C.c_void_p), ("m", C.c_void_p), ("c0", C.c_void_p), ("n", C.c_void_p),
+        ("k", C.c_void_p), ("woff", C.c_void_p), ("voff", C.c_void_p), ("zoff", C.c_void_p),
+        ("a_blk", C.c_void_p), ("a_j0", C.c_void_p), ("a_j1", C.c_void_p),
+        ("a_excl", C.c_void_p), ("num_items", C.c_longlong), ("t_ptr", C.c_void_p),
+        ("t_blk", C.c_void_p), ("num_tiles", C.c_longlong), ("N", C.c_longlong),
+        ("num_zrows", C.c_longlong),
+    ]
+
+
+TILE_ROWS = 64
+ITEM_COLS = 2048
+
+
+def _nbytes_csr(nnz, m, itemsize):
+    # data + int32 indices + int32 indptr (scipy's index dtype for these sizes)
+    return nnz * (itemsize + 4) + (m + 1) * 4
+
+
+class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
+    """A compressed form factor (view factor) matrix
+    (src/flux/compressed_form_factors.py:701-873)."""
+
+    def __init__(self, shape_model, tol=1e-5, min_size=16384, max_depth=None,
+                 force_max_depth=False, RootBlock=None, *, leaf_size=64, eta=1.0, rmax=64,
+                 nverify=4, dtype=None, eps=None, **kwargs):
+        if tol < 0:
+            raise RuntimeError('tol should be a nonnegative float')
+        if max_depth is not None and not isinstance(max_depth, int):
+            raise RuntimeError('invalid max_depth type: %s' % str(type(max_depth)))
+        if isinstance(max_depth, int) and max_depth <= 0:
+            raise RuntimeError('invalid max_depth value: %d' % max_depth)
+        if force_max_depth and max_depth is None:
+            raise RuntimeError('force_max_depth is True, but max_depth not specified')
+        if rmax < 1 or rmax > 64:
+            raise ValueError("rmax must be in [1, 64]")
+        if RootBlock is None:
+            RootBlock = FormFactorQuadtreeBlock
+        self.shape_model = shape_model
+        self._tol = tol
+        self._min_size = min_size
+        self._max_depth = max_depth
+        self._force_max_depth = force_max_depth
+        self._RootBlock = RootBlock
+        self._leaf_size = leaf_size
+        self._eta = eta
+        self._rmax = rmax
+        self._nverify = nverify
+        self._eps = config.DEFAULT_EPS if eps is None else eps
+        self._store_dtype = np.dtype(shape_model.dtype if dtype is None else dtype)
+        if self._store_dtype not in (np.float64, np.float32):
+            raise ValueError("dtype must be float64 or float32")
+        self._root_cache = None
+        self.stats = {}
+        self._build()
+
+    @classmethod
+    def from_shape_model(cls, shape_model, **kwargs):
+        """Build from a shape model (alias of the constructor)."""
+        return cls(shape_model, **kwargs)
+
+    # -- LinearOperator plumbing ----------------------------------------
+    @property
+    def dtype(self):
+        return self.shape_model.dtype
+
+    @property
+    def num_faces(self):
+        return self.shape_model.num_faces
+
+    @property
+    def shape(self):
+        return self.shape_model.num_faces, self.shape_model.num_faces
+
+    @property
+    def ndim(self):
+        return 2
+
+    @property
+    def sparsity_threshold(self):
+        return 2.0 / 3.0
+
+    # -- build ------------------------------------------------------------
+    def _build(self):
+        import time
+        t_start = time.perf_counter()
+        sm = self.shape_model
+        dev = sm._device
+        P = np.asarray(sm.P, dtype=np.float64)
+        ndim = 3 if issubclass(self._RootBlock, FormFactorOctreeBlock) else 2
+        tree = ClusterTree(P, ndim, leaf_size=self._leaf_size)
+        self._tree = tree
+        lo3, hi3 = _bbox3(P, tree)
+        N = P.shape[0]
+        perm_d = torch.as_tensor(tree.perm, device=dev)
+        self._perm_d = perm_d
+        iperm = np.empty_like(tree.perm)
+        iperm[tree.perm] = np.arange(N)
+        self._iperm_d = torch.as_tensor(iperm, device=dev)
+
+        # block records
+        rows, cols, parent, kind, child0, depth = [], [], [], [], [], []
+        rank, pool_off = [], []
+
+        def add(r, c, p, d):
+            rows.append(r); cols.append(c); parent.append(p); kind.append(-1)
+            child0.append(-1); depth.append(d); rank.append(0); pool_off.append(-1)
+            return len(rows) - 1
+
+        root = add(0, 0, -1, 0)
+        kind[root] = NODE
+        ch_root = tree.children[0]
+        if ch_root is None:
+            # a single cluster: one exact leaf below a 1 x 1 root
+            level = [add(0, 0, root, 1)]
+            child0[root] = level[0]
+            self._root_bshape = (1, 1)
+        else:
+            level = []
+            for r in ch_root:
+                for c in ch_root:
+                    level.append(add(r, c, root, 1))
+            child0[root] = level[0]
+            self._root_bshape = (len(ch_root), len(ch_root))
+
+        tol = float(self._tol)
+        maxd = self._max_depth
+        exact = []
+        aca_pool_parts = []
+        aca_total = 0
+        t_aca = 0.0
+        n_aca_blocks = 0
+        n_aca_failed = 0
+        while level:
+            cand_aca = []
+            next_level = []
+            for b in level:
+                r, c, d = rows[b], cols[b], depth[b]
+                m, n = tree.size[r], tree.size[c]
+                if m == 0 or n == 0:
+                    kind[b] = LEAF_ZERO
+                    continue
+                at_max = maxd is not None and d >= maxd
+                can_split = (tree.children[r] is not None and tree.children[c] is not None
+                             and not at_max)
+                if self._force_max_depth and maxd is not None and not at_max and can_split:
+                    self._split(b, tree, rows, cols, parent, kind, child0, depth, rank,
+                                pool_off, next_level, add)
+                    continue
+                if m * n < self._min_size and not self._force_max_depth:
+                    exact.append(b)
+                    continue
+                if tol > 0 and self._admissible(lo3, hi3, r, c):
+                    cand_aca.append(b)
+                    continue
+                if can_split:
+                    self._split(b, tree, rows, cols, parent, kind, child0, depth, rank,
+                                pool_off, next_level, add)
+                else:
+                    exact.append(b)
+            if cand_aca:
+                t0 = time.perf_counter()
+                ranks, offs, pool = self._run_aca(cand_aca, rows, cols, tree, perm_d, aca_total)
+                t_aca += time.perf_counter() - t0
+                n_aca_blocks += len(cand_aca)
+                if pool is not None:
+                    aca_pool_parts.append(pool)
+                    aca_total += pool.numel()
+                for b, k, off in zip(cand_aca, ranks, offs):
+                    if k >= 0:
+                        kind[b] = LEAF_LOWRANK
+                        rank[b] = int(k)
+                        pool_off[b] = int(off)
+                    else:
+                        n_aca_failed += 1
+                        r, c, d = rows[b], cols[b], depth[b]
+                        at_max = maxd is not None and d >= maxd
+                        if (tree.children[r] is not None and tree.children[c] is not None
+                                and not at_max):
+                            self._split(b, tree, rows, cols, parent, kind, child0, depth, rank,
+                                        pool_off, next_level, add)
+                        else:
+                            exact.append(b)
+            level = next_level
+
+        self._rows = np.array(rows, np.int64)
+        self._cols = np.array(cols, np.int64)
+        self._parent = np.array(parent, np.int64)
+        self._kind = np.array(kind, np.int64)
+        self._child0 = np.array(child0, np.int64)
+        self._depth = np.array(depth, np.int64)
+        self._rank = np.array(rank, np.int64)
+        t0 = time.perf_counter()
+        self._assemble(exact, aca_pool_parts, pool_off)
+        t_exact = time.perf_counter() - t0
+        torch.cuda.synchronize()
+        self.stats.update(build_s=time.perf_counter() - t_start, aca_s=t_aca, exact_s=t_exact,
+                          aca_blocks=n_aca_blocks, aca_failed=n_aca_failed,
+                          lowrank_blocks=int((self._kind == LEAF_LOWRANK).sum()),
+                          exact_blocks=len(exact), num_blocks=len(rows),
+                          lowrank_entries=int(sum(self._rank[b] * (tree.size[self._rows[b]] +
+                                                                   tree.size[self._cols[b]])
+                                                  for b in np.where(self._kind == LEAF_LOWRANK)[0])))
+
+    def _split(self, b, tree, rows, cols, parent, kind, child0, depth, rank, pool_off,
+               next_level, add):
+        r, c, d = rows[b], cols[b], depth[b]
+        kind[b] = NODE
+        first = None
+        for rc in tree.children[r]:
+            for cc in tree.children[c]:
+                nb = add(rc, cc, b, d + 1)
+                if first is None:
+                    first = nb
+                next_level.append(nb)
+        child0[b] = first
+
+    def _admissible(self, lo3, hi3, r, c):
+        dr = np.linalg.norm(hi3[r] - lo3[r])
+        dc = np.linalg.norm(hi3[c] - lo3[c])
+        gap = np.maximum(0.0, np.maximum(lo3[r] - hi3[c], lo3[c] - hi3[r]))
+        dist = np.linalg.norm(gap)
+        return min(dr, dc) <= self._eta * dist and dist > 0
+
+    def _run_aca(self, blocks, rows, cols, tree, perm_d, pool_base):
+        sm = self.shape_model
+        dev = sm._device
+        if np.dtype(sm.dtype) != np.float64:
+            raise NotImplementedError("low-rank compression needs a float64 shape model")
+        P, Nn, A = sm.device_geometry()
+        # largest blocks first
+        sizes = np.array([tree.size[rows[b]] * tree.size[cols[b]] for b in blocks])
+        order = np.argsort(-sizes, kind="stable")
+        blocks_sorted = [blocks[i] for i in order]
+        r0 = np.array([tree.start[rows[b]] for b in blocks_sorted], np.int32)
+        m = np.array([tree.size[rows[b]] for b in blocks_sorted], np.int32)
+        c0 = np.array([tree.start[cols[b]] for b in blocks_sorted], np.int32)
+        n = np.array([tree.size[cols[b]] for b in blocks_sorted], np.int32)
+        nb = len(blocks_sorted)
+        mmax, nmax = int(m.max()), int(n.max())
+        rmax = self._rmax
+        per_cta = C.c_longlong()
+        _lib.call("fgb_aca_scratch_floats", rmax, mmax, nmax, C.byref(per_cta))
+        num_ctas = int(min(nb, 152 * 4))
+        # cap the scratch at ~8 GB
+        while num_ctas > 1 and num_ctas * per_cta.value * 4 > 8 * 2**30:
+            num_ctas //= 2
+        scratch = torch.empty(num_ctas * per_cta.value, dtype=torch.float32, device=dev)
+        cap_k = np.minimum(rmax, np.maximum(1, (m.astype(np.int64) * n) // (2 * (m.astype(np.int64) + n))))
+        capacity = int((cap_k * (m.astype(np.int64) + n)).sum())
+        pool = torch.empty(max(capacity, 1), dtype=torch.float32, device=dev)
+        used = torch.zeros(1, dtype=torch.int64, device=dev)
+        rank_out = torch.empty(nb, dtype=torch.int32, device=dev)
+        off_out = torch.empty(nb, dtype=torch.int64, device=dev)
+        queue = torch.zeros(1, dtype=torch.int32, device=dev)
+        flags = torch.zeros(1, dtype=torch.int32, device=dev)
+        t = lambda a: torch.as_tensor(a, device=dev)
+        r0_d, m_d, c0_d, n_d = t(r0), t(m), t(c0), t(n)
+        _lib.call("fgb_aca_f64", sm.bvh.handle, _lib.ptr(P), _lib.ptr(Nn), _lib.ptr(A),
+                  _lib.ptr(perm_d), nb, _lib.ptr(r0_d), _lib.ptr(m_d), _lib.ptr(c0_d),
+                  _lib.ptr(n_d), mmax, nmax, float(self._eps), sm.semantics, float(self._tol),
+                  rmax, self._nverify, _lib.ptr(scratch), num_ctas, _lib.ptr(pool), capacity,
+                  _lib.ptr(used), _lib.ptr(rank_out), _lib.ptr(off_out), _lib.ptr(queue),
+                  _lib.ptr(flags), _lib.stream_handle())
+        fl = int(flags.item())
+        if fl & _lib.FLAG_STACK_OVERFLOW:
+            raise RuntimeError("BVH traversal stack overflow during compression")
+        ranks_s = rank_out.cpu().numpy()
+        offs_s = off_out.cpu().numpy()
+        nused = int(used.item())
+        del scratch
+        ranks = np.empty(nb, np.int64)
+        offs = np.empty(nb, np.int64)
+        ranks[order] = ranks_s
+        offs[order] = np.where(offs_s >= 0, offs_s + pool_base, -1)
+        return ranks, offs, (pool[:nused] if nused else None)
+
+    def _assemble(self, exact, aca_pool_parts, pool_off):
+        """Exact leaves -> dense device blocks; flat operator layout."""
+        sm = self.shape_model
+        dev = sm._device
+        tree = self._tree
+        perm_d = self._perm_d
+        sdt = self._store_dtype
+        tdt = torch.float64 if sdt == np.float64 else torch.float32
+        exact = np.array(sorted(exact), dtype=np.int64)
+        ex_r = self._rows[exact] if exact.size else np.zeros(0, np.int64)
+        ex_c = self._cols[exact] if exact.size else np.zeros(0, np.int64)
+        ex_m = tree.size[ex_r]
+        ex_n = tree.size[ex_c]
+        dense_entries = int((ex_m * ex_n).sum())
+        if dense_entries * np.dtype(sdt).itemsize > 96 * 2**30:
+            raise MemoryError("exact leaves would need more than 96 GB as dense blocks; "
+                              "use a larger max_depth / smaller min_size")
+        self._leaf_nnz = np.zeros(len(self._rows), np.int64)
+        if exact.size:
+            tcsr = ff_tiles(sm, perm_d, perm_d, tree.start[ex_r], ex_m, tree.start[ex_c], ex_n,
+                            self._eps)
+            self.stats["exact_nnz"] = int(tcsr.data.numel())
+            self.stats["kept_pairs"] = tcsr.kept_pairs
+            self.stats["near_edge_pairs"] = tcsr.near_edge_pairs
+            dense_off = np.zeros(exact.size + 1, np.int64)
+            np.cumsum(ex_m * ex_n, out=dense_off[1:])
+            dense = torch.zeros(max(dense_entries, 1), dtype=tdt, device=dev)
+            # scatter CSR entries to W = D^T: W[off + j*m + i]
+            R = int(tcsr.row_off[-1])
+            indptr = tcsr.indptr
+            nnz_per_row = (indptr[1:] - indptr[:-1])
+            tile_of_row = torch.repeat_interleave(
+                torch.arange(exact.size, device=dev),
+                torch.as_tensor(ex_m, device=dev))
+            row_local = torch.arange(R, device=dev) - torch.as_tensor(tcsr.row_off[:-1], device=dev)[tile_of_row]
+            ent_tile = torch.repeat_interleave(tile_of_row, nnz_per_row)
+            ent_row = torch.repeat_interleave(row_local, nnz_per_row)
+            m_d = torch.as_tensor(ex_m, device=dev)
+            off_d = torch.as_tensor(dense_off[:-1], device=dev)
+            pos = off_d[ent_tile] + tcsr.indices.to(torch.int64) * m_d[ent_tile] + ent_row
+            dense[pos] = tcsr.data.to(tdt)
+            nnz_tile = torch.zeros(exact.size, dtype=torch.int64, device=dev)
+            nnz_tile.index_add_(0, tile_of_row, nnz_per_row)
+            self._leaf_nnz[exact] = nnz_tile.cpu().numpy()
+            self._exact_csr = (tcsr, exact)
+        else:
+            dense = torch.zeros(1, dtype=tdt, device=dev)
+            dense_off = np.zeros(1, np.int64)
+            self._exact_csr = None
+        # classify exact leaves as the reference would (zero / dense / CSR by bytes)
+        isz = np.dtype(self.shape_model.dtype).itemsize
+        for q, b in enumerate(exact):
+            nnz = self._leaf_nnz[b]
+            m, n = ex_m[q], ex_n[q]
+            if nnz == 0:
+                self._kind[b] = LEAF_ZERO
+            elif m * n < self._min_size and m * n * isz < _nbytes_csr(nnz, m, isz):
+                self._kind[b] = LEAF_DENSE
+            else:
+                self._kind[b] = LEAF_SPARSE
+        self._dense_off = dict(zip(exact.tolist(), dense_off[:-1].tolist()))
+
+        # pool: [ACA factors (fp32) | dense exact blocks], in the storage dtype
+        aca = (torch.cat(aca_pool_parts) if aca_pool_parts else
+               torch.zeros(0, dtype=torch.float32, device=dev))
+        aca_n = aca.numel()
+        self._aca_n = aca_n
+        pool = torch.cat([aca.to(tdt), dense[:max(dense_entries, 0)]]) if dense_entries else aca.to(tdt)
+        if pool.numel() == 0:
+            pool = torch.zeros(1, dtype=tdt, device=dev)
+        self._pool = pool
+        self._pool_f32 = None
+        self._pool_bf16 = None
+
+        # device block list: LR with rank > 0, exact with nnz > 0
+        lr = np.where((self._kind == LEAF_LOWRANK) & (self._rank > 0))[0]
+        ex_nz = np.array([b for b in exact if self._leaf_nnz[b] > 0], dtype=np.int64)
+        blocks = np.concatenate([lr, ex_nz]).astype(np.int64)
+        nbk = blocks.size
+        r0 = tree.start[self._rows[blocks]]
+        m = tree.size[self._rows[blocks]]
+        c0 = tree.start[self._cols[blocks]]
+        n = tree.size[self._cols[blocks]]
+        k = np.where(np.arange(nbk) < lr.size, self._rank[blocks], n)
+        woff = np.empty(nbk, np.int64)
+        voff = np.full(nbk, -1, np.int64)
+        zoff = np.full(nbk, -1, np.int64)
+        pool_off = np.asarray(pool_off, np.int64)
+        woff[:lr.size] = pool_off[lr]
+        voff[:lr.size] = pool_off[lr] + self._rank[lr] * m[:lr.size]
+        zc = np.zeros(lr.size + 1, np.int64)
+        np.cumsum(self._rank[lr], out=zc[1:])
+        zoff[:lr.size] = zc[:-1]
+        woff[lr.size:] = aca_n + np.array([self._dense_off[b] for b in ex_nz], np.int64)
+        self._num_zrows = int(zc[-1])
+        # phase A items: column chunks of LR blocks
+        it_blk, it_j0, it_j1, it_ex = [], [], [], []
+        for q in range(lr.size):
+            nn = int(n[q])
+            nchunk = (nn + ITEM_COLS - 1) // ITEM_COLS
+            for ci in range(nchunk):
+                it_blk.append(q)
+                it_j0.append(ci * ITEM_COLS)
+                it_j1.append(min(nn, (ci + 1) * ITEM_COLS))
+                it_ex.append(1 if nchunk == 1 else 0)
+        self._needs_zero_z = any(e == 0 for e in it_ex)
+        # phase B tiles
+        N = self.num_faces
+        ntiles = (N + TILE_ROWS - 1) // TILE_ROWS
+        t_first = r0 // TILE_ROWS
+        t_last = (r0 + m - 1) // TILE_ROWS
+        cnt = (t_last - t_first + 1).astype(np.int64)
+        pair_blk = np.repeat(np.arange(nbk), cnt)
+        pair_t = (np.repeat(t_first, cnt) +
+                  (np.arange(cnt.sum()) - np.repeat(np.cumsum(cnt) - cnt, cnt)))
+        order = np.argsort(pair_t, kind="stable")
+        t_blk = pair_blk[order].astype(np.int32)
+        t_ptr = np.zeros(ntiles + 1, np.int64)
+        np.cumsum(np.bincount(pair_t, minlength=ntiles), out=t_ptr[1:])
+
+        def d(a, dt):
+            a = np.asarray(a, dtype=dt)
+            return torch.as_tensor(a if a.size else np.zeros(1, dt), device=dev)
+
+        self._dev = dict(
+            r0=d(r0, np.int32), m=d(m, np.int32), c0=d(c0, np.int32), n=d(n, np.int32),
+            k=d(k, np.int32), woff=d(woff, np.int64), voff=d(voff, np.int64),
+            zoff=d(zoff, np.int64), a_blk=d(it_blk, np.int32), a_j0=d(it_j0, np.int32),
+            a_j1=d(it_j1, np.int32), a_excl=d(it_ex, np.uint8), t_ptr=d(t_ptr, np.int64),
+            t_blk=d(t_blk, np.int32))
+        desc = fgb_op_desc()
+        for key in ("r0", "m", "c0", "n", "k", "woff", "voff", "zoff", "a_blk", "a_j0", "a_j1",
+                    "a_excl", "t_ptr", "t_blk"):
+            setattr(desc, key, self._dev[key].data_ptr())
+        desc.num_items = len(it_blk)
+        desc.num_tiles = ntiles
+        desc.N = N
+        desc.num_zrows = self._num_zrows
+        self._desc = desc
+        self._dev_blocks = blocks
+        self.stats.update(num_items=len(it_blk), num_tiles=ntiles, tile_pairs=int(t_blk.size),
+                          pool_entries=int(self._pool.numel()), zrows=self._num_zrows)
+
+    # -- device products --------------------------------------------------
+    def pool(self, precision):
+        """The factor/dense pool in 'fp64', 'fp32' or 'bf16'."""
+        if precision == "fp64":
+            if self._pool.dtype != torch.float64:
+                raise ValueError("this operator was stored in float32")
+            return self._pool
+        if precision == "fp32":
+            if self._pool.dtype == torch.float32:
+                return self._pool
+            if self._pool_f32 is None:
+                self._pool_f32 = self._pool.to(torch.float32)
+            return self._pool_f32
+        if precision == "bf16":
+            if self._pool_bf16 is None:
+                self._pool_bf16 = self._pool.to(torch.bfloat16)
+            return self._pool_bf16
+        raise ValueError(precision)
+
+    def permute(self, x: torch.Tensor) -> torch.Tensor:
+        """Facet order -> cluster order (rows)."""
+        return x.index_select(0, self._perm_d)
+
+    def unpermute(self, xp: torch.Tensor) -> torch.Tensor:
+        return xp.index_select(0, self._iperm_d)
+
+    def matvec_permuted(self, xp, precision="fp32", out=None, add=None, alpha=1.0, z=None):
+        """y = F x (or add + alpha F x) in cluster order, K = 1."""
+        if precision == "fp64":
+            V = torch.float64
+            fn = "fgb_matvec_f64"
+        else:
+            V = torch.float32
+            fn = "fgb_matvec_f32"
+        xp = xp.to(V).contiguous()
+        if out is None:
+            out = torch.empty_like(xp)
+        if z is None:
+            z = torch.empty(max(self._num_zrows, 1), dtype=V, device=xp.device)
+        pool = self.pool("fp64" if precision == "fp64" else "fp32")
+        _lib.call(fn, C.byref(self._desc), _lib.ptr(pool), _lib.ptr(pool), _lib.ptr(xp),
+                  _lib.ptr(z), _lib.ptr(out), _lib.ptr(add), float(alpha),
+                  int(self._needs_zero_z), _lib.stream_handle())
+        return out
+
+    def matmat_permuted(self, Xp, precision="fp32", out=None, add=None, alpha=1.0, Z=None):
+        """Y = F X for K right-hand sides in cluster order (X: N x K)."""
+        K = Xp.shape[1]
+        if precision == "fp64":
+            # FP64: one column at a time (reference-precision path)
+            cols = [self.matvec_permuted(Xp[:, c].contiguous(), "fp64",
+                                         add=None if add is None else add[:, c].contiguous(),
+                                         alpha=alpha) for c in range(K)]
+            res = torch.stack(cols, 1)
+            if out is not None:
+                out.copy_(res)
+                return out
+            return res
+        if precision == "fp32":
+            Xp = Xp.to(torch.float32).contiguous()
+            if out is None:
+                out = torch.empty_like(Xp)
+            if Z is None:
+                Z = torch.empty((max(self._num_zrows, 1), K), dtype=torch.float32, device=Xp.device)
+            pool = self.pool("fp32")
+            _lib.call("fgb_matmat_f32", C.byref(self._desc), _lib.ptr(pool), _lib.ptr(pool),
+                      _lib.ptr(Xp), _lib.ptr(Z), _lib.ptr(out), K, _lib.ptr(add), float(alpha),
+                      int(self._needs_zero_z), _lib.stream_handle())
+            return out
+        if precision == "bf16":
+            return self._matmat_bf16(Xp, out=out, add=add, alpha=alpha, Z=Z)
+        raise ValueError(precision)
+
+    def _matmat_bf16(self, Xp, out=None, add=None, alpha=1.0, Z=None):
+        K = Xp.shape[1]
+        Xb = Xp.to(torch.bfloat16).contiguous()
+        if out is None:
+            out = torch.empty(Xp.shape, dtype=torch.float32, device=Xp.device)
+        if Z is None:
+            Z = torch.empty((max(self._num_zrows, 1), K), dtype=torch.float32, device=Xp.device)
+        Zb = torch.empty((max(self._num_zrows, 1), K), dtype=torch.bfloat16, device=Xp.device)
+        pool = self.pool("bf16")
+        _lib.call("fgb_matmat_bf16", C.byref(self._desc), _lib.ptr(pool), _lib.ptr(pool),
+                  _lib.ptr(Xb), _lib.ptr(Z), _lib.ptr(Zb), _lib.ptr(out), K, _lib.ptr(add),
+                  float(alpha), int(self._needs_zero_z), _lib.stream_handle())
+        return out
+
+    def _default_precision(self):
+        return "fp64" if self._pool.dtype == torch.float64 else "fp32"
+
+    def _matmat(self, x):
+        """Product with host or device input (shape (N,) or (N, K))."""
+        on_dev = isinstance(x, torch.Tensor)
+        dev = self.shape_model._device
+        prec = self._default_precision()
+        V = torch.float64 if prec == "fp64" else torch.float32
+        xt = x if on_dev else torch.as_tensor(np.asarray(x), device=dev)
+        if xt.dtype not in (torch.float32, torch.float64):
+            xt = xt.to(V)
+        orig_dtype = xt.dtype
+        vec = xt.ndim == 1
+        xp = self.permute(xt.to(V))
+        if vec:
+            yp = self.matvec_permuted(xp, prec)
+        else:
+            yp = self.matmat_permuted(xp, prec)
+        y = self.unpermute(yp)
+        if on_dev:
+            return y.to(orig_dtype)
+        return y.cpu().numpy().astype(self.dtype, copy=False)
+
+    def _matvec(self, x):
+        return self._matmat(x)
+
+    def _rmatvec(self, x):
+        raise NotImplementedError("the reference defines no transpose product here "
+                                  "(compressed_form_factors.py:701-873)")
+
+    def __matmul__(self, x):
+        if isinstance(x, torch.Tensor):
+            return self._matmat(x)
+        if isinstance(x, np.ndarray) and x.ndim in (1, 2):
+            if x.shape[0] != self.shape[1]:
+                raise ValueError("dimension mismatch")
+            return self._matmat(x)
+        return super().__matmul__(x)
+
+    def matvec(self, x):
+        return self._matmat(x)
+
+    def matmat(self, X):
+        return self._matmat(X)
+
+    def dot(self, x):
+        return self @ x
+
+    # -- reference API: size / structure ---------------------------------
+    @property
+    def nbytes(self):
+        return self._root.nbytes
+
+    @property
+    def device_nbytes(self):
+        """Bytes held on the device by the operator (pool + tables)."""
+        tot = self._pool.numel() * self._pool.element_size()
+        for v in self._dev.values():
+            tot += v.numel() * v.element_size()
+        return tot
+
+    @property
+    def depth(self):
+        return self._root.depth
+
+    @property
+    def _root(self):
+        if self._root_cache is None:
+            self._root_cache = _make_tree_block(self, 0, None)
+        return self._root_cache
+
+    def get_blocks_at_depth(self, depth):
+        if depth > self.depth:
+            raise Exception('specified depth (%d) exceeds tree depth (%d)' % (depth, self.depth))
+        if depth == 0 or self._root.is_leaf:
+            yield self._root
+        else:
+            yield from self._root._get_blocks_at_depth(depth)
+
+    def get_row_inds_at_depth(self, depth):
+        if depth > self.depth:
+            raise Exception('specified depth (%d) exceeds tree depth (%d)' % (depth, self.depth))
+        row_inds = np.arange(self.num_faces)
+        if depth == 0:
+            yield row_inds
+        else:
+            yield from self._root._get_row_inds_at_depth(depth, row_inds)
+
+    def get_row_blocks(self, row_ind):
+        if not (0 <= row_ind and row_ind < self.num_faces):
+            raise Exception('row_ind (== %d) should be in range [0, %d)' % (row_ind, self.num_faces))
+        block, row_inds = self._root, np.arange(self.num_faces)
+        if block.is_leaf:
+            yield block
+        else:
+            yield from block._get_row_blocks(row_ind, row_inds)
+
+    def get_col_inds_for_row(self, row_ind):
+        if not (0 <= row_ind and row_ind < self.num_faces):
+            raise Exception('row_ind (== %d) should be in range [0, %d)' % (row_ind, self.num_faces))
+        row_inds = np.arange(self.num_faces)
+        col_inds = np.arange(self.num_faces)
+        if self._root.is_leaf:
+            yield col_inds
+        else:
+            yield from self._root._get_col_inds_for_row(row_ind, row_inds, col_inds)
+
+    def toarray(self):
+        n = self.num_faces
+        eye = np.eye(n, dtype=self.dtype)
+        return np.asarray(self @ eye)
+
+    def tocsr(self):
+        return scipy.sparse.csr_matrix(self.toarray())
+
+    # -- persistence -------------------------------------------------------
+    def save(self, path):
+        with open(path, 'wb') as f:
+            pickle.dump(self, f)
+
+    @staticmethod
+    def from_file(path):
+        with open(path, 'rb') as f:
+            return pickle.load(f)
+
+    def __getstate__(self):
+        st = dict(self.__dict__)
+        st["_root_cache"] = None
+        st["_desc"] = None
+        st["_pool_f32"] = None
+        st["_pool_bf16"] = None
+        for key in ("_pool", "_perm_d", "_iperm_d"):
+            st[key] = st[key].cpu()
+        st["_dev"] = {k: v.cpu() for k, v in st["_dev"].items()}
+        if st.get("_exact_csr") is not None:
+            tcsr, ex = st["_exact_csr"]
+            st["_exact_csr"] = ({"indptr": tcsr.indptr.cpu(), "indices": tcsr.indices.cpu(),
+                                 "data": tcsr.data.cpu(), "row_off": tcsr.row_off}, ex)
+        return st
+
+    def __setstate__(self, st):
+        self.__dict__.update(st)
+        dev = self.shape_model._device
+        for key in ("_pool", "_perm_d", "_iperm_d"):
+            setattr(self, key, getattr(self, key).to(dev))
+        self._dev = {k: v.to(dev) for k, v in self._dev.items()}
+        if self._exact_csr is not None:
+            d, ex = self._exact_csr
+            from .form_factors import TileCSR
+            self._exact_csr = (TileCSR(d["indptr"].to(dev), d["indices"].to(dev), d["data"].to(dev),
+                                       d["row_off"], 0, 0), ex)
+        desc = fgb_op_desc()
+        for key in ("r0", "m", "c0", "n", "k", "woff", "voff", "zoff", "a_blk", "a_j0", "a_j1",
+                    "a_excl", "t_ptr", "t_blk"):
+            setattr(desc, key, self._dev[key].data_ptr())
+        desc.num_items = int(self.stats["num_items"])
+        desc.num_tiles = int(self.stats["num_tiles"])
+        desc.N = self.num_faces
+        desc.num_zrows = self._num_zrows
+        self._desc = desc
+
+    # -- leaf data for the Python block objects --------------------------
+    def _leaf_dense(self, b):
+        """Dense (m x n) array of an exact leaf, in the shape dtype."""
+        tree = self._tree
+        m, n = tree.size[self._rows[b]], tree.size[self._cols[b]]
+        off = self._dense_off.get(int(b))
+        if off is None:
+            return np.zeros((m, n), dtype=self.dtype)
+        aca_n = self._aca_n
+        w = self._pool[aca_n + off: aca_n + off + m * n].cpu().numpy()
+        mat = w.reshape(n, m).T.astype(self.dtype)
+        # cluster order -> the reference's ascending-id order of the block
+        ri = np.argsort(tree.indices(self._rows[b]), kind="stable")
+        ci = np.argsort(tree.indices(self._cols[b]), kind="stable")
+        return mat[ri][:, ci]
+
+    def _leaf_lowrank(self, b):
+        tree = self._tree
+        m, n = tree.size[self._rows[b]], tree.size[self._cols[b]]
+        k = int(self._rank[b])
+        q = np.where(self._dev_blocks == b)[0]
+        if k == 0 or q.size == 0:
+            return np.zeros((m, 0)), np.zeros(0), np.zeros((0, n))
+        q = int(q[0])
+        woff = int(self._dev["woff"][q].item())
+        voff = int(self._dev["voff"][q].item())
+        Ut = self._pool[woff:woff + k * m].cpu().numpy().reshape(k, m).astype(np.float64)
+        Vt = self._pool[voff:voff + k * n].cpu().numpy().reshape(k, n).astype(np.float64)
+        # orthogonalise to the reference's (u, s, vt) form
+        ri = np.argsort(tree.indices(self._rows[b]), kind="stable")
+        ci = np.argsort(tree.indices(self._cols[b]), kind="stable")
+        Qu, Ru = np.linalg.qr(Ut.T[ri])
+        Qv, Rv = np.linalg.qr(Vt.T[ci])
+        W, s, Xt = np.linalg.svd(Ru @ Rv.T)
+        return Qu @ W, s, Xt @ Qv.T
+
+
+# ------------------------------------------------------- block classes --
+class CompressedFormFactorBlock:
+    """A block of a CompressedFormFactorMatrix (compressed_form_factors.py:35)."""
+
+    def __init__(self, root, shape):
+        self._root = root
+        self.shape = shape
+
+    @property
+    def dtype(self):
+        return self._root.dtype
+
+    @property
+    def size(self):
+        return int(np.prod(self.shape))
+
+    @property
+    def root(self):
+        return self._root
+
+
+class FormFactorLeafBlock(CompressedFormFactorBlock):
+    @property
+    def depth(self):
+        return 0
+
+    @property
+    def is_leaf(self):
+        return True
+
+    def get_blocks_at_depth(self, depth):
+        if depth == 0:
+            yield self
+
+    def _get_blocks_at_depth(self, depth):
+        if depth == 0:
+            yield self
+
+    def __matmul__(self, x):
+        return self._matmat(np.asarray(x))
+
+
+class FormFactorNullBlock(FormFactorLeafBlock):
+    def __init__(self, root, shape):
+        if shape[0] != 0 and shape[1] != 0:
+            raise RuntimeError('a null block must have a degenerate shape')
+        super().__init__(root, shape)
+
+    def _matmat(self, x):
+        if self.shape[1] != x.shape[0]:
+            raise ValueError('multiplying null block with matrix with wrong shape')
+        return np.empty((self.shape[0],) + x.shape[1:], dtype=self.dtype)
+
+    def is_dense(self):
+        return True
+
+    def is_sparse(self):
+        return True
+
+    @property
+    def _mat(self):
+        return np.empty(self.shape, dtype=self.dtype)
+
+    @property
+    def nbytes(self):
+        return 0
+
+    @property
+    def is_empty_leaf(self):
+        return True
+
+
+class FormFactorZeroBlock(FormFactorLeafBlock):
+    def _matmat(self, x):
+        m = self.shape[0]
+        return np.zeros((m,) if x.ndim == 1 else (m, x.shape[1]), dtype=self.dtype)
+
+    def is_dense(self):
+        return False
+
+    def is_sparse(self):
+        return True
+
+    @property
+    def _mat(self):
+        return np.zeros(self.shape, self.dtype)
+
+    @property
+    def nbytes(self):
+        return 0
+
+    def tocsr(self):
+        return scipy.sparse.csr_matrix(self.shape, dtype=self.dtype)
+
+    @property
+    def is_empty_leaf(self):
+        return True
+
+
+class FormFactorDenseBlock(FormFactorLeafBlock):
+    def __init__(self, root, mat):
+        if isinstance(mat, scipy.sparse.spmatrix):
+            mat = mat.toarray()
+        super().__init__(root, mat.shape)
+        self._mat = mat
+
+    @property
+    def nbytes(self):
+        return self._mat.nbytes
+
+    def toarray(self):
+        return self._mat
+
+    def is_dense(self):
+        return True
+
+    def is_sparse(self):
+        return False
+
+    def _matmat(self, x):
+        return self._mat @ x
+
+    @property
+    def is_empty_leaf(self):
+        return False
+
+
+class FormFactorSparseBlock(FormFactorLeafBlock):
+    def _matmat(self, x):
+        return np.array(self._spmat @ x)
+
+    def is_dense(self):
+        return False
+
+    def is_sparse(self):
+        return True
+
+    @property
+    def is_empty_leaf(self):
+        return False
+
+
+class FormFactorCsrBlock(FormFactorSparseBlock):
+    def __init__(self, root, mat):
+        super().__init__(root, mat.shape)
+        self._spmat = mat if isinstance(mat, scipy.sparse.spmatrix) else scipy.sparse.csr_matrix(mat)
+
+    @property
+    def nbytes(self):
+        return self._spmat.data.nbytes
+
+    def tocsr(self):
+        return self._spmat
+
+    @property
+    def _mat(self):
+        return self._spmat.toarray()
+
+
+class FormFactorSvdBlock(FormFactorLeafBlock):
+    """Low-rank leaf, exposed in the reference's (u, s, vt) form."""
+
+    def __init__(self, root, u, s, vt):
+        super().__init__(root, (u.shape[0], vt.shape[1]))
+        self._k = s.size
+        self._u, self._s, self._vt = u, s, vt
+
+    def _matmat(self, x):
+        y = self._vt @ x
+        y = (y.T * self._s).T
+        return self._u @ y
+
+    def is_dense(self):
+        return False
+
+    def is_sparse(self):
+        return False
+
+    @property
+    def is_empty_leaf(self):
+        return False
+
+    @property
+    def nbytes(self):
+        return self._u.nbytes + self._s.nbytes + self._vt.nbytes
+
+    @property
+    def _mat(self):
+        return (self._u * self._s) @ self._vt
+
+
+class FormFactorBlockMatrix(CompressedFormFactorBlock):
+    """Interior block (compressed_form_factors.py:279-510)."""
+
+    def _matmat(self, x):
+        y = np.zeros((self.shape[0],) + x.shape[1:], dtype=self.dtype)
+        for i, row_inds in enumerate(self._row_block_inds):
+            for j, col_inds in enumerate(self._col_block_inds):
+                block = self._blocks[i, j]
+                if block.is_empty_leaf:
+                    continue
+                y[row_inds] += block._matmat(x[col_inds])
+        return y
+
+    def __matmul__(self, x):
+        return self._matmat(np.asarray(x))
+
+    @property
+    def nbytes(self):
+        return sum(I.nbytes for I in self._row_block_inds) \
+            + sum(J.nbytes for J in self._col_block_inds) \
+            + sum(block.nbytes for block in self._blocks.flatten())
+
+    @property
+    def depth(self):
+        return 1 + max(block.depth for block in self._blocks.flatten())
+
+    @property
+    def is_leaf(self):
+        return False
+
+    @property
+    def is_empty_leaf(self):
+        return False
+
+    def is_dense(self):
+        return all(isinstance(b, FormFactorDenseBlock) for b in self._blocks.ravel())
+
+    def is_sparse(self):
+        return all(isinstance(b, (FormFactorSparseBlock, FormFactorZeroBlock))
+                   for b in self._blocks.ravel())
+
+    @property
+    def bshape(self):
+        return (len(self._row_block_inds), len(self._col_block_inds))
+
+    def _get_blocks_at_depth(self, depth):
+        if depth == 0:
+            yield self
+        else:
+            for block in self._blocks.ravel():
+                yield from block._get_blocks_at_depth(depth - 1)
+
+    def _get_row_inds_at_depth(self, depth, parent_inds):
+        if depth == 1:
+            for row_block_inds in self._row_block_inds:
+                yield parent_inds[row_block_inds]
+        else:
+            for row_block_inds, block in zip(self._row_block_inds, np.diag(self._blocks)):
+                if block.is_leaf:
+                    yield parent_inds[row_block_inds]
+                else:
+                    yield from block._get_row_inds_at_depth(depth - 1, parent_inds[row_block_inds])
+
+    def _get_row_blocks(self, row_ind, parent_inds):
+        for row_block_inds, row_blocks in zip(self._row_block_inds, self._blocks):
+            row_inds = parent_inds[row_block_inds]
+            if row_ind in row_inds:
+                for block in row_blocks:
+                    if block.is_leaf:
+                        yield block
+                    else:
+                        yield from block._get_row_blocks(row_ind, row_inds)
+                break
+
+    def _get_col_inds_for_row(self, row_ind, parent_row_inds, parent_col_inds):
+        for row_block_inds, row_blocks in zip(self._row_block_inds, self._blocks):
+            row_inds = parent_row_inds[row_block_inds]
+            if row_ind in row_inds:
+                for block, col_block_inds in zip(row_blocks, self._col_block_inds):
+                    col_inds = parent_col_inds[col_block_inds]
+                    if block.is_leaf:
+                        yield col_inds
+                    else:
+                        yield from block._get_col_inds_for_row(row_ind, row_inds, col_inds)
+                break
+
+    def get_individual_block(self, i, j):
+        tmp = copy.copy(self)
+        tmp._blocks = copy.copy(tmp._blocks)
+        for i_, j_ in it.product(*(range(_) for _ in self.bshape)):
+            if i_ != i or j_ != j:
+                continue
+            tmp._blocks[i, j] = FormFactorZeroBlock(self.root, tmp._blocks[i, j].shape)
+        return tmp
+
+    def get_diag_blocks(self):
+        tmp = copy.copy(self)
+        tmp._blocks = copy.copy(tmp._blocks)
+        for i, j in it.product(*(range(_) for _ in self.bshape)):
+            if i != j:
+                tmp._blocks[i, j] = FormFactorZeroBlock(self.root, tmp._blocks[i, j].shape)
+        return tmp
+
+    def get_off_diag_blocks(self):
+        tmp = copy.copy(self)
+        tmp._blocks = copy.copy(tmp._blocks)
+        for i, j in it.product(*(range(_) for _ in self.bshape)):
+            if i == j:
+                tmp._blocks[i, j] = FormFactorZeroBlock(self.root, tmp._blocks[i, j].shape)
+        return tmp
+
+
+class FormFactor2dTreeBlock(FormFactorBlockMatrix):
+    pass
+
+
+class FormFactorQuadtreeBlock(FormFactor2dTreeBlock):
+    """Quadtree interior block (compressed_form_factors.py:622-641)."""
+
+
+class FormFactorOctreeBlock(FormFactor2dTreeBlock):
+    """Octree interior block (compressed_form_factors.py:643-658)."""
+
+
+def _make_tree_block(op: CompressedFormFactorMatrix, b, parent_nodes):
+    """Materialise block b of the plan as a reference-style block object,
+    applying the reference's collapse of all-dense / all-sparse children
+    (compressed_form_factors.py:369-377)."""
+    tree = op._tree
+    r, c = op._rows[b], op._cols[b]
+    m, n = int(tree.size[r]), int(tree.size[c])
+    kind = op._kind[b]
+    if kind == LEAF_ZERO:
+        return FormFactorZeroBlock(op, (m, n))
+    if kind == LEAF_DENSE:
+        return FormFactorDenseBlock(op, op._leaf_dense(b))
+    if kind == LEAF_SPARSE:
+        return FormFactorCsrBlock(op, scipy.sparse.csr_matrix(op._leaf_dense(b)))
+    if kind == LEAF_LOWRANK:
+        u, s, vt = op._leaf_lowrank(b)
+        if s.size == 0:
+            return FormFactorZeroBlock(op, (m, n))
+        return FormFactorSvdBlock(op, u, s, vt)
+    # interior
+    cls = op._RootBlock if b == 0 else (
+        FormFactorOctreeBlock if tree.ndim == 3 else FormFactorQuadtreeBlock)
+    blk = cls.__new__(cls)
+    CompressedFormFactorBlock.__init__(blk, op, (m, n))
+    first = op._child0[b]
+    if b == 0 and tree.children[0] is None:
+        rch, cch = [0], [0]
+    else:
+        rch, cch = tree.children[r], tree.children[c]
+    nr, nc = len(rch), len(cch)
+    Ip = tree.ref_indices(r)
+    Jp = tree.ref_indices(c)
+    blk._row_block_inds = [np.searchsorted(Ip, tree.ref_indices(x)) for x in rch]
+    blk._col_block_inds = [np.searchsorted(Jp, tree.ref_indices(x)) for x in cch]
+    children = np.empty((nr, nc), dtype=object)
+    for i in range(nr):
+        for j in range(nc):
+            children[i, j] = _make_tree_block(op, first + i * nc + j, None)
+    blk._blocks = children
+    if b != 0:
+        if blk.is_dense():
+            mat = np.zeros((m, n), dtype=op.dtype)
+            for i in range(nr):
+                for j in range(nc):
+                    mat[np.ix_(blk._row_block_inds[i], blk._col_block_inds[j])] = children[i, j]._mat
+            return FormFactorDenseBlock(op, mat)
+        if blk.is_sparse():
+            mat = np.zeros((m, n), dtype=op.dtype)
+            for i in range(nr):
+                for j in range(nc):
+                    if not isinstance(children[i, j], FormFactorZeroBlock):
+                        mat[np.ix_(blk._row_block_inds[i], blk._col_block_inds[j])] = children[i, j]._mat
+            if not mat.any():
+                return FormFactorZeroBlock(op, (m, n))
+            return FormFactorCsrBlock(op, scipy.sparse.csr_matrix(mat))
+    return blk
+
+
+class CompressedKernelMatrix(scipy.sparse.linalg.LinearOperator):
+    """(I - rho F) and its transpose product (compressed_form_factors.py:875-913)."""
+
+    def __init__(self, form_factor_matrix, rho, albedo_placement='right'):
+        self.form_factor_matrix = form_factor_matrix
+        if not (0 < rho <= 1):
+            raise ValueError('need 0 < rho <= 1')
+        self.rho = rho
+        if albedo_placement not in {'left', 'right'}:
+            raise ValueError('albedo_placement must be "left" or "right"')
+        self.albedo_placement = albedo_placement
+
+    @property
+    def shape(self):
+        return self.form_factor_matrix.shape
+
+    @property
+    def dtype(self):
+        return self.form_factor_matrix.dtype
+
+    @property
+    def ndim(self):
+        return 2
+
+    def _matvec(self, x):
+        y = x.copy() if not isinstance(x, torch.Tensor) else x.clone()
+        if self.albedo_placement == 'left':
+            y -= self.rho * (self.form_factor_matrix @ x)
+        elif self.albedo_placement == 'right':
+            y -= self.form_factor_matrix @ (self.rho * x)
+        else:
+            raise RuntimeError('albedo_placement must be "left" or "right"')
+        return y
+
+    def _matmat(self, X):
+        return self._matvec(X)
+
+    def __matmul__(self, x):
+        return self._matvec(x)
+
+    def _rmatvec(self, x):
+        y = x.copy() if not isinstance(x, torch.Tensor) else x.clone()
+        FT = _transpose_product(self.form_factor_matrix)
+        if self.albedo_placement == 'left':
+            y -= FT(self.rho * x)
+        elif self.albedo_placement == 'right':
+            y -= self.rho * FT(x)
+        else:
+            raise RuntimeError('albedo_placement must be "left" or "right"')
+        return y
+
+
+def _transpose_product(F):
+    """x -> x @ F (i.e. F^T x) for scipy matrices and dense arrays."""
+    def apply(x):
+        if isinstance(F, CompressedFormFactorMatrix):
+            raise NotImplementedError("transpose products of the compressed operator "
+                                      "are not provided")
+        return np.asarray(x @ F).ravel() if np.ndim(x) == 1 else np.asarray(x @ F)
+    return apply

@@ -1,0 +1,354 @@
+// Batched adaptive cross approximation (ACA) of admissible form-factor
+// blocks, replacing the reference's assemble-then-ARPACK compression
+// (src/flux/compressed_form_factors.py:345-405 -> src/flux/linalg.py:8-51):
+// the reference evaluates every entry of a block and truncates its SVD at
+// sigma_i / sigma_0 <= tol; here only O(k (m + n)) entries of an admissible
+// block are evaluated (each with its visibility ray), and the rank-k factors
+// U V^T are built by partially pivoted ACA (Bebendorf, "Approximation of
+// boundary element matrices", Numer. Math. 86, 2000) with the Frobenius
+// stopping test |u_k| |v_k| <= tol |S_k|_F.  Because visibility makes blocks
+// patchy, convergence is confirmed on `nverify` random rows whose residual
+// must be negligible; a non-negligible one becomes the next pivot row.
+// A block whose rank would reach its cap (storage no smaller than half the
+// dense block, or rmax) is reported as failed (rank -1) and is subdivided by
+// the host.
+//
+// One CTA per block (persistent CTAs take blocks from a queue, largest
+// first).  The residual row/column, U and V live in a per-CTA FP32 scratch
+// slice of global memory (L2-resident for the small blocks that dominate);
+// norms and Gram products are accumulated in FP64.  Finished factors are
+// copied to a pool with a 64-bit bump allocator: block b gets U^T (k x m)
+// followed by V^T (k x n), row l contiguous.
+#include "common.cuh"
+#include "ffentry.cuh"
+
+namespace fgb {
+BvhView view_of(const void* handle);
+
+namespace {
+
+constexpr int kAcaThreads = 256;
+
+struct AcaArgs {
+  BvhView bvh;
+  const long long* perm;
+  long long nblocks;
+  const int* r0;
+  const int* m;
+  const int* c0;
+  const int* n;
+  int sem;
+  float tol;
+  int rmax;
+  int nverify;
+  float* scratch;
+  long long per_cta;
+  long long mmax, nmax;
+  float* pool;
+  long long pool_capacity;
+  unsigned long long* pool_used;
+  int* rank_out;
+  long long* off_out;
+  int* queue;
+  unsigned* flags;
+};
+
+template <class R>
+struct EntryCtx {
+  const R* P;
+  const R* N;
+  const R* A;
+  R eps;
+};
+
+template <class R>
+__device__ __forceinline__ float entry(const AcaArgs& a, const EntryCtx<R>& e, long long fi,
+                                       long long fj, bool* of) {
+  bool kept = false, ne = false;
+  R v = ff_entry<R>(a.bvh, e.P, e.N, e.A, fi, fj, e.eps, a.sem, &kept, &ne, of);
+  return (float)v;
+}
+
+// Block-wide reductions (kAcaThreads threads).
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x < 32) {
+    t = threadIdx.x < (kAcaThreads / 32) ? sh[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (threadIdx.x == 0) sh[0] = t;
+  }
+  __syncthreads();
+  t = sh[0];
+  __syncthreads();
+  return t;
+}
+
+// argmax of |v| over candidates (idx >= 0); returns (value, index).
+__device__ __forceinline__ void block_argmax(float v, int idx, float* shv, int* shi, float* out_v,
+                                             int* out_i) {
+  float a = idx >= 0 ? fabsf(v) : -1.0f;
+  for (int o = 16; o > 0; o >>= 1) {
+    float a2 = __shfl_xor_sync(0xffffffffu, a, o);
+    int i2 = __shfl_xor_sync(0xffffffffu, idx, o);
+    float v2 = __shfl_xor_sync(0xffffffffu, v, o);
+    if (a2 > a || (a2 == a && i2 >= 0 && (idx < 0 || i2 < idx))) { a = a2; idx = i2; v = v2; }
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) { shv[w] = a; shi[w] = idx; shv[8 + w] = v; }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    float aa = threadIdx.x < 8 ? shv[threadIdx.x] : -1.0f;
+    int ii = threadIdx.x < 8 ? shi[threadIdx.x] : -1;
+    float vv = threadIdx.x < 8 ? shv[8 + threadIdx.x] : 0.0f;
+    for (int o = 16; o > 0; o >>= 1) {
+      float a2 = __shfl_xor_sync(0xffffffffu, aa, o);
+      int i2 = __shfl_xor_sync(0xffffffffu, ii, o);
+      float v2 = __shfl_xor_sync(0xffffffffu, vv, o);
+      if (a2 > aa || (a2 == aa && i2 >= 0 && (ii < 0 || i2 < ii))) { aa = a2; ii = i2; vv = v2; }
+    }
+    if (threadIdx.x == 0) { shv[16] = vv; shi[16] = ii; }
+  }
+  __syncthreads();
+  *out_v = shv[16];
+  *out_i = shi[16];
+  __syncthreads();
+}
+
+__device__ __forceinline__ unsigned lcg(unsigned& s) {
+  s = s * 1664525u + 1013904223u;
+  return s >> 8;
+}
+
+template <class R>
+__global__ void __launch_bounds__(kAcaThreads)
+aca_kernel(AcaArgs a, EntryCtx<R> e) {
+  __shared__ double sh_d[32];
+  __shared__ float sh_v[32];
+  __shared__ int sh_i[32];
+  __shared__ int s_block;
+  __shared__ double s_dot[2][128];
+  const int tid = threadIdx.x;
+  float* U = a.scratch + (long long)blockIdx.x * a.per_cta;  // [rmax][mmax]
+  float* V = U + (long long)a.rmax * a.mmax;                  // [rmax][nmax]
+  float* rowbuf = V + (long long)a.rmax * a.nmax;             // [nmax]
+  float* used_r = rowbuf + a.nmax;                            // [mmax]
+  float* used_c = used_r + a.mmax;                            // [nmax]
+  bool overflow = false;
+
+  while (true) {
+    if (tid == 0) s_block = atomicAdd(a.queue, 1);
+    __syncthreads();
+    const long long b = s_block;
+    __syncthreads();
+    if (b >= a.nblocks) break;
+    const int m = a.m[b], n = a.n[b];
+    const long long r0 = a.r0[b], c0 = a.c0[b];
+    const long long* prow = a.perm + r0;
+    const long long* pcol = a.perm + c0;
+    for (int i = tid; i < m; i += kAcaThreads) used_r[i] = 0.f;
+    for (int j = tid; j < n; j += kAcaThreads) used_c[j] = 0.f;
+    long long cap = ((long long)m * n) / (2LL * (m + n));
+    int kmax = (int)min((long long)a.rmax, max(cap, 1LL));
+    int k = 0;
+    double normS2 = 0.0;
+    unsigned seed = 0x9e3779b9u ^ (unsigned)(b * 2654435761ull);
+    int istar = m / 2;
+    int confirm = 0;  // consecutive negligible rows since the last new term
+    bool failed = false;
+    const int max_iter = (a.rmax + 1) * (a.nverify + 2) + 16;
+    int iter = 0;
+    __syncthreads();
+    while (true) {
+      if (++iter > max_iter) { failed = true; break; }
+      // residual of row istar
+      const long long fi = prow[istar];
+      float lmax_v = 0.f;
+      int lmax_i = -1;
+      double rr = 0.0;
+      for (int j = tid; j < n; j += kAcaThreads) {
+        float val = entry<R>(a, e, fi, pcol[j], &overflow);
+        for (int l = 0; l < k; l++) val -= U[(long long)l * a.mmax + istar] * V[(long long)l * a.nmax + j];
+        rowbuf[j] = val;
+        rr += (double)val * val;
+        if (used_c[j] == 0.f && (lmax_i < 0 || fabsf(val) > fabsf(lmax_v))) { lmax_v = val; lmax_i = j; }
+      }
+      if (tid == 0) used_r[istar] = 1.f;
+      float piv;
+      int jstar;
+      block_argmax(lmax_v, lmax_i, sh_v, sh_i, &piv, &jstar);
+      rr = block_sum(rr, sh_d);
+      // negligible row: m |r|^2 <= (2 tol)^2 |S|_F^2, i.e. rows like this one
+      // would add at most about the requested relative error
+      bool negligible = jstar < 0 || piv == 0.0f ||
+                        (double)m * rr <= 4.0 * (double)a.tol * (double)a.tol * normS2;
+      bool pick_random;
+      if (negligible) {
+        if (++confirm >= a.nverify) break;  // converged (k == 0: zero block)
+        pick_random = true;
+      } else {
+        if (k >= kmax) { failed = true; break; }
+        confirm = 0;
+        // new term: v = row / pivot, u = residual column jstar
+        const float inv = 1.0f / piv;
+        for (int j = tid; j < n; j += kAcaThreads) V[(long long)k * a.nmax + j] = rowbuf[j] * inv;
+        __syncthreads();
+        const long long fj = pcol[jstar];
+        double uu = 0.0;
+        float umax_v = 0.f;
+        int umax_i = -1;
+        for (int i = tid; i < m; i += kAcaThreads) {
+          float val = entry<R>(a, e, prow[i], fj, &overflow);
+          for (int l = 0; l < k; l++) val -= V[(long long)l * a.nmax + jstar] * U[(long long)l * a.mmax + i];
+          U[(long long)k * a.mmax + i] = val;
+          uu += (double)val * val;
+          if (used_r[i] == 0.f && (umax_i < 0 || fabsf(val) > fabsf(umax_v))) { umax_v = val; umax_i = i; }
+        }
+        if (tid == 0) used_c[jstar] = 1.f;
+        double vv = 0.0;
+        for (int j = tid; j < n; j += kAcaThreads) {
+          float v = V[(long long)k * a.nmax + j];
+          vv += (double)v * v;
+        }
+        uu = block_sum(uu, sh_d);
+        vv = block_sum(vv, sh_d);
+        // cross terms 2 sum_l (u.U_l)(v.V_l), one warp per l
+        const int w = tid >> 5, ln = tid & 31;
+        for (int l = w; l < k; l += kAcaThreads / 32) {
+          double du = 0.0, dv = 0.0;
+          for (int i = ln; i < m; i += 32)
+            du += (double)U[(long long)k * a.mmax + i] * U[(long long)l * a.mmax + i];
+          for (int j = ln; j < n; j += 32)
+            dv += (double)V[(long long)k * a.nmax + j] * V[(long long)l * a.nmax + j];
+          for (int o = 16; o > 0; o >>= 1) {
+            du += __shfl_xor_sync(0xffffffffu, du, o);
+            dv += __shfl_xor_sync(0xffffffffu, dv, o);
+          }
+          if (ln == 0) { s_dot[0][l] = du; s_dot[1][l] = dv; }
+        }
+        __syncthreads();
+        if (tid == 0) {
+          double cross = 0.0;
+          for (int l = 0; l < k; l++) cross += s_dot[0][l] * s_dot[1][l];
+          sh_d[31] = cross;
+        }
+        __syncthreads();
+        const double cross = sh_d[31];
+        __syncthreads();
+        normS2 += uu * vv + 2.0 * cross;
+        if (normS2 < 0.0) normS2 = 0.0;
+        k++;
+        float nxt_v;
+        int nxt_i;
+        block_argmax(umax_v, umax_i, sh_v, sh_i, &nxt_v, &nxt_i);
+        pick_random = sqrt(uu * vv) <= (double)a.tol * sqrt(normS2) || nxt_i < 0;
+        if (!pick_random) istar = nxt_i;
+      }
+      if (pick_random) {
+        // next random unused row (all threads draw the same sequence)
+        int cand = -1;
+        for (int t = 0; t < 32 && cand < 0; t++) {
+          int c = (int)(lcg(seed) % (unsigned)m);
+          if (used_r[c] == 0.f) cand = c;
+        }
+        if (cand < 0) {
+          for (int c = 0; c < m; c++)
+            if (used_r[c] == 0.f) { cand = c; break; }
+        }
+        __syncthreads();
+        if (cand < 0) break;  // every row examined
+        istar = cand;
+      }
+    }
+    __syncthreads();
+    if (failed) {
+      if (tid == 0) { a.rank_out[b] = -1; a.off_out[b] = -1; }
+      continue;
+    }
+    // copy out U^T (k x m) then V^T (k x n)
+    __shared__ unsigned long long s_off;
+    if (tid == 0) {
+      unsigned long long need = (unsigned long long)k * (unsigned long long)(m + n);
+      unsigned long long off = need ? atomicAdd(a.pool_used, need) : 0ull;
+      if (off + need > (unsigned long long)a.pool_capacity) {
+        atomicOr(a.flags, kFlagRankCap);
+        s_off = ~0ull;
+      } else {
+        s_off = off;
+      }
+    }
+    __syncthreads();
+    const unsigned long long off = s_off;
+    if (off == ~0ull) {
+      if (tid == 0) { a.rank_out[b] = -2; a.off_out[b] = -1; }
+      continue;
+    }
+    float* dst = a.pool + off;
+    for (int l = 0; l < k; l++)
+      for (int i = tid; i < m; i += kAcaThreads) dst[(long long)l * m + i] = U[(long long)l * a.mmax + i];
+    dst += (long long)k * m;
+    for (int l = 0; l < k; l++)
+      for (int j = tid; j < n; j += kAcaThreads) dst[(long long)l * n + j] = V[(long long)l * a.nmax + j];
+    if (tid == 0) { a.rank_out[b] = k; a.off_out[b] = (long long)off; }
+    __syncthreads();
+  }
+  if (overflow) atomicOr(a.flags, kFlagStackOverflow);
+}
+
+}  // namespace
+}  // namespace fgb
+
+extern "C" {
+
+int fgb_aca_scratch_floats(int rmax, long long mmax, long long nmax, long long* per_cta) {
+  if (rmax < 1 || rmax > 128 || mmax < 1 || nmax < 1) {
+    fgb::set_error("bad ACA sizes (rmax in [1,128])");
+    return FGB_BAD_ARG;
+  }
+  *per_cta = (long long)rmax * (mmax + nmax) + 2 * (mmax + nmax);
+  return FGB_OK;
+}
+
+int fgb_aca_f64(const void* bvh, const double* P, const double* N, const double* A,
+                const long long* perm, long long nblocks, const int* r0, const int* m,
+                const int* c0, const int* n, long long mmax, long long nmax, double eps,
+                int semantics, float tol, int rmax, int nverify, float* scratch, int num_ctas,
+                float* pool, long long pool_capacity, unsigned long long* pool_used,
+                int* rank_out, long long* off_out, int* queue, unsigned* flags, void* stream) {
+  if (!bvh || nblocks < 0 || num_ctas < 1) { fgb::set_error("bad ACA arguments"); return FGB_BAD_ARG; }
+  if (rmax < 1 || rmax > 128) { fgb::set_error("rmax must be in [1, 128]"); return FGB_BAD_ARG; }
+  if (nblocks == 0) return FGB_OK;
+  long long per_cta;
+  int st = fgb_aca_scratch_floats(rmax, mmax, nmax, &per_cta);
+  if (st) return st;
+  fgb::AcaArgs a;
+  a.bvh = fgb::view_of(bvh);
+  a.perm = perm;
+  a.nblocks = nblocks;
+  a.r0 = r0; a.m = m; a.c0 = c0; a.n = n;
+  a.sem = semantics;
+  a.tol = tol;
+  a.rmax = rmax;
+  a.nverify = nverify < 1 ? 1 : nverify;
+  a.scratch = scratch;
+  a.per_cta = per_cta;
+  a.mmax = mmax; a.nmax = nmax;
+  a.pool = pool;
+  a.pool_capacity = pool_capacity;
+  a.pool_used = pool_used;
+  a.rank_out = rank_out;
+  a.off_out = off_out;
+  a.queue = queue;
+  a.flags = flags;
+  fgb::EntryCtx<double> e{P, N, A, eps};
+  fgb::aca_kernel<double><<<num_ctas, fgb::kAcaThreads, 0, fgb::as_stream(stream)>>>(a, e);
+  FGB_LAUNCH_CHECK("aca_kernel");
+  return FGB_OK;
+}
+
+}  // extern "C"

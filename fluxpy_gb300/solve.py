@@ -1,0 +1,273 @@
+"""Radiosity solves on the GPU: drop-in for ``flux.solve``.
+
+``solve_radiosity(FF, E, rho=1, albedo_placement='right', method='jacobi',
+tol=None)`` keeps the reference's signature, default tolerance
+(finfo(E.dtype).resolution * max|E|), Jacobi left/right and CG-left
+iterations, global stopping test, return value ``(B, niter)`` (B is the
+iterate *before* the converged update, as in src/flux/solve.py:36-45) and
+its errors.  The operator products run on the device: a
+``CompressedFormFactorMatrix`` through its block matvec kernels, a scipy
+CSR matrix (get_form_factor_matrix's output) through libfluxgb's CSR
+kernel, in the operator's precision.  Unlike the reference, every loop has an
+iteration cap (``max_iter``) and raises instead of spinning forever (the
+reference loops never stop on closed surfaces with rho = 1).
+
+``solve_radiosity_batched`` is the many-sun-directions path: all K columns
+of E in one set of launches, either plain FP32 Jacobi or BF16 tensor-core
+Jacobi inside FP32 iterative refinement, with per-column stopping at a
+relative residual ``rtol``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time
+
+import numpy as np
+import scipy.sparse
+import torch
+
+from . import _lib
+
+
+class NoConvergence(RuntimeError):
+    pass
+
+
+# ------------------------------------------------------------ operators --
+class _DeviceCSR:
+    """A scipy CSR operator uploaded once to the device."""
+
+    def __init__(self, A, dev, dtype):
+        A = scipy.sparse.csr_matrix(A)
+        self.shape = A.shape
+        self.dtype = dtype
+        self.indptr = torch.as_tensor(A.indptr.astype(np.int64), device=dev)
+        self.indices = torch.as_tensor(A.indices.astype(np.int32), device=dev)
+        self.data = torch.as_tensor(A.data.astype(dtype), device=dev)
+
+    def apply(self, X, add=None, alpha=1.0):
+        vec = X.ndim == 1
+        X2 = X.reshape(X.shape[0], -1).contiguous()
+        K = X2.shape[1]
+        Y = torch.empty((self.shape[0], K), dtype=X2.dtype, device=X2.device)
+        addc = None if add is None else add.reshape(self.shape[0], -1).contiguous()
+        fn = "fgb_csr_spmm_f64" if X2.dtype == torch.float64 else "fgb_csr_spmm_f32"
+        _lib.call(fn, _lib.ptr(self.indptr), _lib.ptr(self.indices), _lib.ptr(self.data),
+                  self.shape[0], _lib.ptr(X2), K, _lib.ptr(Y), _lib.ptr(addc), float(alpha),
+                  _lib.stream_handle())
+        return Y.reshape(-1) if vec else Y
+
+
+_csr_cache: dict = {}
+
+
+def _device_operator(FF, dev, dtype):
+    """Wrap FF as a callable y = F x on device tensors (facet order)."""
+    from .compressed_form_factors import CompressedFormFactorMatrix
+    if isinstance(FF, CompressedFormFactorMatrix):
+        prec = "fp64" if dtype == np.float64 and FF._pool.dtype == torch.float64 else "fp32"
+
+        def apply(X, add=None, alpha=1.0):
+            vec = X.ndim == 1
+            V = torch.float64 if prec == "fp64" else torch.float32
+            Xp = FF.permute(X.to(V))
+            addp = None if add is None else FF.permute(add.to(V))
+            if vec:
+                Yp = FF.matvec_permuted(Xp, prec, add=addp, alpha=alpha)
+            else:
+                Yp = FF.matmat_permuted(Xp, prec, add=addp, alpha=alpha)
+            return FF.unpermute(Yp).to(X.dtype)
+        return apply
+    if scipy.sparse.issparse(FF) or isinstance(FF, np.ndarray):
+        key = id(FF)
+        ent = _csr_cache.get(key)
+        if ent is None or ent[0] is not FF:
+            ent = (FF, _DeviceCSR(FF, dev, dtype))
+            _csr_cache.clear()
+            _csr_cache[key] = ent
+        return ent[1].apply
+    raise TypeError(f"unsupported form factor operator: {type(FF)}")
+
+
+def _to_device(x, dev, dtype):
+    if isinstance(x, torch.Tensor):
+        return x.to(dev, dtype)
+    return torch.as_tensor(np.asarray(x, dtype=dtype), device=dev)
+
+
+def _rho_vec(rho, E_d):
+    if np.isscalar(rho) or np.ndim(rho) == 0:
+        return float(rho)
+    r = _to_device(rho, E_d.device, E_d.dtype)
+    return r.reshape(-1, 1) if E_d.ndim == 2 else r
+
+
+# ---------------------------------------------------- reference solver --
+def solve_radiosity(FF, E, rho=1, albedo_placement='right', method='jacobi', tol=None,
+                    max_iter=100000):
+    """Solve B = E + F (rho B) (right) or B = E + rho F B (left)
+    (src/flux/solve.py:4-22).  Host arrays in, host arrays out; device
+    tensors in, device tensors out."""
+    on_dev = isinstance(E, torch.Tensor)
+    E_np = None if on_dev else np.asarray(E)
+    dtype = np.dtype(E_np.dtype if E_np is not None else
+                     (np.float64 if E.dtype == torch.float64 else np.float32))
+    if tol is None:
+        tol = np.finfo(dtype).resolution
+        tol *= float(abs(E_np).max() if E_np is not None else E.abs().max().item())
+    if albedo_placement not in {'left', 'right'}:
+        raise Exception('albedo_placement must be "left" or "right"')
+    dev = _lib.require_cuda()
+    tdt = torch.float64 if dtype == np.float64 else torch.float32
+    E_d = E.to(dev, tdt) if on_dev else torch.as_tensor(E_np.astype(dtype), device=dev)
+    apply = _device_operator(FF, dev, dtype)
+    rho_v = _rho_vec(rho, E_d)
+    if method == 'jacobi':
+        B, niter = _jacobi(apply, E_d, rho_v, albedo_placement, tol, max_iter)
+    elif method == 'cg':
+        if albedo_placement == 'left':
+            B, niter = _cg_left(apply, E_d, rho_v, tol, max_iter)
+        else:
+            raise NotImplementedError("CG with right albedo placement is not implemented "
+                                      "(src/flux/solve.py:108-109)")
+    else:
+        raise Exception('method must be one of: jacobi, cg')
+    if on_dev:
+        return B, niter
+    return B.cpu().numpy().astype(dtype, copy=False), niter
+
+
+def _jacobi(apply, E, rho, placement, tol, max_iter):
+    B = E.clone()
+    niter = 0
+    while True:
+        niter += 1
+        if placement == 'right':
+            B1 = apply(rho * B, add=E)
+        else:
+            B1 = E + rho * apply(B)
+        if float((B1 - B).abs().max().item()) <= tol:
+            break
+        B = B1
+        if niter >= max_iter:
+            raise NoConvergence(f"Jacobi did not converge in {max_iter} iterations")
+    return B, niter
+
+
+def _cg_left(apply, E, rho, tol, max_iter):
+    # src/flux/solve.py:47-106, with column-wise dots for 2-D E
+    X = torch.zeros_like(E)
+    R = E
+    niter = 0
+    if float(R.abs().max().item()) <= tol:
+        return X, niter
+    P = R
+    while True:
+        KP = P - rho * apply(P)
+        RR = (R * R).sum(0)
+        alpha = RR / (KP * P).sum(0)
+        X1 = X + alpha * P
+        R1 = R - alpha * KP
+        if float(R1.abs().max().item()) <= tol:
+            return X1, niter + 1
+        beta = (R1 * R1).sum(0) / RR
+        P = R1 + beta * P
+        niter += 1
+        X, R = X1, R1
+        if niter >= max_iter:
+            raise NoConvergence(f"CG did not converge in {max_iter} iterations")
+
+
+# ---------------------------------------------------- batched solver --
+def _colmax(t):
+    return t.view(torch.int32).cpu().numpy().view(np.float32)
+
+
+def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_iter=200,
+                            inner=3, E_is_permuted=False, return_permuted=False, stats=None):
+    """Right-placement radiosity solve for K sun directions at once.
+
+    FF: CompressedFormFactorMatrix; E: (N, K) device tensor (facet order, or
+    cluster order with E_is_permuted); rho: scalar or per-facet.
+    precision:
+      'fp32'         plain FP32 Jacobi, FP32 CUDA-core matmat, until the
+                     per-column update max|B1 - B| <= rtol * max|E[:, k]|;
+      'bf16-refine'  FP32 residual R = E - (B - F rho B) (FP32 factors),
+                     correction by `inner` BF16 tensor-core Jacobi sweeps
+                     D <- R + F_bf16(rho D), until max|R[:, k]| <= rtol *
+                     max|E[:, k]| for every column.
+    Returns B (N, K) fp32; fills `stats` (iterations, matmats, residuals).
+    """
+    dev = E.device
+    N, K = E.shape
+    stream = _lib.stream_handle()
+    Ep = E.to(torch.float32).contiguous() if E_is_permuted else FF.permute(E.to(torch.float32)).contiguous()
+    rho_d = None
+    rho_s = 0.0
+    if np.isscalar(rho) or np.ndim(rho) == 0:
+        rho_s = float(rho)
+    else:
+        r = _to_device(rho, dev, torch.float32)
+        rho_d = r if E_is_permuted else FF.permute(r)
+        rho_d = rho_d.contiguous()
+    emax = Ep.abs().amax(0)
+    thresh = (rtol * emax).cpu().numpy().astype(np.float32)
+    colmax = torch.zeros(K, dtype=torch.int32, device=dev)
+    Z32 = torch.empty((max(FF._num_zrows, 1), K), dtype=torch.float32, device=dev)
+    X32 = torch.empty_like(Ep)
+    Y = torch.empty_like(Ep)
+    st = stats if stats is not None else {}
+    st.update(outer=0, fp32_matmats=0, bf16_matmats=0)
+    if precision == "fp32":
+        B = Ep.clone()
+        for it in range(1, max_iter + 1):
+            _lib.call("fgb_scale_rows_f32", _lib.ptr(B), _lib.ptr(rho_d), rho_s, _lib.ptr(X32), N, K,
+                      stream)
+            FF.matmat_permuted(X32, "fp32", out=Y, add=Ep, alpha=1.0, Z=Z32)
+            st["fp32_matmats"] += 1
+            colmax.zero_()
+            _lib.call("fgb_colmax_absdiff", _lib.ptr(Y), _lib.ptr(B), N, K, _lib.ptr(colmax), stream)
+            B, Y = Y, B
+            st["outer"] = it
+            if np.all(_colmax(colmax) <= thresh):
+                break
+        else:
+            raise NoConvergence("FP32 Jacobi did not converge")
+    elif precision == "bf16-refine":
+        B = Ep.clone()
+        R = torch.empty_like(Ep)
+        D = torch.empty_like(Ep)
+        Xb = torch.empty((N, K), dtype=torch.bfloat16, device=dev)
+        Zb = torch.empty((max(FF._num_zrows, 1), K), dtype=torch.bfloat16, device=dev)
+        pool_b = FF.pool("bf16")
+        for it in range(1, max_iter + 1):
+            # residual with the FP32 operator
+            _lib.call("fgb_scale_rows_f32", _lib.ptr(B), _lib.ptr(rho_d), rho_s, _lib.ptr(X32), N, K,
+                      stream)
+            FF.matmat_permuted(X32, "fp32", out=Y, Z=Z32)
+            st["fp32_matmats"] += 1
+            colmax.zero_()
+            _lib.call("fgb_residual", _lib.ptr(Y), _lib.ptr(B), _lib.ptr(Ep), _lib.ptr(R), N, K,
+                      _lib.ptr(colmax), stream)
+            res = _colmax(colmax)
+            st["outer"] = it
+            st["residual"] = float(np.max(res / np.maximum(emax.cpu().numpy(), 1e-30)))
+            if np.all(res <= thresh):
+                break
+            # correction: D <- R + F_bf16 (rho D), `inner` sweeps from D = R
+            D.copy_(R)
+            for _ in range(inner):
+                _lib.call("fgb_scale_rows_bf16", _lib.ptr(D), _lib.ptr(rho_d), rho_s, _lib.ptr(Xb),
+                          N, K, stream)
+                _lib.call("fgb_matmat_bf16", C.byref(FF._desc), _lib.ptr(pool_b), _lib.ptr(pool_b),
+                          _lib.ptr(Xb), _lib.ptr(Z32), _lib.ptr(Zb), _lib.ptr(D), K, _lib.ptr(R),
+                          1.0, int(FF._needs_zero_z), stream)
+                st["bf16_matmats"] += 1
+            _lib.call("fgb_axpy_cols", _lib.ptr(B), _lib.ptr(D), None, N, K, stream)
+        else:
+            raise NoConvergence("refinement did not converge")
+    else:
+        raise ValueError(precision)
+    if return_permuted:
+        return B
+    return FF.unpermute(B)

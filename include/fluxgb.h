@@ -225,6 +225,110 @@ int fgb_ff_fill_f32(const float* P, const float* N, const float* A, const long l
                     const unsigned* bits, const long long* indptr, int* indices, float* data,
                     void* stream);
 
+/* ------------------------------------------- compression (a6-a8) */
+/*
+ * Batched adaptive cross approximation of admissible blocks.  Replaces the
+ * rank estimation of the reference's compressed matrix,
+ *   estimate_rank(spmat, tol, max_nbytes=None, k0=40) / sparse_svd(spmat, k)
+ * (src/flux/linalg.py:8-51) called from FormFactorBlockMatrix._get_svd_block
+ * (src/flux/compressed_form_factors.py:388-405), which needs every entry of
+ * the block; ACA evaluates O(k (m+n)) entries (with their rays).
+ * Block b covers cluster-order rows [r0, r0+m) and columns [c0, c0+n); perm
+ * maps cluster order to facet ids.  Outputs rank_out[b] (-1: did not
+ * converge under its cap, -2: pool full) and off_out[b]: offset in `pool`
+ * of U^T (k x m) followed by V^T (k x n).  scratch: num_ctas *
+ * fgb_aca_scratch_floats(...) floats; queue: one zeroed int.
+ */
+int fgb_aca_scratch_floats(int rmax, long long mmax, long long nmax, long long* per_cta);
+int fgb_aca_f64(const void* bvh, const double* P, const double* N, const double* A,
+                const long long* perm, long long nblocks, const int* r0, const int* m,
+                const int* c0, const int* n, long long mmax, long long nmax, double eps,
+                int semantics, float tol, int rmax, int nverify, float* scratch, int num_ctas,
+                float* pool, long long pool_capacity, unsigned long long* pool_used,
+                int* rank_out, long long* off_out, int* queue, unsigned* flags, void* stream);
+
+/* ----------------------------------------------- block matvec (a9) */
+/*
+ * Flat description of a compressed operator (device arrays; see
+ * fluxpy_gb300/csrc/matvec.cu): per block r0, m, c0, n, k, woff, voff, zoff
+ * (zoff < 0 marks an exact dense leaf); phase-A items (a_blk, a_j0, a_j1,
+ * a_excl); phase-B row tiles of 64 rows (t_ptr, t_blk).
+ */
+struct fgb_op_desc {
+  const int* r0;
+  const int* m;
+  const int* c0;
+  const int* n;
+  const int* k;
+  const long long* woff;
+  const long long* voff;
+  const long long* zoff;
+  const int* a_blk;
+  const int* a_j0;
+  const int* a_j1;
+  const unsigned char* a_excl;
+  long long num_items;
+  const long long* t_ptr;
+  const int* t_blk;
+  long long num_tiles;
+  long long N;
+  long long num_zrows;
+};
+/*
+ * y = F x (or y = add + alpha F x), vectors in cluster order.  Replaces
+ * CompressedFormFactorMatrix._matmat (src/flux/compressed_form_factors.py:805)
+ * and the recursive FormFactorBlockMatrix._matmat (:407-414) with its leaf
+ * products (dense :175, CSR :193, SVD :247-251).
+ */
+int fgb_matvec_f32(const struct fgb_op_desc* d, const float* wpool, const float* vpool,
+                   const float* x, float* z, float* y, const float* add, float alpha, int zero_z,
+                   void* stream);
+int fgb_matvec_f64(const struct fgb_op_desc* d, const double* wpool, const double* vpool,
+                   const double* x, double* z, double* y, const double* add, double alpha,
+                   int zero_z, void* stream);
+/* K right-hand sides (X, Y: N x K row-major): FP32 CUDA cores ... */
+int fgb_matmat_f32(const struct fgb_op_desc* d, const float* wpool, const float* vpool,
+                   const float* X, float* Z, float* Y, int K, const float* add, float alpha,
+                   int zero_z, void* stream);
+/* ... and BF16 tensor cores with FP32 accumulation (X bf16, K % 8 == 0). */
+int fgb_matmat_bf16(const struct fgb_op_desc* d, const void* wpool, const void* vpool,
+                    const void* X, float* Z, void* Zb, float* Y, int K, const float* add,
+                    float alpha, int zero_z, void* stream);
+
+/* --------------------------------------------- solve kernels (a10-a12) */
+/*
+ * Element-wise pieces of solve_radiosity (src/flux/solve.py:4-45) for N x K
+ * FP32 blocks: X = rho .* B (rho per row, or rho_scalar when rho == NULL),
+ * column maxima of |Y - B| (Jacobi stopping test, solve.py:42) and of the
+ * refinement residual R = E - B + Y, B += D, and row gathers between facet
+ * order and cluster order.  colmax holds IEEE bits of non-negative floats.
+ */
+int fgb_scale_rows_f32(const float* B, const float* rho, float rho_scalar, float* X, long long N,
+                       int K, void* stream);
+int fgb_scale_rows_bf16(const float* B, const float* rho, float rho_scalar, void* X, long long N,
+                        int K, void* stream);
+int fgb_colmax_absdiff(const float* Y, const float* B, long long N, int K, unsigned* colmax,
+                       void* stream);
+int fgb_residual(const float* Y, const float* B, const float* E, float* R, long long N, int K,
+                 unsigned* colmax, void* stream);
+int fgb_axpy_cols(float* B, const float* D, const unsigned char* mask, long long N, int K,
+                  void* stream);
+int fgb_gather_rows_f32(const float* in, const long long* idx, float* out, long long N, int K,
+                        void* stream);
+int fgb_gather_rows_f64(const double* in, const long long* idx, double* out, long long N, int K,
+                        void* stream);
+/*
+ * Y = add + alpha * A X for a CSR matrix A (int64 indptr, int32 indices) and
+ * X, Y: n x K row-major — the product with the uncompressed matrix of
+ * get_form_factor_matrix (src/flux/form_factors.py:72) inside
+ * solve_radiosity / compute_steady_state_temp (src/flux/model.py:16).
+ */
+int fgb_csr_spmm_f64(const long long* indptr, const int* indices, const double* data, long long m,
+                     const double* X, int K, double* Y, const double* add, double alpha,
+                     void* stream);
+int fgb_csr_spmm_f32(const long long* indptr, const int* indices, const float* data, long long m,
+                     const float* X, int K, float* Y, const float* add, float alpha, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,172 @@
+"""GPU: compressed form-factor operator (block structure, exact leaves, ACA
+low-rank blocks), its matvec kernels, and the radiosity / steady-state
+solves, against the oracle's exact form factors and the reference's own
+solves (tests/golden/ffref.npz)."""
+import itertools as it
+
+import numpy as np
+import pytest
+import scipy.sparse
+import torch
+
+from oracle import vis
+from tests.conftest import GOLDEN
+from fluxpy_gb300 import shape as gshape, terrain
+from fluxpy_gb300.compressed_form_factors import (
+    CompressedFormFactorMatrix, CompressedKernelMatrix, FormFactorDenseBlock,
+    FormFactorOctreeBlock, FormFactorQuadtreeBlock, FormFactorZeroBlock)
+from fluxpy_gb300.form_factors import get_form_factor_matrix
+from fluxpy_gb300.model import compute_steady_state_temp
+from fluxpy_gb300.solve import solve_radiosity, solve_radiosity_batched
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ffref():
+    return np.load(GOLDEN / "ffref.npz")
+
+
+@pytest.fixture(scope="module")
+def spheres():
+    return np.load(GOLDEN / "spheres.npz")
+
+
+@pytest.mark.parametrize("cls", [gshape.EmbreeTrimeshShapeModel, gshape.CgalTrimeshShapeModel])
+@pytest.mark.parametrize("name", ["icosa_sphere", "icosa_sphere_5"])
+def test_max_depth_1_for_stretched_sphere(spheres, cls, name):
+    # tests/test_compressed_form_factors.py:25-76 of the reference
+    V, F = spheres[f"{name}_V"].copy(), spheres[f"{name}_F"]
+    V *= np.random.default_rng(3).random(3)
+    sm = cls(V, F)
+    outward = (sm.P * sm.N).sum(1) > 0
+    sm.N[outward] *= -1
+    FF = CompressedFormFactorMatrix(sm, tol=0, max_depth=1, force_max_depth=True,
+                                    RootBlock=FormFactorOctreeBlock)
+    FF_gt = get_form_factor_matrix(sm).toarray()
+    assert FF.depth == 1
+    for i, j in it.product(range(8), repeat=2):
+        block = FF._root._blocks[i, j]
+        assert block.is_leaf
+        assert isinstance(block, (FormFactorDenseBlock, FormFactorZeroBlock))
+        I = FF._root._row_block_inds[i]
+        J = FF._root._col_block_inds[j]
+        if I.size and J.size:
+            assert isinstance(block, FormFactorDenseBlock)
+            assert (block._mat == FF_gt[I, :][:, J]).all()
+    E = np.random.default_rng(4).standard_normal(sm.num_faces)
+    B, B_gt = FF @ E, FF_gt @ E
+    assert abs(B - B_gt).max() / abs(B_gt).max() < 1e-14
+
+
+def test_octree_sphere_matches_reference_golden(ffref):
+    sm = gshape.EmbreeTrimeshShapeModel(ffref["octsphere_V"], ffref["octsphere_F"],
+                                        N=ffref["octsphere_N"].copy())
+    FF = CompressedFormFactorMatrix(sm, tol=0, max_depth=1, force_max_depth=True,
+                                    RootBlock=FormFactorOctreeBlock)
+    assert [len(r) for r in FF._root._row_block_inds] == list(ffref["octsphere_rows"])
+    types = [type(b).__name__ for b in FF._root._blocks.ravel()]
+    assert types == list(ffref["octsphere_types"])
+    y = FF @ ffref["octsphere_x"]
+    assert np.allclose(y, ffref["octsphere_y"], rtol=1e-12, atol=1e-15)
+
+
+@pytest.mark.parametrize("max_depth", [1, 2, 3])
+def test_quadtree_crater_exact(ffref, max_depth):
+    # tests/test_compressed_form_factors.py:152-190 (tol = 0): the product
+    # equals the uncompressed matrix's to round-off
+    sm = gshape.EmbreeTrimeshShapeModel(ffref["crater_V"], ffref["crater_F"])
+    FF = CompressedFormFactorMatrix(sm, tol=0, max_depth=max_depth, min_size=4096,
+                                    RootBlock=FormFactorQuadtreeBlock)
+    FF_gt = get_form_factor_matrix(sm)
+    E = ffref["crater_E"]
+    B, B_gt = FF @ E, FF_gt @ E
+    assert abs(B - B_gt).max() / abs(B_gt).max() < np.finfo(np.float64).resolution
+    # and the reference's own compressed product on the same matrix
+    y_ref = ffref[f"crater_quad{max_depth}_y"]
+    assert np.allclose(B, y_ref, rtol=1e-9, atol=1e-12 * abs(y_ref).max())
+
+
+def _terrain_case(n=64, seed=5):
+    V, F = terrain.fbm_terrain(n=n, seed=seed, n_craters=6)
+    return gshape.EmbreeTrimeshShapeModel(V, F)
+
+
+def test_compressed_lowrank_error_vs_exact():
+    sm = _terrain_case(64)
+    FF = CompressedFormFactorMatrix(sm, tol=1e-5, min_size=4096,
+                                    RootBlock=FormFactorOctreeBlock)
+    st = FF.stats
+    assert st["lowrank_blocks"] > 0, st
+    Fx = get_form_factor_matrix(sm)
+    rng = np.random.default_rng(0)
+    for _ in range(3):
+        x = rng.uniform(0, 1, sm.num_faces)
+        y = FF @ x
+        y_gt = Fx @ x
+        err = abs(y - y_gt).max() / abs(y_gt).max()
+        assert err < 1e-4, (err, st)
+    # FP32 and BF16 device products against the FP64 one
+    X = torch.as_tensor(rng.uniform(0, 1, (sm.num_faces, 64)), device="cuda")
+    Xp = FF.permute(X)
+    Y64 = FF.matmat_permuted(Xp[:, :4].contiguous(), "fp64")
+    Y32 = FF.matmat_permuted(Xp, "fp32")
+    Yb = FF.matmat_permuted(Xp, "bf16")
+    y1 = FF.matvec_permuted(Xp[:, 0].contiguous(), "fp32")
+    ref = Y64.abs().max().item()
+    assert (Y32[:, :4].double() - Y64).abs().max().item() / ref < 1e-5
+    assert (y1.double() - Y64[:, 0]).abs().max().item() / ref < 1e-5
+    assert (Yb[:, :4].double() - Y64).abs().max().item() / ref < 2e-2
+
+
+def test_solve_matches_reference_golden(ffref):
+    sm = gshape.EmbreeTrimeshShapeModel(ffref["crater_V"], ffref["crater_F"])
+    FF = get_form_factor_matrix(sm)
+    E = ffref["crater_E"]
+    B, niter = solve_radiosity(FF, E, 0.12, "right", "jacobi")
+    assert niter == int(ffref["crater_niter"])
+    assert np.allclose(B, ffref["crater_B"], rtol=1e-9, atol=1e-9)
+    T = compute_steady_state_temp(FF, E, 0.12, 0.95)
+    assert np.max(np.abs(T - ffref["crater_T"])) < 1e-6
+    B2, n2 = solve_radiosity(FF, ffref["crater_E2"], 0.12, "right", "jacobi")
+    assert n2 == int(ffref["crater_niter2"])
+    assert np.allclose(B2, ffref["crater_B2"], rtol=1e-9, atol=1e-9)
+    T2 = compute_steady_state_temp(FF, ffref["crater_E2"], 0.12, 0.95)
+    assert np.max(np.abs(T2 - ffref["crater_T2"])) < 1e-6
+    # left placement and CG agree with the right-placement solution
+    Bl, _ = solve_radiosity(FF, E, 0.12, "left", "jacobi")
+    Bc, _ = solve_radiosity(FF, E, 0.12, "left", "cg")
+    assert np.allclose(Bl, Bc, rtol=1e-8, atol=1e-8)
+    with pytest.raises(NotImplementedError):
+        solve_radiosity(FF, E, 0.12, "right", "cg")
+
+
+def test_solve_with_compressed_operator_and_kernel_matrix(ffref):
+    sm = gshape.EmbreeTrimeshShapeModel(ffref["crater_V"], ffref["crater_F"])
+    FF = CompressedFormFactorMatrix(sm, tol=0, min_size=4096)
+    E = ffref["crater_E"]
+    B, niter = solve_radiosity(FF, E, 0.12)
+    assert niter == int(ffref["crater_niter"])
+    assert np.allclose(B, ffref["crater_B"], rtol=1e-9, atol=1e-9)
+    Kop = CompressedKernelMatrix(FF, 0.12)
+    r = Kop @ B - E  # (I - rho F) B - E, small at convergence
+    assert abs(r).max() <= 1e-9 * abs(E).max()
+
+
+def test_batched_solvers_reach_rtol():
+    sm = _terrain_case(48, seed=9)
+    FF = CompressedFormFactorMatrix(sm, tol=1e-5, min_size=4096, dtype=np.float32,
+                                    RootBlock=FormFactorOctreeBlock)
+    dirs = terrain.random_sun_directions(64, seed=2)
+    E = sm.get_direct_irradiance_batch(1365.0, dirs, out_dtype=torch.float32)
+    assert E.shape == (sm.num_faces, 64)
+    for prec in ("fp32", "bf16-refine"):
+        st = {}
+        B = solve_radiosity_batched(FF, E, 0.12, rtol=1e-5, precision=prec, stats=st)
+        # residual with the operator in FP64 arithmetic
+        Bp = FF.permute(B.double())
+        FBp = FF.matmat_permuted(Bp[:, :8].contiguous() * 0.12, "fp64")
+        Ep = FF.permute(E.double())[:, :8]
+        R = Ep - (Bp[:, :8] - FBp)
+        rel = (R.abs().amax(0) / Ep.abs().amax(0).clamp_min(1e-30)).max().item()
+        assert rel <= 2e-5, (prec, rel, st)

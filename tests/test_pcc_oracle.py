@@ -28,8 +28,11 @@ def test_oracle_reproduces_golden_files():
     sc.check_against_golden(prof, surf, golden)
 
 
+ZFAC = {40: 1.0817, 60: 1.05, 100: 1.03}
+
+
 def _random_case(rng, n, nz):
-    z = np.concatenate([[0.0], setgrid(nz, 1.0817, 1.0)])
+    z = np.concatenate([[0.0], setgrid(nz, ZFAC.get(nz, 1.0817), 1.0)])
     w = nz + 1
     ti = np.linspace(55, 400, w)
     rhoc = np.full(w, 1.2e6)

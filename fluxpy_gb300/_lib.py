@@ -47,6 +47,7 @@ U32P = C.c_void_p
 SIGNATURES: dict[str, list] = {
     "fgb_last_error": [],
     "fgb_version": [],
+    "fgb_launch_count": [],
     # conduction (a14)
     "fgb_conduction_q_f64": [I32, I32, P, F64, P, P, P, P, P, P, P, P, P, U32P, P],
     "fgb_conduction_q_f32": [I32, I32, P, F32, P, P, P, P, P, P, P, P, P, U32P, P],
@@ -80,8 +81,8 @@ SIGNATURES: dict[str, list] = {
     # block matvec (a9)
     "fgb_matvec_f32": [P, P, P, P, P, P, P, F32, I32, P],
     "fgb_matvec_f64": [P, P, P, P, P, P, P, F64, I32, P],
-    "fgb_matmat_f32": [P, P, P, P, P, P, I32, P, F32, I32, P],
-    "fgb_matmat_bf16": [P, P, P, P, P, P, P, I32, P, F32, I32, P],
+    "fgb_matmat_f32": [P, P, P, P, P, P, I32, P, F32, I32, I32, P],
+    "fgb_matmat_bf16": [P, P, P, P, P, P, P, I32, P, F32, I32, I32, P],
     # solve (a10-a12)
     "fgb_scale_rows_f32": [P, P, F32, P, I64, I32, P],
     "fgb_scale_rows_bf16": [P, P, F32, P, I64, I32, P],
@@ -93,7 +94,8 @@ SIGNATURES: dict[str, list] = {
     "fgb_csr_spmm_f64": [P, P, P, I64, P, I32, P, P, F64, P],
     "fgb_csr_spmm_f32": [P, P, P, I64, P, I32, P, P, F32, P],
 }
-_RESTYPES = {"fgb_last_error": C.c_char_p, "fgb_version": C.c_char_p}
+_RESTYPES = {"fgb_last_error": C.c_char_p, "fgb_version": C.c_char_p,
+             "fgb_launch_count": C.c_longlong}
 
 _lock = threading.Lock()
 _lib = None
@@ -166,6 +168,11 @@ def ptr(t: torch.Tensor | None) -> int | None:
 def stream_handle(stream: torch.cuda.Stream | None = None) -> int:
     s = stream if stream is not None else torch.cuda.current_stream()
     return s.cuda_stream
+
+
+def launch_count() -> int:
+    """Kernels launched by libfluxgb in this process so far."""
+    return int(lib().fgb_launch_count())
 
 
 def loaded_library_path() -> str:

@@ -196,7 +196,7 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
 
     def __init__(self, shape_model, tol=1e-5, min_size=16384, max_depth=None,
                  force_max_depth=False, RootBlock=None, *, leaf_size=64, eta=1.0, rmax=64,
-                 nverify=4, dtype=None, eps=None, **kwargs):
+                 nsample=1024, dtype=None, eps=None, **kwargs):
         if tol < 0:
             raise RuntimeError('tol should be a nonnegative float')
         if max_depth is not None and not isinstance(max_depth, int):
@@ -218,7 +218,7 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         self._leaf_size = leaf_size
         self._eta = eta
         self._rmax = rmax
-        self._nverify = nverify
+        self._nsample = nsample
         self._eps = config.DEFAULT_EPS if eps is None else eps
         self._store_dtype = np.dtype(shape_model.dtype if dtype is None else dtype)
         if self._store_dtype not in (np.float64, np.float32):
@@ -432,7 +432,7 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         _lib.call("fgb_aca_f64", sm.bvh.handle, _lib.ptr(P), _lib.ptr(Nn), _lib.ptr(A),
                   _lib.ptr(perm_d), nb, _lib.ptr(r0_d), _lib.ptr(m_d), _lib.ptr(c0_d),
                   _lib.ptr(n_d), mmax, nmax, float(self._eps), sm.semantics, float(self._tol),
-                  rmax, self._nverify, _lib.ptr(scratch), num_ctas, _lib.ptr(pool), capacity,
+                  rmax, self._nsample, _lib.ptr(scratch), num_ctas, _lib.ptr(pool), capacity,
                   _lib.ptr(used), _lib.ptr(rank_out), _lib.ptr(off_out), _lib.ptr(queue),
                   _lib.ptr(flags), _lib.stream_handle())
         fl = int(flags.item())
@@ -658,7 +658,7 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
             pool = self.pool("fp32")
             _lib.call("fgb_matmat_f32", C.byref(self._desc), _lib.ptr(pool), _lib.ptr(pool),
                       _lib.ptr(Xp), _lib.ptr(Z), _lib.ptr(out), K, _lib.ptr(add), float(alpha),
-                      int(self._needs_zero_z), _lib.stream_handle())
+                      int(self._needs_zero_z), 3, _lib.stream_handle())
             return out
         if precision == "bf16":
             return self._matmat_bf16(Xp, out=out, add=add, alpha=alpha, Z=Z)
@@ -675,7 +675,7 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         pool = self.pool("bf16")
         _lib.call("fgb_matmat_bf16", C.byref(self._desc), _lib.ptr(pool), _lib.ptr(pool),
                   _lib.ptr(Xb), _lib.ptr(Z), _lib.ptr(Zb), _lib.ptr(out), K, _lib.ptr(add),
-                  float(alpha), int(self._needs_zero_z), _lib.stream_handle())
+                  float(alpha), int(self._needs_zero_z), 3, _lib.stream_handle())
         return out
 
     def _default_precision(self):

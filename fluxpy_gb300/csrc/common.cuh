@@ -29,8 +29,12 @@ inline int cuda_status(cudaError_t e, const char* where) {
     if (_e != cudaSuccess) return ::fgb::cuda_status(_e, #expr); \
   } while (0)
 
+// Every kernel launch is followed by this check, which also counts the
+// launch (fgb_launch_count()).
+void count_launch();
 #define FGB_LAUNCH_CHECK(name)                                \
   do {                                                        \
+    ::fgb::count_launch();                                    \
     cudaError_t _e = cudaGetLastError();                      \
     if (_e != cudaSuccess) return ::fgb::cuda_status(_e, name); \
   } while (0)

@@ -7,8 +7,10 @@
 // U V^T are built by partially pivoted ACA (Bebendorf, "Approximation of
 // boundary element matrices", Numer. Math. 86, 2000) with the Frobenius
 // stopping test |u_k| |v_k| <= tol |S_k|_F.  Because visibility makes blocks
-// patchy, convergence is confirmed on `nverify` random rows whose residual
-// must be negligible; a non-negligible one becomes the next pivot row.
+// patchy (a few rows or columns may carry all of a block's mass), the test
+// is confirmed by a Monte Carlo estimate of the residual's Frobenius norm
+// from `nsample` random entries, (m n / S) sum R_ij^2 <= tol^2 |S_k|_F^2; if
+// it fails, the row of the worst sample becomes the next pivot row.
 // A block whose rank would reach its cap (storage no smaller than half the
 // dense block, or rmax) is reported as failed (rank -1) and is subdivided by
 // the host.
@@ -40,7 +42,7 @@ struct AcaArgs {
   int sem;
   float tol;
   int rmax;
-  int nverify;
+  int nsample;
   float* scratch;
   long long per_cta;
   long long mmax, nmax;
@@ -157,43 +159,36 @@ aca_kernel(AcaArgs a, EntryCtx<R> e) {
     int kmax = (int)min((long long)a.rmax, max(cap, 1LL));
     int k = 0;
     double normS2 = 0.0;
-    unsigned seed = 0x9e3779b9u ^ (unsigned)(b * 2654435761ull);
+    const unsigned bseed = 0x9e3779b9u ^ (unsigned)(b * 2654435761ull);
     int istar = m / 2;
-    int confirm = 0;  // consecutive negligible rows since the last new term
     bool failed = false;
-    const int max_iter = (a.rmax + 1) * (a.nverify + 2) + 16;
-    int iter = 0;
+    int rounds = 0;
+    bool verify = false;
+    const int max_rounds = 4 * a.rmax + 8;
     __syncthreads();
     while (true) {
-      if (++iter > max_iter) { failed = true; break; }
-      // residual of row istar
-      const long long fi = prow[istar];
-      float lmax_v = 0.f;
-      int lmax_i = -1;
-      double rr = 0.0;
-      for (int j = tid; j < n; j += kAcaThreads) {
-        float val = entry<R>(a, e, fi, pcol[j], &overflow);
-        for (int l = 0; l < k; l++) val -= U[(long long)l * a.mmax + istar] * V[(long long)l * a.nmax + j];
-        rowbuf[j] = val;
-        rr += (double)val * val;
-        if (used_c[j] == 0.f && (lmax_i < 0 || fabsf(val) > fabsf(lmax_v))) { lmax_v = val; lmax_i = j; }
-      }
-      if (tid == 0) used_r[istar] = 1.f;
-      float piv;
-      int jstar;
-      block_argmax(lmax_v, lmax_i, sh_v, sh_i, &piv, &jstar);
-      rr = block_sum(rr, sh_d);
-      // negligible row: m |r|^2 <= (2 tol)^2 |S|_F^2, i.e. rows like this one
-      // would add at most about the requested relative error
-      bool negligible = jstar < 0 || piv == 0.0f ||
-                        (double)m * rr <= 4.0 * (double)a.tol * (double)a.tol * normS2;
-      bool pick_random;
-      if (negligible) {
-        if (++confirm >= a.nverify) break;  // converged (k == 0: zero block)
-        pick_random = true;
-      } else {
+      if (!verify) {
+        // ---- partially pivoted row step at istar
+        const long long fi = prow[istar];
+        float lmax_v = 0.f;
+        int lmax_i = -1;
+        double rr = 0.0;
+        for (int j = tid; j < n; j += kAcaThreads) {
+          float val = entry<R>(a, e, fi, pcol[j], &overflow);
+          for (int l = 0; l < k; l++) val -= U[(long long)l * a.mmax + istar] * V[(long long)l * a.nmax + j];
+          rowbuf[j] = val;
+          rr += (double)val * val;
+          if (used_c[j] == 0.f && (lmax_i < 0 || fabsf(val) > fabsf(lmax_v))) { lmax_v = val; lmax_i = j; }
+        }
+        if (tid == 0) used_r[istar] = 1.f;
+        float piv;
+        int jstar;
+        block_argmax(lmax_v, lmax_i, sh_v, sh_i, &piv, &jstar);
+        rr = block_sum(rr, sh_d);
+        const bool negligible = jstar < 0 || piv == 0.0f ||
+                                (normS2 > 0.0 && (double)m * rr <= 1e-4 * (double)a.tol * a.tol * normS2);
+        if (negligible) { verify = true; continue; }
         if (k >= kmax) { failed = true; break; }
-        confirm = 0;
         // new term: v = row / pivot, u = residual column jstar
         const float inv = 1.0f / piv;
         for (int j = tid; j < n; j += kAcaThreads) V[(long long)k * a.nmax + j] = rowbuf[j] * inv;
@@ -246,24 +241,49 @@ aca_kernel(AcaArgs a, EntryCtx<R> e) {
         float nxt_v;
         int nxt_i;
         block_argmax(umax_v, umax_i, sh_v, sh_i, &nxt_v, &nxt_i);
-        pick_random = sqrt(uu * vv) <= (double)a.tol * sqrt(normS2) || nxt_i < 0;
-        if (!pick_random) istar = nxt_i;
+        if (sqrt(uu * vv) <= (double)a.tol * sqrt(normS2) || nxt_i < 0) verify = true;
+        else istar = nxt_i;
+        continue;
       }
-      if (pick_random) {
-        // next random unused row (all threads draw the same sequence)
+      // ---- verification: Monte Carlo estimate of |R|_F^2 from nsample random entries
+      if (++rounds > max_rounds) { failed = true; break; }
+      double rs = 0.0;
+      float wmax_v = 0.f;
+      int wmax_i = -1;
+      bool any_nz = false;
+      for (int q = tid; q < a.nsample; q += kAcaThreads) {
+        unsigned h = bseed ^ (unsigned)(rounds * 0x85ebca6bu) ^ (unsigned)(q * 0xc2b2ae35u);
+        h ^= h >> 16; h *= 0x7feb352du; h ^= h >> 15; h *= 0x846ca68bu; h ^= h >> 16;
+        const int i = (int)(h % (unsigned)m);
+        unsigned h2 = h * 0x9e3779b1u + 0x7f4a7c15u;
+        h2 ^= h2 >> 13; h2 *= 0x5bd1e995u; h2 ^= h2 >> 15;
+        const int j = (int)(h2 % (unsigned)n);
+        float val = entry<R>(a, e, prow[i], pcol[j], &overflow);
+        for (int l = 0; l < k; l++) val -= U[(long long)l * a.mmax + i] * V[(long long)l * a.nmax + j];
+        rs += (double)val * val;
+        if (val != 0.f) any_nz = true;
+        if (used_r[i] == 0.f && (wmax_i < 0 || fabsf(val) > fabsf(wmax_v))) { wmax_v = val; wmax_i = i; }
+      }
+      rs = block_sum(rs, sh_d);
+      const int nz = __syncthreads_or(any_nz);
+      float wv;
+      int wi;
+      block_argmax(wmax_v, wmax_i, sh_v, sh_i, &wv, &wi);
+      const double est = rs * ((double)m * (double)n / (double)a.nsample);
+      const bool ok = (normS2 > 0.0) ? (est <= (double)a.tol * a.tol * normS2) : (nz == 0);
+      if (ok) break;
+      if (wi < 0 || wv == 0.0f) {
+        // the worst sample sits on an already used row: fall back to any unused row
         int cand = -1;
-        for (int t = 0; t < 32 && cand < 0; t++) {
-          int c = (int)(lcg(seed) % (unsigned)m);
-          if (used_r[c] == 0.f) cand = c;
-        }
-        if (cand < 0) {
-          for (int c = 0; c < m; c++)
-            if (used_r[c] == 0.f) { cand = c; break; }
-        }
+        for (int c = 0; c < m; c++)
+          if (used_r[c] == 0.f) { cand = c; break; }
         __syncthreads();
-        if (cand < 0) break;  // every row examined
+        if (cand < 0) { failed = true; break; }
         istar = cand;
+      } else {
+        istar = wi;
       }
+      verify = false;
     }
     __syncthreads();
     if (failed) {
@@ -317,7 +337,7 @@ int fgb_aca_scratch_floats(int rmax, long long mmax, long long nmax, long long* 
 int fgb_aca_f64(const void* bvh, const double* P, const double* N, const double* A,
                 const long long* perm, long long nblocks, const int* r0, const int* m,
                 const int* c0, const int* n, long long mmax, long long nmax, double eps,
-                int semantics, float tol, int rmax, int nverify, float* scratch, int num_ctas,
+                int semantics, float tol, int rmax, int nsample, float* scratch, int num_ctas,
                 float* pool, long long pool_capacity, unsigned long long* pool_used,
                 int* rank_out, long long* off_out, int* queue, unsigned* flags, void* stream) {
   if (!bvh || nblocks < 0 || num_ctas < 1) { fgb::set_error("bad ACA arguments"); return FGB_BAD_ARG; }
@@ -334,7 +354,7 @@ int fgb_aca_f64(const void* bvh, const double* P, const double* N, const double*
   a.sem = semantics;
   a.tol = tol;
   a.rmax = rmax;
-  a.nverify = nverify < 1 ? 1 : nverify;
+  a.nsample = nsample < 32 ? 32 : nsample;
   a.scratch = scratch;
   a.per_cta = per_cta;
   a.mmax = mmax; a.nmax = nmax;

@@ -78,37 +78,61 @@ __global__ void phaseA_k1(OpView op, const T* __restrict__ vpool, const V* __res
   }
 }
 
+// Phase B, K = 1: one CTA (8 warps) per 64-row tile.  Warp w takes blocks
+// w, w+8, ... of the tile's list; lane L accumulates rows L and L+32 of the
+// tile; the 8 warp partials are summed in a fixed order (deterministic).
+constexpr int kB1Warps = 8;
+
 template <class T, class V>
-__global__ void __launch_bounds__(kTileRows)
+__global__ void __launch_bounds__(kB1Warps * 32)
 phaseB_k1(OpView op, const T* __restrict__ wpool, const V* __restrict__ x,
           const V* __restrict__ z, V* __restrict__ y, const V* __restrict__ add_vec,
           V alpha) {
-  __shared__ V s_src[256];
+  __shared__ V s_part[kB1Warps][kTileRows];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const long long t = blockIdx.x;
   const long long t0 = t * kTileRows;
-  const long long i = t0 + threadIdx.x;
-  V acc = V(0);
-  for (long long q = op.t_ptr[t]; q < op.t_ptr[t + 1]; q++) {
+  V acc0 = V(0), acc1 = V(0);
+  for (long long q = op.t_ptr[t] + warp; q < op.t_ptr[t + 1]; q += kB1Warps) {
     const int b = op.t_blk[q];
     const long long r0 = op.r0[b];
     const int m = op.m[b], k = op.k[b];
     const bool lr = op.zoff[b] >= 0;
     const V* src = lr ? z + op.zoff[b] : x + op.c0[b];
     const T* w = wpool + op.woff[b];
-    const bool mine = i >= r0 && i < r0 + m;
-    const long long li = i - r0;
-    for (int l0 = 0; l0 < k; l0 += 256) {
-      const int len = min(256, k - l0);
-      __syncthreads();
-      for (int l = threadIdx.x; l < len; l += kTileRows) s_src[l] = src[l0 + l];
-      __syncthreads();
-      if (mine) {
-        const T* wc = w + (long long)l0 * m + li;
-        for (int l = 0; l < len; l++) acc += (V)wc[(long long)l * m] * s_src[l];
+    const long long i0 = t0 + lane, i1 = t0 + lane + 32;
+    const bool in0 = i0 >= r0 && i0 < r0 + m, in1 = i1 >= r0 && i1 < r0 + m;
+    const T* w0 = w + (i0 - r0);
+    const T* w1 = w + (i1 - r0);
+    int l = 0;
+    for (; l + 4 <= k; l += 4) {
+      const V s0 = __ldg(src + l), s1 = __ldg(src + l + 1), s2 = __ldg(src + l + 2),
+              s3 = __ldg(src + l + 3);
+      if (in0) {
+        acc0 += (V)w0[(long long)l * m] * s0 + (V)w0[(long long)(l + 1) * m] * s1 +
+                (V)w0[(long long)(l + 2) * m] * s2 + (V)w0[(long long)(l + 3) * m] * s3;
+      }
+      if (in1) {
+        acc1 += (V)w1[(long long)l * m] * s0 + (V)w1[(long long)(l + 1) * m] * s1 +
+                (V)w1[(long long)(l + 2) * m] * s2 + (V)w1[(long long)(l + 3) * m] * s3;
       }
     }
+    for (; l < k; l++) {
+      const V sv = __ldg(src + l);
+      if (in0) acc0 += (V)w0[(long long)l * m] * sv;
+      if (in1) acc1 += (V)w1[(long long)l * m] * sv;
+    }
   }
-  if (i < op.N) y[i] = add_vec ? add_vec[i] + alpha * acc : acc;
+  s_part[warp][lane] = acc0;
+  s_part[warp][lane + 32] = acc1;
+  __syncthreads();
+  if (threadIdx.x < kTileRows) {
+    V sum = V(0);
+#pragma unroll
+    for (int wv = 0; wv < kB1Warps; wv++) sum += s_part[wv][threadIdx.x];
+    const long long i = t0 + threadIdx.x;
+    if (i < op.N) y[i] = add_vec ? add_vec[i] + alpha * sum : sum;
+  }
 }
 
 // ------------------------------------------------- K RHS, FP32 FFMA ----
@@ -492,7 +516,7 @@ int fgb_matvec_f32(const fgb_op_desc* d, const float* wpool, const float* vpool,
     FGB_LAUNCH_CHECK("phaseA_k1");
   }
   if (op.num_tiles > 0) {
-    fgb::phaseB_k1<float, float><<<(unsigned)op.num_tiles, fgb::kTileRows, 0, s>>>(op, wpool, x, z, y, add, alpha);
+    fgb::phaseB_k1<float, float><<<(unsigned)op.num_tiles, fgb::kB1Warps * 32, 0, s>>>(op, wpool, x, z, y, add, alpha);
     FGB_LAUNCH_CHECK("phaseB_k1");
   }
   return FGB_OK;
@@ -512,7 +536,7 @@ int fgb_matvec_f64(const fgb_op_desc* d, const double* wpool, const double* vpoo
     FGB_LAUNCH_CHECK("phaseA_k1");
   }
   if (op.num_tiles > 0) {
-    fgb::phaseB_k1<double, double><<<(unsigned)op.num_tiles, fgb::kTileRows, 0, s>>>(op, wpool, x, z, y, add, alpha);
+    fgb::phaseB_k1<double, double><<<(unsigned)op.num_tiles, fgb::kB1Warps * 32, 0, s>>>(op, wpool, x, z, y, add, alpha);
     FGB_LAUNCH_CHECK("phaseB_k1");
   }
   return FGB_OK;
@@ -524,21 +548,21 @@ int fgb_matvec_f64(const fgb_op_desc* d, const double* wpool, const double* vpoo
  */
 int fgb_matmat_f32(const fgb_op_desc* d, const float* wpool, const float* vpool, const float* X,
                    float* Z, float* Y, int K, const float* add, float alpha, int zero_z,
-                   void* stream) {
+                   int phases, void* stream) {
   fgb::OpView op = fgb::to_view(d);
   int st = fgb::check_op(op);
   if (st) return st;
   if (K < 1) { fgb::set_error("K must be >= 1"); return FGB_BAD_ARG; }
   cudaStream_t s = fgb::as_stream(stream);
-  if (zero_z && d->num_zrows > 0)
+  if ((phases & 1) && zero_z && d->num_zrows > 0)
     FGB_CUDA_TRY(cudaMemsetAsync(Z, 0, sizeof(float) * d->num_zrows * (size_t)K, s));
   unsigned ky = (unsigned)((K + fgb::kKT - 1) / fgb::kKT);
-  if (op.num_items > 0) {
+  if ((phases & 1) && op.num_items > 0) {
     dim3 g((unsigned)op.num_items, ky);
     fgb::phaseA_kn_f32<<<g, 256, 0, s>>>(op, vpool, X, Z, K);
     FGB_LAUNCH_CHECK("phaseA_kn_f32");
   }
-  if (op.num_tiles > 0) {
+  if ((phases & 2) && op.num_tiles > 0) {
     dim3 g((unsigned)op.num_tiles, ky);
     fgb::phaseB_kn_f32<<<g, 256, 0, s>>>(op, wpool, X, Z, Y, K, add, alpha);
     FGB_LAUNCH_CHECK("phaseB_kn_f32");
@@ -554,7 +578,7 @@ int fgb_matmat_f32(const fgb_op_desc* d, const float* wpool, const float* vpool,
  */
 int fgb_matmat_bf16(const fgb_op_desc* d, const void* wpool, const void* vpool, const void* X,
                     float* Z, void* Zb, float* Y, int K, const float* add, float alpha,
-                    int zero_z, void* stream) {
+                    int zero_z, int phases, void* stream) {
   fgb::OpView op = fgb::to_view(d);
   int st = fgb::check_op(op);
   if (st) return st;
@@ -569,7 +593,7 @@ int fgb_matmat_bf16(const fgb_op_desc* d, const void* wpool, const void* vpool, 
   const __nv_bfloat16* x = static_cast<const __nv_bfloat16*>(X);
   __nv_bfloat16* zb = static_cast<__nv_bfloat16*>(Zb);
   unsigned kx = (unsigned)((K + fgb::kBT - 1) / fgb::kBT);
-  if (op.num_items > 0) {
+  if ((phases & 1) && op.num_items > 0) {
     if (zero_z) FGB_CUDA_TRY(cudaMemsetAsync(Z, 0, sizeof(float) * d->num_zrows * (size_t)K, s));
     dim3 g(kx, (unsigned)op.num_items);
     fgb::phaseA_kn_bf16<<<g, 128, 0, s>>>(op, v, x, K, Z, K, K);
@@ -578,7 +602,7 @@ int fgb_matmat_bf16(const fgb_op_desc* d, const void* wpool, const void* vpool, 
     fgb::f32_to_bf16_kernel<<<fgb::grid_for(nz, 256), 256, 0, s>>>(Z, zb, nz);
     FGB_LAUNCH_CHECK("f32_to_bf16_kernel");
   }
-  if (op.num_tiles > 0) {
+  if ((phases & 2) && op.num_tiles > 0) {
     dim3 g(kx, (unsigned)op.num_tiles);
     fgb::phaseB_kn_bf16<<<g, 128, 0, s>>>(op, w, x, K, zb, K, Y, K, K, add, K, alpha);
     FGB_LAUNCH_CHECK("phaseB_kn_bf16");

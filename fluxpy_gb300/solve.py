@@ -104,10 +104,19 @@ def _rho_vec(rho, E_d):
 
 # ---------------------------------------------------- reference solver --
 def solve_radiosity(FF, E, rho=1, albedo_placement='right', method='jacobi', tol=None,
-                    max_iter=100000):
+                    max_iter=100000, rtol=1e-5):
     """Solve B = E + F (rho B) (right) or B = E + rho F B (left)
     (src/flux/solve.py:4-22).  Host arrays in, host arrays out; device
-    tensors in, device tensors out."""
+    tensors in, device tensors out.
+
+    Besides the reference's 'jacobi' and 'cg', method may be 'batched-fp32'
+    or 'batched-bf16' (right placement, compressed operator, E of shape
+    (N, K)): every column is solved to a relative residual ``rtol`` by
+    ``solve_radiosity_batched``; the returned niter is the number of outer
+    iterations.  Host input (numpy or a pinned CPU tensor) is copied to the
+    device and the result back to the host."""
+    if method in ('batched-fp32', 'batched-bf16'):
+        return _solve_batched_public(FF, E, rho, albedo_placement, method, rtol)
     on_dev = isinstance(E, torch.Tensor)
     E_np = None if on_dev else np.asarray(E)
     dtype = np.dtype(E_np.dtype if E_np is not None else
@@ -135,6 +144,33 @@ def solve_radiosity(FF, E, rho=1, albedo_placement='right', method='jacobi', tol
     if on_dev:
         return B, niter
     return B.cpu().numpy().astype(dtype, copy=False), niter
+
+
+def _solve_batched_public(FF, E, rho, placement, method, rtol):
+    if placement != 'right':
+        raise ValueError("batched solves use right albedo placement")
+    dev = _lib.require_cuda()
+    host_in = not (isinstance(E, torch.Tensor) and E.is_cuda)
+    if isinstance(E, torch.Tensor):
+        E_d = E.to(dev, torch.float32, non_blocking=True)
+    else:
+        E_d = torch.as_tensor(np.asarray(E, dtype=np.float32), device=dev)
+    vec = E_d.ndim == 1
+    if vec:
+        E_d = E_d.reshape(-1, 1)
+    st = {}
+    B = solve_radiosity_batched(FF, E_d, rho, rtol=rtol,
+                                precision="fp32" if method == "batched-fp32" else "bf16-refine",
+                                stats=st)
+    if vec:
+        B = B.reshape(-1)
+    if host_in:
+        if isinstance(E, torch.Tensor):
+            out = torch.empty(B.shape, dtype=torch.float32, pin_memory=E.is_pinned())
+            out.copy_(B)
+            return out, st["outer"]
+        return B.cpu().numpy(), st["outer"]
+    return B, st["outer"]
 
 
 def _jacobi(apply, E, rho, placement, tol, max_iter):
@@ -199,7 +235,14 @@ def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_
     Returns B (N, K) fp32; fills `stats` (iterations, matmats, residuals).
     """
     dev = E.device
-    N, K = E.shape
+    N, K0 = E.shape
+    if precision == "bf16-refine" and K0 % 8:
+        pad = 8 - K0 % 8
+        E = torch.cat([E, torch.zeros((N, pad), dtype=E.dtype, device=dev)], 1)
+        B = solve_radiosity_batched(FF, E, rho, rtol, precision, max_iter, inner, E_is_permuted,
+                                    return_permuted, stats)
+        return B[:, :K0].contiguous()
+    K = K0
     stream = _lib.stream_handle()
     Ep = E.to(torch.float32).contiguous() if E_is_permuted else FF.permute(E.to(torch.float32)).contiguous()
     rho_d = None
@@ -212,6 +255,7 @@ def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_
         rho_d = rho_d.contiguous()
     emax = Ep.abs().amax(0)
     thresh = (rtol * emax).cpu().numpy().astype(np.float32)
+    thresh[thresh == 0] = 0.0
     colmax = torch.zeros(K, dtype=torch.int32, device=dev)
     Z32 = torch.empty((max(FF._num_zrows, 1), K), dtype=torch.float32, device=dev)
     X32 = torch.empty_like(Ep)
@@ -261,7 +305,7 @@ def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_
                           N, K, stream)
                 _lib.call("fgb_matmat_bf16", C.byref(FF._desc), _lib.ptr(pool_b), _lib.ptr(pool_b),
                           _lib.ptr(Xb), _lib.ptr(Z32), _lib.ptr(Zb), _lib.ptr(D), K, _lib.ptr(R),
-                          1.0, int(FF._needs_zero_z), stream)
+                          1.0, int(FF._needs_zero_z), 3, stream)
                 st["bf16_matmats"] += 1
             _lib.call("fgb_axpy_cols", _lib.ptr(B), _lib.ptr(D), None, N, K, stream)
         else:

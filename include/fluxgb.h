@@ -56,6 +56,8 @@ enum fgb_status {
 const char* fgb_last_error(void);
 /* Library version string. */
 const char* fgb_version(void);
+/* Number of kernels this library has launched in the process so far. */
+long long fgb_launch_count(void);
 
 /* ------------------------------------------------ 1-D conduction (a14) */
 /*
@@ -243,7 +245,7 @@ int fgb_aca_scratch_floats(int rmax, long long mmax, long long nmax, long long* 
 int fgb_aca_f64(const void* bvh, const double* P, const double* N, const double* A,
                 const long long* perm, long long nblocks, const int* r0, const int* m,
                 const int* c0, const int* n, long long mmax, long long nmax, double eps,
-                int semantics, float tol, int rmax, int nverify, float* scratch, int num_ctas,
+                int semantics, float tol, int rmax, int nsample, float* scratch, int num_ctas,
                 float* pool, long long pool_capacity, unsigned long long* pool_used,
                 int* rank_out, long long* off_out, int* queue, unsigned* flags, void* stream);
 
@@ -286,14 +288,15 @@ int fgb_matvec_f32(const struct fgb_op_desc* d, const float* wpool, const float*
 int fgb_matvec_f64(const struct fgb_op_desc* d, const double* wpool, const double* vpool,
                    const double* x, double* z, double* y, const double* add, double alpha,
                    int zero_z, void* stream);
-/* K right-hand sides (X, Y: N x K row-major): FP32 CUDA cores ... */
+/* K right-hand sides (X, Y: N x K row-major): FP32 CUDA cores ...
+ * phases: 1 = phase A only (Z = Vt X), 2 = phase B only (Y from Z), 3 = both. */
 int fgb_matmat_f32(const struct fgb_op_desc* d, const float* wpool, const float* vpool,
                    const float* X, float* Z, float* Y, int K, const float* add, float alpha,
-                   int zero_z, void* stream);
+                   int zero_z, int phases, void* stream);
 /* ... and BF16 tensor cores with FP32 accumulation (X bf16, K % 8 == 0). */
 int fgb_matmat_bf16(const struct fgb_op_desc* d, const void* wpool, const void* vpool,
                     const void* X, float* Z, void* Zb, float* Y, int K, const float* add,
-                    float alpha, int zero_z, void* stream);
+                    float alpha, int zero_z, int phases, void* stream);
 
 /* --------------------------------------------- solve kernels (a10-a12) */
 /*

@@ -457,6 +457,14 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         sdt = self._store_dtype
         tdt = torch.float64 if sdt == np.float64 else torch.float32
         exact = np.array(sorted(exact), dtype=np.int64)
+        if exact.size:
+            # order by (row range, first column) so that horizontally adjacent
+            # exact leaves of one row cluster are contiguous in the pool and
+            # can be merged into one wider dense block on the device
+            er = tree.start[self._rows[exact]]
+            em = tree.size[self._rows[exact]]
+            ec = tree.start[self._cols[exact]]
+            exact = exact[np.lexsort((ec, em, er))]
         ex_r = self._rows[exact] if exact.size else np.zeros(0, np.int64)
         ex_c = self._cols[exact] if exact.size else np.zeros(0, np.int64)
         ex_m = tree.size[ex_r]
@@ -522,16 +530,41 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         self._pool_f32 = None
         self._pool_bf16 = None
 
-        # device block list: LR with rank > 0, exact with nnz > 0
+        # device block list: LR leaves with rank > 0, then merged runs of
+        # exact leaves (same row range, adjacent column ranges, contiguous in
+        # the pool) with at least one nonzero
         lr = np.where((self._kind == LEAF_LOWRANK) & (self._rank > 0))[0]
-        ex_nz = np.array([b for b in exact if self._leaf_nnz[b] > 0], dtype=np.int64)
-        blocks = np.concatenate([lr, ex_nz]).astype(np.int64)
-        nbk = blocks.size
-        r0 = tree.start[self._rows[blocks]]
-        m = tree.size[self._rows[blocks]]
-        c0 = tree.start[self._cols[blocks]]
-        n = tree.size[self._cols[blocks]]
-        k = np.where(np.arange(nbk) < lr.size, self._rank[blocks], n)
+        run_r0, run_m, run_c0, run_n, run_off = [], [], [], [], []
+        prev = None
+        run_nnz = 0
+        for q, b in enumerate(exact):
+            r0b, mb = int(tree.start[ex_r[q]]), int(ex_m[q])
+            c0b, nb_ = int(tree.start[ex_c[q]]), int(ex_n[q])
+            if prev is not None and prev[0] == r0b and prev[1] == mb and prev[2] + prev[3] == c0b:
+                run_n[-1] += nb_
+                prev = (r0b, mb, prev[2], prev[3] + nb_)
+                run_nnz_list[-1] += int(self._leaf_nnz[b])
+                continue
+            if prev is None:
+                run_nnz_list = []
+            run_r0.append(r0b); run_m.append(mb); run_c0.append(c0b); run_n.append(nb_)
+            run_off.append(int(dense_off[q]))
+            run_nnz_list.append(int(self._leaf_nnz[b]))
+            prev = (r0b, mb, c0b, nb_)
+        keep = [i for i, z in enumerate(run_nnz_list)] if exact.size else []
+        keep = [i for i in keep if run_nnz_list[i] > 0]
+        ex_r0 = np.array([run_r0[i] for i in keep], np.int64)
+        ex_mm = np.array([run_m[i] for i in keep], np.int64)
+        ex_c0 = np.array([run_c0[i] for i in keep], np.int64)
+        ex_nn = np.array([run_n[i] for i in keep], np.int64)
+        ex_off = np.array([run_off[i] for i in keep], np.int64)
+        nbk = lr.size + ex_r0.size
+        blocks = np.concatenate([lr, np.full(ex_r0.size, -1, np.int64)]).astype(np.int64)
+        r0 = np.concatenate([tree.start[self._rows[lr]], ex_r0])
+        m = np.concatenate([tree.size[self._rows[lr]], ex_mm])
+        c0 = np.concatenate([tree.start[self._cols[lr]], ex_c0])
+        n = np.concatenate([tree.size[self._cols[lr]], ex_nn])
+        k = np.where(np.arange(nbk) < lr.size, np.concatenate([self._rank[lr], ex_nn]), n)
         woff = np.empty(nbk, np.int64)
         voff = np.full(nbk, -1, np.int64)
         zoff = np.full(nbk, -1, np.int64)
@@ -541,7 +574,8 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         zc = np.zeros(lr.size + 1, np.int64)
         np.cumsum(self._rank[lr], out=zc[1:])
         zoff[:lr.size] = zc[:-1]
-        woff[lr.size:] = aca_n + np.array([self._dense_off[b] for b in ex_nz], np.int64)
+        woff[lr.size:] = aca_n + ex_off
+        self.stats["dense_runs"] = int(ex_r0.size)
         self._num_zrows = int(zc[-1])
         # phase A items: column chunks of LR blocks
         it_blk, it_j0, it_j1, it_ex = [], [], [], []
@@ -595,9 +629,11 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
     def pool(self, precision):
         """The factor/dense pool in 'fp64', 'fp32' or 'bf16'."""
         if precision == "fp64":
-            if self._pool.dtype != torch.float64:
-                raise ValueError("this operator was stored in float32")
-            return self._pool
+            if self._pool.dtype == torch.float64:
+                return self._pool
+            if getattr(self, "_pool_f64", None) is None:
+                self._pool_f64 = self._pool.to(torch.float64)
+            return self._pool_f64
         if precision == "fp32":
             if self._pool.dtype == torch.float32:
                 return self._pool
@@ -810,6 +846,7 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         st["_desc"] = None
         st["_pool_f32"] = None
         st["_pool_bf16"] = None
+        st["_pool_f64"] = None
         for key in ("_pool", "_perm_d", "_iperm_d"):
             st[key] = st[key].cpu()
         st["_dev"] = {k: v.cpu() for k, v in st["_dev"].items()}

@@ -147,8 +147,9 @@ phaseA_kn_f32(OpView op, const float* __restrict__ vpool, const float* __restric
   __shared__ float s_v[64][kJC + 1];
   __shared__ float s_x[kJC][kKT];
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  const long long it = blockIdx.x;
-  const int c_base = blockIdx.y * kKT;
+  const int nkt = (K + kKT - 1) / kKT;
+  const long long it = blockIdx.x / nkt;
+  const int c_base = (int)(blockIdx.x % nkt) * kKT;
   const int b = op.a_blk[it];
   const int j0 = op.a_j0[it], j1 = op.a_j1[it];
   const int n = op.n[b], k = op.k[b];
@@ -207,9 +208,10 @@ phaseB_kn_f32(OpView op, const float* __restrict__ wpool, const float* __restric
   __shared__ float s_w[kJC][kTileRows + 1];
   __shared__ float s_s[kJC][kKT];
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  const long long t = blockIdx.x;
+  const int nkt = (K + kKT - 1) / kKT;
+  const long long t = blockIdx.x / nkt;
   const long long t0 = t * kTileRows;
-  const int c_base = blockIdx.y * kKT;
+  const int c_base = (int)(blockIdx.x % nkt) * kKT;
   float acc[4][4];
 #pragma unroll
   for (int r = 0; r < 4; r++)
@@ -306,8 +308,9 @@ phaseA_kn_bf16(OpView op, const __nv_bfloat16* __restrict__ vpool,
   __shared__ __align__(16) __nv_bfloat16 s_a[64][kAPad];
   __shared__ __align__(16) __nv_bfloat16 s_b[kBK][kBPad];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int c_base = blockIdx.x * kBT;
-  const long long it = blockIdx.y;
+  const int nkt = (K + kBT - 1) / kBT;
+  const int c_base = (int)(blockIdx.x % nkt) * kBT;
+  const long long it = blockIdx.x / nkt;
   const int b = op.a_blk[it];
   const int j0 = op.a_j0[it], j1 = op.a_j1[it];
   const int n = op.n[b], k = op.k[b];
@@ -398,8 +401,9 @@ phaseB_kn_bf16(OpView op, const __nv_bfloat16* __restrict__ wpool,
   __shared__ __align__(16) __nv_bfloat16 s_w[kBK][kMPad];   // [l][row]
   __shared__ __align__(16) __nv_bfloat16 s_s[kBK][kBPad];   // [l][col]
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int c_base = blockIdx.x * kBT;
-  const long long t = blockIdx.y;
+  const int nkt = (K + kBT - 1) / kBT;
+  const int c_base = (int)(blockIdx.x % nkt) * kBT;
+  const long long t = blockIdx.x / nkt;
   const long long t0 = t * kTileRows;
   const __nv_bfloat16 zero = __float2bfloat16(0.f);
   float acc[16][4];
@@ -558,12 +562,12 @@ int fgb_matmat_f32(const fgb_op_desc* d, const float* wpool, const float* vpool,
     FGB_CUDA_TRY(cudaMemsetAsync(Z, 0, sizeof(float) * d->num_zrows * (size_t)K, s));
   unsigned ky = (unsigned)((K + fgb::kKT - 1) / fgb::kKT);
   if ((phases & 1) && op.num_items > 0) {
-    dim3 g((unsigned)op.num_items, ky);
+    dim3 g((unsigned)(op.num_items * ky));
     fgb::phaseA_kn_f32<<<g, 256, 0, s>>>(op, vpool, X, Z, K);
     FGB_LAUNCH_CHECK("phaseA_kn_f32");
   }
   if ((phases & 2) && op.num_tiles > 0) {
-    dim3 g((unsigned)op.num_tiles, ky);
+    dim3 g((unsigned)(op.num_tiles * ky));
     fgb::phaseB_kn_f32<<<g, 256, 0, s>>>(op, wpool, X, Z, Y, K, add, alpha);
     FGB_LAUNCH_CHECK("phaseB_kn_f32");
   }
@@ -595,7 +599,7 @@ int fgb_matmat_bf16(const fgb_op_desc* d, const void* wpool, const void* vpool, 
   unsigned kx = (unsigned)((K + fgb::kBT - 1) / fgb::kBT);
   if ((phases & 1) && op.num_items > 0) {
     if (zero_z) FGB_CUDA_TRY(cudaMemsetAsync(Z, 0, sizeof(float) * d->num_zrows * (size_t)K, s));
-    dim3 g(kx, (unsigned)op.num_items);
+    dim3 g((unsigned)(op.num_items * kx));
     fgb::phaseA_kn_bf16<<<g, 128, 0, s>>>(op, v, x, K, Z, K, K);
     FGB_LAUNCH_CHECK("phaseA_kn_bf16");
     long long nz = d->num_zrows * (long long)K;
@@ -603,7 +607,7 @@ int fgb_matmat_bf16(const fgb_op_desc* d, const void* wpool, const void* vpool, 
     FGB_LAUNCH_CHECK("f32_to_bf16_kernel");
   }
   if ((phases & 2) && op.num_tiles > 0) {
-    dim3 g(kx, (unsigned)op.num_tiles);
+    dim3 g((unsigned)(op.num_tiles * kx));
     fgb::phaseB_kn_bf16<<<g, 128, 0, s>>>(op, w, x, K, zb, K, Y, K, K, add, K, alpha);
     FGB_LAUNCH_CHECK("phaseB_kn_bf16");
   }

@@ -302,8 +302,8 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
     Z32 = torch.empty((max(FF._num_zrows, 1), K), dtype=torch.float32, device=dev)
     Zb = torch.empty((max(FF._num_zrows, 1), K), dtype=torch.bfloat16, device=dev)
     Y = torch.empty_like(Ep)
-    pool_b = FF.pool("bf16")
-    pool_f = FF.pool("fp32")
+    panel_b, vpanel_b = FF.panels("bf16")
+    panel_f, vpanel_f = FF.panels("fp32")
 
     def t_events(fn, reps=5):
         fn()
@@ -318,12 +318,12 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
         return a.elapsed_time(b) / reps
 
     def bf16(phases):
-        _lib.call("fgb_matmat_bf16", C.byref(FF._desc), _lib.ptr(pool_b), _lib.ptr(pool_b),
+        _lib.call("fgb_matmat_bf16", C.byref(FF._desc), _lib.ptr(panel_b), _lib.ptr(vpanel_b),
                   _lib.ptr(Xb), _lib.ptr(Z32), _lib.ptr(Zb), _lib.ptr(Y), K, _lib.ptr(Ep), 1.0,
                   int(FF._needs_zero_z), phases, _lib.stream_handle())
 
     def f32(phases):
-        _lib.call("fgb_matmat_f32", C.byref(FF._desc), _lib.ptr(pool_f), _lib.ptr(pool_f),
+        _lib.call("fgb_matmat_f32", C.byref(FF._desc), _lib.ptr(panel_f), _lib.ptr(vpanel_f),
                   _lib.ptr(X32), _lib.ptr(Z32), _lib.ptr(Y), K, None, 1.0,
                   int(FF._needs_zero_z), phases, _lib.stream_handle())
 
@@ -331,18 +331,15 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
     tB = t_events(lambda: bf16(2))
     tA32 = t_events(lambda: f32(1))
     tB32 = t_events(lambda: f32(2))
-    d = FF._dev
-    kk = d["k"].cpu().numpy().astype(np.int64)
-    mm = d["m"].cpu().numpy().astype(np.int64)
-    nn = d["n"].cpu().numpy().astype(np.int64)
-    lr = d["zoff"].cpu().numpy() >= 0
-    # algorithmic bytes per launch (each stored operand read once, outputs written once)
-    wB = int((kk * mm).sum())                  # W entries (U^T and dense D^T)
-    vA = int((kk[lr] * nn[lr]).sum())          # V^T entries
+    # algorithmic bytes per launch: every stored weight read once, every
+    # distinct source row read once per launch, outputs written once
+    wB = int(FF._panel_rows) * 64              # phase-B panel weights
+    vA = int(FF._vpanel_size)                  # phase-A panel weights
     zrows = int(FF._num_zrows)
-    srcB = (zrows + int(nn[~lr].sum())) * K    # phase-B sources: Z rows + dense X slices
+    srcB = int(torch.unique(FF._dev["src"]).numel()) * K   # distinct source rows
+    xA = int(FF._dev["g_n"].sum().item()) * K             # X rows read by phase A groups
     bytes_B_bf16 = wB * 2 + srcB * 2 + N * K * 4 * 2       # + Y write + add read (fp32)
-    bytes_A_bf16 = vA * 2 + int(nn[lr].sum()) * K * 2 + zrows * K * 4
+    bytes_A_bf16 = vA * 2 + xA * 2 + zrows * K * 4
     flops_B = 2.0 * wB * K
     flops_A = 2.0 * vA * K
     peaks = {}
@@ -358,7 +355,7 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
                  "phaseB_f32": tB32 * stats[-1]["fp32_matmats"]}
     dom = max(per_solve, key=per_solve.get)
     kern = {"phaseA_bf16": (tA, bytes_A_bf16, flops_A), "phaseB_bf16": (tB, bytes_B_bf16, flops_B),
-            "phaseA_f32": (tA32, vA * 4 + int(nn[lr].sum()) * K * 4 + zrows * K * 4, flops_A),
+            "phaseA_f32": (tA32, vA * 4 + xA * 4 + zrows * K * 4, flops_A),
             "phaseB_f32": (tB32, wB * 4 + srcB * 4 + N * K * 4, flops_B)}
     t_ms, byts, fl = kern[dom]
     achieved = byts / (t_ms * 1e-3) / 1e9
@@ -400,19 +397,12 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
     cols = torch.arange(0, K, K // 8, device=dev)[:8]
     Bp = B[:, cols].double().contiguous()
     Epc = Ep[:, cols].double()
-    pool64 = FF._pool.double()
-    FFd = FF
     res = []
-    z64 = torch.empty(max(FF._num_zrows, 1), dtype=torch.float64, device=dev)
     for q in range(Bp.shape[1]):
-        x = (RHO * Bp[:, q]).contiguous()
-        y = torch.empty_like(x)
-        _lib.call("fgb_matvec_f64", C.byref(FF._desc), _lib.ptr(pool64), _lib.ptr(pool64),
-                  _lib.ptr(x), _lib.ptr(z64), _lib.ptr(y), None, 1.0, int(FF._needs_zero_z),
-                  _lib.stream_handle())
+        y = FF.matvec_permuted((RHO * Bp[:, q]).contiguous(), "fp64")
         r = Epc[:, q] - (Bp[:, q] - y)
         res.append(float(r.abs().max() / Epc[:, q].abs().max()))
-    del pool64
+    FF._panels.pop("fp64", None)
     rng = np.random.default_rng(0)
     rows = rng.choice(N, 16, replace=False)
     facet_rows = FF._tree.perm[rows]

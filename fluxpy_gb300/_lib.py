@@ -76,9 +76,19 @@ SIGNATURES: dict[str, list] = {
     "fgb_ff_fill_f32": [P, P, P, P, P, P, P, P, P, P, P, I64, I64, P, P, P, P, P],
     # compression (a6-a8)
     "fgb_aca_scratch_floats": [I32, I64, I64, P],
-    "fgb_aca_f64": [P, P, P, P, P, I64, P, P, P, P, I64, I64, F64, I32, F32, I32, I32, P, I32,
-                    P, I64, P, P, P, P, U32P, P],
+    "fgb_aca_f64": [P, P, P, P, P, I64, P, P, P, P, I64, I64, F64, I32, F32, I32, I32, I64, P,
+                    P, I32, P, I64, P, P, P, P, U32P, P],
     # block matvec (a9)
+    "fgb_build_panel_f32_f32": [P, I64, P, P, P, P, P, I64, P, P],
+    "fgb_build_panel_f32_bf16": [P, I64, P, P, P, P, P, I64, P, P],
+    "fgb_build_panel_f64_f64": [P, I64, P, P, P, P, P, I64, P, P],
+    "fgb_build_panel_f64_f32": [P, I64, P, P, P, P, P, I64, P, P],
+    "fgb_build_panel_f64_bf16": [P, I64, P, P, P, P, P, I64, P, P],
+    "fgb_build_vpanel_f32_f32": [P, I64, P, P, P, P, P],
+    "fgb_build_vpanel_f32_bf16": [P, I64, P, P, P, P, P],
+    "fgb_build_vpanel_f64_f64": [P, I64, P, P, P, P, P],
+    "fgb_build_vpanel_f64_f32": [P, I64, P, P, P, P, P],
+    "fgb_build_vpanel_f64_bf16": [P, I64, P, P, P, P, P],
     "fgb_matvec_f32": [P, P, P, P, P, P, P, F32, I32, P],
     "fgb_matvec_f64": [P, P, P, P, P, P, P, F64, I32, P],
     "fgb_matmat_f32": [P, P, P, P, P, P, I32, P, F32, I32, I32, P],

@@ -171,13 +171,14 @@ class _DeviceOperator:
 
 
 class fgb_op_desc(C.Structure):
+    """ctypes mirror of struct fgb_op_desc (include/fluxgb.h)."""
     _fields_ = [
-        ("r0", C.c_void_p), ("m", C.c_void_p), ("c0", C.c_void_p), ("n", C.c_void_p),
-        ("k", C.c_void_p), ("woff", C.c_void_p), ("voff", C.c_void_p), ("zoff", C.c_void_p),
-        ("a_blk", C.c_void_p), ("a_j0", C.c_void_p), ("a_j1", C.c_void_p),
-        ("a_excl", C.c_void_p), ("num_items", C.c_longlong), ("t_ptr", C.c_void_p),
-        ("t_blk", C.c_void_p), ("num_tiles", C.c_longlong), ("N", C.c_longlong),
-        ("num_zrows", C.c_longlong),
+        ("g_c0", C.c_void_p), ("g_n", C.c_void_p), ("g_kz", C.c_void_p), ("g_ldv", C.c_void_p),
+        ("g_voff", C.c_void_p), ("g_z0", C.c_void_p), ("a_grp", C.c_void_p),
+        ("a_j0", C.c_void_p), ("a_j1", C.c_void_p), ("a_excl", C.c_void_p),
+        ("num_items", C.c_longlong), ("t_p0", C.c_void_p), ("src", C.c_void_p),
+        ("num_tiles", C.c_longlong), ("N", C.c_longlong), ("num_zrows", C.c_longlong),
+        ("max_group_tiles", C.c_int),
     ]
 
 
@@ -196,7 +197,7 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
 
     def __init__(self, shape_model, tol=1e-5, min_size=16384, max_depth=None,
                  force_max_depth=False, RootBlock=None, *, leaf_size=64, eta=1.0, rmax=64,
-                 nsample=1024, dtype=None, eps=None, **kwargs):
+                 nsample=1024, exact_aca_max=65536, dtype=None, eps=None, **kwargs):
         if tol < 0:
             raise RuntimeError('tol should be a nonnegative float')
         if max_depth is not None and not isinstance(max_depth, int):
@@ -219,6 +220,7 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         self._eta = eta
         self._rmax = rmax
         self._nsample = nsample
+        self._exact_aca_max = int(exact_aca_max)
         self._eps = config.DEFAULT_EPS if eps is None else eps
         self._store_dtype = np.dtype(shape_model.dtype if dtype is None else dtype)
         if self._store_dtype not in (np.float64, np.float32):
@@ -419,6 +421,8 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         while num_ctas > 1 and num_ctas * per_cta.value * 4 > 8 * 2**30:
             num_ctas //= 2
         scratch = torch.empty(num_ctas * per_cta.value, dtype=torch.float32, device=dev)
+        ex_max = self._exact_aca_max
+        dscratch = torch.empty(max(num_ctas * ex_max, 1), dtype=torch.float32, device=dev)
         cap_k = np.minimum(rmax, np.maximum(1, (m.astype(np.int64) * n) // (2 * (m.astype(np.int64) + n))))
         capacity = int((cap_k * (m.astype(np.int64) + n)).sum())
         pool = torch.empty(max(capacity, 1), dtype=torch.float32, device=dev)
@@ -432,7 +436,7 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         _lib.call("fgb_aca_f64", sm.bvh.handle, _lib.ptr(P), _lib.ptr(Nn), _lib.ptr(A),
                   _lib.ptr(perm_d), nb, _lib.ptr(r0_d), _lib.ptr(m_d), _lib.ptr(c0_d),
                   _lib.ptr(n_d), mmax, nmax, float(self._eps), sm.semantics, float(self._tol),
-                  rmax, self._nsample, _lib.ptr(scratch), num_ctas, _lib.ptr(pool), capacity,
+                  rmax, self._nsample, ex_max, _lib.ptr(dscratch), _lib.ptr(scratch), num_ctas, _lib.ptr(pool), capacity,
                   _lib.ptr(used), _lib.ptr(rank_out), _lib.ptr(off_out), _lib.ptr(queue),
                   _lib.ptr(flags), _lib.stream_handle())
         fl = int(flags.item())
@@ -441,7 +445,7 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         ranks_s = rank_out.cpu().numpy()
         offs_s = off_out.cpu().numpy()
         nused = int(used.item())
-        del scratch
+        del scratch, dscratch
         ranks = np.empty(nb, np.int64)
         offs = np.empty(nb, np.int64)
         ranks[order] = ranks_s
@@ -527,8 +531,6 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         if pool.numel() == 0:
             pool = torch.zeros(1, dtype=tdt, device=dev)
         self._pool = pool
-        self._pool_f32 = None
-        self._pool_bf16 = None
 
         # device block list: LR leaves with rank > 0, then merged runs of
         # exact leaves (same row range, adjacent column ranges, contiguous in
@@ -558,93 +560,182 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         ex_c0 = np.array([run_c0[i] for i in keep], np.int64)
         ex_nn = np.array([run_n[i] for i in keep], np.int64)
         ex_off = np.array([run_off[i] for i in keep], np.int64)
-        nbk = lr.size + ex_r0.size
-        blocks = np.concatenate([lr, np.full(ex_r0.size, -1, np.int64)]).astype(np.int64)
-        r0 = np.concatenate([tree.start[self._rows[lr]], ex_r0])
-        m = np.concatenate([tree.size[self._rows[lr]], ex_mm])
-        c0 = np.concatenate([tree.start[self._cols[lr]], ex_c0])
-        n = np.concatenate([tree.size[self._cols[lr]], ex_nn])
-        k = np.where(np.arange(nbk) < lr.size, np.concatenate([self._rank[lr], ex_nn]), n)
-        woff = np.empty(nbk, np.int64)
-        voff = np.full(nbk, -1, np.int64)
-        zoff = np.full(nbk, -1, np.int64)
-        pool_off = np.asarray(pool_off, np.int64)
-        woff[:lr.size] = pool_off[lr]
-        voff[:lr.size] = pool_off[lr] + self._rank[lr] * m[:lr.size]
-        zc = np.zeros(lr.size + 1, np.int64)
-        np.cumsum(self._rank[lr], out=zc[1:])
-        zoff[:lr.size] = zc[:-1]
-        woff[lr.size:] = aca_n + ex_off
         self.stats["dense_runs"] = int(ex_r0.size)
-        self._num_zrows = int(zc[-1])
-        # phase A items: column chunks of LR blocks
-        it_blk, it_j0, it_j1, it_ex = [], [], [], []
-        for q in range(lr.size):
-            nn = int(n[q])
-            nchunk = (nn + ITEM_COLS - 1) // ITEM_COLS
-            for ci in range(nchunk):
-                it_blk.append(q)
-                it_j0.append(ci * ITEM_COLS)
-                it_j1.append(min(nn, (ci + 1) * ITEM_COLS))
-                it_ex.append(1 if nchunk == 1 else 0)
-        self._needs_zero_z = any(e == 0 for e in it_ex)
-        # phase B tiles
+        self._layout(lr, pool_off, aca_n, ex_r0, ex_mm, ex_c0, ex_nn, ex_off)
+
+    def _layout(self, lr, pool_off, aca_n, ex_r0, ex_mm, ex_c0, ex_nn, ex_off):
+        """Panel layout consumed by libfluxgb's matvec kernels (matvec.cu)."""
+        tree = self._tree
+        dev = self.shape_model._device
+        pool_off = np.asarray(pool_off, np.int64)
         N = self.num_faces
+        # ---- low-rank blocks, grouped by column range (phase A)
+        lr_r0 = tree.start[self._rows[lr]].astype(np.int64)
+        lr_m = tree.size[self._rows[lr]].astype(np.int64)
+        lr_c0 = tree.start[self._cols[lr]].astype(np.int64)
+        lr_n = tree.size[self._cols[lr]].astype(np.int64)
+        lr_k = self._rank[lr].astype(np.int64)
+        lr_u = pool_off[lr]
+        lr_v = lr_u + lr_k * lr_m
+        order = np.lexsort((lr_n, lr_c0))
+        lr, lr_r0, lr_m, lr_c0, lr_n, lr_k, lr_u, lr_v = (a[order] for a in
+                                                         (lr, lr_r0, lr_m, lr_c0, lr_n, lr_k,
+                                                          lr_u, lr_v))
+        nlr = lr.size
+        newg = np.ones(nlr, bool)
+        if nlr:
+            newg[1:] = (lr_c0[1:] != lr_c0[:-1]) | (lr_n[1:] != lr_n[:-1])
+        gid = np.cumsum(newg) - 1
+        ng = int(gid[-1]) + 1 if nlr else 0
+        g_first = np.flatnonzero(newg)
+        g_c0 = lr_c0[g_first]
+        g_n = lr_n[g_first]
+        g_kz = np.bincount(gid, weights=lr_k, minlength=ng).astype(np.int64) if nlr else np.zeros(0, np.int64)
+        g_ldv = (g_n + 7) // 8 * 8
+        g_voff = np.zeros(ng + 1, np.int64)
+        np.cumsum(g_kz * g_ldv, out=g_voff[1:])
+        g_z0 = np.zeros(ng + 1, np.int64)
+        np.cumsum(g_kz, out=g_z0[1:])
+        # each LR block's first Z row: group start + earlier members' ranks
+        cum_k = np.cumsum(lr_k) - lr_k
+        lr_z = cum_k - (np.cumsum(lr_k) - lr_k)[g_first][gid] + g_z0[gid] if nlr else np.zeros(0, np.int64)
+        self._num_zrows = int(g_z0[-1])
+        # stacked V^T rows: (pool offset, panel offset, length)
+        rows_k = lr_k
+        vr_blk = np.repeat(np.arange(nlr), rows_k)
+        vr_l = np.arange(rows_k.sum()) - np.repeat(np.cumsum(rows_k) - rows_k, rows_k)
+        vr_src = lr_v[vr_blk] + vr_l * lr_n[vr_blk]
+        vr_row_in_group = (lr_z[vr_blk] - g_z0[gid[vr_blk]]) + vr_l
+        vr_dst = g_voff[gid[vr_blk]] + vr_row_in_group * g_ldv[gid[vr_blk]]
+        vr_n = lr_n[vr_blk]
+        # phase A items: column chunks of each group
+        nchunk = (g_n + ITEM_COLS - 1) // ITEM_COLS
+        a_grp = np.repeat(np.arange(ng), nchunk)
+        ci = np.arange(nchunk.sum()) - np.repeat(np.cumsum(nchunk) - nchunk, nchunk)
+        a_j0 = ci * ITEM_COLS
+        a_j1 = np.minimum(g_n[a_grp], (ci + 1) * ITEM_COLS)
+        a_ex = (nchunk[a_grp] == 1).astype(np.uint8)
+        self._needs_zero_z = bool((a_ex == 0).any())
+        max_gt = int(((g_kz + 63) // 64).max()) if ng else 1
+        # ---- phase B: contributors (LR blocks: U^T rows -> Z rows; dense runs:
+        # D^T rows -> X rows), split by 64-row tile
+        c_r0 = np.concatenate([lr_r0, ex_r0]).astype(np.int64)
+        c_m = np.concatenate([lr_m, ex_mm]).astype(np.int64)
+        c_k = np.concatenate([lr_k, ex_nn]).astype(np.int64)
+        c_w = np.concatenate([lr_u, aca_n + ex_off]).astype(np.int64)
+        c_src = np.concatenate([lr_z, self._num_zrows + ex_c0]).astype(np.int64)
         ntiles = (N + TILE_ROWS - 1) // TILE_ROWS
-        t_first = r0 // TILE_ROWS
-        t_last = (r0 + m - 1) // TILE_ROWS
-        cnt = (t_last - t_first + 1).astype(np.int64)
-        pair_blk = np.repeat(np.arange(nbk), cnt)
-        pair_t = (np.repeat(t_first, cnt) +
-                  (np.arange(cnt.sum()) - np.repeat(np.cumsum(cnt) - cnt, cnt)))
-        order = np.argsort(pair_t, kind="stable")
-        t_blk = pair_blk[order].astype(np.int32)
-        t_ptr = np.zeros(ntiles + 1, np.int64)
-        np.cumsum(np.bincount(pair_t, minlength=ntiles), out=t_ptr[1:])
+        t_first = c_r0 // TILE_ROWS
+        t_last = (c_r0 + c_m - 1) // TILE_ROWS
+        cnt = t_last - t_first + 1
+        pc = np.repeat(np.arange(c_r0.size), cnt)
+        pt = np.repeat(t_first, cnt) + (np.arange(cnt.sum()) - np.repeat(np.cumsum(cnt) - cnt, cnt))
+        o = np.argsort(pt, kind="stable")
+        pc, pt = pc[o], pt[o]
+        pk = c_k[pc]
+        L = np.bincount(pt, weights=pk, minlength=ntiles).astype(np.int64)
+        Lpad = (L + 31) // 32 * 32
+        t_p0 = np.zeros(ntiles + 1, np.int64)
+        np.cumsum(Lpad, out=t_p0[1:])
+        # pair panel offsets: tile start + running k within the tile
+        run = np.cumsum(pk) - pk
+        tile_start_run = np.zeros(ntiles, np.int64)
+        first_of_tile = np.ones(pt.size, bool)
+        first_of_tile[1:] = pt[1:] != pt[:-1]
+        tile_start_run[pt[first_of_tile]] = run[first_of_tile]
+        pair_p0 = t_p0[pt] + run - tile_start_run[pt]
+        # padding pairs (k = 0) at the end of every tile with padded rows
+        pad_t = np.flatnonzero(Lpad > L)
+        pad_p0 = t_p0[pad_t] + L[pad_t]
+        all_p0 = np.concatenate([pair_p0, pad_p0])
+        all_w = np.concatenate([c_w[pc], np.zeros(pad_t.size, np.int64)])
+        all_m = np.concatenate([c_m[pc], np.ones(pad_t.size, np.int64)])
+        all_shift = np.concatenate([pt * TILE_ROWS - c_r0[pc], np.zeros(pad_t.size, np.int64)])
+        all_k = np.concatenate([pk, np.zeros(pad_t.size, np.int64)])
+        oo = np.argsort(all_p0, kind="stable")
+        all_p0, all_w, all_m, all_shift, all_k = (a[oo] for a in (all_p0, all_w, all_m, all_shift,
+                                                                 all_k))
+        total_rows = int(t_p0[-1])
+        # source index of every panel row
+        src = np.zeros(total_rows, np.int64)
+        rk = pk
+        rows_pair = np.repeat(np.arange(pk.size), rk)
+        rows_l = np.arange(rk.sum()) - np.repeat(np.cumsum(rk) - rk, rk)
+        src[pair_p0[rows_pair] + rows_l] = c_src[pc[rows_pair]] + rows_l
+        if src.size and src.max() >= 2**31:
+            raise OverflowError("operator too large for 32-bit panel sources")
 
         def d(a, dt):
             a = np.asarray(a, dtype=dt)
             return torch.as_tensor(a if a.size else np.zeros(1, dt), device=dev)
 
         self._dev = dict(
-            r0=d(r0, np.int32), m=d(m, np.int32), c0=d(c0, np.int32), n=d(n, np.int32),
-            k=d(k, np.int32), woff=d(woff, np.int64), voff=d(voff, np.int64),
-            zoff=d(zoff, np.int64), a_blk=d(it_blk, np.int32), a_j0=d(it_j0, np.int32),
-            a_j1=d(it_j1, np.int32), a_excl=d(it_ex, np.uint8), t_ptr=d(t_ptr, np.int64),
-            t_blk=d(t_blk, np.int32))
+            g_c0=d(g_c0, np.int32), g_n=d(g_n, np.int32), g_kz=d(g_kz, np.int32),
+            g_ldv=d(g_ldv, np.int32), g_voff=d(g_voff[:-1], np.int64), g_z0=d(g_z0[:-1], np.int64),
+            a_grp=d(a_grp, np.int32), a_j0=d(a_j0, np.int32), a_j1=d(a_j1, np.int32),
+            a_excl=d(a_ex, np.uint8), t_p0=d(t_p0, np.int64), src=d(src, np.int32))
+        self._build_dev = dict(
+            vr_src=d(vr_src, np.int64), vr_dst=d(vr_dst, np.int64), vr_n=d(vr_n, np.int32),
+            p_p0=d(all_p0, np.int64), p_w=d(all_w, np.int64), p_m=d(all_m, np.int32),
+            p_shift=d(all_shift, np.int64), p_k=d(all_k, np.int32))
+        self._panel_rows = total_rows
+        self._vpanel_size = int(g_voff[-1])
+        self._num_vrows = int(vr_src.size)
+        self._num_pairs = int(all_p0.size)
         desc = fgb_op_desc()
-        for key in ("r0", "m", "c0", "n", "k", "woff", "voff", "zoff", "a_blk", "a_j0", "a_j1",
-                    "a_excl", "t_ptr", "t_blk"):
+        for key in ("g_c0", "g_n", "g_kz", "g_ldv", "g_voff", "g_z0", "a_grp", "a_j0", "a_j1",
+                    "a_excl", "t_p0", "src"):
             setattr(desc, key, self._dev[key].data_ptr())
-        desc.num_items = len(it_blk)
+        desc.num_items = int(a_grp.size)
         desc.num_tiles = ntiles
         desc.N = N
         desc.num_zrows = self._num_zrows
+        desc.max_group_tiles = max_gt
         self._desc = desc
-        self._dev_blocks = blocks
-        self.stats.update(num_items=len(it_blk), num_tiles=ntiles, tile_pairs=int(t_blk.size),
-                          pool_entries=int(self._pool.numel()), zrows=self._num_zrows)
+        self._lr_blocks = lr
+        self._lr_u, self._lr_v = lr_u, lr_v
+        self._panels = {}
+        self.stats.update(num_items=int(a_grp.size), num_tiles=ntiles, groups=ng,
+                          panel_rows=total_rows, tile_pairs=int(pk.size),
+                          pool_entries=int(self._pool.numel()), zrows=self._num_zrows,
+                          operator_entries=int(total_rows * TILE_ROWS + g_voff[-1]))
 
     # -- device products --------------------------------------------------
     def pool(self, precision):
-        """The factor/dense pool in 'fp64', 'fp32' or 'bf16'."""
-        if precision == "fp64":
-            if self._pool.dtype == torch.float64:
-                return self._pool
-            if getattr(self, "_pool_f64", None) is None:
-                self._pool_f64 = self._pool.to(torch.float64)
-            return self._pool_f64
-        if precision == "fp32":
-            if self._pool.dtype == torch.float32:
-                return self._pool
-            if self._pool_f32 is None:
-                self._pool_f32 = self._pool.to(torch.float32)
-            return self._pool_f32
-        if precision == "bf16":
-            if self._pool_bf16 is None:
-                self._pool_bf16 = self._pool.to(torch.bfloat16)
-            return self._pool_bf16
-        raise ValueError(precision)
+        """The factor / dense pool (block storage) in 'fp64' or its own dtype."""
+        if precision == "fp64" and self._pool.dtype != torch.float64:
+            return self._pool.to(torch.float64)
+        return self._pool
+
+    _TDT = {"fp64": torch.float64, "fp32": torch.float32, "bf16": torch.bfloat16}
+
+    def panels(self, precision):
+        """(phase-B panel, phase-A panel) in 'fp64', 'fp32' or 'bf16', built
+        on first use from the pool."""
+        got = self._panels.get(precision)
+        if got is not None:
+            return got
+        tdt = self._TDT[precision]
+        dev = self._pool.device
+        pin = "f64" if self._pool.dtype == torch.float64 else "f32"
+        pout = {"fp64": "f64", "fp32": "f32", "bf16": "bf16"}[precision]
+        if pin == "f32" and pout == "f64":
+            src = self._pool.to(torch.float64)
+            pin = "f64"
+        else:
+            src = self._pool
+        panel = torch.empty(max(self._panel_rows * TILE_ROWS, 8), dtype=tdt, device=dev)
+        vpanel = torch.empty(max(self._vpanel_size, 8), dtype=tdt, device=dev)
+        b = self._build_dev
+        st = _lib.stream_handle()
+        _lib.call(f"fgb_build_panel_{pin}_{pout}", _lib.ptr(src), self._panel_rows,
+                  _lib.ptr(b["p_p0"]), _lib.ptr(b["p_w"]), _lib.ptr(b["p_m"]),
+                  _lib.ptr(b["p_shift"]), _lib.ptr(b["p_k"]), self._num_pairs, _lib.ptr(panel), st)
+        _lib.call(f"fgb_build_vpanel_{pin}_{pout}", _lib.ptr(src), self._num_vrows,
+                  _lib.ptr(b["vr_src"]), _lib.ptr(b["vr_dst"]), _lib.ptr(b["vr_n"]),
+                  _lib.ptr(vpanel), st)
+        self._panels[precision] = (panel, vpanel)
+        return panel, vpanel
 
     def permute(self, x: torch.Tensor) -> torch.Tensor:
         """Facet order -> cluster order (rows)."""
@@ -666,8 +757,8 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
             out = torch.empty_like(xp)
         if z is None:
             z = torch.empty(max(self._num_zrows, 1), dtype=V, device=xp.device)
-        pool = self.pool("fp64" if precision == "fp64" else "fp32")
-        _lib.call(fn, C.byref(self._desc), _lib.ptr(pool), _lib.ptr(pool), _lib.ptr(xp),
+        panel, vpanel = self.panels("fp64" if precision == "fp64" else "fp32")
+        _lib.call(fn, C.byref(self._desc), _lib.ptr(panel), _lib.ptr(vpanel), _lib.ptr(xp),
                   _lib.ptr(z), _lib.ptr(out), _lib.ptr(add), float(alpha),
                   int(self._needs_zero_z), _lib.stream_handle())
         return out
@@ -691,8 +782,8 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
                 out = torch.empty_like(Xp)
             if Z is None:
                 Z = torch.empty((max(self._num_zrows, 1), K), dtype=torch.float32, device=Xp.device)
-            pool = self.pool("fp32")
-            _lib.call("fgb_matmat_f32", C.byref(self._desc), _lib.ptr(pool), _lib.ptr(pool),
+            panel, vpanel = self.panels("fp32")
+            _lib.call("fgb_matmat_f32", C.byref(self._desc), _lib.ptr(panel), _lib.ptr(vpanel),
                       _lib.ptr(Xp), _lib.ptr(Z), _lib.ptr(out), K, _lib.ptr(add), float(alpha),
                       int(self._needs_zero_z), 3, _lib.stream_handle())
             return out
@@ -708,8 +799,8 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         if Z is None:
             Z = torch.empty((max(self._num_zrows, 1), K), dtype=torch.float32, device=Xp.device)
         Zb = torch.empty((max(self._num_zrows, 1), K), dtype=torch.bfloat16, device=Xp.device)
-        pool = self.pool("bf16")
-        _lib.call("fgb_matmat_bf16", C.byref(self._desc), _lib.ptr(pool), _lib.ptr(pool),
+        panel, vpanel = self.panels("bf16")
+        _lib.call("fgb_matmat_bf16", C.byref(self._desc), _lib.ptr(panel), _lib.ptr(vpanel),
                   _lib.ptr(Xb), _lib.ptr(Z), _lib.ptr(Zb), _lib.ptr(out), K, _lib.ptr(add),
                   float(alpha), int(self._needs_zero_z), 3, _lib.stream_handle())
         return out
@@ -770,10 +861,12 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
 
     @property
     def device_nbytes(self):
-        """Bytes held on the device by the operator (pool + tables)."""
+        """Bytes held on the device by the operator (pool, panels, tables)."""
         tot = self._pool.numel() * self._pool.element_size()
-        for v in self._dev.values():
+        for v in list(self._dev.values()) + list(self._build_dev.values()):
             tot += v.numel() * v.element_size()
+        for pnl, vp in self._panels.values():
+            tot += pnl.numel() * pnl.element_size() + vp.numel() * vp.element_size()
         return tot
 
     @property
@@ -844,12 +937,11 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         st = dict(self.__dict__)
         st["_root_cache"] = None
         st["_desc"] = None
-        st["_pool_f32"] = None
-        st["_pool_bf16"] = None
-        st["_pool_f64"] = None
+        st["_panels"] = {}
         for key in ("_pool", "_perm_d", "_iperm_d"):
             st[key] = st[key].cpu()
         st["_dev"] = {k: v.cpu() for k, v in st["_dev"].items()}
+        st["_build_dev"] = {k: v.cpu() for k, v in st["_build_dev"].items()}
         if st.get("_exact_csr") is not None:
             tcsr, ex = st["_exact_csr"]
             st["_exact_csr"] = ({"indptr": tcsr.indptr.cpu(), "indices": tcsr.indices.cpu(),
@@ -862,19 +954,22 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         for key in ("_pool", "_perm_d", "_iperm_d"):
             setattr(self, key, getattr(self, key).to(dev))
         self._dev = {k: v.to(dev) for k, v in self._dev.items()}
+        self._build_dev = {k: v.to(dev) for k, v in self._build_dev.items()}
         if self._exact_csr is not None:
             d, ex = self._exact_csr
             from .form_factors import TileCSR
             self._exact_csr = (TileCSR(d["indptr"].to(dev), d["indices"].to(dev), d["data"].to(dev),
                                        d["row_off"], 0, 0), ex)
         desc = fgb_op_desc()
-        for key in ("r0", "m", "c0", "n", "k", "woff", "voff", "zoff", "a_blk", "a_j0", "a_j1",
-                    "a_excl", "t_ptr", "t_blk"):
+        for key in ("g_c0", "g_n", "g_kz", "g_ldv", "g_voff", "g_z0", "a_grp", "a_j0", "a_j1",
+                    "a_excl", "t_p0", "src"):
             setattr(desc, key, self._dev[key].data_ptr())
         desc.num_items = int(self.stats["num_items"])
         desc.num_tiles = int(self.stats["num_tiles"])
         desc.N = self.num_faces
         desc.num_zrows = self._num_zrows
+        desc.max_group_tiles = int(((self._dev["g_kz"].cpu().numpy().astype(np.int64) + 63)
+                                    // 64).max())
         self._desc = desc
 
     # -- leaf data for the Python block objects --------------------------
@@ -897,12 +992,12 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         tree = self._tree
         m, n = tree.size[self._rows[b]], tree.size[self._cols[b]]
         k = int(self._rank[b])
-        q = np.where(self._dev_blocks == b)[0]
+        q = np.where(self._lr_blocks == b)[0]
         if k == 0 or q.size == 0:
             return np.zeros((m, 0)), np.zeros(0), np.zeros((0, n))
         q = int(q[0])
-        woff = int(self._dev["woff"][q].item())
-        voff = int(self._dev["voff"][q].item())
+        woff = int(self._lr_u[q])
+        voff = int(self._lr_v[q])
         Ut = self._pool[woff:woff + k * m].cpu().numpy().reshape(k, m).astype(np.float64)
         Vt = self._pool[voff:voff + k * n].cpu().numpy().reshape(k, n).astype(np.float64)
         # orthogonalise to the reference's (u, s, vt) form

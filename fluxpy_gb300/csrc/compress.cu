@@ -43,6 +43,8 @@ struct AcaArgs {
   float tol;
   int rmax;
   int nsample;
+  long long exact_max;
+  float* dense_scratch;
   float* scratch;
   long long per_cta;
   long long mmax, nmax;
@@ -166,6 +168,48 @@ aca_kernel(AcaArgs a, EntryCtx<R> e) {
     bool verify = false;
     const int max_rounds = 4 * a.rmax + 8;
     __syncthreads();
+    if ((long long)m * n <= a.exact_max) {
+      // ---- small block: evaluate every entry once, then cross approximation
+      // with full pivoting on the exact residual (exact Frobenius control)
+      float* Rm = a.dense_scratch + (long long)blockIdx.x * a.exact_max;
+      const long long mn = (long long)m * n;
+      double a2 = 0.0;
+      float pv = 0.f;
+      int pq = -1;
+      for (long long q = tid; q < mn; q += kAcaThreads) {
+        const int i = (int)(q / n), j = (int)(q % n);
+        const float val = entry<R>(a, e, prow[i], pcol[j], &overflow);
+        Rm[q] = val;
+        a2 += (double)val * val;
+        if (pq < 0 || fabsf(val) > fabsf(pv)) { pv = val; pq = (int)q; }
+      }
+      a2 = block_sum(a2, sh_d);
+      double res2 = a2;
+      while (res2 > (double)a.tol * a.tol * a2) {
+        float piv;
+        int qs;
+        block_argmax(pv, pq, sh_v, sh_i, &piv, &qs);
+        if (qs < 0 || piv == 0.0f) break;
+        if (k >= kmax) { failed = true; break; }
+        const int is = qs / n, js = qs % n;
+        const float inv = 1.0f / piv;
+        for (int i = tid; i < m; i += kAcaThreads) U[(long long)k * a.mmax + i] = Rm[(long long)i * n + js];
+        for (int j = tid; j < n; j += kAcaThreads) V[(long long)k * a.nmax + j] = Rm[(long long)is * n + j] * inv;
+        __syncthreads();
+        double r2 = 0.0;
+        pv = 0.f;
+        pq = -1;
+        for (long long q = tid; q < mn; q += kAcaThreads) {
+          const int i = (int)(q / n), j = (int)(q % n);
+          const float val = Rm[q] - U[(long long)k * a.mmax + i] * V[(long long)k * a.nmax + j];
+          Rm[q] = val;
+          r2 += (double)val * val;
+          if (pq < 0 || fabsf(val) > fabsf(pv)) { pv = val; pq = (int)q; }
+        }
+        res2 = block_sum(r2, sh_d);
+        k++;
+      }
+    } else
     while (true) {
       if (!verify) {
         // ---- partially pivoted row step at istar
@@ -337,7 +381,8 @@ int fgb_aca_scratch_floats(int rmax, long long mmax, long long nmax, long long* 
 int fgb_aca_f64(const void* bvh, const double* P, const double* N, const double* A,
                 const long long* perm, long long nblocks, const int* r0, const int* m,
                 const int* c0, const int* n, long long mmax, long long nmax, double eps,
-                int semantics, float tol, int rmax, int nsample, float* scratch, int num_ctas,
+                int semantics, float tol, int rmax, int nsample, long long exact_max,
+                float* dense_scratch, float* scratch, int num_ctas,
                 float* pool, long long pool_capacity, unsigned long long* pool_used,
                 int* rank_out, long long* off_out, int* queue, unsigned* flags, void* stream) {
   if (!bvh || nblocks < 0 || num_ctas < 1) { fgb::set_error("bad ACA arguments"); return FGB_BAD_ARG; }
@@ -355,6 +400,8 @@ int fgb_aca_f64(const void* bvh, const double* P, const double* N, const double*
   a.tol = tol;
   a.rmax = rmax;
   a.nsample = nsample < 32 ? 32 : nsample;
+  a.exact_max = dense_scratch ? exact_max : 0;
+  a.dense_scratch = dense_scratch;
   a.scratch = scratch;
   a.per_cta = per_cta;
   a.mmax = mmax; a.nmax = nmax;

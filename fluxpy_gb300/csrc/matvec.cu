@@ -4,21 +4,27 @@
 // (src/flux/compressed_form_factors.py:805 -> FormFactorBlockMatrix._matmat
 // :407-414 -> leaf blocks: dense :175, CSR :193, SVD :247-251).
 //
-// Layout (built by the host, all in HBM; "permuted" = cluster order, where
-// every block's rows and columns are contiguous ranges):
-//   block b: rows [r0, r0+m), cols [c0, c0+n), "inner size" k
-//     LR (rank-k factors):  W = U^T (k x m) at wpool + woff, Vt (k x n) at
-//                           vpool + voff, Z rows [zoff, zoff+k)
-//     DENSE (exact leaf):   W = D^T (n x m, i.e. column j of D contiguous),
-//                           k = n, no Vt / Z
-//   Phase A (LR blocks only): Z[zoff+l, :] = sum_j Vt[l, j] X[c0+j, :],
-//     over work items (block, j0, j1) so that long blocks are split; items
-//     that do not own their whole block accumulate with atomics.
-//   Phase B: row tiles of kTileRows rows; tile t lists the blocks that
-//     overlap it.  Y[i, :] = sum_blocks sum_l W[l, i-r0] S[l, :] with
-//     S = Z[zoff..] (LR) or X[c0..] (DENSE).  Every Y row is written by one
-//     CTA exactly once: no atomics, no separate zeroing.
-// X and Y are (N x K) row-major, K = 1 for the single-RHS path.
+// Everything is in cluster order, where each block's rows and columns are
+// contiguous ranges.  The operator is F ~= sum_LR U_b V_b^T + sum_dense D_b.
+// It is applied in two phases, each a dense "gather-GEMM" over panels built
+// once at setup (no per-block loops in the hot kernels):
+//
+//   Phase A (low-rank blocks, grouped by their column range):
+//     group g = all LR blocks with columns [c0, c0+n): their V^T rows
+//     stacked into one panel Vg (kz x n, row stride ldv = n rounded up to 8);
+//     Z[z0 + r, :] = sum_j Vg[r, j] X[c0 + j, :]   for r < kz
+//     Work items (g, j0, j1) split long groups; items that do not cover the
+//     whole group accumulate with atomics into a zeroed Z.
+//
+//   Phase B (row tiles of 64 rows):
+//     tile t owns panel rows [p0, p1) (a multiple of 32 rows); panel row l
+//     holds 64 weights W[l, i] for the tile's rows i and a source index
+//     src[l]: a row of Z (src < num_zrows: U^T rows of an LR block) or a row
+//     of X (src - num_zrows: D^T rows of an exact dense block, i.e. its
+//     columns).  Y[t0 + i, :] = sum_l W[l, i] S[src[l], :].
+//     Padding rows have zero weights and src 0.
+// Every Y row is written once by the CTA of its tile: deterministic, no
+// atomics in phase B.
 #include "common.cuh"
 
 #include <cuda_bf16.h>
@@ -28,133 +34,116 @@ namespace {
 
 constexpr int kTileRows = 64;
 
-struct OpView {
-  const int* r0;
-  const int* m;
-  const int* c0;
-  const int* n;
-  const int* k;
-  const long long* woff;
-  const long long* voff;
-  const long long* zoff;
-  // phase A items
-  const int* a_blk;
+struct PanelView {
+  // phase A
+  const int* g_c0;
+  const int* g_n;
+  const int* g_kz;
+  const int* g_ldv;
+  const long long* g_voff;
+  const long long* g_z0;
+  const int* a_grp;
   const int* a_j0;
   const int* a_j1;
-  const unsigned char* a_excl;  // 1: the item covers its whole block
+  const unsigned char* a_excl;
   long long num_items;
-  // phase B tiles
-  const long long* t_ptr;
-  const int* t_blk;
+  // phase B
+  const long long* t_p0;  // num_tiles + 1 panel row offsets
+  const int* src;         // per panel row
   long long num_tiles;
   long long N;
+  long long num_zrows;
 };
 
 // ------------------------------------------------------------ K = 1 ----
 template <class T, class V>
-__global__ void phaseA_k1(OpView op, const T* __restrict__ vpool, const V* __restrict__ x,
+__global__ void phaseA_k1(PanelView op, const T* __restrict__ vpanel, const V* __restrict__ x,
                           V* __restrict__ z) {
   const int lane = threadIdx.x & 31;
   const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
   for (long long it = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; it < op.num_items;
        it += warps) {
-    const int b = op.a_blk[it];
+    const int g = op.a_grp[it];
     const int j0 = op.a_j0[it], j1 = op.a_j1[it];
-    const int n = op.n[b], k = op.k[b];
-    const V* xb = x + op.c0[b];
-    const T* vt = vpool + op.voff[b];
-    V* zb = z + op.zoff[b];
+    const int kz = op.g_kz[g], ldv = op.g_ldv[g];
+    const V* xb = x + op.g_c0[g];
+    const T* vg = vpanel + op.g_voff[g];
+    V* zg = z + op.g_z0[g];
     const bool excl = op.a_excl[it];
-    for (int l = 0; l < k; l++) {
-      const T* row = vt + (long long)l * n;
+    for (int r = 0; r < kz; r++) {
+      const T* row = vg + (long long)r * ldv;
       V s = V(0);
       for (int j = j0 + lane; j < j1; j += 32) s += (V)row[j] * __ldg(xb + j);
       for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
       if (lane == 0) {
-        if (excl) zb[l] = s;
-        else atomicAdd(zb + l, s);
+        if (excl) zg[r] = s;
+        else atomicAdd(zg + r, s);
       }
     }
   }
 }
 
-// Phase B, K = 1: one CTA (8 warps) per 64-row tile.  Warp w takes blocks
-// w, w+8, ... of the tile's list; lane L accumulates rows L and L+32 of the
-// tile; the 8 warp partials are summed in a fixed order (deterministic).
-constexpr int kB1Warps = 8;
-
+// One CTA per tile: thread (i, q) = (tid % 64, tid / 64) accumulates row i
+// over panel rows l = p0 + q, p0 + q + 4, ...; fixed-order reduction.
 template <class T, class V>
-__global__ void __launch_bounds__(kB1Warps * 32)
-phaseB_k1(OpView op, const T* __restrict__ wpool, const V* __restrict__ x,
-          const V* __restrict__ z, V* __restrict__ y, const V* __restrict__ add_vec,
-          V alpha) {
-  __shared__ V s_part[kB1Warps][kTileRows];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+__global__ void __launch_bounds__(256)
+phaseB_k1(PanelView op, const T* __restrict__ panel, const V* __restrict__ x,
+          const V* __restrict__ z, V* __restrict__ y, const V* __restrict__ add_vec, V alpha) {
+  __shared__ V s_part[4][kTileRows];
+  const int i = threadIdx.x & (kTileRows - 1), q = threadIdx.x >> 6;
   const long long t = blockIdx.x;
-  const long long t0 = t * kTileRows;
-  V acc0 = V(0), acc1 = V(0);
-  for (long long q = op.t_ptr[t] + warp; q < op.t_ptr[t + 1]; q += kB1Warps) {
-    const int b = op.t_blk[q];
-    const long long r0 = op.r0[b];
-    const int m = op.m[b], k = op.k[b];
-    const bool lr = op.zoff[b] >= 0;
-    const V* src = lr ? z + op.zoff[b] : x + op.c0[b];
-    const T* w = wpool + op.woff[b];
-    const long long i0 = t0 + lane, i1 = t0 + lane + 32;
-    const bool in0 = i0 >= r0 && i0 < r0 + m, in1 = i1 >= r0 && i1 < r0 + m;
-    const T* w0 = w + (i0 - r0);
-    const T* w1 = w + (i1 - r0);
-    int l = 0;
-    for (; l + 4 <= k; l += 4) {
-      const V s0 = __ldg(src + l), s1 = __ldg(src + l + 1), s2 = __ldg(src + l + 2),
-              s3 = __ldg(src + l + 3);
-      if (in0) {
-        acc0 += (V)w0[(long long)l * m] * s0 + (V)w0[(long long)(l + 1) * m] * s1 +
-                (V)w0[(long long)(l + 2) * m] * s2 + (V)w0[(long long)(l + 3) * m] * s3;
-      }
-      if (in1) {
-        acc1 += (V)w1[(long long)l * m] * s0 + (V)w1[(long long)(l + 1) * m] * s1 +
-                (V)w1[(long long)(l + 2) * m] * s2 + (V)w1[(long long)(l + 3) * m] * s3;
-      }
-    }
-    for (; l < k; l++) {
-      const V sv = __ldg(src + l);
-      if (in0) acc0 += (V)w0[(long long)l * m] * sv;
-      if (in1) acc1 += (V)w1[(long long)l * m] * sv;
-    }
+  const long long p0 = op.t_p0[t], p1 = op.t_p0[t + 1];
+  const long long nz = op.num_zrows;
+  V acc = V(0);
+  long long l = p0 + q;
+  for (; l + 12 < p1; l += 16) {
+    const int s0 = op.src[l], s1 = op.src[l + 4], s2 = op.src[l + 8], s3 = op.src[l + 12];
+    const V v0 = s0 < nz ? __ldg(z + s0) : __ldg(x + (s0 - nz));
+    const V v1 = s1 < nz ? __ldg(z + s1) : __ldg(x + (s1 - nz));
+    const V v2 = s2 < nz ? __ldg(z + s2) : __ldg(x + (s2 - nz));
+    const V v3 = s3 < nz ? __ldg(z + s3) : __ldg(x + (s3 - nz));
+    acc += (V)panel[l * kTileRows + i] * v0 + (V)panel[(l + 4) * kTileRows + i] * v1 +
+           (V)panel[(l + 8) * kTileRows + i] * v2 + (V)panel[(l + 12) * kTileRows + i] * v3;
   }
-  s_part[warp][lane] = acc0;
-  s_part[warp][lane + 32] = acc1;
+  for (; l < p1; l += 4) {
+    const int s0 = op.src[l];
+    const V v0 = s0 < nz ? __ldg(z + s0) : __ldg(x + (s0 - nz));
+    acc += (V)panel[l * kTileRows + i] * v0;
+  }
+  s_part[q][i] = acc;
   __syncthreads();
   if (threadIdx.x < kTileRows) {
-    V sum = V(0);
-#pragma unroll
-    for (int wv = 0; wv < kB1Warps; wv++) sum += s_part[wv][threadIdx.x];
-    const long long i = t0 + threadIdx.x;
-    if (i < op.N) y[i] = add_vec ? add_vec[i] + alpha * sum : sum;
+    const V sum = (s_part[0][i] + s_part[1][i]) + (s_part[2][i] + s_part[3][i]);
+    const long long row = t * kTileRows + i;
+    if (row < op.N) y[row] = add_vec ? add_vec[row] + alpha * sum : sum;
   }
 }
 
 // ------------------------------------------------- K RHS, FP32 FFMA ----
-// Phase A: CTA per (item, 64-column K tile); Z block (k x 64) accumulated
-// in registers: thread (ty, tx) owns rows l = ty + 16 r, columns tx*4..+4.
-constexpr int kKT = 64;   // K columns per CTA
+constexpr int kKT = 64;   // K columns per CTA (FP32 kernels)
 constexpr int kJC = 32;   // reduction chunk
 
+// Phase A: CTA per (item, 64-row slice of the group's panel, 64 columns).
 __global__ void __launch_bounds__(256)
-phaseA_kn_f32(OpView op, const float* __restrict__ vpool, const float* __restrict__ X,
-              float* __restrict__ Z, int K) {
+phaseA_kn_f32(PanelView op, const float* __restrict__ vpanel, const float* __restrict__ X,
+              long long ldx, float* __restrict__ Z, long long ldz, int K, int mt_per_item) {
   __shared__ float s_v[64][kJC + 1];
   __shared__ float s_x[kJC][kKT];
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
   const int nkt = (K + kKT - 1) / kKT;
-  const long long it = blockIdx.x / nkt;
-  const int c_base = (int)(blockIdx.x % nkt) * kKT;
-  const int b = op.a_blk[it];
+  long long bid = blockIdx.x;
+  const int c_base = (int)(bid % nkt) * kKT;
+  bid /= nkt;
+  const int mt = (int)(bid % mt_per_item);
+  const long long it = bid / mt_per_item;
+  const int g = op.a_grp[it];
+  const int kz = op.g_kz[g];
+  const int r_base = mt * 64;
+  if (r_base >= kz) return;
   const int j0 = op.a_j0[it], j1 = op.a_j1[it];
-  const int n = op.n[b], k = op.k[b];
-  const long long c0 = op.c0[b];
-  const float* vt = vpool + op.voff[b];
+  const int ldv = op.g_ldv[g];
+  const long long c0 = op.g_c0[g];
+  const float* vg = vpanel + op.g_voff[g];
   float acc[4][4];
 #pragma unroll
   for (int r = 0; r < 4; r++)
@@ -163,12 +152,12 @@ phaseA_kn_f32(OpView op, const float* __restrict__ vpool, const float* __restric
   for (int jc = j0; jc < j1; jc += kJC) {
     __syncthreads();
     for (int q = threadIdx.x; q < 64 * kJC; q += 256) {
-      int l = q / kJC, j = q % kJC;
-      s_v[l][j] = (l < k && jc + j < j1) ? vt[(long long)l * n + jc + j] : 0.f;
+      int r = q / kJC, j = q % kJC;
+      s_v[r][j] = (r_base + r < kz && jc + j < j1) ? vg[(long long)(r_base + r) * ldv + jc + j] : 0.f;
     }
     for (int q = threadIdx.x; q < kJC * kKT; q += 256) {
       int j = q / kKT, c = q % kKT;
-      s_x[j][c] = (jc + j < j1 && c_base + c < K) ? X[(c0 + jc + j) * (long long)K + c_base + c] : 0.f;
+      s_x[j][c] = (jc + j < j1 && c_base + c < K) ? X[(c0 + jc + j) * ldx + c_base + c] : 0.f;
     }
     __syncthreads();
 #pragma unroll 4
@@ -185,93 +174,86 @@ phaseA_kn_f32(OpView op, const float* __restrict__ vpool, const float* __restric
     }
   }
   const bool excl = op.a_excl[it];
-  float* zb = Z + op.zoff[b] * (long long)K;
+  float* zg = Z + op.g_z0[g] * ldz;
 #pragma unroll
   for (int r = 0; r < 4; r++) {
-    int l = ty + 16 * r;
-    if (l >= k) continue;
+    int row = r_base + ty + 16 * r;
+    if (row >= kz) continue;
 #pragma unroll
     for (int c = 0; c < 4; c++) {
       int col = c_base + tx * 4 + c;
       if (col >= K) continue;
-      if (excl) zb[(long long)l * K + col] = acc[r][c];
-      else atomicAdd(zb + (long long)l * K + col, acc[r][c]);
+      if (excl) zg[(long long)row * ldz + col] = acc[r][c];
+      else atomicAdd(zg + (long long)row * ldz + col, acc[r][c]);
     }
   }
 }
 
-// Phase B: CTA per (row tile of 64, 64 columns); thread owns 4 rows x 4 cols.
+// Phase B: CTA per (tile, 64 columns); thread owns 4 rows x 4 cols.
 __global__ void __launch_bounds__(256)
-phaseB_kn_f32(OpView op, const float* __restrict__ wpool, const float* __restrict__ X,
-              const float* __restrict__ Z, float* __restrict__ Y, int K,
-              const float* __restrict__ add_mat, float alpha) {
-  __shared__ float s_w[kJC][kTileRows + 1];
+phaseB_kn_f32(PanelView op, const float* __restrict__ panel, const float* __restrict__ X,
+              long long ldx, const float* __restrict__ Z, long long ldz, float* __restrict__ Y,
+              long long ldy, int K, const float* __restrict__ add_mat, long long ld_add,
+              float alpha) {
+  __shared__ float s_w[kJC][kTileRows + 4];
   __shared__ float s_s[kJC][kKT];
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
   const int nkt = (K + kKT - 1) / kKT;
   const long long t = blockIdx.x / nkt;
-  const long long t0 = t * kTileRows;
   const int c_base = (int)(blockIdx.x % nkt) * kKT;
+  const long long p0 = op.t_p0[t], p1 = op.t_p0[t + 1];
   float acc[4][4];
 #pragma unroll
   for (int r = 0; r < 4; r++)
 #pragma unroll
     for (int c = 0; c < 4; c++) acc[r][c] = 0.f;
-  for (long long q = op.t_ptr[t]; q < op.t_ptr[t + 1]; q++) {
-    const int b = op.t_blk[q];
-    const long long r0 = op.r0[b];
-    const int m = op.m[b], k = op.k[b];
-    const bool lr = op.zoff[b] >= 0;
-    const float* src = lr ? Z + op.zoff[b] * (long long)K : X + (long long)op.c0[b] * K;
-    const float* w = wpool + op.woff[b];
-    const long long lo = max(t0, r0), hi = min(t0 + kTileRows, r0 + (long long)m);
-    for (int l0 = 0; l0 < k; l0 += kJC) {
-      __syncthreads();
-      for (int e = threadIdx.x; e < kJC * kTileRows; e += 256) {
-        int l = e / kTileRows, ri = e % kTileRows;
-        long long i = t0 + ri;
-        s_w[l][ri] = (l0 + l < k && i >= lo && i < hi) ? w[(long long)(l0 + l) * m + (i - r0)] : 0.f;
-      }
-      for (int e = threadIdx.x; e < kJC * kKT; e += 256) {
-        int l = e / kKT, c = e % kKT;
-        s_s[l][c] = (l0 + l < k && c_base + c < K) ? src[(long long)(l0 + l) * K + c_base + c] : 0.f;
-      }
-      __syncthreads();
+  for (long long l0 = p0; l0 < p1; l0 += kJC) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < kJC * kTileRows / 4; e += 256) {
+      int l = e / (kTileRows / 4), i4 = (e % (kTileRows / 4)) * 4;
+      float4 w = *reinterpret_cast<const float4*>(panel + (l0 + l) * kTileRows + i4);
+      s_w[l][i4] = w.x; s_w[l][i4 + 1] = w.y; s_w[l][i4 + 2] = w.z; s_w[l][i4 + 3] = w.w;
+    }
+    for (int e = threadIdx.x; e < kJC * kKT; e += 256) {
+      int l = e / kKT, c = e % kKT;
+      const int sidx = op.src[l0 + l];
+      const float* srow = sidx < op.num_zrows ? Z + (long long)sidx * ldz
+                                              : X + (long long)(sidx - op.num_zrows) * ldx;
+      s_s[l][c] = (c_base + c < K) ? srow[c_base + c] : 0.f;
+    }
+    __syncthreads();
 #pragma unroll 4
-      for (int l = 0; l < kJC; l++) {
-        float sv[4];
+    for (int l = 0; l < kJC; l++) {
+      float sv[4];
 #pragma unroll
-        for (int c = 0; c < 4; c++) sv[c] = s_s[l][tx * 4 + c];
+      for (int c = 0; c < 4; c++) sv[c] = s_s[l][tx * 4 + c];
 #pragma unroll
-        for (int r = 0; r < 4; r++) {
-          float wv = s_w[l][ty + 16 * r];
+      for (int r = 0; r < 4; r++) {
+        float wv = s_w[l][ty + 16 * r];
 #pragma unroll
-          for (int c = 0; c < 4; c++) acc[r][c] += wv * sv[c];
-        }
+        for (int c = 0; c < 4; c++) acc[r][c] += wv * sv[c];
       }
     }
   }
 #pragma unroll
   for (int r = 0; r < 4; r++) {
-    long long i = t0 + ty + 16 * r;
+    long long i = t * kTileRows + ty + 16 * r;
     if (i >= op.N) continue;
 #pragma unroll
     for (int c = 0; c < 4; c++) {
       int col = c_base + tx * 4 + c;
       if (col >= K) continue;
       float v = acc[r][c];
-      if (add_mat) v = add_mat[i * K + col] + alpha * v;
-      Y[i * K + col] = v;
+      if (add_mat) v = add_mat[i * ld_add + col] + alpha * v;
+      Y[i * ldy + col] = v;
     }
   }
 }
 
 // ------------------------------------------ K RHS, BF16 tensor cores ----
-// mma.sync.m16n8k16 (bf16 x bf16 -> fp32).  Fragments are loaded from shared
-// memory with ldmatrix (.trans where the operand is stored k-major).
-// CTA: 4 warps, tile 64 x 128 (Phase A: rows = factor rows l <= 64, warp w
-// owns columns 32w..32w+31; Phase B: rows = Y rows, warp w owns rows
-// 16w..16w+15 and all 128 columns), reduction chunk 32.
+// mma.sync.m16n8k16 (bf16 x bf16 -> fp32).  Fragments come from shared
+// memory through ldmatrix (.trans where the operand is stored k-major).
+// CTA: 4 warps, tile 64 x 128, reduction chunk 32, double-buffered cp.async.
 constexpr int kBT = 128;     // columns per CTA
 constexpr int kBK = 32;      // reduction chunk
 constexpr int kAPad = 40;    // smem row length (elements) for 32-wide rows
@@ -299,85 +281,116 @@ __device__ __forceinline__ void mma_bf16(float* c, unsigned a0, unsigned a1, uns
       : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
       : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
 }
+// 16-byte async copy; src_size 0 zero-fills (the address must still be valid)
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem, bool pred) {
+  const unsigned s = smem_u32(smem);
+  const int n = pred ? 16 : 0;
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(n));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
 
-// Phase A: Z[zoff + l, c] (+)= sum_j Vt[l, j] X[c0 + j, c]
+// Phase A: Z[z0 + r, c] (+)= sum_j Vg[r, j] X[c0 + j, c], r in a 64-row slice.
 __global__ void __launch_bounds__(128)
-phaseA_kn_bf16(OpView op, const __nv_bfloat16* __restrict__ vpool,
+phaseA_kn_bf16(PanelView op, const __nv_bfloat16* __restrict__ vpanel,
                const __nv_bfloat16* __restrict__ X, long long ldx, float* __restrict__ Z,
-               long long ldz, int K) {
-  __shared__ __align__(16) __nv_bfloat16 s_a[64][kAPad];
-  __shared__ __align__(16) __nv_bfloat16 s_b[kBK][kBPad];
+               long long ldz, int K, int mt_per_item) {
+  __shared__ __align__(16) __nv_bfloat16 s_a[2][64][kAPad];
+  __shared__ __align__(16) __nv_bfloat16 s_b[2][kBK][kBPad];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nkt = (K + kBT - 1) / kBT;
-  const int c_base = (int)(blockIdx.x % nkt) * kBT;
-  const long long it = blockIdx.x / nkt;
-  const int b = op.a_blk[it];
+  long long bid = blockIdx.x;
+  const int c_base = (int)(bid % nkt) * kBT;
+  bid /= nkt;
+  const int mt = (int)(bid % mt_per_item);
+  const long long it = bid / mt_per_item;
+  const int g = op.a_grp[it];
+  const int kz = op.g_kz[g];
+  const int r_base = mt * 64;
+  if (r_base >= kz) return;
   const int j0 = op.a_j0[it], j1 = op.a_j1[it];
-  const int n = op.n[b], k = op.k[b];
-  const long long c0 = op.c0[b];
-  const __nv_bfloat16* vt = vpool + op.voff[b];
-  const __nv_bfloat16 zero = __float2bfloat16(0.f);
+  const int ldv = op.g_ldv[g];
+  const long long c0 = op.g_c0[g];
+  const __nv_bfloat16* vg = vpanel + op.g_voff[g] + (long long)r_base * ldv;
+  const int rows = min(64, kz - r_base);
   float acc[4][4][4];
 #pragma unroll
-  for (int mt = 0; mt < 4; mt++)
+  for (int m2 = 0; m2 < 4; m2++)
 #pragma unroll
     for (int nt = 0; nt < 4; nt++)
 #pragma unroll
-      for (int e = 0; e < 4; e++) acc[mt][nt][e] = 0.f;
-  const int mtiles = (k + 15) >> 4;
-  for (int jc = j0; jc < j1; jc += kBK) {
-    __syncthreads();
-    for (int q = threadIdx.x; q < 64 * kBK; q += 128) {
-      int l = q / kBK, j = q % kBK;
-      s_a[l][j] = (l < k && jc + j < j1) ? vt[(long long)l * n + jc + j] : zero;
+      for (int e = 0; e < 4; e++) acc[m2][nt][e] = 0.f;
+  const int mtiles = (rows + 15) >> 4;
+  auto load = [&](int buf, int jc) {
+    // A: 64 panel rows x 32 columns (rows padded to ldv % 8 == 0: 16-byte aligned)
+    for (int q = threadIdx.x; q < 64 * (kBK / 8); q += 128) {
+      int r = q / (kBK / 8), j8 = (q % (kBK / 8)) * 8;
+      bool ok = r < rows && jc + j8 < j1;
+      const __nv_bfloat16* src = vg + (ok ? (long long)r * ldv + jc + j8 : 0);
+      cp_async16(&s_a[buf][r][j8], src, ok);
     }
     for (int q = threadIdx.x; q < kBK * (kBT / 8); q += 128) {
       int j = q / (kBT / 8), c8 = (q % (kBT / 8)) * 8;
-      uint4 v = make_uint4(0, 0, 0, 0);
-      if (jc + j < j1 && c_base + c8 < K)
-        v = *reinterpret_cast<const uint4*>(X + (c0 + jc + j) * ldx + c_base + c8);
-      *reinterpret_cast<uint4*>(&s_b[j][c8]) = v;
+      bool ok = jc + j < j1 && c_base + c8 < K;
+      const __nv_bfloat16* src = X + (ok ? (c0 + jc + j) * ldx + c_base + c8 : 0);
+      cp_async16(&s_b[buf][j][c8], src, ok);
+    }
+    cp_async_commit();
+  };
+  int buf = 0;
+  load(0, j0);
+  for (int jc = j0; jc < j1; jc += kBK) {
+    if (jc + kBK < j1) {
+      load(buf ^ 1, jc + kBK);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
     }
     __syncthreads();
+    // A columns beyond j1 were zero-filled; X rows beyond j1 too.  The panel
+    // pads each row to a multiple of 8 with zeros, so 8-wide A chunks that
+    // start before j1 and end after it read zero weights.
 #pragma unroll
     for (int kk = 0; kk < kBK; kk += 16) {
       unsigned bf[4][2];
 #pragma unroll
       for (int np = 0; np < 2; np++) {
-        // two n8 tiles per ldmatrix.x4.trans: matrices (k 0-7, n), (k 8-15, n), (k 0-7, n+8), (k 8-15, n+8)
         const int mi = lane >> 3, r = lane & 7;
         const int krow = kk + r + ((mi & 1) ? 8 : 0);
         const int ncol = warp * 32 + np * 16 + ((mi & 2) ? 8 : 0);
-        ldm_x4_t(smem_u32(&s_b[krow][ncol]), bf[2 * np][0], bf[2 * np][1], bf[2 * np + 1][0],
+        ldm_x4_t(smem_u32(&s_b[buf][krow][ncol]), bf[2 * np][0], bf[2 * np][1], bf[2 * np + 1][0],
                  bf[2 * np + 1][1]);
       }
 #pragma unroll
-      for (int mt = 0; mt < 4; mt++) {
-        if (mt >= mtiles) break;
+      for (int m2 = 0; m2 < 4; m2++) {
+        if (m2 >= mtiles) break;
         unsigned a0, a1, a2, a3;
         const int mi = lane >> 3, r = lane & 7;
-        const int row = mt * 16 + r + ((mi & 1) ? 8 : 0);
+        const int row = m2 * 16 + r + ((mi & 1) ? 8 : 0);
         const int col = kk + ((mi & 2) ? 8 : 0);
-        ldm_x4(smem_u32(&s_a[row][col]), a0, a1, a2, a3);
+        ldm_x4(smem_u32(&s_a[buf][row][col]), a0, a1, a2, a3);
 #pragma unroll
-        for (int nt = 0; nt < 4; nt++) mma_bf16(acc[mt][nt], a0, a1, a2, a3, bf[nt][0], bf[nt][1]);
+        for (int nt = 0; nt < 4; nt++) mma_bf16(acc[m2][nt], a0, a1, a2, a3, bf[nt][0], bf[nt][1]);
       }
     }
+    __syncthreads();
+    buf ^= 1;
   }
   const bool excl = op.a_excl[it];
-  float* zb = Z + op.zoff[b] * ldz;
-  const int g = lane >> 2, tg = lane & 3;
+  float* zg = Z + (op.g_z0[g] + r_base) * ldz;
+  const int gq = lane >> 2, tg = lane & 3;
 #pragma unroll
-  for (int mt = 0; mt < 4; mt++) {
+  for (int m2 = 0; m2 < 4; m2++) {
 #pragma unroll
     for (int nt = 0; nt < 4; nt++) {
 #pragma unroll
       for (int e = 0; e < 4; e++) {
-        int l = mt * 16 + g + ((e & 2) ? 8 : 0);
+        int r = m2 * 16 + gq + ((e & 2) ? 8 : 0);
         int col = c_base + warp * 32 + nt * 8 + tg * 2 + (e & 1);
-        if (l < k && col < K) {
-          if (excl) zb[(long long)l * ldz + col] = acc[mt][nt][e];
-          else atomicAdd(zb + (long long)l * ldz + col, acc[mt][nt][e]);
+        if (r < rows && col < K) {
+          if (excl) zg[(long long)r * ldz + col] = acc[m2][nt][e];
+          else atomicAdd(zg + (long long)r * ldz + col, acc[m2][nt][e]);
         }
       }
     }
@@ -391,79 +404,81 @@ __global__ void f32_to_bf16_kernel(const float* __restrict__ in, __nv_bfloat16* 
     out[i] = __float2bfloat16(in[i]);
 }
 
-// Phase B: Y[i, c] = (add[i, c] + alpha *) sum_blocks sum_l W[l, i - r0] S[l, c]
+// Phase B: Y[t0 + i, c] = (add + alpha *) sum_l W[l, i] S[src[l], c]
 __global__ void __launch_bounds__(128)
-phaseB_kn_bf16(OpView op, const __nv_bfloat16* __restrict__ wpool,
+phaseB_kn_bf16(PanelView op, const __nv_bfloat16* __restrict__ panel,
                const __nv_bfloat16* __restrict__ X, long long ldx,
                const __nv_bfloat16* __restrict__ Zb, long long ldz, float* __restrict__ Y,
                long long ldy, int K, const float* __restrict__ add_mat, long long ld_add,
                float alpha) {
-  __shared__ __align__(16) __nv_bfloat16 s_w[kBK][kMPad];   // [l][row]
-  __shared__ __align__(16) __nv_bfloat16 s_s[kBK][kBPad];   // [l][col]
+  __shared__ __align__(16) __nv_bfloat16 s_w[2][kBK][kMPad];   // [l][row]
+  __shared__ __align__(16) __nv_bfloat16 s_s[2][kBK][kBPad];   // [l][col]
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nkt = (K + kBT - 1) / kBT;
   const int c_base = (int)(blockIdx.x % nkt) * kBT;
   const long long t = blockIdx.x / nkt;
-  const long long t0 = t * kTileRows;
-  const __nv_bfloat16 zero = __float2bfloat16(0.f);
+  const long long p0 = op.t_p0[t], p1 = op.t_p0[t + 1];
   float acc[16][4];
 #pragma unroll
   for (int nt = 0; nt < 16; nt++)
 #pragma unroll
     for (int e = 0; e < 4; e++) acc[nt][e] = 0.f;
-  for (long long q = op.t_ptr[t]; q < op.t_ptr[t + 1]; q++) {
-    const int b = op.t_blk[q];
-    const long long r0 = op.r0[b];
-    const int m = op.m[b], k = op.k[b];
-    const bool lr = op.zoff[b] >= 0;
-    const __nv_bfloat16* src = lr ? Zb + op.zoff[b] * ldz : X + (long long)op.c0[b] * ldx;
-    const long long lds = lr ? ldz : ldx;
-    const __nv_bfloat16* w = wpool + op.woff[b];
-    const long long lo = max(t0, r0), hi = min(t0 + kTileRows, r0 + (long long)m);
-    for (int l0 = 0; l0 < k; l0 += kBK) {
-      __syncthreads();
-      for (int e = threadIdx.x; e < kBK * kTileRows; e += 128) {
-        int l = e / kTileRows, ri = e % kTileRows;
-        long long i = t0 + ri;
-        s_w[l][ri] = (l0 + l < k && i >= lo && i < hi) ? w[(long long)(l0 + l) * m + (i - r0)] : zero;
-      }
-      for (int e = threadIdx.x; e < kBK * (kBT / 8); e += 128) {
-        int l = e / (kBT / 8), c8 = (e % (kBT / 8)) * 8;
-        uint4 v = make_uint4(0, 0, 0, 0);
-        if (l0 + l < k && c_base + c8 < K)
-          v = *reinterpret_cast<const uint4*>(src + (long long)(l0 + l) * lds + c_base + c8);
-        *reinterpret_cast<uint4*>(&s_s[l][c8]) = v;
-      }
-      __syncthreads();
+  auto load = [&](int buf, long long l0) {
+    // W: 32 panel rows x 64 weights (128 B each, contiguous)
+    for (int q = threadIdx.x; q < kBK * (kTileRows / 8); q += 128) {
+      int l = q / (kTileRows / 8), i8 = (q % (kTileRows / 8)) * 8;
+      cp_async16(&s_w[buf][l][i8], panel + (l0 + l) * kTileRows + i8, true);
+    }
+    // S: 32 gathered rows x 128 columns
+    for (int q = threadIdx.x; q < kBK * (kBT / 8); q += 128) {
+      int l = q / (kBT / 8), c8 = (q % (kBT / 8)) * 8;
+      const int sidx = op.src[l0 + l];
+      const __nv_bfloat16* srow = sidx < op.num_zrows ? Zb + (long long)sidx * ldz
+                                                      : X + (long long)(sidx - op.num_zrows) * ldx;
+      const bool ok = c_base + c8 < K;
+      cp_async16(&s_s[buf][l][c8], ok ? srow + c_base + c8 : srow, ok);
+    }
+    cp_async_commit();
+  };
+  int buf = 0;
+  if (p0 < p1) load(0, p0);
+  for (long long l0 = p0; l0 < p1; l0 += kBK) {
+    if (l0 + kBK < p1) {
+      load(buf ^ 1, l0 + kBK);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncthreads();
 #pragma unroll
-      for (int kk = 0; kk < kBK; kk += 16) {
-        unsigned a0, a1, a2, a3;
-        {
-          // A = W^T (rows x l) stored [l][row]: ldmatrix.x4.trans
-          const int mi = lane >> 3, r = lane & 7;
-          const int lrow = kk + r + ((mi & 2) ? 8 : 0);
-          const int rcol = warp * 16 + ((mi & 1) ? 8 : 0);
-          ldm_x4_t(smem_u32(&s_w[lrow][rcol]), a0, a1, a2, a3);
-        }
+    for (int kk = 0; kk < kBK; kk += 16) {
+      unsigned a0, a1, a2, a3;
+      {
+        const int mi = lane >> 3, r = lane & 7;
+        const int lrow = kk + r + ((mi & 2) ? 8 : 0);
+        const int rcol = warp * 16 + ((mi & 1) ? 8 : 0);
+        ldm_x4_t(smem_u32(&s_w[buf][lrow][rcol]), a0, a1, a2, a3);
+      }
 #pragma unroll
-        for (int np = 0; np < 8; np++) {
-          unsigned b0, b1, b2, b3;
-          const int mi = lane >> 3, r = lane & 7;
-          const int krow = kk + r + ((mi & 1) ? 8 : 0);
-          const int ncol = np * 16 + ((mi & 2) ? 8 : 0);
-          ldm_x4_t(smem_u32(&s_s[krow][ncol]), b0, b1, b2, b3);
-          mma_bf16(acc[2 * np], a0, a1, a2, a3, b0, b1);
-          mma_bf16(acc[2 * np + 1], a0, a1, a2, a3, b2, b3);
-        }
+      for (int np = 0; np < 8; np++) {
+        unsigned b0, b1, b2, b3;
+        const int mi = lane >> 3, r = lane & 7;
+        const int krow = kk + r + ((mi & 1) ? 8 : 0);
+        const int ncol = np * 16 + ((mi & 2) ? 8 : 0);
+        ldm_x4_t(smem_u32(&s_s[buf][krow][ncol]), b0, b1, b2, b3);
+        mma_bf16(acc[2 * np], a0, a1, a2, a3, b0, b1);
+        mma_bf16(acc[2 * np + 1], a0, a1, a2, a3, b2, b3);
       }
     }
+    __syncthreads();
+    buf ^= 1;
   }
-  const int g = lane >> 2, tg = lane & 3;
+  const int gq = lane >> 2, tg = lane & 3;
 #pragma unroll
   for (int nt = 0; nt < 16; nt++) {
 #pragma unroll
     for (int e = 0; e < 4; e++) {
-      long long i = t0 + warp * 16 + g + ((e & 2) ? 8 : 0);
+      long long i = t * kTileRows + warp * 16 + gq + ((e & 2) ? 8 : 0);
       int col = c_base + nt * 8 + tg * 2 + (e & 1);
       if (i < op.N && col < K) {
         float v = acc[nt][e];
@@ -474,144 +489,216 @@ phaseB_kn_bf16(OpView op, const __nv_bfloat16* __restrict__ wpool,
   }
 }
 
-int check_op(const OpView& op) {
-  if (op.N < 0 || op.num_tiles < 0 || op.num_items < 0) { set_error("bad operator sizes"); return FGB_BAD_ARG; }
+// -------------------------------------------------------------- setup ----
+// Phase-B panels: panel row p (of pair q) = 64 weights from row l of the
+// pair's source matrix (row length m, first operator row r0) for the tile's
+// rows t0 .. t0+63 (zero outside [r0, r0+m)).  One warp per panel row.
+template <class TI, class TO>
+__global__ void build_panel_kernel(const TI* __restrict__ pool, long long num_rows,
+                                   const long long* __restrict__ pair_p0,
+                                   const long long* __restrict__ pair_w,
+                                   const int* __restrict__ pair_m,
+                                   const long long* __restrict__ pair_shift,
+                                   const int* __restrict__ pair_k, long long num_pairs,
+                                   TO* __restrict__ panel) {
+  const int lane = threadIdx.x & 31;
+  const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+  for (long long p = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; p < num_rows;
+       p += warps) {
+    long long lo = 0, hi = num_pairs - 1;
+    while (lo < hi) {
+      long long mid = (lo + hi + 1) >> 1;
+      if (pair_p0[mid] <= p) lo = mid; else hi = mid - 1;
+    }
+    const long long l = p - pair_p0[lo];
+    TO* out = panel + p * kTileRows;
+    if (l >= pair_k[lo]) {  // padding row
+      out[lane] = TO(0.f);
+      out[lane + 32] = TO(0.f);
+      continue;
+    }
+    const int m = pair_m[lo];
+    const long long shift = pair_shift[lo];  // t0 - r0
+    const TI* w = pool + pair_w[lo] + l * (long long)m;
+    for (int i = lane; i < kTileRows; i += 32) {
+      const long long s = shift + i;
+      out[i] = (s >= 0 && s < m) ? (TO)w[s] : TO(0.f);
+    }
+  }
+}
+
+// Phase-A panels: row r of the stacked panel = one V^T row of a member block
+// (length n, row stride (n + 7) & ~7, zero-padded).
+template <class TI, class TO>
+__global__ void build_vpanel_kernel(const TI* __restrict__ pool, long long num_rows,
+                                    const long long* __restrict__ row_src,
+                                    const long long* __restrict__ row_dst,
+                                    const int* __restrict__ row_n, TO* __restrict__ vpanel) {
+  const int lane = threadIdx.x & 31;
+  const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+  for (long long r = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; r < num_rows;
+       r += warps) {
+    const TI* src = pool + row_src[r];
+    TO* dst = vpanel + row_dst[r];
+    const int n = row_n[r];
+    const int ld = (n + 7) & ~7;
+    for (int j = lane; j < ld; j += 32) dst[j] = j < n ? (TO)src[j] : TO(0.f);
+  }
+}
+
+int check_op(const PanelView& op) {
+  if (op.N < 0 || op.num_tiles < 0 || op.num_items < 0 || op.num_zrows < 0) {
+    set_error("bad operator sizes");
+    return FGB_BAD_ARG;
+  }
   return FGB_OK;
 }
 
-}  // namespace
-}  // namespace fgb
-
-
-namespace fgb {
-namespace {
-OpView to_view(const fgb_op_desc* d) {
-  OpView v;
-  v.r0 = d->r0; v.m = d->m; v.c0 = d->c0; v.n = d->n; v.k = d->k;
-  v.woff = d->woff; v.voff = d->voff; v.zoff = d->zoff;
-  v.a_blk = d->a_blk; v.a_j0 = d->a_j0; v.a_j1 = d->a_j1; v.a_excl = d->a_excl;
+PanelView to_view(const fgb_op_desc* d) {
+  PanelView v;
+  v.g_c0 = d->g_c0; v.g_n = d->g_n; v.g_kz = d->g_kz; v.g_ldv = d->g_ldv;
+  v.g_voff = d->g_voff; v.g_z0 = d->g_z0;
+  v.a_grp = d->a_grp; v.a_j0 = d->a_j0; v.a_j1 = d->a_j1; v.a_excl = d->a_excl;
   v.num_items = d->num_items;
-  v.t_ptr = d->t_ptr; v.t_blk = d->t_blk; v.num_tiles = d->num_tiles;
+  v.t_p0 = d->t_p0; v.src = d->src; v.num_tiles = d->num_tiles;
   v.N = d->N;
+  v.num_zrows = d->num_zrows;
   return v;
 }
+
 }  // namespace
 }  // namespace fgb
 
 extern "C" {
 
-/*
- * y = F x (+ optional y = add + alpha * F x), single right-hand side, FP32
- * factors.  x, y, add: N floats in cluster (permuted) order.  z: scratch of
- * num_zrows floats (phase A output); it is fully overwritten for blocks
- * processed by one item and must be zeroed by the caller when some block
- * is split into several items (fgb_op_desc.a_excl == 0 somewhere): pass
- * zero_z != 0 to have it zeroed here.
- */
-int fgb_matvec_f32(const fgb_op_desc* d, const float* wpool, const float* vpool, const float* x,
+int fgb_matvec_f32(const fgb_op_desc* d, const float* panel, const float* vpanel, const float* x,
                    float* z, float* y, const float* add, float alpha, int zero_z, void* stream) {
-  fgb::OpView op = fgb::to_view(d);
+  fgb::PanelView op = fgb::to_view(d);
   int st = fgb::check_op(op);
   if (st) return st;
   cudaStream_t s = fgb::as_stream(stream);
   if (zero_z && d->num_zrows > 0) FGB_CUDA_TRY(cudaMemsetAsync(z, 0, sizeof(float) * d->num_zrows, s));
   if (op.num_items > 0) {
-    fgb::phaseA_k1<float, float><<<fgb::grid_for(op.num_items * 32, 256, 152LL * 64), 256, 0, s>>>(op, vpool, x, z);
+    fgb::phaseA_k1<float, float><<<fgb::grid_for(op.num_items * 32, 256, 152LL * 64), 256, 0, s>>>(op, vpanel, x, z);
     FGB_LAUNCH_CHECK("phaseA_k1");
   }
   if (op.num_tiles > 0) {
-    fgb::phaseB_k1<float, float><<<(unsigned)op.num_tiles, fgb::kB1Warps * 32, 0, s>>>(op, wpool, x, z, y, add, alpha);
+    fgb::phaseB_k1<float, float><<<(unsigned)op.num_tiles, 256, 0, s>>>(op, panel, x, z, y, add, alpha);
     FGB_LAUNCH_CHECK("phaseB_k1");
   }
   return FGB_OK;
 }
 
-/* Same with FP64 factors and FP64 vectors (reference-precision path). */
-int fgb_matvec_f64(const fgb_op_desc* d, const double* wpool, const double* vpool, const double* x,
-                   double* z, double* y, const double* add, double alpha, int zero_z,
-                   void* stream) {
-  fgb::OpView op = fgb::to_view(d);
+int fgb_matvec_f64(const fgb_op_desc* d, const double* panel, const double* vpanel,
+                   const double* x, double* z, double* y, const double* add, double alpha,
+                   int zero_z, void* stream) {
+  fgb::PanelView op = fgb::to_view(d);
   int st = fgb::check_op(op);
   if (st) return st;
   cudaStream_t s = fgb::as_stream(stream);
   if (zero_z && d->num_zrows > 0) FGB_CUDA_TRY(cudaMemsetAsync(z, 0, sizeof(double) * d->num_zrows, s));
   if (op.num_items > 0) {
-    fgb::phaseA_k1<double, double><<<fgb::grid_for(op.num_items * 32, 256, 152LL * 64), 256, 0, s>>>(op, vpool, x, z);
+    fgb::phaseA_k1<double, double><<<fgb::grid_for(op.num_items * 32, 256, 152LL * 64), 256, 0, s>>>(op, vpanel, x, z);
     FGB_LAUNCH_CHECK("phaseA_k1");
   }
   if (op.num_tiles > 0) {
-    fgb::phaseB_k1<double, double><<<(unsigned)op.num_tiles, fgb::kB1Warps * 32, 0, s>>>(op, wpool, x, z, y, add, alpha);
+    fgb::phaseB_k1<double, double><<<(unsigned)op.num_tiles, 256, 0, s>>>(op, panel, x, z, y, add, alpha);
     FGB_LAUNCH_CHECK("phaseB_k1");
   }
   return FGB_OK;
 }
 
-/*
- * Y = F X (+ add + alpha F X) for K right-hand sides, FP32 factors and FP32
- * CUDA-core arithmetic.  X, Y, add: N x K row-major; Z: num_zrows x K.
- */
-int fgb_matmat_f32(const fgb_op_desc* d, const float* wpool, const float* vpool, const float* X,
+int fgb_matmat_f32(const fgb_op_desc* d, const float* panel, const float* vpanel, const float* X,
                    float* Z, float* Y, int K, const float* add, float alpha, int zero_z,
                    int phases, void* stream) {
-  fgb::OpView op = fgb::to_view(d);
+  fgb::PanelView op = fgb::to_view(d);
   int st = fgb::check_op(op);
   if (st) return st;
   if (K < 1) { fgb::set_error("K must be >= 1"); return FGB_BAD_ARG; }
   cudaStream_t s = fgb::as_stream(stream);
-  if ((phases & 1) && zero_z && d->num_zrows > 0)
-    FGB_CUDA_TRY(cudaMemsetAsync(Z, 0, sizeof(float) * d->num_zrows * (size_t)K, s));
   unsigned ky = (unsigned)((K + fgb::kKT - 1) / fgb::kKT);
   if ((phases & 1) && op.num_items > 0) {
-    dim3 g((unsigned)(op.num_items * ky));
-    fgb::phaseA_kn_f32<<<g, 256, 0, s>>>(op, vpool, X, Z, K);
+    if (zero_z && d->num_zrows > 0)
+      FGB_CUDA_TRY(cudaMemsetAsync(Z, 0, sizeof(float) * d->num_zrows * (size_t)K, s));
+    const int mt = d->max_group_tiles;
+    fgb::phaseA_kn_f32<<<(unsigned)(op.num_items * mt * ky), 256, 0, s>>>(op, vpanel, X, K, Z, K, K, mt);
     FGB_LAUNCH_CHECK("phaseA_kn_f32");
   }
   if ((phases & 2) && op.num_tiles > 0) {
-    dim3 g((unsigned)(op.num_tiles * ky));
-    fgb::phaseB_kn_f32<<<g, 256, 0, s>>>(op, wpool, X, Z, Y, K, add, alpha);
+    fgb::phaseB_kn_f32<<<(unsigned)(op.num_tiles * ky), 256, 0, s>>>(op, panel, X, K, Z, K, Y, K, K,
+                                                                      add, K, alpha);
     FGB_LAUNCH_CHECK("phaseB_kn_f32");
   }
   return FGB_OK;
 }
 
-/*
- * Y = F X (+ add + alpha F X) for K right-hand sides on the tensor cores:
- * BF16 factors and BF16 X, FP32 accumulation, FP32 Y.  X: N x K bf16
- * (row stride K, K a multiple of 8), Z: num_zrows x K fp32 scratch, Zb: the
- * same in bf16, Y / add: N x K fp32.
- */
-int fgb_matmat_bf16(const fgb_op_desc* d, const void* wpool, const void* vpool, const void* X,
+int fgb_matmat_bf16(const fgb_op_desc* d, const void* panel, const void* vpanel, const void* X,
                     float* Z, void* Zb, float* Y, int K, const float* add, float alpha,
                     int zero_z, int phases, void* stream) {
-  fgb::OpView op = fgb::to_view(d);
+  fgb::PanelView op = fgb::to_view(d);
   int st = fgb::check_op(op);
   if (st) return st;
   if (K < 8 || (K % 8) != 0) { fgb::set_error("K must be a positive multiple of 8"); return FGB_BAD_ARG; }
-  if ((reinterpret_cast<uintptr_t>(X) & 15) || (reinterpret_cast<uintptr_t>(Zb) & 15)) {
-    fgb::set_error("X and Zb must be 16-byte aligned");
+  if ((reinterpret_cast<uintptr_t>(X) & 15) || (reinterpret_cast<uintptr_t>(Zb) & 15) ||
+      (reinterpret_cast<uintptr_t>(panel) & 15) || (reinterpret_cast<uintptr_t>(vpanel) & 15)) {
+    fgb::set_error("X, Zb and the panels must be 16-byte aligned");
     return FGB_BAD_ARG;
   }
   cudaStream_t s = fgb::as_stream(stream);
-  const __nv_bfloat16* w = static_cast<const __nv_bfloat16*>(wpool);
-  const __nv_bfloat16* v = static_cast<const __nv_bfloat16*>(vpool);
+  const __nv_bfloat16* w = static_cast<const __nv_bfloat16*>(panel);
+  const __nv_bfloat16* v = static_cast<const __nv_bfloat16*>(vpanel);
   const __nv_bfloat16* x = static_cast<const __nv_bfloat16*>(X);
   __nv_bfloat16* zb = static_cast<__nv_bfloat16*>(Zb);
   unsigned kx = (unsigned)((K + fgb::kBT - 1) / fgb::kBT);
   if ((phases & 1) && op.num_items > 0) {
     if (zero_z) FGB_CUDA_TRY(cudaMemsetAsync(Z, 0, sizeof(float) * d->num_zrows * (size_t)K, s));
-    dim3 g((unsigned)(op.num_items * kx));
-    fgb::phaseA_kn_bf16<<<g, 128, 0, s>>>(op, v, x, K, Z, K, K);
+    const int mt = d->max_group_tiles;
+    fgb::phaseA_kn_bf16<<<(unsigned)(op.num_items * mt * kx), 128, 0, s>>>(op, v, x, K, Z, K, K, mt);
     FGB_LAUNCH_CHECK("phaseA_kn_bf16");
     long long nz = d->num_zrows * (long long)K;
     fgb::f32_to_bf16_kernel<<<fgb::grid_for(nz, 256), 256, 0, s>>>(Z, zb, nz);
     FGB_LAUNCH_CHECK("f32_to_bf16_kernel");
   }
   if ((phases & 2) && op.num_tiles > 0) {
-    dim3 g((unsigned)(op.num_tiles * kx));
-    fgb::phaseB_kn_bf16<<<g, 128, 0, s>>>(op, w, x, K, zb, K, Y, K, K, add, K, alpha);
+    fgb::phaseB_kn_bf16<<<(unsigned)(op.num_tiles * kx), 128, 0, s>>>(op, w, x, K, zb, K, Y, K, K,
+                                                                       add, K, alpha);
     FGB_LAUNCH_CHECK("phaseB_kn_bf16");
   }
   return FGB_OK;
 }
+
+#define FGB_PANEL_BUILD(NAME, TI, TO)                                                         \
+  int NAME(const TI* pool, long long num_rows, const long long* pair_p0,                     \
+           const long long* pair_w, const int* pair_m, const long long* pair_shift,          \
+           const int* pair_k, long long num_pairs, void* panel, void* stream) {              \
+    if (num_rows <= 0) return FGB_OK;                                                         \
+    fgb::build_panel_kernel<TI, TO><<<fgb::grid_for(num_rows * 32, 256, 152LL * 64), 256, 0, \
+                                       fgb::as_stream(stream)>>>(                             \
+        pool, num_rows, pair_p0, pair_w, pair_m, pair_shift, pair_k, num_pairs,              \
+        static_cast<TO*>(panel));                                                             \
+    FGB_LAUNCH_CHECK("build_panel_kernel");                                                  \
+    return FGB_OK;                                                                            \
+  }
+FGB_PANEL_BUILD(fgb_build_panel_f32_f32, float, float)
+FGB_PANEL_BUILD(fgb_build_panel_f32_bf16, float, __nv_bfloat16)
+FGB_PANEL_BUILD(fgb_build_panel_f64_f64, double, double)
+FGB_PANEL_BUILD(fgb_build_panel_f64_f32, double, float)
+FGB_PANEL_BUILD(fgb_build_panel_f64_bf16, double, __nv_bfloat16)
+
+#define FGB_VPANEL_BUILD(NAME, TI, TO)                                                          \
+  int NAME(const TI* pool, long long num_rows, const long long* row_src,                       \
+           const long long* row_dst, const int* row_n, void* vpanel, void* stream) {           \
+    if (num_rows <= 0) return FGB_OK;                                                           \
+    fgb::build_vpanel_kernel<TI, TO><<<fgb::grid_for(num_rows * 32, 256, 152LL * 64), 256, 0,  \
+                                        fgb::as_stream(stream)>>>(                              \
+        pool, num_rows, row_src, row_dst, row_n, static_cast<TO*>(vpanel));                     \
+    FGB_LAUNCH_CHECK("build_vpanel_kernel");                                                   \
+    return FGB_OK;                                                                              \
+  }
+FGB_VPANEL_BUILD(fgb_build_vpanel_f32_f32, float, float)
+FGB_VPANEL_BUILD(fgb_build_vpanel_f32_bf16, float, __nv_bfloat16)
+FGB_VPANEL_BUILD(fgb_build_vpanel_f64_f64, double, double)
+FGB_VPANEL_BUILD(fgb_build_vpanel_f64_f32, double, float)
+FGB_VPANEL_BUILD(fgb_build_vpanel_f64_bf16, double, __nv_bfloat16)
 
 }  // extern "C"

@@ -283,7 +283,7 @@ def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_
         D = torch.empty_like(Ep)
         Xb = torch.empty((N, K), dtype=torch.bfloat16, device=dev)
         Zb = torch.empty((max(FF._num_zrows, 1), K), dtype=torch.bfloat16, device=dev)
-        pool_b = FF.pool("bf16")
+        panel_b, vpanel_b = FF.panels("bf16")
         for it in range(1, max_iter + 1):
             # residual with the FP32 operator
             _lib.call("fgb_scale_rows_f32", _lib.ptr(B), _lib.ptr(rho_d), rho_s, _lib.ptr(X32), N, K,
@@ -296,6 +296,7 @@ def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_
             res = _colmax(colmax)
             st["outer"] = it
             st["residual"] = float(np.max(res / np.maximum(emax.cpu().numpy(), 1e-30)))
+            st.setdefault("history", []).append(st["residual"])
             if np.all(res <= thresh):
                 break
             # correction: D <- R + F_bf16 (rho D), `inner` sweeps from D = R
@@ -303,7 +304,7 @@ def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_
             for _ in range(inner):
                 _lib.call("fgb_scale_rows_bf16", _lib.ptr(D), _lib.ptr(rho_d), rho_s, _lib.ptr(Xb),
                           N, K, stream)
-                _lib.call("fgb_matmat_bf16", C.byref(FF._desc), _lib.ptr(pool_b), _lib.ptr(pool_b),
+                _lib.call("fgb_matmat_bf16", C.byref(FF._desc), _lib.ptr(panel_b), _lib.ptr(vpanel_b),
                           _lib.ptr(Xb), _lib.ptr(Z32), _lib.ptr(Zb), _lib.ptr(D), K, _lib.ptr(R),
                           1.0, int(FF._needs_zero_z), 3, stream)
                 st["bf16_matmats"] += 1

@@ -239,64 +239,109 @@ int fgb_ff_fill_f32(const float* P, const float* N, const float* A, const long l
  * maps cluster order to facet ids.  Outputs rank_out[b] (-1: did not
  * converge under its cap, -2: pool full) and off_out[b]: offset in `pool`
  * of U^T (k x m) followed by V^T (k x n).  scratch: num_ctas *
- * fgb_aca_scratch_floats(...) floats; queue: one zeroed int.
+ * fgb_aca_scratch_floats(...) floats; queue: one zeroed int.  Blocks with
+ * m*n <= exact_max are evaluated in full into dense_scratch (num_ctas *
+ * exact_max floats) and approximated with full pivoting on the exact
+ * residual; larger blocks use partial pivoting with the residual norm
+ * estimated from nsample random entries.
  */
 int fgb_aca_scratch_floats(int rmax, long long mmax, long long nmax, long long* per_cta);
 int fgb_aca_f64(const void* bvh, const double* P, const double* N, const double* A,
                 const long long* perm, long long nblocks, const int* r0, const int* m,
                 const int* c0, const int* n, long long mmax, long long nmax, double eps,
-                int semantics, float tol, int rmax, int nsample, float* scratch, int num_ctas,
+                int semantics, float tol, int rmax, int nsample, long long exact_max,
+                float* dense_scratch, float* scratch, int num_ctas,
                 float* pool, long long pool_capacity, unsigned long long* pool_used,
                 int* rank_out, long long* off_out, int* queue, unsigned* flags, void* stream);
 
 /* ----------------------------------------------- block matvec (a9) */
 /*
- * Flat description of a compressed operator (device arrays; see
- * fluxpy_gb300/csrc/matvec.cu): per block r0, m, c0, n, k, woff, voff, zoff
- * (zoff < 0 marks an exact dense leaf); phase-A items (a_blk, a_j0, a_j1,
- * a_excl); phase-B row tiles of 64 rows (t_ptr, t_blk).
+ * Flat description of a compressed operator in cluster order (device
+ * arrays; layout in fluxpy_gb300/csrc/matvec.cu):
+ *   phase A groups g (low-rank blocks sharing a column range): g_c0, g_n,
+ *     g_kz (stacked rank), g_ldv (panel row stride, n rounded up to 8),
+ *     g_voff (panel offset), g_z0 (first Z row); work items a_grp, a_j0,
+ *     a_j1, a_excl (1: the item covers its whole group);
+ *   phase B row tiles of 64 rows: t_p0[num_tiles+1] panel-row offsets (each
+ *     tile a multiple of 32 rows), src[row] = source row (< num_zrows: a row
+ *     of Z; else a row of X at src - num_zrows).
  */
 struct fgb_op_desc {
-  const int* r0;
-  const int* m;
-  const int* c0;
-  const int* n;
-  const int* k;
-  const long long* woff;
-  const long long* voff;
-  const long long* zoff;
-  const int* a_blk;
+  const int* g_c0;
+  const int* g_n;
+  const int* g_kz;
+  const int* g_ldv;
+  const long long* g_voff;
+  const long long* g_z0;
+  const int* a_grp;
   const int* a_j0;
   const int* a_j1;
   const unsigned char* a_excl;
   long long num_items;
-  const long long* t_ptr;
-  const int* t_blk;
+  const long long* t_p0;
+  const int* src;
   long long num_tiles;
   long long N;
   long long num_zrows;
+  int max_group_tiles; /* max over groups of ceil(g_kz / 64) */
 };
 /*
  * y = F x (or y = add + alpha F x), vectors in cluster order.  Replaces
  * CompressedFormFactorMatrix._matmat (src/flux/compressed_form_factors.py:805)
  * and the recursive FormFactorBlockMatrix._matmat (:407-414) with its leaf
- * products (dense :175, CSR :193, SVD :247-251).
+ * products (dense :175, CSR :193, SVD :247-251).  panel / vpanel: the
+ * phase-B and phase-A panels in the function's precision; z: num_zrows
+ * scratch (zeroed here when zero_z != 0, needed when some a_excl == 0).
  */
-int fgb_matvec_f32(const struct fgb_op_desc* d, const float* wpool, const float* vpool,
+int fgb_matvec_f32(const struct fgb_op_desc* d, const float* panel, const float* vpanel,
                    const float* x, float* z, float* y, const float* add, float alpha, int zero_z,
                    void* stream);
-int fgb_matvec_f64(const struct fgb_op_desc* d, const double* wpool, const double* vpool,
+int fgb_matvec_f64(const struct fgb_op_desc* d, const double* panel, const double* vpanel,
                    const double* x, double* z, double* y, const double* add, double alpha,
                    int zero_z, void* stream);
-/* K right-hand sides (X, Y: N x K row-major): FP32 CUDA cores ...
- * phases: 1 = phase A only (Z = Vt X), 2 = phase B only (Y from Z), 3 = both. */
-int fgb_matmat_f32(const struct fgb_op_desc* d, const float* wpool, const float* vpool,
+/* K right-hand sides (X, Y, add: N x K row-major; Z: num_zrows x K):
+ * FP32 CUDA cores ...  phases: 1 = phase A only, 2 = phase B only, 3 = both. */
+int fgb_matmat_f32(const struct fgb_op_desc* d, const float* panel, const float* vpanel,
                    const float* X, float* Z, float* Y, int K, const float* add, float alpha,
                    int zero_z, int phases, void* stream);
-/* ... and BF16 tensor cores with FP32 accumulation (X bf16, K % 8 == 0). */
-int fgb_matmat_bf16(const struct fgb_op_desc* d, const void* wpool, const void* vpool,
+/* ... and BF16 tensor cores with FP32 accumulation (X, panels bf16, K % 8 == 0;
+ * Zb: num_zrows x K bf16 scratch). */
+int fgb_matmat_bf16(const struct fgb_op_desc* d, const void* panel, const void* vpanel,
                     const void* X, float* Z, void* Zb, float* Y, int K, const float* add,
                     float alpha, int zero_z, int phases, void* stream);
+/*
+ * Panel construction (setup).  Phase B: pairs q (tile, contributing block)
+ * with pair_p0 (first panel row, sorted), pair_w (pool offset of the block's
+ * weight row 0), pair_m (weight row length = block rows), pair_shift (tile
+ * first row - block first row), pair_k (weight rows; panel rows beyond it
+ * are zero padding).  Phase A: one stacked row per (row_src pool offset,
+ * row_dst panel offset, row_n length).  Suffix: pool type _ panel type.
+ */
+int fgb_build_panel_f32_f32(const float* pool, long long num_rows, const long long* pair_p0,
+                          const long long* pair_w, const int* pair_m, const long long* pair_shift,
+                          const int* pair_k, long long num_pairs, void* panel, void* stream);
+int fgb_build_panel_f32_bf16(const float* pool, long long num_rows, const long long* pair_p0,
+                          const long long* pair_w, const int* pair_m, const long long* pair_shift,
+                          const int* pair_k, long long num_pairs, void* panel, void* stream);
+int fgb_build_panel_f64_f64(const double* pool, long long num_rows, const long long* pair_p0,
+                          const long long* pair_w, const int* pair_m, const long long* pair_shift,
+                          const int* pair_k, long long num_pairs, void* panel, void* stream);
+int fgb_build_panel_f64_f32(const double* pool, long long num_rows, const long long* pair_p0,
+                          const long long* pair_w, const int* pair_m, const long long* pair_shift,
+                          const int* pair_k, long long num_pairs, void* panel, void* stream);
+int fgb_build_panel_f64_bf16(const double* pool, long long num_rows, const long long* pair_p0,
+                          const long long* pair_w, const int* pair_m, const long long* pair_shift,
+                          const int* pair_k, long long num_pairs, void* panel, void* stream);
+int fgb_build_vpanel_f32_f32(const float* pool, long long num_rows, const long long* row_src,
+                           const long long* row_dst, const int* row_n, void* vpanel, void* stream);
+int fgb_build_vpanel_f32_bf16(const float* pool, long long num_rows, const long long* row_src,
+                           const long long* row_dst, const int* row_n, void* vpanel, void* stream);
+int fgb_build_vpanel_f64_f64(const double* pool, long long num_rows, const long long* row_src,
+                           const long long* row_dst, const int* row_n, void* vpanel, void* stream);
+int fgb_build_vpanel_f64_f32(const double* pool, long long num_rows, const long long* row_src,
+                           const long long* row_dst, const int* row_n, void* vpanel, void* stream);
+int fgb_build_vpanel_f64_bf16(const double* pool, long long num_rows, const long long* row_src,
+                           const long long* row_dst, const int* row_n, void* vpanel, void* stream);
 
 /* --------------------------------------------- solve kernels (a10-a12) */
 /*

@@ -152,24 +152,6 @@ def _bbox3(P, tree):
 LEAF_ZERO, LEAF_DENSE, LEAF_SPARSE, LEAF_LOWRANK, NODE = 0, 1, 2, 3, 4
 
 
-class _Plan:
-    """The block tree as flat arrays: one record per block (leaf or node)."""
-
-    def __init__(self):
-        self.rows = []      # row cluster node id
-        self.cols = []      # col cluster node id
-        self.parent = []    # parent block id (-1 for root)
-        self.kind = []      # LEAF_* or NODE
-        self.child0 = []    # first child block id (NODE)
-
-
-class _DeviceOperator:
-    """Flat device layout consumed by libfluxgb's matvec kernels."""
-
-    def __init__(self, dev):
-        self.dev = dev
-
-
 class fgb_op_desc(C.Structure):
     """ctypes mirror of struct fgb_op_desc (include/fluxgb.h)."""
     _fields_ = [

@@ -120,6 +120,15 @@ phaseB_k1(PanelView op, const T* __restrict__ panel, const V* __restrict__ x,
 }
 
 // ------------------------------------------------- K RHS, FP32 FFMA ----
+// s += x with Kahan compensation c (the _rn intrinsics keep the compiler
+// from re-associating the compensation away).
+__device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
+  const float y = __fsub_rn(x, c);
+  const float t = __fadd_rn(s, y);
+  c = __fsub_rn(__fsub_rn(t, s), y);
+  s = t;
+}
+
 constexpr int kKT = 64;   // K columns per CTA (FP32 kernels)
 constexpr int kJC = 32;   // reduction chunk
 
@@ -149,6 +158,11 @@ phaseA_kn_f32(PanelView op, const float* __restrict__ vpanel, const float* __res
   for (int r = 0; r < 4; r++)
 #pragma unroll
     for (int c = 0; c < 4; c++) acc[r][c] = 0.f;
+  float comp[4][4];
+#pragma unroll
+  for (int r = 0; r < 4; r++)
+#pragma unroll
+    for (int c = 0; c < 4; c++) comp[r][c] = 0.f;
   for (int jc = j0; jc < j1; jc += kJC) {
     __syncthreads();
     for (int q = threadIdx.x; q < 64 * kJC; q += 256) {
@@ -160,6 +174,13 @@ phaseA_kn_f32(PanelView op, const float* __restrict__ vpanel, const float* __res
       s_x[j][c] = (jc + j < j1 && c_base + c < K) ? X[(c0 + jc + j) * ldx + c_base + c] : 0.f;
     }
     __syncthreads();
+    // per-chunk partial sums, added to the running sums with Kahan
+    // compensation so that long reductions keep FP32 accuracy
+    float part[4][4];
+#pragma unroll
+    for (int r = 0; r < 4; r++)
+#pragma unroll
+      for (int c = 0; c < 4; c++) part[r][c] = 0.f;
 #pragma unroll 4
     for (int j = 0; j < kJC; j++) {
       float xv[4];
@@ -169,9 +190,13 @@ phaseA_kn_f32(PanelView op, const float* __restrict__ vpanel, const float* __res
       for (int r = 0; r < 4; r++) {
         float v = s_v[ty + 16 * r][j];
 #pragma unroll
-        for (int c = 0; c < 4; c++) acc[r][c] += v * xv[c];
+        for (int c = 0; c < 4; c++) part[r][c] += v * xv[c];
       }
     }
+#pragma unroll
+    for (int r = 0; r < 4; r++)
+#pragma unroll
+      for (int c = 0; c < 4; c++) kahan_add(acc[r][c], comp[r][c], part[r][c]);
   }
   const bool excl = op.a_excl[it];
   float* zg = Z + op.g_z0[g] * ldz;
@@ -207,6 +232,11 @@ phaseB_kn_f32(PanelView op, const float* __restrict__ panel, const float* __rest
   for (int r = 0; r < 4; r++)
 #pragma unroll
     for (int c = 0; c < 4; c++) acc[r][c] = 0.f;
+  float comp[4][4];
+#pragma unroll
+  for (int r = 0; r < 4; r++)
+#pragma unroll
+    for (int c = 0; c < 4; c++) comp[r][c] = 0.f;
   for (long long l0 = p0; l0 < p1; l0 += kJC) {
     __syncthreads();
     for (int e = threadIdx.x; e < kJC * kTileRows / 4; e += 256) {
@@ -222,6 +252,11 @@ phaseB_kn_f32(PanelView op, const float* __restrict__ panel, const float* __rest
       s_s[l][c] = (c_base + c < K) ? srow[c_base + c] : 0.f;
     }
     __syncthreads();
+    float part[4][4];
+#pragma unroll
+    for (int r = 0; r < 4; r++)
+#pragma unroll
+      for (int c = 0; c < 4; c++) part[r][c] = 0.f;
 #pragma unroll 4
     for (int l = 0; l < kJC; l++) {
       float sv[4];
@@ -231,9 +266,13 @@ phaseB_kn_f32(PanelView op, const float* __restrict__ panel, const float* __rest
       for (int r = 0; r < 4; r++) {
         float wv = s_w[l][ty + 16 * r];
 #pragma unroll
-        for (int c = 0; c < 4; c++) acc[r][c] += wv * sv[c];
+        for (int c = 0; c < 4; c++) part[r][c] += wv * sv[c];
       }
     }
+#pragma unroll
+    for (int r = 0; r < 4; r++)
+#pragma unroll
+      for (int c = 0; c < 4; c++) kahan_add(acc[r][c], comp[r][c], part[r][c]);
   }
 #pragma unroll
   for (int r = 0; r < 4; r++) {

@@ -222,15 +222,21 @@ aca_kernel(AcaArgs a, EntryCtx<R> e) {
           for (int l = 0; l < k; l++) val -= U[(long long)l * a.mmax + istar] * V[(long long)l * a.nmax + j];
           rowbuf[j] = val;
           rr += (double)val * val;
-          if (used_c[j] == 0.f && (lmax_i < 0 || fabsf(val) > fabsf(lmax_v))) { lmax_v = val; lmax_i = j; }
+          if (lmax_i < 0 || fabsf(val) > fabsf(lmax_v)) { lmax_v = val; lmax_i = j; }
         }
         if (tid == 0) used_r[istar] = 1.f;
         float piv;
         int jstar;
         block_argmax(lmax_v, lmax_i, sh_v, sh_i, &piv, &jstar);
         rr = block_sum(rr, sh_d);
-        const bool negligible = jstar < 0 || piv == 0.0f ||
-                                (normS2 > 0.0 && (double)m * rr <= 1e-4 * (double)a.tol * a.tol * normS2);
+        // The pivot is the row's largest residual over all columns, so the
+        // new v has |v| <= 1.  A row whose largest residual sits on an
+        // already used column holds FP32 rounding noise only (the residual
+        // of pivot columns is zero up to rounding): treat it as negligible,
+        // as any row whose residual norm would add less than (tol/4)^2 of
+        // |S|_F^2 when repeated over all m rows.
+        const bool negligible = jstar < 0 || piv == 0.0f || used_c[jstar] != 0.f ||
+                                (normS2 > 0.0 && (double)m * rr <= 0.0625 * (double)a.tol * a.tol * normS2);
         if (negligible) { verify = true; continue; }
         if (k >= kmax) { failed = true; break; }
         // new term: v = row / pivot, u = residual column jstar
@@ -330,6 +336,17 @@ aca_kernel(AcaArgs a, EntryCtx<R> e) {
       verify = false;
     }
     __syncthreads();
+    // factors must be finite (a degenerate pivot would show up here)
+    {
+      bool bad = false;
+      for (int l = 0; l < k && !failed; l++) {
+        for (int i = tid; i < m; i += kAcaThreads)
+          if (!isfinite(U[(long long)l * a.mmax + i])) bad = true;
+        for (int j = tid; j < n; j += kAcaThreads)
+          if (!isfinite(V[(long long)l * a.nmax + j])) bad = true;
+      }
+      if (__syncthreads_or(bad)) failed = true;
+    }
     if (failed) {
       if (tid == 0) { a.rank_out[b] = -1; a.off_out[b] = -1; }
       continue;

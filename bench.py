@@ -399,10 +399,9 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
     Epc = Ep[:, cols].double()
     res = []
     for q in range(Bp.shape[1]):
-        y = FF.matvec_permuted((RHO * Bp[:, q]).contiguous(), "fp64")
+        y = FF.matvec_permuted((RHO * Bp[:, q]).contiguous(), "fp32-fp64")
         r = Epc[:, q] - (Bp[:, q] - y)
         res.append(float(r.abs().max() / Epc[:, q].abs().max()))
-    FF._panels.pop("fp64", None)
     rng = np.random.default_rng(0)
     rows = rng.choice(N, 16, replace=False)
     facet_rows = FF._tree.perm[rows]

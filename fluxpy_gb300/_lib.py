@@ -91,6 +91,7 @@ SIGNATURES: dict[str, list] = {
     "fgb_build_vpanel_f64_bf16": [P, I64, P, P, P, P, P],
     "fgb_matvec_f32": [P, P, P, P, P, P, P, F32, I32, P],
     "fgb_matvec_f64": [P, P, P, P, P, P, P, F64, I32, P],
+    "fgb_matvec_f32_f64": [P, P, P, P, P, P, P, F64, I32, P],
     "fgb_matmat_f32": [P, P, P, P, P, P, I32, P, F32, I32, I32, P],
     "fgb_matmat_bf16": [P, P, P, P, P, P, P, I32, P, F32, I32, I32, P],
     # solve (a10-a12)

@@ -691,6 +691,15 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
 
     _TDT = {"fp64": torch.float64, "fp32": torch.float32, "bf16": torch.bfloat16}
 
+    def offload_pool(self, precisions=("fp32", "bf16")):
+        """Build the panels of the given precisions, then move the block pool
+        (needed only for other precisions and for block introspection) to
+        host memory, freeing its device copy."""
+        for p_ in precisions:
+            self.panels(p_)
+        self._pool = self._pool.cpu()
+        torch.cuda.empty_cache()
+
     def panels(self, precision):
         """(phase-B panel, phase-A panel) in 'fp64', 'fp32' or 'bf16', built
         on first use from the pool."""
@@ -698,7 +707,9 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         if got is not None:
             return got
         tdt = self._TDT[precision]
-        dev = self._pool.device
+        dev = self._perm_d.device
+        if self._pool.device != dev:
+            self._pool = self._pool.to(dev)
         pin = "f64" if self._pool.dtype == torch.float64 else "f32"
         pout = {"fp64": "f64", "fp32": "f32", "bf16": "bf16"}[precision]
         if pin == "f32" and pout == "f64":
@@ -727,19 +738,29 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         return xp.index_select(0, self._iperm_d)
 
     def matvec_permuted(self, xp, precision="fp32", out=None, add=None, alpha=1.0, z=None):
-        """y = F x (or add + alpha F x) in cluster order, K = 1."""
+        """y = F x (or add + alpha F x) in cluster order, K = 1.
+
+        precision: 'fp32' (FP32 panels and arithmetic), 'fp64' (FP64 panels
+        and arithmetic), 'fp32-fp64' (the FP32-stored operator applied in FP64
+        arithmetic)."""
         if precision == "fp64":
             V = torch.float64
             fn = "fgb_matvec_f64"
+            pp = "fp64"
+        elif precision == "fp32-fp64":
+            V = torch.float64
+            fn = "fgb_matvec_f32_f64"
+            pp = "fp32"
         else:
             V = torch.float32
             fn = "fgb_matvec_f32"
+            pp = "fp32"
         xp = xp.to(V).contiguous()
         if out is None:
             out = torch.empty_like(xp)
         if z is None:
             z = torch.empty(max(self._num_zrows, 1), dtype=V, device=xp.device)
-        panel, vpanel = self.panels("fp64" if precision == "fp64" else "fp32")
+        panel, vpanel = self.panels(pp)
         _lib.call(fn, C.byref(self._desc), _lib.ptr(panel), _lib.ptr(vpanel), _lib.ptr(xp),
                   _lib.ptr(z), _lib.ptr(out), _lib.ptr(add), float(alpha),
                   int(self._needs_zero_z), _lib.stream_handle())

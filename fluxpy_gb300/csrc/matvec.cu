@@ -647,6 +647,26 @@ int fgb_matvec_f64(const fgb_op_desc* d, const double* panel, const double* vpan
   return FGB_OK;
 }
 
+/* FP32 panels, FP64 vectors and accumulation (residual checks). */
+int fgb_matvec_f32_f64(const fgb_op_desc* d, const float* panel, const float* vpanel,
+                       const double* x, double* z, double* y, const double* add, double alpha,
+                       int zero_z, void* stream) {
+  fgb::PanelView op = fgb::to_view(d);
+  int st = fgb::check_op(op);
+  if (st) return st;
+  cudaStream_t s = fgb::as_stream(stream);
+  if (zero_z && d->num_zrows > 0) FGB_CUDA_TRY(cudaMemsetAsync(z, 0, sizeof(double) * d->num_zrows, s));
+  if (op.num_items > 0) {
+    fgb::phaseA_k1<float, double><<<fgb::grid_for(op.num_items * 32, 256, 152LL * 64), 256, 0, s>>>(op, vpanel, x, z);
+    FGB_LAUNCH_CHECK("phaseA_k1");
+  }
+  if (op.num_tiles > 0) {
+    fgb::phaseB_k1<float, double><<<(unsigned)op.num_tiles, 256, 0, s>>>(op, panel, x, z, y, add, alpha);
+    FGB_LAUNCH_CHECK("phaseB_k1");
+  }
+  return FGB_OK;
+}
+
 int fgb_matmat_f32(const fgb_op_desc* d, const float* panel, const float* vpanel, const float* X,
                    float* Z, float* Y, int K, const float* add, float alpha, int zero_z,
                    int phases, void* stream) {

@@ -219,8 +219,16 @@ def _colmax(t):
     return t.view(torch.int32).cpu().numpy().view(np.float32)
 
 
+def _auto_chunk(FF, N, K):
+    free, _ = torch.cuda.mem_get_info()
+    per_col = N * (6 * 4 + 2) + max(FF._num_zrows, 1) * 6
+    c = int(0.6 * free / per_col) // 8 * 8
+    return max(8, min(K, c))
+
+
 def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_iter=200,
-                            inner=3, E_is_permuted=False, return_permuted=False, stats=None):
+                            inner=3, E_is_permuted=False, return_permuted=False, stats=None,
+                            chunk=None):
     """Right-placement radiosity solve for K sun directions at once.
 
     FF: CompressedFormFactorMatrix; E: (N, K) device tensor (facet order, or
@@ -236,6 +244,25 @@ def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_
     """
     dev = E.device
     N, K0 = E.shape
+    if chunk is None:
+        chunk = _auto_chunk(FF, N, K0)
+    if K0 > chunk:
+        # the columns are independent: solve them in chunks that fit in memory
+        parts = []
+        st_all = stats if stats is not None else {}
+        agg = {}
+        for c0 in range(0, K0, chunk):
+            st = {}
+            parts.append(solve_radiosity_batched(FF, E[:, c0:c0 + chunk].contiguous(), rho, rtol,
+                                                 precision, max_iter, inner, E_is_permuted,
+                                                 return_permuted, st, chunk=chunk))
+            for k_, v_ in st.items():
+                if isinstance(v_, (int, float)) and k_ != "residual":
+                    agg[k_] = agg.get(k_, 0) + v_
+            agg["residual"] = max(agg.get("residual", 0.0), st.get("residual", 0.0))
+        agg["chunks"] = len(parts)
+        st_all.update(agg)
+        return torch.cat(parts, 1)
     if precision == "bf16-refine" and K0 % 8:
         pad = 8 - K0 % 8
         E = torch.cat([E, torch.zeros((N, pad), dtype=E.dtype, device=dev)], 1)

@@ -299,6 +299,11 @@ int fgb_matvec_f32(const struct fgb_op_desc* d, const float* panel, const float*
 int fgb_matvec_f64(const struct fgb_op_desc* d, const double* panel, const double* vpanel,
                    const double* x, double* z, double* y, const double* add, double alpha,
                    int zero_z, void* stream);
+/* FP32 panels with FP64 vectors and FP64 accumulation (residual checks of the
+ * stored FP32 operator in FP64 arithmetic). */
+int fgb_matvec_f32_f64(const struct fgb_op_desc* d, const float* panel, const float* vpanel,
+                       const double* x, double* z, double* y, const double* add, double alpha,
+                       int zero_z, void* stream);
 /* K right-hand sides (X, Y, add: N x K row-major; Z: num_zrows x K):
  * FP32 CUDA cores ...  phases: 1 = phase A only, 2 = phase B only, 3 = both. */
 int fgb_matmat_f32(const struct fgb_op_desc* d, const float* panel, const float* vpanel,

@@ -257,7 +257,7 @@ def main():
             dist.destroy_process_group()
         return
     # operator entries for the CPU reference arm's scaling
-    entries = int(FF.stats["pool_entries"])
+    entries = int(FF.stats["operator_entries"])
     try:
         (ROOT / "profiles").mkdir(exist_ok=True)
         (ROOT / "profiles" / "operator_entries.json").write_text(
@@ -430,7 +430,7 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
                   "d2h_bytes_per_step": N * K * 4, "ms_per_step": t_e2e * 1e3}
     # ---- CPU baseline (oracle port, bounded sample)
     try:
-        out["cpu_baseline"] = cpu_baseline(int(FF.stats["pool_entries"]))
+        out["cpu_baseline"] = cpu_baseline(int(FF.stats["operator_entries"]))
     except Exception as e:  # the checker must not break the GPU measurement
         out["cpu_baseline"] = {"value": None, "error": str(e)}
     return out

@@ -74,6 +74,14 @@ SIGNATURES: dict[str, list] = {
     "fgb_ff_count_f32": [P, P, P, P, P, P, P, P, P, P, P, P, I64, I64, F32, I32, P, P, P, U32P, P],
     "fgb_ff_fill_f64": [P, P, P, P, P, P, P, P, P, P, P, I64, I64, P, P, P, P, P],
     "fgb_ff_fill_f32": [P, P, P, P, P, P, P, P, P, P, P, I64, I64, P, P, P, P, P],
+    "fgb_ff_fill_f64_to_f32": [P, P, P, P, P, P, P, P, P, P, P, I64, I64, P, P, P, P, P],
+    "fgb_nf_pair_masks": [P, P, P, I64, I64, P, P, P, P, P, P, P, P, P],
+    "fgb_nf_enumerate": [P, P, P, I64, P, P, P, P, P, P],
+    "fgb_nf_fill_f32_f32": [P, P, I64, P, P, P, P, P, P, P, P, P, P, P, I64, P, P],
+    "fgb_nf_fill_f32_bf16": [P, P, I64, P, P, P, P, P, P, P, P, P, P, P, I64, P, P],
+    "fgb_nf_fill_f64_f64": [P, P, I64, P, P, P, P, P, P, P, P, P, P, P, I64, P, P],
+    "fgb_nf_fill_f64_f32": [P, P, I64, P, P, P, P, P, P, P, P, P, P, P, I64, P, P],
+    "fgb_nf_fill_f64_bf16": [P, P, I64, P, P, P, P, P, P, P, P, P, P, P, I64, P, P],
     # compression (a6-a8)
     "fgb_aca_scratch_floats": [I32, I64, I64, P],
     "fgb_aca_f64": [P, P, P, P, P, I64, P, P, P, P, I64, I64, F64, I32, F32, I32, I32, I64, P,

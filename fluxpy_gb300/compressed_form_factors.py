@@ -435,7 +435,8 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         return ranks, offs, (pool[:nused] if nused else None)
 
     def _assemble(self, exact, aca_pool_parts, pool_off):
-        """Exact leaves -> dense device blocks; flat operator layout."""
+        """Exact leaves (sparse, from the pair kernel) and low-rank factors ->
+        the flat panel layout of the device matvec."""
         sm = self.shape_model
         dev = sm._device
         tree = self._tree
@@ -444,52 +445,28 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         tdt = torch.float64 if sdt == np.float64 else torch.float32
         exact = np.array(sorted(exact), dtype=np.int64)
         if exact.size:
-            # order by (row range, first column) so that horizontally adjacent
-            # exact leaves of one row cluster are contiguous in the pool and
-            # can be merged into one wider dense block on the device
             er = tree.start[self._rows[exact]]
             em = tree.size[self._rows[exact]]
             ec = tree.start[self._cols[exact]]
             exact = exact[np.lexsort((ec, em, er))]
-        ex_r = self._rows[exact] if exact.size else np.zeros(0, np.int64)
-        ex_c = self._cols[exact] if exact.size else np.zeros(0, np.int64)
-        ex_m = tree.size[ex_r]
-        ex_n = tree.size[ex_c]
-        dense_entries = int((ex_m * ex_n).sum())
-        if dense_entries * np.dtype(sdt).itemsize > 96 * 2**30:
-            raise MemoryError("exact leaves would need more than 96 GB as dense blocks; "
-                              "use a larger max_depth / smaller min_size")
+        ex_r0 = tree.start[self._rows[exact]].astype(np.int64) if exact.size else np.zeros(0, np.int64)
+        ex_m = tree.size[self._rows[exact]].astype(np.int64) if exact.size else np.zeros(0, np.int64)
+        ex_c0 = tree.start[self._cols[exact]].astype(np.int64) if exact.size else np.zeros(0, np.int64)
+        ex_n = tree.size[self._cols[exact]].astype(np.int64) if exact.size else np.zeros(0, np.int64)
         self._leaf_nnz = np.zeros(len(self._rows), np.int64)
+        self._exact = exact
+        self._exact_index = {int(b): q for q, b in enumerate(exact)}
         if exact.size:
-            tcsr = ff_tiles(sm, perm_d, perm_d, tree.start[ex_r], ex_m, tree.start[ex_c], ex_n,
-                            self._eps)
+            tcsr = ff_tiles(sm, perm_d, perm_d, ex_r0, ex_m, ex_c0, ex_n, self._eps,
+                            keep_bits=True, out_dtype=tdt)
             self.stats["exact_nnz"] = int(tcsr.data.numel())
             self.stats["kept_pairs"] = tcsr.kept_pairs
             self.stats["near_edge_pairs"] = tcsr.near_edge_pairs
-            dense_off = np.zeros(exact.size + 1, np.int64)
-            np.cumsum(ex_m * ex_n, out=dense_off[1:])
-            dense = torch.zeros(max(dense_entries, 1), dtype=tdt, device=dev)
-            # scatter CSR entries to W = D^T: W[off + j*m + i]
-            R = int(tcsr.row_off[-1])
-            indptr = tcsr.indptr
-            nnz_per_row = (indptr[1:] - indptr[:-1])
-            tile_of_row = torch.repeat_interleave(
-                torch.arange(exact.size, device=dev),
-                torch.as_tensor(ex_m, device=dev))
-            row_local = torch.arange(R, device=dev) - torch.as_tensor(tcsr.row_off[:-1], device=dev)[tile_of_row]
-            ent_tile = torch.repeat_interleave(tile_of_row, nnz_per_row)
-            ent_row = torch.repeat_interleave(row_local, nnz_per_row)
-            m_d = torch.as_tensor(ex_m, device=dev)
-            off_d = torch.as_tensor(dense_off[:-1], device=dev)
-            pos = off_d[ent_tile] + tcsr.indices.to(torch.int64) * m_d[ent_tile] + ent_row
-            dense[pos] = tcsr.data.to(tdt)
-            nnz_tile = torch.zeros(exact.size, dtype=torch.int64, device=dev)
-            nnz_tile.index_add_(0, tile_of_row, nnz_per_row)
-            self._leaf_nnz[exact] = nnz_tile.cpu().numpy()
-            self._exact_csr = (tcsr, exact)
+            ro = torch.as_tensor(tcsr.row_off, device=dev)
+            nnz_leaf = (tcsr.indptr[ro[1:]] - tcsr.indptr[ro[:-1]]).cpu().numpy()
+            self._leaf_nnz[exact] = nnz_leaf
+            self._exact_csr = tcsr
         else:
-            dense = torch.zeros(1, dtype=tdt, device=dev)
-            dense_off = np.zeros(1, np.int64)
             self._exact_csr = None
         # classify exact leaves as the reference would (zero / dense / CSR by bytes)
         isz = np.dtype(self.shape_model.dtype).itemsize
@@ -502,55 +479,24 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
                 self._kind[b] = LEAF_DENSE
             else:
                 self._kind[b] = LEAF_SPARSE
-        self._dense_off = dict(zip(exact.tolist(), dense_off[:-1].tolist()))
-
-        # pool: [ACA factors (fp32) | dense exact blocks], in the storage dtype
         aca = (torch.cat(aca_pool_parts) if aca_pool_parts else
-               torch.zeros(0, dtype=torch.float32, device=dev))
-        aca_n = aca.numel()
-        self._aca_n = aca_n
-        pool = torch.cat([aca.to(tdt), dense[:max(dense_entries, 0)]]) if dense_entries else aca.to(tdt)
-        if pool.numel() == 0:
-            pool = torch.zeros(1, dtype=tdt, device=dev)
-        self._pool = pool
-
-        # device block list: LR leaves with rank > 0, then merged runs of
-        # exact leaves (same row range, adjacent column ranges, contiguous in
-        # the pool) with at least one nonzero
+               torch.zeros(1, dtype=torch.float32, device=dev))
+        self._pool = aca.to(tdt)
         lr = np.where((self._kind == LEAF_LOWRANK) & (self._rank > 0))[0]
-        run_r0, run_m, run_c0, run_n, run_off = [], [], [], [], []
-        prev = None
-        run_nnz = 0
-        for q, b in enumerate(exact):
-            r0b, mb = int(tree.start[ex_r[q]]), int(ex_m[q])
-            c0b, nb_ = int(tree.start[ex_c[q]]), int(ex_n[q])
-            if prev is not None and prev[0] == r0b and prev[1] == mb and prev[2] + prev[3] == c0b:
-                run_n[-1] += nb_
-                prev = (r0b, mb, prev[2], prev[3] + nb_)
-                run_nnz_list[-1] += int(self._leaf_nnz[b])
-                continue
-            if prev is None:
-                run_nnz_list = []
-            run_r0.append(r0b); run_m.append(mb); run_c0.append(c0b); run_n.append(nb_)
-            run_off.append(int(dense_off[q]))
-            run_nnz_list.append(int(self._leaf_nnz[b]))
-            prev = (r0b, mb, c0b, nb_)
-        keep = [i for i, z in enumerate(run_nnz_list)] if exact.size else []
-        keep = [i for i in keep if run_nnz_list[i] > 0]
-        ex_r0 = np.array([run_r0[i] for i in keep], np.int64)
-        ex_mm = np.array([run_m[i] for i in keep], np.int64)
-        ex_c0 = np.array([run_c0[i] for i in keep], np.int64)
-        ex_nn = np.array([run_n[i] for i in keep], np.int64)
-        ex_off = np.array([run_off[i] for i in keep], np.int64)
-        self.stats["dense_runs"] = int(ex_r0.size)
-        self._layout(lr, pool_off, aca_n, ex_r0, ex_mm, ex_c0, ex_nn, ex_off)
+        self._layout(lr, pool_off, ex_r0, ex_m, ex_c0, ex_n)
 
-    def _layout(self, lr, pool_off, aca_n, ex_r0, ex_mm, ex_c0, ex_nn, ex_off):
+    def _layout(self, lr, pool_off, ex_r0, ex_m, ex_c0, ex_n):
         """Panel layout consumed by libfluxgb's matvec kernels (matvec.cu)."""
         tree = self._tree
         dev = self.shape_model._device
         pool_off = np.asarray(pool_off, np.int64)
         N = self.num_faces
+        stream = _lib.stream_handle()
+
+        def d(a, dt):
+            a = np.asarray(a, dtype=dt)
+            return torch.as_tensor(a if a.size else np.zeros(1, dt), device=dev)
+
         # ---- low-rank blocks, grouped by column range (phase A)
         lr_r0 = tree.start[self._rows[lr]].astype(np.int64)
         lr_m = tree.size[self._rows[lr]].astype(np.int64)
@@ -572,25 +518,20 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         g_first = np.flatnonzero(newg)
         g_c0 = lr_c0[g_first]
         g_n = lr_n[g_first]
-        g_kz = np.bincount(gid, weights=lr_k, minlength=ng).astype(np.int64) if nlr else np.zeros(0, np.int64)
+        g_kz = (np.bincount(gid, weights=lr_k, minlength=ng).astype(np.int64) if nlr
+                else np.zeros(0, np.int64))
         g_ldv = (g_n + 7) // 8 * 8
         g_voff = np.zeros(ng + 1, np.int64)
         np.cumsum(g_kz * g_ldv, out=g_voff[1:])
         g_z0 = np.zeros(ng + 1, np.int64)
         np.cumsum(g_kz, out=g_z0[1:])
-        # each LR block's first Z row: group start + earlier members' ranks
-        cum_k = np.cumsum(lr_k) - lr_k
-        lr_z = cum_k - (np.cumsum(lr_k) - lr_k)[g_first][gid] + g_z0[gid] if nlr else np.zeros(0, np.int64)
+        lr_z = np.cumsum(lr_k) - lr_k          # groups are contiguous: first Z row
         self._num_zrows = int(g_z0[-1])
-        # stacked V^T rows: (pool offset, panel offset, length)
-        rows_k = lr_k
-        vr_blk = np.repeat(np.arange(nlr), rows_k)
-        vr_l = np.arange(rows_k.sum()) - np.repeat(np.cumsum(rows_k) - rows_k, rows_k)
+        vr_blk = np.repeat(np.arange(nlr), lr_k)
+        vr_l = np.arange(lr_k.sum()) - np.repeat(np.cumsum(lr_k) - lr_k, lr_k)
         vr_src = lr_v[vr_blk] + vr_l * lr_n[vr_blk]
-        vr_row_in_group = (lr_z[vr_blk] - g_z0[gid[vr_blk]]) + vr_l
-        vr_dst = g_voff[gid[vr_blk]] + vr_row_in_group * g_ldv[gid[vr_blk]]
+        vr_dst = g_voff[gid[vr_blk]] + (lr_z[vr_blk] - g_z0[gid[vr_blk]] + vr_l) * g_ldv[gid[vr_blk]]
         vr_n = lr_n[vr_blk]
-        # phase A items: column chunks of each group
         nchunk = (g_n + ITEM_COLS - 1) // ITEM_COLS
         a_grp = np.repeat(np.arange(ng), nchunk)
         ci = np.arange(nchunk.sum()) - np.repeat(np.cumsum(nchunk) - nchunk, nchunk)
@@ -599,63 +540,118 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         a_ex = (nchunk[a_grp] == 1).astype(np.uint8)
         self._needs_zero_z = bool((a_ex == 0).any())
         max_gt = int(((g_kz + 63) // 64).max()) if ng else 1
-        # ---- phase B: contributors (LR blocks: U^T rows -> Z rows; dense runs:
-        # D^T rows -> X rows), split by 64-row tile
-        c_r0 = np.concatenate([lr_r0, ex_r0]).astype(np.int64)
-        c_m = np.concatenate([lr_m, ex_mm]).astype(np.int64)
-        c_k = np.concatenate([lr_k, ex_nn]).astype(np.int64)
-        c_w = np.concatenate([lr_u, aca_n + ex_off]).astype(np.int64)
-        c_src = np.concatenate([lr_z, self._num_zrows + ex_c0]).astype(np.int64)
         ntiles = (N + TILE_ROWS - 1) // TILE_ROWS
-        t_first = c_r0 // TILE_ROWS
-        t_last = (c_r0 + c_m - 1) // TILE_ROWS
-        cnt = t_last - t_first + 1
-        pc = np.repeat(np.arange(c_r0.size), cnt)
-        pt = np.repeat(t_first, cnt) + (np.arange(cnt.sum()) - np.repeat(np.cumsum(cnt) - cnt, cnt))
-        o = np.argsort(pt, kind="stable")
-        pc, pt = pc[o], pt[o]
-        pk = c_k[pc]
-        L = np.bincount(pt, weights=pk, minlength=ntiles).astype(np.int64)
+
+        def tile_pairs(r0, m):
+            t_first = r0 // TILE_ROWS
+            cnt = (r0 + m - 1) // TILE_ROWS - t_first + 1
+            pc = np.repeat(np.arange(r0.size), cnt)
+            pt = np.repeat(t_first, cnt) + (np.arange(cnt.sum()) - np.repeat(np.cumsum(cnt) - cnt, cnt))
+            return pc, pt
+
+        # ---- phase B, low-rank part: (tile, LR block) pairs, k rows each
+        lpc, lpt = tile_pairs(lr_r0, lr_m)
+        o = np.argsort(lpt, kind="stable")
+        lpc, lpt = lpc[o], lpt[o]
+        lpk = lr_k[lpc]
+        L_lr = np.bincount(lpt, weights=lpk, minlength=ntiles).astype(np.int64)
+        # ---- phase B, near field: (tile, exact leaf) pairs, compacted columns
+        nex = ex_r0.size
+        tcsr = self._exact_csr
+        self._nf = None
+        if nex:
+            npc, npt = tile_pairs(ex_r0, ex_m)
+            o = np.argsort(npt, kind="stable")
+            npc, npt = npc[o], npt[o]
+            wpr = (ex_n + 31) // 32
+            moff = np.zeros(npc.size + 1, np.int64)
+            np.cumsum(wpr[npc], out=moff[1:])
+            self._nf = dict(
+                pair_q=d(npc, np.int32), pair_t0=d(npt * TILE_ROWS, np.int64),
+                pair_moff=d(moff[:-1], np.int64), leaf_r0=d(ex_r0, np.int64),
+                leaf_m=d(ex_m, np.int32), leaf_wpr=d(wpr, np.int32),
+                leaf_word_off=d(tcsr.word_off[:-1], np.int64),
+                leaf_row_off=d(tcsr.row_off[:-1], np.int64))
+            mask = torch.empty(max(int(moff[-1]), 1), dtype=torch.int32, device=dev)
+            cnt = torch.zeros(max(npc.size, 1), dtype=torch.int32, device=dev)
+            nf = self._nf
+            _lib.call("fgb_nf_pair_masks", _lib.ptr(nf["pair_q"]), _lib.ptr(nf["pair_t0"]),
+                      _lib.ptr(nf["pair_moff"]), npc.size, int(moff[-1]), _lib.ptr(nf["leaf_r0"]),
+                      _lib.ptr(nf["leaf_m"]), _lib.ptr(nf["leaf_wpr"]),
+                      _lib.ptr(nf["leaf_word_off"]), _lib.ptr(nf["leaf_row_off"]),
+                      _lib.ptr(tcsr.bits), _lib.ptr(mask), _lib.ptr(cnt), stream)
+            npk = cnt[:npc.size].cpu().numpy().astype(np.int64)
+            L_nf = np.bincount(npt, weights=npk, minlength=ntiles).astype(np.int64)
+        else:
+            npc = npt = npk = np.zeros(0, np.int64)
+            L_nf = np.zeros(ntiles, np.int64)
+            mask = None
+        L = L_lr + L_nf
         Lpad = (L + 31) // 32 * 32
         t_p0 = np.zeros(ntiles + 1, np.int64)
         np.cumsum(Lpad, out=t_p0[1:])
-        # pair panel offsets: tile start + running k within the tile
-        run = np.cumsum(pk) - pk
-        tile_start_run = np.zeros(ntiles, np.int64)
-        first_of_tile = np.ones(pt.size, bool)
-        first_of_tile[1:] = pt[1:] != pt[:-1]
-        tile_start_run[pt[first_of_tile]] = run[first_of_tile]
-        pair_p0 = t_p0[pt] + run - tile_start_run[pt]
-        # padding pairs (k = 0) at the end of every tile with padded rows
-        pad_t = np.flatnonzero(Lpad > L)
-        pad_p0 = t_p0[pad_t] + L[pad_t]
-        all_p0 = np.concatenate([pair_p0, pad_p0])
-        all_w = np.concatenate([c_w[pc], np.zeros(pad_t.size, np.int64)])
-        all_m = np.concatenate([c_m[pc], np.ones(pad_t.size, np.int64)])
-        all_shift = np.concatenate([pt * TILE_ROWS - c_r0[pc], np.zeros(pad_t.size, np.int64)])
-        all_k = np.concatenate([pk, np.zeros(pad_t.size, np.int64)])
+        total_rows = int(t_p0[-1])
+
+        def offsets_within_tile(pt, pk):
+            run = np.cumsum(pk) - pk
+            first = np.ones(pt.size, bool)
+            first[1:] = pt[1:] != pt[:-1]
+            start = np.zeros(ntiles, np.int64)
+            start[pt[first]] = run[first]
+            return run - start[pt]
+
+        lp0 = t_p0[lpt] + offsets_within_tile(lpt, lpk) if lpt.size else np.zeros(0, np.int64)
+        np0 = (t_p0[npt] + L_lr[npt] + offsets_within_tile(npt, npk)) if npt.size else np.zeros(0, np.int64)
+        # build-kernel pairs: LR pairs, plus one zero pair at every tile's
+        # first near-field / padding row (rows past a pair's k are zeroed)
+        tail_t = np.flatnonzero(Lpad > L_lr)
+        tail_p0 = t_p0[tail_t] + L_lr[tail_t]
+        all_p0 = np.concatenate([lp0, tail_p0])
+        all_w = np.concatenate([lr_u[lpc], np.zeros(tail_t.size, np.int64)])
+        all_m = np.concatenate([lr_m[lpc], np.ones(tail_t.size, np.int64)])
+        all_shift = np.concatenate([lpt * TILE_ROWS - lr_r0[lpc], np.zeros(tail_t.size, np.int64)])
+        all_k = np.concatenate([lpk, np.zeros(tail_t.size, np.int64)])
         oo = np.argsort(all_p0, kind="stable")
         all_p0, all_w, all_m, all_shift, all_k = (a[oo] for a in (all_p0, all_w, all_m, all_shift,
                                                                  all_k))
-        total_rows = int(t_p0[-1])
-        # source index of every panel row
+        # panel-row sources: LR rows -> Z rows (host), near-field rows -> X rows (device)
         src = np.zeros(total_rows, np.int64)
-        rk = pk
-        rows_pair = np.repeat(np.arange(pk.size), rk)
-        rows_l = np.arange(rk.sum()) - np.repeat(np.cumsum(rk) - rk, rk)
-        src[pair_p0[rows_pair] + rows_l] = c_src[pc[rows_pair]] + rows_l
-        if src.size and src.max() >= 2**31:
+        rows_pair = np.repeat(np.arange(lpk.size), lpk)
+        rows_l = np.arange(lpk.sum()) - np.repeat(np.cumsum(lpk) - lpk, lpk)
+        src[lp0[rows_pair] + rows_l] = lr_z[lpc[rows_pair]] + rows_l
+        src_d = d(src, np.int32)
+        if npk.size and npk.sum() > 0:
+            ndesc = int(npk.sum())
+            desc_off = np.zeros(npk.size + 1, np.int64)
+            np.cumsum(npk, out=desc_off[1:])
+            desc_pair = torch.empty(ndesc, dtype=torch.int32, device=dev)
+            desc_col = torch.empty(ndesc, dtype=torch.int32, device=dev)
+            desc_off_d = d(desc_off[:-1], np.int64)
+            nf = self._nf
+            _lib.call("fgb_nf_enumerate", _lib.ptr(nf["pair_q"]), _lib.ptr(nf["pair_t0"]),
+                      _lib.ptr(nf["pair_moff"]), npk.size, _lib.ptr(nf["leaf_wpr"]),
+                      _lib.ptr(mask), _lib.ptr(desc_off_d), _lib.ptr(desc_pair),
+                      _lib.ptr(desc_col), stream)
+            # panel row of each descriptor: pair start row + rank within the pair
+            dp = desc_pair.to(torch.int64)
+            np0_d = torch.as_tensor(np0, device=dev)
+            rank = torch.arange(ndesc, device=dev) - desc_off_d[dp]
+            desc_row = np0_d[dp] + rank
+            q_of = nf["pair_q"].to(torch.int64)[dp]
+            c0_d = torch.as_tensor(ex_c0, device=dev)
+            src_d[desc_row] = (self._num_zrows + c0_d[q_of] + desc_col.to(torch.int64)).to(torch.int32)
+            self._nf.update(desc_pair=desc_pair, desc_col=desc_col, desc_row=desc_row)
+            self._num_desc = ndesc
+        else:
+            self._num_desc = 0
+        del mask
+        if src.size and (self._num_zrows + N) >= 2**31:
             raise OverflowError("operator too large for 32-bit panel sources")
-
-        def d(a, dt):
-            a = np.asarray(a, dtype=dt)
-            return torch.as_tensor(a if a.size else np.zeros(1, dt), device=dev)
-
         self._dev = dict(
             g_c0=d(g_c0, np.int32), g_n=d(g_n, np.int32), g_kz=d(g_kz, np.int32),
             g_ldv=d(g_ldv, np.int32), g_voff=d(g_voff[:-1], np.int64), g_z0=d(g_z0[:-1], np.int64),
             a_grp=d(a_grp, np.int32), a_j0=d(a_j0, np.int32), a_j1=d(a_j1, np.int32),
-            a_excl=d(a_ex, np.uint8), t_p0=d(t_p0, np.int64), src=d(src, np.int32))
+            a_excl=d(a_ex, np.uint8), t_p0=d(t_p0, np.int64), src=src_d)
         self._build_dev = dict(
             vr_src=d(vr_src, np.int64), vr_dst=d(vr_dst, np.int64), vr_n=d(vr_n, np.int32),
             p_p0=d(all_p0, np.int64), p_w=d(all_w, np.int64), p_m=d(all_m, np.int32),
@@ -664,23 +660,27 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         self._vpanel_size = int(g_voff[-1])
         self._num_vrows = int(vr_src.size)
         self._num_pairs = int(all_p0.size)
-        desc = fgb_op_desc()
-        for key in ("g_c0", "g_n", "g_kz", "g_ldv", "g_voff", "g_z0", "a_grp", "a_j0", "a_j1",
-                    "a_excl", "t_p0", "src"):
-            setattr(desc, key, self._dev[key].data_ptr())
-        desc.num_items = int(a_grp.size)
-        desc.num_tiles = ntiles
-        desc.N = N
-        desc.num_zrows = self._num_zrows
-        desc.max_group_tiles = max_gt
-        self._desc = desc
+        self._desc = self._make_desc(int(a_grp.size), ntiles, max_gt)
         self._lr_blocks = lr
         self._lr_u, self._lr_v = lr_u, lr_v
         self._panels = {}
         self.stats.update(num_items=int(a_grp.size), num_tiles=ntiles, groups=ng,
-                          panel_rows=total_rows, tile_pairs=int(pk.size),
+                          panel_rows=total_rows, nearfield_rows=int(L_nf.sum()),
+                          lowrank_rows=int(L_lr.sum()), max_group_tiles=max_gt,
                           pool_entries=int(self._pool.numel()), zrows=self._num_zrows,
                           operator_entries=int(total_rows * TILE_ROWS + g_voff[-1]))
+
+    def _make_desc(self, num_items, ntiles, max_gt):
+        desc = fgb_op_desc()
+        for key in ("g_c0", "g_n", "g_kz", "g_ldv", "g_voff", "g_z0", "a_grp", "a_j0", "a_j1",
+                    "a_excl", "t_p0", "src"):
+            setattr(desc, key, self._dev[key].data_ptr())
+        desc.num_items = num_items
+        desc.num_tiles = ntiles
+        desc.N = self.num_faces
+        desc.num_zrows = self._num_zrows
+        desc.max_group_tiles = max_gt
+        return desc
 
     # -- device products --------------------------------------------------
     def pool(self, precision):
@@ -698,6 +698,10 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         for p_ in precisions:
             self.panels(p_)
         self._pool = self._pool.cpu()
+        tc = self._exact_csr
+        if tc is not None:
+            tc.data, tc.indptr, tc.bits, tc.indices = (tc.data.cpu(), tc.indptr.cpu(),
+                                                       tc.bits.cpu(), tc.indices.cpu())
         torch.cuda.empty_cache()
 
     def panels(self, precision):
@@ -727,6 +731,22 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         _lib.call(f"fgb_build_vpanel_{pin}_{pout}", _lib.ptr(src), self._num_vrows,
                   _lib.ptr(b["vr_src"]), _lib.ptr(b["vr_dst"]), _lib.ptr(b["vr_n"]),
                   _lib.ptr(vpanel), st)
+        if self._num_desc:
+            tc = self._exact_csr
+            if tc.data.device != dev:
+                tc.data, tc.indptr, tc.bits = tc.data.to(dev), tc.indptr.to(dev), tc.bits.to(dev)
+            data = tc.data
+            din = "f64" if data.dtype == torch.float64 else "f32"
+            if din == "f32" and pout == "f64":
+                data = data.to(torch.float64)
+                din = "f64"
+            nf = self._nf
+            _lib.call(f"fgb_nf_fill_{din}_{pout}", _lib.ptr(nf["pair_q"]), _lib.ptr(nf["pair_t0"]),
+                      int(nf["pair_q"].numel()), _lib.ptr(nf["leaf_r0"]), _lib.ptr(nf["leaf_m"]),
+                      _lib.ptr(nf["leaf_wpr"]), _lib.ptr(nf["leaf_word_off"]),
+                      _lib.ptr(nf["leaf_row_off"]), _lib.ptr(tc.bits), _lib.ptr(tc.indptr),
+                      _lib.ptr(data), _lib.ptr(nf["desc_pair"]), _lib.ptr(nf["desc_col"]),
+                      _lib.ptr(nf["desc_row"]), self._num_desc, _lib.ptr(panel), st)
         self._panels[precision] = (panel, vpanel)
         return panel, vpanel
 
@@ -936,6 +956,8 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         with open(path, 'rb') as f:
             return pickle.load(f)
 
+    _DEV_DICTS = ("_dev", "_build_dev", "_nf")
+
     def __getstate__(self):
         st = dict(self.__dict__)
         st["_root_cache"] = None
@@ -943,50 +965,51 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         st["_panels"] = {}
         for key in ("_pool", "_perm_d", "_iperm_d"):
             st[key] = st[key].cpu()
-        st["_dev"] = {k: v.cpu() for k, v in st["_dev"].items()}
-        st["_build_dev"] = {k: v.cpu() for k, v in st["_build_dev"].items()}
-        if st.get("_exact_csr") is not None:
-            tcsr, ex = st["_exact_csr"]
-            st["_exact_csr"] = ({"indptr": tcsr.indptr.cpu(), "indices": tcsr.indices.cpu(),
-                                 "data": tcsr.data.cpu(), "row_off": tcsr.row_off}, ex)
+        for key in self._DEV_DICTS:
+            if st.get(key) is not None:
+                st[key] = {k: v.cpu() for k, v in st[key].items()}
+        tc = st.get("_exact_csr")
+        if tc is not None:
+            st["_exact_csr"] = {"indptr": tc.indptr.cpu(), "indices": tc.indices.cpu(),
+                                "data": tc.data.cpu(), "row_off": tc.row_off,
+                                "bits": tc.bits.cpu(), "word_off": tc.word_off}
         return st
 
     def __setstate__(self, st):
+        from .form_factors import TileCSR
         self.__dict__.update(st)
         dev = self.shape_model._device
         for key in ("_pool", "_perm_d", "_iperm_d"):
             setattr(self, key, getattr(self, key).to(dev))
-        self._dev = {k: v.to(dev) for k, v in self._dev.items()}
-        self._build_dev = {k: v.to(dev) for k, v in self._build_dev.items()}
+        for key in self._DEV_DICTS:
+            if getattr(self, key, None) is not None:
+                setattr(self, key, {k: v.to(dev) for k, v in getattr(self, key).items()})
         if self._exact_csr is not None:
-            d, ex = self._exact_csr
-            from .form_factors import TileCSR
-            self._exact_csr = (TileCSR(d["indptr"].to(dev), d["indices"].to(dev), d["data"].to(dev),
-                                       d["row_off"], 0, 0), ex)
-        desc = fgb_op_desc()
-        for key in ("g_c0", "g_n", "g_kz", "g_ldv", "g_voff", "g_z0", "a_grp", "a_j0", "a_j1",
-                    "a_excl", "t_p0", "src"):
-            setattr(desc, key, self._dev[key].data_ptr())
-        desc.num_items = int(self.stats["num_items"])
-        desc.num_tiles = int(self.stats["num_tiles"])
-        desc.N = self.num_faces
-        desc.num_zrows = self._num_zrows
-        desc.max_group_tiles = int(((self._dev["g_kz"].cpu().numpy().astype(np.int64) + 63)
-                                    // 64).max())
-        self._desc = desc
+            dct = self._exact_csr
+            self._exact_csr = TileCSR(dct["indptr"].to(dev), dct["indices"].to(dev),
+                                      dct["data"].to(dev), dct["row_off"], 0, 0,
+                                      dct["bits"].to(dev), dct["word_off"])
+        self._desc = self._make_desc(int(self.stats["num_items"]), int(self.stats["num_tiles"]),
+                                     int(self.stats["max_group_tiles"]))
 
     # -- leaf data for the Python block objects --------------------------
     def _leaf_dense(self, b):
-        """Dense (m x n) array of an exact leaf, in the shape dtype."""
+        """Dense (m x n) array of an exact leaf in the shape dtype, rows and
+        columns in the reference's ascending-id order."""
         tree = self._tree
-        m, n = tree.size[self._rows[b]], tree.size[self._cols[b]]
-        off = self._dense_off.get(int(b))
-        if off is None:
-            return np.zeros((m, n), dtype=self.dtype)
-        aca_n = self._aca_n
-        w = self._pool[aca_n + off: aca_n + off + m * n].cpu().numpy()
-        mat = w.reshape(n, m).T.astype(self.dtype)
-        # cluster order -> the reference's ascending-id order of the block
+        m, n = int(tree.size[self._rows[b]]), int(tree.size[self._cols[b]])
+        q = self._exact_index.get(int(b))
+        mat = np.zeros((m, n), dtype=self.dtype)
+        tc = self._exact_csr
+        if q is None or tc is None:
+            return mat
+        r0, r1 = int(tc.row_off[q]), int(tc.row_off[q + 1])
+        ip = tc.indptr[r0:r1 + 1].cpu().numpy()
+        a, bnd = int(ip[0]), int(ip[-1])
+        cols = tc.indices[a:bnd].cpu().numpy()
+        vals = tc.data[a:bnd].cpu().numpy()
+        rows = np.repeat(np.arange(m), np.diff(ip))
+        mat[rows, cols] = vals
         ri = np.argsort(tree.indices(self._rows[b]), kind="stable")
         ci = np.argsort(tree.indices(self._cols[b]), kind="stable")
         return mat[ri][:, ci]

@@ -84,13 +84,13 @@ __global__ void ff_count_kernel(BvhView b, const R* __restrict__ P, const R* __r
   }
 }
 
-template <class R, class IDX>
+template <class R, class IDX, class RO>
 __global__ void ff_fill_kernel(const R* __restrict__ P, const R* __restrict__ A,
                                const R* __restrict__ N, const long long* __restrict__ I,
                                const long long* __restrict__ J, TileArgs ta,
                                const unsigned* __restrict__ bits,
                                const long long* __restrict__ indptr, IDX* __restrict__ indices,
-                               R* __restrict__ data) {
+                               RO* __restrict__ data) {
   const int lane = threadIdx.x & 31;
   const long long warps_total = (long long)gridDim.x * (blockDim.x >> 5);
   const long long rows_total = ta.row_off[ta.T];
@@ -113,7 +113,7 @@ __global__ void ff_fill_kernel(const R* __restrict__ P, const R* __restrict__ A,
         R num = ff_num(P, N, i, j);
         long long q = pos + __popc(word & lt);
         indices[q] = (IDX)col;
-        data[q] = ff_value(P, A, i, j, num);
+        data[q] = (RO)ff_value(P, A, i, j, num);
       }
       pos += __popc(word);
     }
@@ -144,16 +144,16 @@ int ff_count(const void* bvh, const R* P, const R* N, const R* A, const long lon
   return FGB_OK;
 }
 
-template <class R, class IDX>
+template <class R, class IDX, class RO>
 int ff_fill(const R* P, const R* N, const R* A, const long long* I, const long long* J,
             const long long* row0, const long long* nrows, const long long* col0,
             const long long* ncols, const long long* word_off, const long long* row_off,
             long long T, long long total_rows, const unsigned* bits, const long long* indptr,
-            IDX* indices, R* data, void* stream) {
+            IDX* indices, RO* data, void* stream) {
   if (T < 1) { set_error("need at least one tile"); return FGB_BAD_ARG; }
   if (total_rows == 0) return FGB_OK;
   TileArgs ta{row0, nrows, col0, ncols, word_off, row_off, T};
-  ff_fill_kernel<R, IDX><<<grid_for(total_rows * 32, 128, 152LL * 64), 128, 0, as_stream(stream)>>>(
+  ff_fill_kernel<R, IDX, RO><<<grid_for(total_rows * 32, 128, 152LL * 64), 128, 0, as_stream(stream)>>>(
       P, A, N, I, J, ta, bits, indptr, indices, data);
   FGB_LAUNCH_CHECK("ff_fill_kernel");
   return FGB_OK;
@@ -192,8 +192,20 @@ int fgb_ff_fill_f64(const double* P, const double* N, const double* A, const lon
                     const long long* row_off, long long num_tiles, long long total_rows,
                     const unsigned* bits, const long long* indptr, int* indices, double* data,
                     void* stream) {
-  return fgb::ff_fill<double, int>(P, N, A, I, J, row0, nrows, col0, ncols, word_off, row_off,
-                                   num_tiles, total_rows, bits, indptr, indices, data, stream);
+  return fgb::ff_fill<double, int, double>(P, N, A, I, J, row0, nrows, col0, ncols, word_off,
+                                           row_off, num_tiles, total_rows, bits, indptr, indices,
+                                           data, stream);
+}
+
+int fgb_ff_fill_f64_to_f32(const double* P, const double* N, const double* A, const long long* I,
+                           const long long* J, const long long* row0, const long long* nrows,
+                           const long long* col0, const long long* ncols,
+                           const long long* word_off, const long long* row_off,
+                           long long num_tiles, long long total_rows, const unsigned* bits,
+                           const long long* indptr, int* indices, float* data, void* stream) {
+  return fgb::ff_fill<double, int, float>(P, N, A, I, J, row0, nrows, col0, ncols, word_off,
+                                          row_off, num_tiles, total_rows, bits, indptr, indices,
+                                          data, stream);
 }
 
 int fgb_ff_fill_f32(const float* P, const float* N, const float* A, const long long* I,
@@ -202,8 +214,9 @@ int fgb_ff_fill_f32(const float* P, const float* N, const float* A, const long l
                     const long long* row_off, long long num_tiles, long long total_rows,
                     const unsigned* bits, const long long* indptr, int* indices, float* data,
                     void* stream) {
-  return fgb::ff_fill<float, int>(P, N, A, I, J, row0, nrows, col0, ncols, word_off, row_off,
-                                  num_tiles, total_rows, bits, indptr, indices, data, stream);
+  return fgb::ff_fill<float, int, float>(P, N, A, I, J, row0, nrows, col0, ncols, word_off,
+                                         row_off, num_tiles, total_rows, bits, indptr, indices,
+                                         data, stream);
 }
 
 }  // extern "C"

@@ -25,16 +25,20 @@ class TileCSR:
     tile t are [row_off[t], row_off[t+1]) of ``indptr``; column indices are
     local to the tile."""
 
-    def __init__(self, indptr, indices, data, row_off, kept_pairs, near_edge_pairs):
+    def __init__(self, indptr, indices, data, row_off, kept_pairs, near_edge_pairs, bits=None,
+                 word_off=None):
         self.indptr = indptr
         self.indices = indices
         self.data = data
         self.row_off = row_off
         self.kept_pairs = kept_pairs
         self.near_edge_pairs = near_edge_pairs
+        self.bits = bits          # visible-pair bitmask (kept when asked for)
+        self.word_off = word_off  # per-tile offsets into bits
 
 
-def ff_tiles(shape_model, I_d, J_d, row0, nrows, col0, ncols, eps=None) -> TileCSR:
+def ff_tiles(shape_model, I_d, J_d, row0, nrows, col0, ncols, eps=None, keep_bits=False,
+             out_dtype=None) -> TileCSR:
     """Evaluate the form factors of a list of tiles on the device.
 
     I_d, J_d: int64 device tensors of facet ids; tile t covers rows
@@ -78,15 +82,21 @@ def ff_tiles(shape_model, I_d, J_d, row0, nrows, col0, ncols, eps=None) -> TileC
     nnz = int(indptr[-1].item())
     if int(flags.item()) & _lib.FLAG_STACK_OVERFLOW:
         raise RuntimeError("BVH traversal stack overflow")
-    tdt = P.dtype
+    tdt = P.dtype if out_dtype is None else out_dtype
     indices = torch.empty(max(nnz, 1), dtype=torch.int32, device=dev)
     data = torch.empty(max(nnz, 1), dtype=tdt, device=dev)
-    _lib.call(f"fgb_ff_fill_{sfx}", _lib.ptr(P), _lib.ptr(N), _lib.ptr(A), _lib.ptr(I_d),
+    fill = f"fgb_ff_fill_{sfx}"
+    if tdt != P.dtype:
+        if not (P.dtype == torch.float64 and tdt == torch.float32):
+            raise ValueError("unsupported output dtype")
+        fill = "fgb_ff_fill_f64_to_f32"
+    _lib.call(fill, _lib.ptr(P), _lib.ptr(N), _lib.ptr(A), _lib.ptr(I_d),
               _lib.ptr(J_d), _lib.ptr(t_row0), _lib.ptr(t_nrows), _lib.ptr(t_col0),
               _lib.ptr(t_ncols), _lib.ptr(t_woff), _lib.ptr(t_roff), T, R, _lib.ptr(bits),
               _lib.ptr(indptr), _lib.ptr(indices), _lib.ptr(data), stream)
     st = stats.cpu().numpy()
-    return TileCSR(indptr, indices[:nnz], data[:nnz], row_off, int(st[0]), int(st[1]))
+    return TileCSR(indptr, indices[:nnz], data[:nnz], row_off, int(st[0]), int(st[1]),
+                   bits if keep_bits else None, word_off if keep_bits else None)
 
 
 def _as_index(x, n):

@@ -220,6 +220,12 @@ int fgb_ff_fill_f64(const double* P, const double* N, const double* A, const lon
                     const long long* row_off, long long num_tiles, long long total_rows,
                     const unsigned* bits, const long long* indptr, int* indices, double* data,
                     void* stream);
+int fgb_ff_fill_f64_to_f32(const double* P, const double* N, const double* A, const long long* I,
+                           const long long* J, const long long* row0, const long long* nrows,
+                           const long long* col0, const long long* ncols,
+                           const long long* word_off, const long long* row_off,
+                           long long num_tiles, long long total_rows, const unsigned* bits,
+                           const long long* indptr, int* indices, float* data, void* stream);
 int fgb_ff_fill_f32(const float* P, const float* N, const float* A, const long long* I,
                     const long long* J, const long long* row0, const long long* nrows,
                     const long long* col0, const long long* ncols, const long long* word_off,
@@ -347,6 +353,59 @@ int fgb_build_vpanel_f64_f32(const double* pool, long long num_rows, const long 
                            const long long* row_dst, const int* row_n, void* vpanel, void* stream);
 int fgb_build_vpanel_f64_bf16(const double* pool, long long num_rows, const long long* row_src,
                            const long long* row_dst, const int* row_n, void* vpanel, void* stream);
+
+
+/* ------------------------------------------ near-field panels (a7, a9) */
+/*
+ * Column-compacted phase-B panel rows of the exact leaves, built from the
+ * pair kernel's bitmask and CSR (fgb_ff_count_* / fgb_ff_fill_*) — the exact
+ * counterpart of the reference's dense / CSR leaf blocks
+ * (src/flux/compressed_form_factors.py:151-229, chosen at :330-341).  Pair p
+ * = (64-row tile starting at pair_t0[p], exact leaf pair_q[p]); leaves give
+ * their first cluster row, rows, mask words per row and offsets into the
+ * bitmask / CSR.  fgb_nf_pair_masks ORs the tile's row masks (count[p] must
+ * be zeroed); fgb_nf_enumerate writes one (pair, column) descriptor per set
+ * bit from desc_off[p]; fgb_nf_fill_* writes 64 weights per descriptor at
+ * panel row desc_row[d].
+ */
+int fgb_nf_pair_masks(const int* pair_q, const long long* pair_t0, const long long* pair_moff,
+                      long long num_pairs, long long total_words, const long long* leaf_r0,
+                      const int* leaf_m, const int* leaf_wpr, const long long* leaf_word_off,
+                      const long long* leaf_row_off, const unsigned* bits, unsigned* mask,
+                      int* count, void* stream);
+int fgb_nf_enumerate(const int* pair_q, const long long* pair_t0, const long long* pair_moff,
+                     long long num_pairs, const int* leaf_wpr, const unsigned* mask,
+                     const long long* desc_off, int* desc_pair, int* desc_col, void* stream);
+int fgb_nf_fill_f32_f32(const int* pair_q, const long long* pair_t0, long long num_pairs,
+                        const long long* leaf_r0, const int* leaf_m, const int* leaf_wpr,
+                        const long long* leaf_word_off, const long long* leaf_row_off,
+                        const unsigned* bits, const long long* indptr, const float* data,
+                        const int* desc_pair, const int* desc_col, const long long* desc_row,
+                        long long num_desc, void* panel, void* stream);
+int fgb_nf_fill_f32_bf16(const int* pair_q, const long long* pair_t0, long long num_pairs,
+                        const long long* leaf_r0, const int* leaf_m, const int* leaf_wpr,
+                        const long long* leaf_word_off, const long long* leaf_row_off,
+                        const unsigned* bits, const long long* indptr, const float* data,
+                        const int* desc_pair, const int* desc_col, const long long* desc_row,
+                        long long num_desc, void* panel, void* stream);
+int fgb_nf_fill_f64_f64(const int* pair_q, const long long* pair_t0, long long num_pairs,
+                        const long long* leaf_r0, const int* leaf_m, const int* leaf_wpr,
+                        const long long* leaf_word_off, const long long* leaf_row_off,
+                        const unsigned* bits, const long long* indptr, const double* data,
+                        const int* desc_pair, const int* desc_col, const long long* desc_row,
+                        long long num_desc, void* panel, void* stream);
+int fgb_nf_fill_f64_f32(const int* pair_q, const long long* pair_t0, long long num_pairs,
+                        const long long* leaf_r0, const int* leaf_m, const int* leaf_wpr,
+                        const long long* leaf_word_off, const long long* leaf_row_off,
+                        const unsigned* bits, const long long* indptr, const double* data,
+                        const int* desc_pair, const int* desc_col, const long long* desc_row,
+                        long long num_desc, void* panel, void* stream);
+int fgb_nf_fill_f64_bf16(const int* pair_q, const long long* pair_t0, long long num_pairs,
+                        const long long* leaf_r0, const int* leaf_m, const int* leaf_wpr,
+                        const long long* leaf_word_off, const long long* leaf_row_off,
+                        const unsigned* bits, const long long* indptr, const double* data,
+                        const int* desc_pair, const int* desc_col, const long long* desc_row,
+                        long long num_desc, void* panel, void* stream);
 
 /* --------------------------------------------- solve kernels (a10-a12) */
 /*

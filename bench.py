@@ -185,6 +185,9 @@ def main():
     if args.impl == "reference":
         run_reference(args)
         return
+    # the operator and the solver's buffers take most of the device: let the
+    # caching allocator grow segments instead of fragmenting
+    os.environ.setdefault("PYTORCH_CUDA_ALLOC_CONF", "expandable_segments:True")
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -294,16 +297,23 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
     from fluxpy_gb300.form_factors import get_form_factor_matrix
     from fluxpy_gb300.solve import solve_radiosity, solve_radiosity_batched
     out = {}
-    N, K = Ep.shape
+    N, K_all = Ep.shape
     stream = torch.cuda.current_stream()
-    # ---- dominant kernels, timed alone with CUDA events
-    Xb = (RHO * Ep).to(torch.bfloat16)
-    X32 = (RHO * Ep).contiguous()
+    torch.cuda.empty_cache()
+    # ---- dominant kernels, timed alone with CUDA events, on the column
+    # block the solver works on (it solves the 1,024 columns in blocks that
+    # fit in memory)
+    from fluxpy_gb300.solve import _auto_chunk
+    K = min(K_all, _auto_chunk(FF, N, K_all))
+    Ek = Ep[:, :K].contiguous()
+    Xb = (RHO * Ek).to(torch.bfloat16)
+    X32 = (RHO * Ek).contiguous()
     Z32 = torch.empty((max(FF._num_zrows, 1), K), dtype=torch.float32, device=dev)
     Zb = torch.empty((max(FF._num_zrows, 1), K), dtype=torch.bfloat16, device=dev)
-    Y = torch.empty_like(Ep)
+    Y = torch.empty_like(Ek)
     panel_b, vpanel_b = FF.panels("bf16")
     panel_f, vpanel_f = FF.panels("fp32")
+    flags = FF.device_flags()
 
     def t_events(fn, reps=5):
         fn()
@@ -319,8 +329,13 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
 
     def bf16(phases):
         _lib.call("fgb_matmat_bf16", C.byref(FF._desc), _lib.ptr(panel_b), _lib.ptr(vpanel_b),
-                  _lib.ptr(Xb), _lib.ptr(Z32), _lib.ptr(Zb), _lib.ptr(Y), K, _lib.ptr(Ep), 1.0,
+                  _lib.ptr(Xb), _lib.ptr(Z32), _lib.ptr(Zb), _lib.ptr(Y), K, _lib.ptr(Ek), 1.0,
                   int(FF._needs_zero_z), phases, _lib.stream_handle())
+
+    def bf16_tc_b():
+        _lib.call("fgb_matmat_bf16_tc_phase_b", C.byref(FF._desc), _lib.ptr(panel_b),
+                  _lib.ptr(Xb), _lib.ptr(Zb), _lib.ptr(Y), K, _lib.ptr(Ek), 1.0,
+                  _lib.ptr(flags), _lib.stream_handle())
 
     def f32(phases):
         _lib.call("fgb_matmat_f32", C.byref(FF._desc), _lib.ptr(panel_f), _lib.ptr(vpanel_f),
@@ -328,7 +343,9 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
                   int(FF._needs_zero_z), phases, _lib.stream_handle())
 
     tA = t_events(lambda: bf16(1))
-    tB = t_events(lambda: bf16(2))
+    tB = t_events(bf16_tc_b)
+    tB_mma = t_events(lambda: bf16(2))
+    FF.check_device_flags()
     tA32 = t_events(lambda: f32(1))
     tB32 = t_events(lambda: f32(2))
     # algorithmic bytes per launch: every stored weight read once, every
@@ -358,14 +375,26 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
             "phaseA_f32": (tA32, vA * 4 + xA * 4 + zrows * K * 4, flops_A),
             "phaseB_f32": (tB32, wB * 4 + srcB * 4 + N * K * 4, flops_B)}
     t_ms, byts, fl = kern[dom]
-    achieved = byts / (t_ms * 1e-3) / 1e9
-    out["roofline"] = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": hbm,
-                       "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
-                       "peak_source": src, "algorithmic_bytes": byts, "ms_per_launch": t_ms,
-                       "tensor_tflops": fl / (t_ms * 1e-3) / 1e12 if "bf16" in dom else None,
-                       "tensor_peak_tflops": tf}
-    out["kernel_ms"] = {"phaseA_bf16": tA, "phaseB_bf16": tB, "phaseA_f32": tA32,
-                        "phaseB_f32": tB32, "per_solve_ms": per_solve}
+    gbs = byts / (t_ms * 1e-3) / 1e9
+    tfl = fl / (t_ms * 1e-3) / 1e12
+    if "bf16" in dom:
+        # BF16 tensor-core GEMM over the panels: bounded by the tensor pipe
+        out["roofline"] = {"kernel": dom, "bound": "tensor", "achieved": tfl, "peak": tf,
+                           "unit": "TFLOP/s", "frac": tfl / tf, "traffic": None,
+                           "peak_source": src, "algorithmic_flops": fl,
+                           "algorithmic_bytes": byts, "ms_per_launch": t_ms,
+                           "hbm_gbs_algorithmic": gbs, "hbm_peak": hbm}
+    else:
+        out["roofline"] = {"kernel": dom, "bound": "hbm", "achieved": gbs, "peak": hbm,
+                           "unit": "GB/s", "frac": gbs / hbm, "traffic": None,
+                           "peak_source": src, "algorithmic_bytes": byts,
+                           "algorithmic_flops": fl, "ms_per_launch": t_ms,
+                           "fp32_tflops": tfl}
+    out["kernel_ms"] = {"columns": K, "phaseA_bf16": tA, "phaseB_bf16_tc": tB,
+                        "phaseB_bf16_mma_sync": tB_mma, "phaseA_f32": tA32, "phaseB_f32": tB32,
+                        "per_solve_ms": per_solve}
+    del Xb, X32, Z32, Zb, Y, Ek
+    torch.cuda.empty_cache()
     # ---- plain FP32 GPU paths
     st = {}
     torch.cuda.synchronize()

@@ -35,6 +35,7 @@ FLAG_PREDCORR_MAX = 1 << 5
 FLAG_STACK_OVERFLOW = 1 << 6
 FLAG_INDEX_RANGE = 1 << 7
 FLAG_RANK_CAP = 1 << 8
+FLAG_DEVICE_TIMEOUT = 1 << 9
 
 P = C.c_void_p
 I32 = C.c_int
@@ -102,6 +103,7 @@ SIGNATURES: dict[str, list] = {
     "fgb_matvec_f32_f64": [P, P, P, P, P, P, P, F64, I32, P],
     "fgb_matmat_f32": [P, P, P, P, P, P, I32, P, F32, I32, I32, P],
     "fgb_matmat_bf16": [P, P, P, P, P, P, P, I32, P, F32, I32, I32, P],
+    "fgb_matmat_bf16_tc_phase_b": [P, P, P, P, P, I32, P, F32, P, P],
     # solve (a10-a12)
     "fgb_scale_rows_f32": [P, P, F32, P, I64, I32, P],
     "fgb_scale_rows_bf16": [P, P, F32, P, I64, I32, P],

@@ -166,6 +166,9 @@ class fgb_op_desc(C.Structure):
 
 TILE_ROWS = 64
 ITEM_COLS = 2048
+# panel rows per tile are padded to this multiple (the tensor-core phase-B
+# kernel consumes 64 panel rows per pipeline stage)
+PANEL_ALIGN = 64
 
 
 def _nbytes_csr(nnz, m, itemsize):
@@ -587,7 +590,7 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
             L_nf = np.zeros(ntiles, np.int64)
             mask = None
         L = L_lr + L_nf
-        Lpad = (L + 31) // 32 * 32
+        Lpad = (L + PANEL_ALIGN - 1) // PANEL_ALIGN * PANEL_ALIGN
         t_p0 = np.zeros(ntiles + 1, np.int64)
         np.cumsum(Lpad, out=t_p0[1:])
         total_rows = int(t_p0[-1])
@@ -814,7 +817,7 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
             return self._matmat_bf16(Xp, out=out, add=add, alpha=alpha, Z=Z)
         raise ValueError(precision)
 
-    def _matmat_bf16(self, Xp, out=None, add=None, alpha=1.0, Z=None):
+    def _matmat_bf16(self, Xp, out=None, add=None, alpha=1.0, Z=None, engine="tc"):
         K = Xp.shape[1]
         Xb = Xp.to(torch.bfloat16).contiguous()
         if out is None:
@@ -822,11 +825,42 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         if Z is None:
             Z = torch.empty((max(self._num_zrows, 1), K), dtype=torch.float32, device=Xp.device)
         Zb = torch.empty((max(self._num_zrows, 1), K), dtype=torch.bfloat16, device=Xp.device)
-        panel, vpanel = self.panels("bf16")
-        _lib.call("fgb_matmat_bf16", C.byref(self._desc), _lib.ptr(panel), _lib.ptr(vpanel),
-                  _lib.ptr(Xb), _lib.ptr(Z), _lib.ptr(Zb), _lib.ptr(out), K, _lib.ptr(add),
-                  float(alpha), int(self._needs_zero_z), 3, _lib.stream_handle())
+        self.bf16_product(Xb, Z, Zb, out, add, alpha, engine)
         return out
+
+    def bf16_product(self, Xb, Z, Zb, Y, add=None, alpha=1.0, engine="tc"):
+        """Y = add + alpha F X with BF16 operands (X: N x K bf16, K % 8 == 0)
+        and FP32 accumulation, in cluster order; Z (FP32) and Zb (BF16) are
+        num_zrows x K scratch.  engine 'tc': phase B on the tcgen05 tensor
+        cores (TMEM accumulators); 'mma': both phases with mma.sync."""
+        K = Xb.shape[1]
+        panel, vpanel = self.panels("bf16")
+        st = _lib.stream_handle()
+        phases = 1 if engine == "tc" else 3
+        _lib.call("fgb_matmat_bf16", C.byref(self._desc), _lib.ptr(panel), _lib.ptr(vpanel),
+                  _lib.ptr(Xb), _lib.ptr(Z), _lib.ptr(Zb), _lib.ptr(Y), K, _lib.ptr(add),
+                  float(alpha), int(self._needs_zero_z), phases, st)
+        if engine == "tc":
+            _lib.call("fgb_matmat_bf16_tc_phase_b", C.byref(self._desc), _lib.ptr(panel),
+                      _lib.ptr(Xb), _lib.ptr(Zb), _lib.ptr(Y), K, _lib.ptr(add), float(alpha),
+                      _lib.ptr(self.device_flags()), st)
+        return Y
+
+    def device_flags(self):
+        """Device status word (FGB_FLAG_*) of the operator's kernels."""
+        f = getattr(self, "_flags_d", None)
+        if f is None or f.device != self._perm_d.device:
+            f = self._flags_d = torch.zeros(1, dtype=torch.int32, device=self._perm_d.device)
+        return f
+
+    def check_device_flags(self):
+        """Raise if a kernel of this operator reported a failure (synchronises)."""
+        f = int(self.device_flags().item())
+        if f:
+            self._flags_d.zero_()
+            if f & _lib.FLAG_DEVICE_TIMEOUT:
+                raise RuntimeError("tensor-core product: a bounded device wait ran out")
+            raise RuntimeError(f"operator kernel reported flags 0x{f:x}")
 
     def _default_precision(self):
         return "fp64" if self._pool.dtype == torch.float64 else "fp32"

@@ -228,7 +228,7 @@ def _auto_chunk(FF, N, K):
 
 def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_iter=200,
                             inner=3, E_is_permuted=False, return_permuted=False, stats=None,
-                            chunk=None):
+                            chunk=None, inner0=4, engine="tc"):
     """Right-placement radiosity solve for K sun directions at once.
 
     FF: CompressedFormFactorMatrix; E: (N, K) device tensor (facet order, or
@@ -236,10 +236,15 @@ def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_
     precision:
       'fp32'         plain FP32 Jacobi, FP32 CUDA-core matmat, until the
                      per-column update max|B1 - B| <= rtol * max|E[:, k]|;
-      'bf16-refine'  FP32 residual R = E - (B - F rho B) (FP32 factors),
-                     correction by `inner` BF16 tensor-core Jacobi sweeps
-                     D <- R + F_bf16(rho D), until max|R[:, k]| <= rtol *
-                     max|E[:, k]| for every column.
+      'bf16-refine'  iterative refinement from B = 0: the first correction
+                     solves D = E + F_bf16(rho D) by `inner0` BF16
+                     tensor-core Jacobi sweeps from D = E; afterwards the
+                     FP32 residual R = E - (B - F rho B) (FP32 factors) is
+                     corrected by `inner` sweeps D <- R + F_bf16(rho D),
+                     until max|R[:, k]| <= rtol * max|E[:, k]| for every
+                     column (each solve ends on a checked FP32 residual).
+    engine: 'tc' (tcgen05 tensor cores for the BF16 phase B) or 'mma'
+    (mma.sync kernels).
     Returns B (N, K) fp32; fills `stats` (iterations, matmats, residuals).
     """
     dev = E.device
@@ -255,7 +260,8 @@ def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_
             st = {}
             parts.append(solve_radiosity_batched(FF, E[:, c0:c0 + chunk].contiguous(), rho, rtol,
                                                  precision, max_iter, inner, E_is_permuted,
-                                                 return_permuted, st, chunk=chunk))
+                                                 return_permuted, st, chunk=chunk,
+                                                 inner0=inner0, engine=engine))
             for k_, v_ in st.items():
                 if isinstance(v_, (int, float)) and k_ != "residual":
                     agg[k_] = agg.get(k_, 0) + v_
@@ -267,7 +273,8 @@ def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_
         pad = 8 - K0 % 8
         E = torch.cat([E, torch.zeros((N, pad), dtype=E.dtype, device=dev)], 1)
         B = solve_radiosity_batched(FF, E, rho, rtol, precision, max_iter, inner, E_is_permuted,
-                                    return_permuted, stats)
+                                    return_permuted, stats, chunk=chunk, inner0=inner0,
+                                    engine=engine)
         return B[:, :K0].contiguous()
     K = K0
     stream = _lib.stream_handle()
@@ -305,37 +312,44 @@ def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_
         else:
             raise NoConvergence("FP32 Jacobi did not converge")
     elif precision == "bf16-refine":
-        B = Ep.clone()
+        B = torch.empty_like(Ep)
         R = torch.empty_like(Ep)
         D = torch.empty_like(Ep)
         Xb = torch.empty((N, K), dtype=torch.bfloat16, device=dev)
         Zb = torch.empty((max(FF._num_zrows, 1), K), dtype=torch.bfloat16, device=dev)
-        panel_b, vpanel_b = FF.panels("bf16")
+        emax_h = np.maximum(emax.cpu().numpy(), 1e-30)
         for it in range(1, max_iter + 1):
-            # residual with the FP32 operator
-            _lib.call("fgb_scale_rows_f32", _lib.ptr(B), _lib.ptr(rho_d), rho_s, _lib.ptr(X32), N, K,
-                      stream)
-            FF.matmat_permuted(X32, "fp32", out=Y, Z=Z32)
-            st["fp32_matmats"] += 1
-            colmax.zero_()
-            _lib.call("fgb_residual", _lib.ptr(Y), _lib.ptr(B), _lib.ptr(Ep), _lib.ptr(R), N, K,
-                      _lib.ptr(colmax), stream)
-            res = _colmax(colmax)
-            st["outer"] = it
-            st["residual"] = float(np.max(res / np.maximum(emax.cpu().numpy(), 1e-30)))
-            st.setdefault("history", []).append(st["residual"])
-            if np.all(res <= thresh):
-                break
-            # correction: D <- R + F_bf16 (rho D), `inner` sweeps from D = R
-            D.copy_(R)
-            for _ in range(inner):
+            if it == 1:
+                # B = 0: the residual is E itself
+                rhs, sweeps = Ep, inner0
+            else:
+                # residual with the FP32 operator
+                _lib.call("fgb_scale_rows_f32", _lib.ptr(B), _lib.ptr(rho_d), rho_s,
+                          _lib.ptr(X32), N, K, stream)
+                FF.matmat_permuted(X32, "fp32", out=Y, Z=Z32)
+                st["fp32_matmats"] += 1
+                colmax.zero_()
+                _lib.call("fgb_residual", _lib.ptr(Y), _lib.ptr(B), _lib.ptr(Ep), _lib.ptr(R), N,
+                          K, _lib.ptr(colmax), stream)
+                res = _colmax(colmax)
+                FF.check_device_flags()
+                st["outer"] = it - 1
+                st["residual"] = float(np.max(res / emax_h))
+                st.setdefault("history", []).append(st["residual"])
+                if np.all(res <= thresh):
+                    break
+                rhs, sweeps = R, inner
+            # correction: D <- rhs + F_bf16 (rho D), `sweeps` sweeps from D = rhs
+            D.copy_(rhs)
+            for _ in range(sweeps):
                 _lib.call("fgb_scale_rows_bf16", _lib.ptr(D), _lib.ptr(rho_d), rho_s, _lib.ptr(Xb),
                           N, K, stream)
-                _lib.call("fgb_matmat_bf16", C.byref(FF._desc), _lib.ptr(panel_b), _lib.ptr(vpanel_b),
-                          _lib.ptr(Xb), _lib.ptr(Z32), _lib.ptr(Zb), _lib.ptr(D), K, _lib.ptr(R),
-                          1.0, int(FF._needs_zero_z), 3, stream)
+                FF.bf16_product(Xb, Z32, Zb, D, add=rhs, alpha=1.0, engine=engine)
                 st["bf16_matmats"] += 1
-            _lib.call("fgb_axpy_cols", _lib.ptr(B), _lib.ptr(D), None, N, K, stream)
+            if it == 1:
+                B.copy_(D)
+            else:
+                _lib.call("fgb_axpy_cols", _lib.ptr(B), _lib.ptr(D), None, N, K, stream)
         else:
             raise NoConvergence("refinement did not converge")
     else:

@@ -51,6 +51,7 @@ enum fgb_status {
 #define FGB_FLAG_STACK_OVERFLOW (1u << 6) /* BVH traversal stack exhausted  */
 #define FGB_FLAG_INDEX_RANGE    (1u << 7)
 #define FGB_FLAG_RANK_CAP       (1u << 8) /* ACA reached its rank cap       */
+#define FGB_FLAG_DEVICE_TIMEOUT (1u << 9) /* a bounded device-side wait ran out */
 
 /* Message of the last failed call on this host thread ("" if none). */
 const char* fgb_last_error(void);
@@ -320,6 +321,13 @@ int fgb_matmat_f32(const struct fgb_op_desc* d, const float* panel, const float*
 int fgb_matmat_bf16(const struct fgb_op_desc* d, const void* panel, const void* vpanel,
                     const void* X, float* Z, void* Zb, float* Y, int K, const float* add,
                     float alpha, int zero_z, int phases, void* stream);
+/* Phase B of fgb_matmat_bf16 on the tcgen05 tensor cores (TMEM accumulators):
+ * Y = add + alpha * (panel rows x gathered [Zb; X] rows), tiles' panel rows a
+ * multiple of 64, K % 8 == 0, Zb (num_zrows x K) and X (N x K) bf16 with row
+ * stride K.  Bounded device waits: FGB_FLAG_DEVICE_TIMEOUT in *flags. */
+int fgb_matmat_bf16_tc_phase_b(const struct fgb_op_desc* d, const void* panel, const void* X,
+                               const void* Zb, float* Y, int K, const float* add, float alpha,
+                               unsigned* flags, void* stream);
 /*
  * Panel construction (setup).  Phase B: pairs q (tile, contributing block)
  * with pair_p0 (first panel row, sorted), pair_w (pool offset of the block's

@@ -170,3 +170,35 @@ def test_batched_solvers_reach_rtol():
         R = Ep - (Bp[:, :8] - FBp)
         rel = (R.abs().amax(0) / Ep.abs().amax(0).clamp_min(1e-30)).max().item()
         assert rel <= 2e-5, (prec, rel, st)
+
+
+@pytest.mark.parametrize("K", [256, 200, 1024])
+def test_tensor_core_phase_b_matches_mma(K):
+    """The tcgen05 phase-B kernel against the mma.sync kernels on the same
+    BF16 operands (FP32 accumulation in both: only the summation order
+    differs), and both against the FP64 product."""
+    sm = _terrain_case(64)
+    FF = CompressedFormFactorMatrix(sm, tol=1e-5, min_size=4096, dtype=np.float32,
+                                    RootBlock=FormFactorOctreeBlock)
+    N = sm.num_faces
+    g = torch.Generator(device="cuda").manual_seed(K)
+    Xp = torch.rand((N, K), device="cuda", generator=g)
+    Xb = Xp.to(torch.bfloat16).contiguous()
+    add = torch.rand((N, K), device="cuda", generator=g)
+    zr = max(FF._num_zrows, 1)
+    outs = {}
+    for eng in ("mma", "tc"):
+        Z = torch.empty((zr, K), dtype=torch.float32, device="cuda")
+        Zb = torch.empty((zr, K), dtype=torch.bfloat16, device="cuda")
+        Y = torch.full((N, K), float("nan"), device="cuda")
+        FF.bf16_product(Xb, Z, Zb, Y, add=add, alpha=0.5, engine=eng)
+        outs[eng] = Y
+    FF.check_device_flags()
+    assert torch.isfinite(outs["tc"]).all()
+    ref = (outs["mma"] - add).abs().max().item()
+    d = (outs["tc"] - outs["mma"]).abs().max().item()
+    assert d <= 1e-5 * max(ref, 1e-30) + 1e-6, (d, ref)
+    # against FP64 (BF16 rounding of operator and sources)
+    Y64 = FF.matmat_permuted(Xp[:, :4].double().contiguous(), "fp64")
+    yt = (outs["tc"][:, :4].double() - add[:, :4].double()) / 0.5
+    assert (yt - Y64).abs().max().item() <= 2e-2 * Y64.abs().max().item()

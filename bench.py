@@ -234,6 +234,8 @@ def main():
     ev1 = torch.cuda.Event(enable_timing=True)
     launches0 = _lib.launch_count()
     torch.cuda.synchronize()
+    # an NVTX range marks the timed steps (profilers can filter on it)
+    torch.cuda.nvtx.range_push("timed_steps")
     ev0.record(stream)
     stats = []
     for _ in range(args.steps):
@@ -241,6 +243,7 @@ def main():
         stats.append(st)
     ev1.record(stream)
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
     launches = _lib.launch_count() - launches0
     clk = clocks.stop()
     ms_total = ev0.elapsed_time(ev1)

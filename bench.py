@@ -277,8 +277,9 @@ def main():
         "data": "synthetic", "config": _config(args, nf), "clocks": clk,
         "gpu_launches": int(launches),
         "solver": {"outer": [s["outer"] for s in stats], "bf16_matmats": stats[-1]["bf16_matmats"],
-                   "fp32_matmats": stats[-1]["fp32_matmats"],
-                   "residual_fp32": stats[-1].get("residual")},
+                   "split_bf16_matmats": stats[-1].get("split_matmats", 0),
+                   "fp32_matmats": stats[-1]["fp32_matmats"], "chunks": stats[-1].get("chunks", 1),
+                   "residual_checked": stats[-1].get("residual")},
         "setup_s": setup_s, "build": {k: (round(v, 3) if isinstance(v, float) else v)
                                       for k, v in FF.stats.items()},
     }
@@ -308,15 +309,21 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
     # fit in memory)
     from fluxpy_gb300.solve import _auto_chunk
     K = min(K_all, _auto_chunk(FF, N, K_all))
+    zr = max(FF._num_zrows, 1)
     Ek = Ep[:, :K].contiguous()
-    Xb = (RHO * Ek).to(torch.bfloat16)
     X32 = (RHO * Ek).contiguous()
-    Z32 = torch.empty((max(FF._num_zrows, 1), K), dtype=torch.float32, device=dev)
-    Zb = torch.empty((max(FF._num_zrows, 1), K), dtype=torch.bfloat16, device=dev)
+    xh = torch.empty((N, K), dtype=torch.bfloat16, device=dev)
+    xl = torch.empty_like(xh)
+    Z32 = torch.zeros((zr, K), dtype=torch.float32, device=dev)
+    zh = torch.zeros((zr, K), dtype=torch.bfloat16, device=dev)
+    zl = torch.zeros_like(zh)
     Y = torch.empty_like(Ek)
-    panel_b, vpanel_b = FF.panels("bf16")
+    tc = FF.tc_operands(split=True)
     panel_f, vpanel_f = FF.panels("fp32")
     flags = FF.device_flags()
+    desc = C.byref(FF._desc)
+    st = _lib.stream_handle
+    _lib.call("fgb_split_bf16", _lib.ptr(X32), _lib.ptr(xh), _lib.ptr(xl), N * K, st())
 
     def t_events(fn, reps=5):
         fn()
@@ -330,38 +337,42 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
         torch.cuda.synchronize()
         return a.elapsed_time(b) / reps
 
-    def bf16(phases):
-        _lib.call("fgb_matmat_bf16", C.byref(FF._desc), _lib.ptr(panel_b), _lib.ptr(vpanel_b),
-                  _lib.ptr(Xb), _lib.ptr(Z32), _lib.ptr(Zb), _lib.ptr(Y), K, _lib.ptr(Ek), 1.0,
-                  int(FF._needs_zero_z), phases, _lib.stream_handle())
+    def tc_a(split):
+        _lib.call("fgb_tc_phase_a", desc, _lib.ptr(tc["vt_hi"]),
+                  _lib.ptr(tc["vt_lo"]) if split else None, _lib.ptr(xh),
+                  _lib.ptr(xl) if split else None, _lib.ptr(Z32), K, int(FF._needs_zero_z),
+                  _lib.ptr(flags), st())
 
-    def bf16_tc_b():
-        _lib.call("fgb_matmat_bf16_tc_phase_b", C.byref(FF._desc), _lib.ptr(panel_b),
-                  _lib.ptr(Xb), _lib.ptr(Zb), _lib.ptr(Y), K, _lib.ptr(Ek), 1.0,
-                  _lib.ptr(flags), _lib.stream_handle())
+    def tc_b(split):
+        _lib.call("fgb_tc_phase_b", desc, _lib.ptr(tc["w_hi"]),
+                  _lib.ptr(tc["w_lo"]) if split else None, _lib.ptr(xh),
+                  _lib.ptr(xl) if split else None, _lib.ptr(zh), _lib.ptr(zl) if split else None,
+                  _lib.ptr(Y), K, _lib.ptr(Ek), 1.0, _lib.ptr(flags), st())
 
     def f32(phases):
-        _lib.call("fgb_matmat_f32", C.byref(FF._desc), _lib.ptr(panel_f), _lib.ptr(vpanel_f),
-                  _lib.ptr(X32), _lib.ptr(Z32), _lib.ptr(Y), K, None, 1.0,
-                  int(FF._needs_zero_z), phases, _lib.stream_handle())
+        _lib.call("fgb_matmat_f32", desc, _lib.ptr(panel_f), _lib.ptr(vpanel_f), _lib.ptr(X32),
+                  _lib.ptr(Z32), _lib.ptr(Y), K, None, 1.0, int(FF._needs_zero_z), phases, st())
 
-    tA = t_events(lambda: bf16(1))
-    tB = t_events(bf16_tc_b)
-    tB_mma = t_events(lambda: bf16(2))
+    ms = {"phaseA_tc": t_events(lambda: tc_a(False)), "phaseB_tc": t_events(lambda: tc_b(False)),
+          "phaseA_tc_split": t_events(lambda: tc_a(True)),
+          "phaseB_tc_split": t_events(lambda: tc_b(True)),
+          "phaseA_f32": t_events(lambda: f32(1), 3), "phaseB_f32": t_events(lambda: f32(2), 3)}
     FF.check_device_flags()
-    tA32 = t_events(lambda: f32(1))
-    tB32 = t_events(lambda: f32(2))
-    # algorithmic bytes per launch: every stored weight read once, every
-    # distinct source row read once per launch, outputs written once
+    # algorithmic work per launch: every stored weight read once, every
+    # distinct source row read once, outputs written once; flops 2 per
+    # weight and right-hand side (x3 for the split products)
     wB = int(FF._panel_rows) * 64              # phase-B panel weights
-    vA = int(FF._vpanel_size)                  # phase-A panel weights
+    vA = int(FF._vpanel_size)                  # phase-A panel weights (rows padded to 8)
     zrows = int(FF._num_zrows)
     srcB = int(torch.unique(FF._dev["src"]).numel()) * K   # distinct source rows
     xA = int(FF._dev["g_n"].sum().item()) * K             # X rows read by phase A groups
-    bytes_B_bf16 = wB * 2 + srcB * 2 + N * K * 4 * 2       # + Y write + add read (fp32)
-    bytes_A_bf16 = vA * 2 + xA * 2 + zrows * K * 4
-    flops_B = 2.0 * wB * K
-    flops_A = 2.0 * vA * K
+    work = {
+        "phaseA_tc": (vA * 2 + xA * 2 + zrows * K * 4, 2.0 * vA * K),
+        "phaseB_tc": (wB * 2 + srcB * 2 + N * K * 4 * 2, 2.0 * wB * K),
+        "phaseA_tc_split": (vA * 4 + xA * 4 + zrows * K * 4, 6.0 * vA * K),
+        "phaseB_tc_split": (wB * 4 + srcB * 4 + N * K * 4 * 2, 6.0 * wB * K),
+        "phaseA_f32": (vA * 4 + xA * 4 + zrows * K * 4, 2.0 * vA * K),
+        "phaseB_f32": (wB * 4 + srcB * 4 + N * K * 4, 2.0 * wB * K)}
     peaks = {}
     pk = ROOT / "MEASURED_PEAKS.json"
     if pk.exists():
@@ -369,19 +380,20 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
     hbm = float(peaks.get("hbm_gbs", 6800.0))
     tf = float(peaks.get("bf16_tflops", 1900.0))
     src = "measured" if pk.exists() else "fallback"
-    per_solve = {"phaseA_bf16": tA * stats[-1]["bf16_matmats"],
-                 "phaseB_bf16": tB * stats[-1]["bf16_matmats"],
-                 "phaseA_f32": tA32 * stats[-1]["fp32_matmats"],
-                 "phaseB_f32": tB32 * stats[-1]["fp32_matmats"]}
-    dom = max(per_solve, key=per_solve.get)
-    kern = {"phaseA_bf16": (tA, bytes_A_bf16, flops_A), "phaseB_bf16": (tB, bytes_B_bf16, flops_B),
-            "phaseA_f32": (tA32, vA * 4 + xA * 4 + zrows * K * 4, flops_A),
-            "phaseB_f32": (tB32, wB * 4 + srcB * 4 + N * K * 4, flops_B)}
-    t_ms, byts, fl = kern[dom]
+    s_last = stats[-1]
+    nb, ns, nf = (s_last.get("bf16_matmats", 0), s_last.get("split_matmats", 0),
+                  s_last.get("fp32_matmats", 0))
+    per_step = {"phaseA_tc": ms["phaseA_tc"] * nb, "phaseB_tc": ms["phaseB_tc"] * nb,
+                "phaseA_tc_split": ms["phaseA_tc_split"] * ns,
+                "phaseB_tc_split": ms["phaseB_tc_split"] * ns,
+                "phaseA_f32": ms["phaseA_f32"] * nf, "phaseB_f32": ms["phaseB_f32"] * nf}
+    dom = max(per_step, key=per_step.get)
+    t_ms = ms[dom]
+    byts, fl = work[dom]
     gbs = byts / (t_ms * 1e-3) / 1e9
     tfl = fl / (t_ms * 1e-3) / 1e12
-    if "bf16" in dom:
-        # BF16 tensor-core GEMM over the panels: bounded by the tensor pipe
+    if "tc" in dom:
+        # BF16 tensor-core gather-GEMM over the panels: bounded by the tensor pipe
         out["roofline"] = {"kernel": dom, "bound": "tensor", "achieved": tfl, "peak": tf,
                            "unit": "TFLOP/s", "frac": tfl / tf, "traffic": None,
                            "peak_source": src, "algorithmic_flops": fl,
@@ -391,13 +403,12 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
         out["roofline"] = {"kernel": dom, "bound": "hbm", "achieved": gbs, "peak": hbm,
                            "unit": "GB/s", "frac": gbs / hbm, "traffic": None,
                            "peak_source": src, "algorithmic_bytes": byts,
-                           "algorithmic_flops": fl, "ms_per_launch": t_ms,
-                           "fp32_tflops": tfl}
-    out["kernel_ms"] = {"columns": K, "phaseA_bf16": tA, "phaseB_bf16_tc": tB,
-                        "phaseB_bf16_mma_sync": tB_mma, "phaseA_f32": tA32, "phaseB_f32": tB32,
-                        "per_solve_ms": per_solve}
-    del Xb, X32, Z32, Zb, Y, Ek
+                           "algorithmic_flops": fl, "ms_per_launch": t_ms, "fp32_tflops": tfl}
+    out["kernel_ms"] = {"columns": K, **ms, "per_step_ms": per_step,
+                        "tflops": {k: work[k][1] / (ms[k] * 1e-3) / 1e12 for k in ms}}
+    del X32, xh, xl, Z32, zh, zl, Y, Ek
     torch.cuda.empty_cache()
+    K = K_all
     # ---- plain FP32 GPU paths
     st = {}
     torch.cuda.synchronize()
@@ -435,18 +446,29 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
         r = Epc[:, q] - (Bp[:, q] - y)
         res.append(float(r.abs().max() / Epc[:, q].abs().max()))
     rng = np.random.default_rng(0)
-    rows = rng.choice(N, 16, replace=False)
+    nrows = 64
+    rows = rng.choice(N, nrows, replace=False)
     facet_rows = FF._tree.perm[rows]
-    Fx = get_form_factor_matrix(sm, facet_rows)          # exact rows (all columns)
+    Fx = get_form_factor_matrix(sm, facet_rows)          # exact FP64 rows (all columns)
     x = rng.uniform(0, 1, N)
     y_exact = Fx @ x
     y_c = FF @ x
     comp = float(np.max(np.abs(y_c[facet_rows] - y_exact)) / np.max(np.abs(y_exact)))
+    # residual of the computed solution against the exact, uncompressed FP64
+    # operator on those rows: E - (B - rho F_exact B), per column
+    Bf = FF.unpermute(B[:, cols]).double().cpu().numpy()
+    Ef = FF.unpermute(Ep[:, cols]).double().cpu().numpy()
+    FB = Fx @ (RHO * Bf)
+    r_ex = Ef[facet_rows] - (Bf[facet_rows] - FB)
+    res_exact = float(np.max(np.abs(r_ex).max(0) / np.maximum(np.abs(Ef).max(0), 1e-30)))
     out["error"] = {"residual_rel_fp64_max": max(res), "columns": len(res),
-                    "compression_rel_err_sampled_rows": comp, "rows": 16,
+                    "residual_vs_exact_operator_rows": res_exact,
+                    "compression_rel_err_sampled_rows": comp, "rows": nrows,
                     "note": ("residual: max|E - (B - F rho B)| / max|E| per column, FP64 "
-                             "arithmetic on the stored operator; compression: |(F~ - F) x| on 16 "
-                             "random rows vs exactly assembled rows, relative to max|F x|")}
+                             "arithmetic on the stored (compressed FP32) operator; "
+                             "residual_vs_exact_operator_rows: the same with exactly assembled "
+                             "FP64 rows of the uncompressed F on 64 random rows; compression: "
+                             "|(F~ - F) x| on those rows relative to max|F x|")}
     # ---- e2e through the public API with host buffers
     E_host = torch.empty((N, K), dtype=torch.float32, pin_memory=True)
     E_host.copy_(E.cpu())

@@ -103,7 +103,10 @@ SIGNATURES: dict[str, list] = {
     "fgb_matvec_f32_f64": [P, P, P, P, P, P, P, F64, I32, P],
     "fgb_matmat_f32": [P, P, P, P, P, P, I32, P, F32, I32, I32, P],
     "fgb_matmat_bf16": [P, P, P, P, P, P, P, I32, P, F32, I32, I32, P],
-    "fgb_matmat_bf16_tc_phase_b": [P, P, P, P, P, I32, P, F32, P, P],
+    "fgb_tc_phase_a": [P, P, P, P, P, P, I32, I32, P, P],
+    "fgb_tc_phase_b": [P, P, P, P, P, P, P, P, I32, P, F32, P, P],
+    "fgb_split_bf16": [P, P, P, I64, P],
+    "fgb_vpanel_transpose_bf16": [P, P, P, P, P, I64, P, P, P],
     # solve (a10-a12)
     "fgb_scale_rows_f32": [P, P, F32, P, I64, I32, P],
     "fgb_scale_rows_bf16": [P, P, F32, P, I64, I32, P],

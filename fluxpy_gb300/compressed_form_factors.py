@@ -160,7 +160,8 @@ class fgb_op_desc(C.Structure):
         ("a_j0", C.c_void_p), ("a_j1", C.c_void_p), ("a_excl", C.c_void_p),
         ("num_items", C.c_longlong), ("t_p0", C.c_void_p), ("src", C.c_void_p),
         ("num_tiles", C.c_longlong), ("N", C.c_longlong), ("num_zrows", C.c_longlong),
-        ("max_group_tiles", C.c_int),
+        ("max_group_tiles", C.c_int), ("g_kzp", C.c_void_p), ("g_vtoff", C.c_void_p),
+        ("a_woff", C.c_void_p), ("num_work", C.c_longlong),
     ]
 
 
@@ -543,6 +544,21 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         a_ex = (nchunk[a_grp] == 1).astype(np.uint8)
         self._needs_zero_z = bool((a_ex == 0).any())
         max_gt = int(((g_kz + 63) // 64).max()) if ng else 1
+        # tensor-core phase A: groups stored transposed (n x kz rounded up to
+        # 64) and one work slice per (item, 64 rows of the group)
+        g_kzp = (g_kz + 63) // 64 * 64
+        g_vtoff = np.zeros(ng + 1, np.int64)
+        np.cumsum(g_n * g_kzp, out=g_vtoff[1:])
+        a_wn = (g_kz[a_grp] + 63) // 64
+        a_woff = np.zeros(a_grp.size + 1, np.int64)
+        np.cumsum(a_wn, out=a_woff[1:])
+        tsl = g_kzp // 64
+        tjb = (g_n + 63) // 64
+        tcnt = tsl * tjb
+        vt_g = np.repeat(np.arange(ng), tcnt)
+        vt_i = np.arange(tcnt.sum()) - np.repeat(np.cumsum(tcnt) - tcnt, tcnt)
+        vt_s = vt_i // np.repeat(tjb, tcnt)
+        vt_j = vt_i % np.repeat(tjb, tcnt)
         ntiles = (N + TILE_ROWS - 1) // TILE_ROWS
 
         def tile_pairs(r0, m):
@@ -654,35 +670,42 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
             g_c0=d(g_c0, np.int32), g_n=d(g_n, np.int32), g_kz=d(g_kz, np.int32),
             g_ldv=d(g_ldv, np.int32), g_voff=d(g_voff[:-1], np.int64), g_z0=d(g_z0[:-1], np.int64),
             a_grp=d(a_grp, np.int32), a_j0=d(a_j0, np.int32), a_j1=d(a_j1, np.int32),
-            a_excl=d(a_ex, np.uint8), t_p0=d(t_p0, np.int64), src=src_d)
+            a_excl=d(a_ex, np.uint8), t_p0=d(t_p0, np.int64), src=src_d,
+            g_kzp=d(g_kzp, np.int32), g_vtoff=d(g_vtoff[:-1], np.int64),
+            a_woff=d(a_woff, np.int64))
         self._build_dev = dict(
+            vt_g=d(vt_g, np.int32), vt_s=d(vt_s, np.int32), vt_j=d(vt_j, np.int32),
             vr_src=d(vr_src, np.int64), vr_dst=d(vr_dst, np.int64), vr_n=d(vr_n, np.int32),
             p_p0=d(all_p0, np.int64), p_w=d(all_w, np.int64), p_m=d(all_m, np.int32),
             p_shift=d(all_shift, np.int64), p_k=d(all_k, np.int32))
         self._panel_rows = total_rows
         self._vpanel_size = int(g_voff[-1])
+        self._vtpanel_size = int(g_vtoff[-1])
+        self._num_vt_tiles = int(vt_g.size)
         self._num_vrows = int(vr_src.size)
         self._num_pairs = int(all_p0.size)
-        self._desc = self._make_desc(int(a_grp.size), ntiles, max_gt)
+        self._desc = self._make_desc(int(a_grp.size), ntiles, max_gt, int(a_woff[-1]))
         self._lr_blocks = lr
         self._lr_u, self._lr_v = lr_u, lr_v
         self._panels = {}
+        self._tc = {}
         self.stats.update(num_items=int(a_grp.size), num_tiles=ntiles, groups=ng,
                           panel_rows=total_rows, nearfield_rows=int(L_nf.sum()),
                           lowrank_rows=int(L_lr.sum()), max_group_tiles=max_gt,
                           pool_entries=int(self._pool.numel()), zrows=self._num_zrows,
                           operator_entries=int(total_rows * TILE_ROWS + g_voff[-1]))
 
-    def _make_desc(self, num_items, ntiles, max_gt):
+    def _make_desc(self, num_items, ntiles, max_gt, num_work):
         desc = fgb_op_desc()
         for key in ("g_c0", "g_n", "g_kz", "g_ldv", "g_voff", "g_z0", "a_grp", "a_j0", "a_j1",
-                    "a_excl", "t_p0", "src"):
+                    "a_excl", "t_p0", "src", "g_kzp", "g_vtoff", "a_woff"):
             setattr(desc, key, self._dev[key].data_ptr())
         desc.num_items = num_items
         desc.num_tiles = ntiles
         desc.N = self.num_faces
         desc.num_zrows = self._num_zrows
         desc.max_group_tiles = max_gt
+        desc.num_work = num_work
         return desc
 
     # -- device products --------------------------------------------------
@@ -694,7 +717,7 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
 
     _TDT = {"fp64": torch.float64, "fp32": torch.float32, "bf16": torch.bfloat16}
 
-    def offload_pool(self, precisions=("fp32", "bf16")):
+    def offload_pool(self, precisions=("fp32",)):
         """Build the panels of the given precisions, then move the block pool
         (needed only for other precisions and for block introspection) to
         host memory, freeing its device copy."""
@@ -828,22 +851,95 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         self.bf16_product(Xb, Z, Zb, out, add, alpha, engine)
         return out
 
+    def tc_operands(self, split=False):
+        """BF16 operands of the tensor-core products, built once from the
+        FP32 panels: 'w_hi' (phase-B panel), 'vt_hi' (transposed phase-A
+        panel) and, for split products, their low parts 'w_lo', 'vt_lo'
+        (hi = bf16(v), lo = bf16(v - hi))."""
+        tc = self.__dict__.setdefault("_tc", {})
+        if "w_hi" in tc and (not split or "w_lo" in tc):
+            return tc
+        panel, vpanel = self.panels("fp32")
+        dev = panel.device
+        st = _lib.stream_handle()
+        w_hi = tc.get("w_hi")
+        if w_hi is None:
+            w_hi = torch.empty(panel.numel(), dtype=torch.bfloat16, device=dev)
+        w_lo = torch.empty(panel.numel(), dtype=torch.bfloat16, device=dev) if split else None
+        _lib.call("fgb_split_bf16", _lib.ptr(panel), _lib.ptr(w_hi), _lib.ptr(w_lo),
+                  panel.numel(), st)
+        nvt = max(self._vtpanel_size, 8)
+        vt_hi = tc.get("vt_hi")
+        if vt_hi is None:
+            vt_hi = torch.zeros(nvt, dtype=torch.bfloat16, device=dev)
+        vt_lo = torch.zeros(nvt, dtype=torch.bfloat16, device=dev) if split else None
+        b = self._build_dev
+        _lib.call("fgb_vpanel_transpose_bf16", C.byref(self._desc), _lib.ptr(vpanel),
+                  _lib.ptr(b["vt_g"]), _lib.ptr(b["vt_s"]), _lib.ptr(b["vt_j"]),
+                  self._num_vt_tiles, _lib.ptr(vt_hi), _lib.ptr(vt_lo), st)
+        tc.update(w_hi=w_hi, vt_hi=vt_hi)
+        if split:
+            tc.update(w_lo=w_lo, vt_lo=vt_lo)
+        return tc
+
     def bf16_product(self, Xb, Z, Zb, Y, add=None, alpha=1.0, engine="tc"):
         """Y = add + alpha F X with BF16 operands (X: N x K bf16, K % 8 == 0)
         and FP32 accumulation, in cluster order; Z (FP32) and Zb (BF16) are
-        num_zrows x K scratch.  engine 'tc': phase B on the tcgen05 tensor
-        cores (TMEM accumulators); 'mma': both phases with mma.sync."""
+        num_zrows x K scratch.  engine 'tc': both phases on the tcgen05
+        tensor cores (TMEM accumulators); 'mma': mma.sync kernels."""
         K = Xb.shape[1]
-        panel, vpanel = self.panels("bf16")
         st = _lib.stream_handle()
-        phases = 1 if engine == "tc" else 3
-        _lib.call("fgb_matmat_bf16", C.byref(self._desc), _lib.ptr(panel), _lib.ptr(vpanel),
-                  _lib.ptr(Xb), _lib.ptr(Z), _lib.ptr(Zb), _lib.ptr(Y), K, _lib.ptr(add),
-                  float(alpha), int(self._needs_zero_z), phases, st)
-        if engine == "tc":
-            _lib.call("fgb_matmat_bf16_tc_phase_b", C.byref(self._desc), _lib.ptr(panel),
-                      _lib.ptr(Xb), _lib.ptr(Zb), _lib.ptr(Y), K, _lib.ptr(add), float(alpha),
-                      _lib.ptr(self.device_flags()), st)
+        if engine == "mma":
+            panel, vpanel = self.panels("bf16")
+            _lib.call("fgb_matmat_bf16", C.byref(self._desc), _lib.ptr(panel), _lib.ptr(vpanel),
+                      _lib.ptr(Xb), _lib.ptr(Z), _lib.ptr(Zb), _lib.ptr(Y), K, _lib.ptr(add),
+                      float(alpha), int(self._needs_zero_z), 3, st)
+            return Y
+        tc = self.tc_operands()
+        flags = _lib.ptr(self.device_flags())
+        if self._num_zrows > 0:
+            _lib.call("fgb_tc_phase_a", C.byref(self._desc), _lib.ptr(tc["vt_hi"]), None,
+                      _lib.ptr(Xb), None, _lib.ptr(Z), K, int(self._needs_zero_z), flags, st)
+            _lib.call("fgb_split_bf16", _lib.ptr(Z), _lib.ptr(Zb), None,
+                      self._num_zrows * K, st)
+        _lib.call("fgb_tc_phase_b", C.byref(self._desc), _lib.ptr(tc["w_hi"]), None,
+                  _lib.ptr(Xb), None, _lib.ptr(Zb), None, _lib.ptr(Y), K, _lib.ptr(add),
+                  float(alpha), flags, st)
+        return Y
+
+    def split_product(self, X, Y, add=None, alpha=1.0, work=None):
+        """Y = add + alpha F X for FP32 X (N x K, K % 8 == 0) on the tensor
+        cores with split-BF16 operands (hi.hi + lo.hi + hi.lo, FP32
+        accumulation): each product term is exact, the represented operator
+        and sources differ from the FP32 ones by at most 2^-16 relative, so
+        |error| <= ~3 * 2^-17 * (|F| |X|) elementwise, near the FP32 product's
+        own rounding.  work: optional dict of scratch tensors (reused)."""
+        N, K = X.shape
+        dev = X.device
+        st = _lib.stream_handle()
+        zr = max(self._num_zrows, 1)
+        w = work if work is not None else {}
+
+        def buf(name, shape, dt):
+            t = w.get(name)
+            if t is None or tuple(t.shape) != tuple(shape) or t.dtype != dt:
+                t = w[name] = torch.empty(shape, dtype=dt, device=dev)
+            return t
+        xh, xl = buf("x_hi", (N, K), torch.bfloat16), buf("x_lo", (N, K), torch.bfloat16)
+        z = buf("z", (zr, K), torch.float32)
+        zh, zl = buf("z_hi", (zr, K), torch.bfloat16), buf("z_lo", (zr, K), torch.bfloat16)
+        tc = self.tc_operands(split=True)
+        flags = _lib.ptr(self.device_flags())
+        _lib.call("fgb_split_bf16", _lib.ptr(X), _lib.ptr(xh), _lib.ptr(xl), N * K, st)
+        if self._num_zrows > 0:
+            _lib.call("fgb_tc_phase_a", C.byref(self._desc), _lib.ptr(tc["vt_hi"]),
+                      _lib.ptr(tc["vt_lo"]), _lib.ptr(xh), _lib.ptr(xl), _lib.ptr(z), K,
+                      int(self._needs_zero_z), flags, st)
+            _lib.call("fgb_split_bf16", _lib.ptr(z), _lib.ptr(zh), _lib.ptr(zl),
+                      self._num_zrows * K, st)
+        _lib.call("fgb_tc_phase_b", C.byref(self._desc), _lib.ptr(tc["w_hi"]),
+                  _lib.ptr(tc["w_lo"]), _lib.ptr(xh), _lib.ptr(xl), _lib.ptr(zh), _lib.ptr(zl),
+                  _lib.ptr(Y), K, _lib.ptr(add), float(alpha), flags, st)
         return Y
 
     def device_flags(self):
@@ -997,6 +1093,8 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         st["_root_cache"] = None
         st["_desc"] = None
         st["_panels"] = {}
+        st["_tc"] = {}
+        st["_flags_d"] = None
         for key in ("_pool", "_perm_d", "_iperm_d"):
             st[key] = st[key].cpu()
         for key in self._DEV_DICTS:
@@ -1024,7 +1122,8 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
                                       dct["data"].to(dev), dct["row_off"], 0, 0,
                                       dct["bits"].to(dev), dct["word_off"])
         self._desc = self._make_desc(int(self.stats["num_items"]), int(self.stats["num_tiles"]),
-                                     int(self.stats["max_group_tiles"]))
+                                     int(self.stats["max_group_tiles"]),
+                                     int(self._dev["a_woff"][-1].item()))
 
     # -- leaf data for the Python block objects --------------------------
     def _leaf_dense(self, b):

@@ -1,28 +1,39 @@
-// Phase B of the K-right-hand-side block product on the 5th-generation
-// tensor cores (tcgen05.mma, accumulators in tensor memory).
+// The K-right-hand-side block product of the compressed operator on the
+// 5th-generation tensor cores (tcgen05.mma, FP32 accumulators in tensor
+// memory), for both phases of the panel layout of matvec.cu:
 //
-// Same operator layout as matvec.cu (phase B): tile t owns 64 operator rows
-// and the panel rows [p0, p1) (a multiple of 64 here); panel row l holds 64
-// BF16 weights W[l, i] for the tile's rows i and a source index src[l] into
-// the stacked source S = [Zb; X] (num_zrows + N rows, K BF16 columns each).
-//   Y[t*64 + i, c] = add[., c] + alpha * sum_l W[l, i] S[src[l], c].
-// For the tensor core the product is taken transposed, so that the long
-// right-hand-side dimension is the MMA's M:
-//   D (M = 128 columns of S, N = 64 tile rows) += A (S^T chunk) . B (W chunk)
-// with the reduction over panel rows, 16 per MMA.  Both operands are stored
-// "MN-major" (their contiguous dimension is M resp. N), in the canonical
-// 128-byte-swizzled layout: for each 64-element block along M (or N) the
-// K rows are 128-byte lines, eight lines to a 1 KiB swizzle atom, the
-// 16-byte chunks of line k permuted by XOR with (k mod 8).
+//   phase B (row tiles): tile t owns 64 operator rows and the panel rows
+//     [p0, p1) (a multiple of 64); panel row l holds 64 BF16 weights W[l, i]
+//     for the tile's rows i and a source index src[l] into S = [Z; X]:
+//       Y[t*64 + i, c] = add[., c] + alpha * sum_l W[l, i] S[src[l], c];
+//   phase A (low-rank groups): group g (kz stacked V^T rows, columns
+//     [c0, c0 + n)) is stored transposed, Vt[j, r], and work slice s of an
+//     item (columns [j0, j1) of the group) computes
+//       Z[z0 + 64 s + r, c] (+)= sum_j Vt[j, 64 s + r] X[c0 + j, c].
 //
-// CTA = (tile, slice of NC = 256 right-hand-side columns); 8 warps.  All
-// warps gather the next chunks (64 panel rows: W 8 KiB, S 32 KiB) with
-// cp.async into a 4-stage ring; thread 0 issues the MMAs of the current
-// chunk (4 k-steps x 2 M-halves) and commits them to the stage's mbarrier,
-// which the producers wait on before they refill that stage.  The FP32
-// accumulators (2 x 64 TMEM columns, 128 lanes) are read back with
-// tcgen05.ld by all warps (warp w reads lanes 32 (w mod 4) ..) for the
-// epilogue, whose stores are coalesced along the right-hand-side columns.
+// Both are one "gather GEMM" with the reduction over rows l (panel rows, or
+// group columns j): the product is taken transposed so that the long
+// right-hand-side dimension is the MMA's M,
+//   D (M = 128 columns of S, N = 64 output rows) += A (S^T chunk) . B (W chunk),
+// 16 reduction rows per MMA.  Both operands are stored "MN-major" (their
+// contiguous dimension is M resp. N) in the canonical 128-byte-swizzled
+// layout: per 64-element block along M (or N) the reduction rows are
+// 128-byte lines, eight lines to a 1 KiB swizzle atom, the 16-byte chunks of
+// line k permuted by XOR with (k mod 8).
+//
+// Split mode: each FP32 operand v is given as hi = bf16(v), lo = bf16(v -
+// hi); the chunk loads W_hi, W_lo, S_hi, S_lo and issues three MMAs per
+// k-step into the same accumulator, hi.hi + lo.hi + hi.lo (the lo.lo term is
+// below 2^-16 relative and dropped).
+//
+// CTA = (tile or work slice, slice of NC = 256 right-hand-side columns), 8
+// warps.  All warps gather the next chunks with cp.async into a 5-stage ring
+// (40 KiB a stage: 64 rows, or 32 rows in split mode); thread 0 issues the
+// MMAs of the current chunk and commits them to the stage's mbarrier, which
+// the producers wait on before they refill that stage.  The accumulators (2
+// x 64 TMEM columns, 128 lanes) are read back with tcgen05.ld (warp w reads
+// lanes 32 (w mod 4) ..) for an epilogue whose stores are coalesced along the
+// right-hand-side columns.
 //
 // Every mbarrier wait is bounded (about 2 s of global time); a wait that
 // runs out sets FGB_FLAG_DEVICE_TIMEOUT in the caller's flag word and the
@@ -34,17 +45,16 @@
 namespace fgb {
 namespace {
 
-constexpr int kTcTileRows = 64;   // operator rows per tile (MMA N)
-constexpr int kTcChunk = 64;      // panel rows per pipeline stage
-constexpr int kTcNC = 256;        // right-hand-side columns per CTA (2 x MMA M)
-constexpr int kTcStages = 4;
+constexpr int kTcRows = 64;        // output rows per CTA (MMA N)
+constexpr int kTcNC = 256;         // right-hand-side columns per CTA (2 x MMA M)
+constexpr int kTcStages = 5;
 constexpr int kTcThreads = 256;
-constexpr int kTcWBytes = kTcChunk * kTcTileRows * 2;          // 8 KiB
-constexpr int kTcSBytes = kTcChunk * kTcNC * 2;                // 32 KiB
-constexpr int kTcStageBytes = kTcWBytes + kTcSBytes;           // 40 KiB
-constexpr int kTcSmemBytes = kTcStages * kTcStageBytes + 1024; // + alignment slack
-constexpr int kTcTmemCols = 128;                               // 2 accumulators x 64
-constexpr unsigned long long kWaitNs = 2000000000ull;          // 2 s
+constexpr int kTcStageBytes = 40 * 1024;
+constexpr int kTcSmemBytes = kTcStages * kTcStageBytes + 1024;  // + alignment slack
+constexpr int kTcTmemCols = 128;                                // 2 accumulators x 64
+constexpr unsigned long long kWaitNs = 2000000000ull;           // 2 s
+
+enum { kModeA = 0, kModeB = 1 };
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -86,7 +96,10 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
 
 // tcgen05 shared-memory matrix descriptor: start address, leading and stride
 // byte offsets (16-byte units), the fixed version bits 46-48 = 0b001 and the
-// layout type in bits 61-63 (2 = 128-byte swizzle).
+// layout type in bits 61-63 (2 = 128-byte swizzle).  For these MN-major
+// operands the leading offset is the stride between 64-element blocks along
+// M / N and the stride offset the stride between 8-line groups along the
+// reduction.
 __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
   return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
          ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46) | (2ull << 61);
@@ -95,14 +108,14 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr, uint32_t lbo, uin
 // (bits 7-9, 10-12 = 1), A and B MN-major (bits 15, 16), N >> 3 in bits
 // 17-22, M >> 4 in bits 24-28.
 constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (1u << 15) | (1u << 16) |
-                            ((uint32_t)(kTcTileRows >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+                            ((uint32_t)(kTcRows >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
 
 __device__ __forceinline__ void mma_bf16_tc(uint32_t dtmem, uint64_t adesc, uint64_t bdesc,
-                                            uint32_t idesc, uint32_t accumulate) {
+                                            uint32_t accumulate) {
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
       " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
-      ::"r"(dtmem), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate) : "memory");
+      ::"r"(dtmem), "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate) : "memory");
 }
 __device__ __forceinline__ void mma_commit(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
@@ -135,37 +148,96 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
   for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
 
-struct TcPhaseB {
+struct TcArgs {
+  // phase B
   const long long* t_p0;
   const int* src;
-  long long num_tiles;
   long long N;
   long long num_zrows;
+  // phase A
+  const int* a_grp;
+  const int* a_j0;
+  const int* a_j1;
+  const unsigned char* a_excl;
+  const long long* a_woff;
+  long long num_items;
+  const int* g_c0;
+  const int* g_kz;
+  const int* g_kzp;
+  const long long* g_vtoff;
+  const long long* g_z0;
+  // operands (lo: split mode only)
+  const __nv_bfloat16* w_hi;
+  const __nv_bfloat16* w_lo;
+  const __nv_bfloat16* x_hi;
+  const __nv_bfloat16* x_lo;
+  const __nv_bfloat16* z_hi;
+  const __nv_bfloat16* z_lo;
+  long long lds;           // row stride of X and Z (= K)
+  int K;
+  float* out;              // Y (phase B) or Z (phase A), row stride K
+  const float* add;
+  float alpha;
+  unsigned* flags;
 };
 
-__global__ void __launch_bounds__(kTcThreads, 1)
-phaseB_tc_bf16(TcPhaseB op, const __nv_bfloat16* __restrict__ panel,
-               const __nv_bfloat16* __restrict__ X, const __nv_bfloat16* __restrict__ Zb,
-               long long lds, float* __restrict__ Y, long long ldy, int K,
-               const float* __restrict__ add_mat, long long ld_add, float alpha,
-               unsigned* __restrict__ flags) {
+template <int MODE, bool SPLIT>
+__global__ void __launch_bounds__(kTcThreads, 1) tc_gather_gemm(TcArgs a) {
+  constexpr int CH = SPLIT ? 32 : 64;                 // reduction rows per stage
+  constexpr int WB = CH * kTcRows * 2;                 // W bytes per stage (per part)
+  constexpr int SB = CH * kTcNC * 2;                   // S bytes per stage (per part)
+  constexpr int BLK = CH * 128;                        // 64-column block of S
+  static_assert((SPLIT ? 2 : 1) * (WB + SB) == kTcStageBytes, "stage size");
   extern __shared__ uint8_t smem_raw[];
-  __shared__ __align__(8) unsigned long long bars[kTcStages + 1];
+  __shared__ __align__(8) unsigned long long bars[kTcStages];
   __shared__ uint32_t tmem_slot;
   __shared__ int abort_flag;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int nks = (K + kTcNC - 1) / kTcNC;
-  const long long t = blockIdx.x / nks;
+  const int nks = (a.K + kTcNC - 1) / kTcNC;
+  const long long unit = blockIdx.x / nks;
   const int c_base = (int)(blockIdx.x % nks) * kTcNC;
-  const long long p0 = op.t_p0[t], p1 = op.t_p0[t + 1];
-  const int nch = (int)((p1 - p0) / kTcChunk);
-  if (tid == 0 && ((p1 - p0) % kTcChunk) != 0) atomicOr(flags, FGB_FLAG_INDEX_RANGE);
+
+  // ---- the CTA's reduction range and output rows
+  long long r_first = 0, r_end = 0;   // reduction rows (panel rows / group columns)
+  long long out_row0 = 0;             // first output row
+  int out_rows = kTcRows;             // valid output rows
+  const __nv_bfloat16* wbase_hi = a.w_hi;
+  const __nv_bfloat16* wbase_lo = a.w_lo;
+  long long wstride = kTcRows;        // elements between consecutive W rows
+  long long xrow0 = 0;                // phase A: X row of reduction row 0
+  bool excl = true;
+  if (MODE == kModeB) {
+    r_first = a.t_p0[unit];
+    r_end = a.t_p0[unit + 1];
+    out_row0 = unit * kTcRows;
+    out_rows = (int)min((long long)kTcRows, a.N - out_row0);
+    if (tid == 0 && ((r_end - r_first) % 64) != 0) atomicOr(a.flags, FGB_FLAG_INDEX_RANGE);
+  } else {
+    long long lo = 0, hi = a.num_items - 1;
+    while (lo < hi) {
+      const long long mid = (lo + hi + 1) >> 1;
+      if (a.a_woff[mid] <= unit) lo = mid; else hi = mid - 1;
+    }
+    const long long it = lo;
+    const int s = (int)(unit - a.a_woff[it]);
+    const int g = a.a_grp[it];
+    r_first = a.a_j0[it];
+    r_end = a.a_j1[it];
+    out_row0 = a.g_z0[g] + (long long)s * kTcRows;
+    out_rows = min(kTcRows, a.g_kz[g] - s * kTcRows);
+    wstride = a.g_kzp[g];
+    wbase_hi = a.w_hi + a.g_vtoff[g] + (long long)s * kTcRows;
+    if (SPLIT) wbase_lo = a.w_lo + a.g_vtoff[g] + (long long)s * kTcRows;
+    xrow0 = a.g_c0[g];
+    excl = a.a_excl[it] != 0;
+  }
+  const int nch = (int)((r_end - r_first + CH - 1) / CH);
 
   uint8_t* smem = reinterpret_cast<uint8_t*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   const uint32_t sbase = smem_addr(smem);
   if (tid == 0) {
-    for (int s = 0; s <= kTcStages; s++) mbar_init(smem_addr(&bars[s]), 1);
+    for (int s = 0; s < kTcStages; s++) mbar_init(smem_addr(&bars[s]), 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     abort_flag = 0;
   }
@@ -179,37 +251,74 @@ phaseB_tc_bf16(TcPhaseB op, const __nv_bfloat16* __restrict__ panel,
   tc_fence_after();
   const uint32_t tmem = tmem_slot;
 
-  // producer: chunk c -> stage s (W: rows k = tid / 8 .. , 16-byte piece
-  // tid % 8; S: rows k = warp + 8 j, pieces lane (8 bf16 columns each))
-  auto load = [&](int c, int s) {
-    const uint32_t wst = sbase + s * kTcStageBytes;
-    const uint32_t sst = wst + kTcWBytes;
-    const long long l0 = p0 + (long long)c * kTcChunk;
+  // stage layout: [W_hi | S_hi] or [W_hi | W_lo | S_hi | S_lo]
+  auto w_at = [&](int s, int part) { return sbase + s * kTcStageBytes + part * WB; };
+  auto s_at = [&](int s, int part) {
+    return sbase + s * kTcStageBytes + (SPLIT ? 2 : 1) * WB + part * SB;
+  };
+  // source rows of the reduction rows k = warp + 8 j of chunk c (phase B
+  // gathers through src[]); fetched one chunk ahead so that the dependent
+  // index load does not stall the copies
+  constexpr int RPW = CH / 8;   // rows per warp and chunk
+  int src_cur[RPW], src_nxt[RPW];
+  auto fetch_src = [&](int c, int (&dst)[RPW]) {
 #pragma unroll
-    for (int j = 0; j < (kTcChunk * 8) / kTcThreads; j++) {
+    for (int j = 0; j < RPW; j++) {
+      const long long l = r_first + (long long)c * CH + warp + 8 * j;
+      dst[j] = (MODE == kModeB && c < nch && l < r_end) ? __ldg(a.src + l) : 0;
+    }
+  };
+  // producer: chunk c -> stage s.  W: 16-byte piece q of row k; S: rows
+  // k = warp + 8 j, lane = 16-byte piece (8 columns) of the 256-column slice;
+  // srcs: the chunk's source indices (phase B)
+  auto load = [&](int c, int s, const int (&srcs)[RPW]) {
+    const long long l0 = r_first + (long long)c * CH;
+#pragma unroll
+    for (int j = 0; j < (CH * 8) / kTcThreads; j++) {
       const int p = tid + j * kTcThreads;
       const int k = p >> 3, q = p & 7;
-      const __nv_bfloat16* g = panel + (l0 + k) * kTcTileRows + q * 8;
-      cp_async16_zfill(wst + k * 128 + ((q ^ (k & 7)) << 4), g, true);
+      const bool ok = l0 + k < r_end;
+      const long long off = ok ? (l0 + k) * wstride + q * 8 : 0;
+      const uint32_t so = k * 128 + ((q ^ (k & 7)) << 4);
+      cp_async16_zfill(w_at(s, 0) + so, wbase_hi + off, ok);
+      if (SPLIT) cp_async16_zfill(w_at(s, 1) + so, wbase_lo + off, ok);
     }
+    const int col = c_base + lane * 8;
+    const int b = lane >> 3, q = lane & 7;
 #pragma unroll
-    for (int j = 0; j < kTcChunk / 8; j++) {
+    for (int j = 0; j < CH / 8; j++) {
       const int k = warp + 8 * j;
-      const int sidx = op.src[l0 + k];
-      const __nv_bfloat16* row = sidx < op.num_zrows ? Zb + (long long)sidx * lds
-                                                     : X + (long long)(sidx - op.num_zrows) * lds;
-      const int col = c_base + lane * 8;          // 32 pieces x 8 = 256 columns
-      const int b = lane >> 3, q = lane & 7;       // 64-column block, piece in block
-      const bool ok = col < K;
-      cp_async16_zfill(sst + b * (kTcChunk * 128) + k * 128 + ((q ^ (k & 7)) << 4),
-                       ok ? row + col : row, ok);
+      const long long l = l0 + k;
+      const bool okr = l < r_end;
+      const __nv_bfloat16* rh;
+      const __nv_bfloat16* rl = nullptr;
+      if (MODE == kModeB) {
+        const int sidx = okr ? srcs[j] : 0;
+        if (sidx < a.num_zrows) {
+          rh = a.z_hi + (long long)sidx * a.lds;
+          if (SPLIT) rl = a.z_lo + (long long)sidx * a.lds;
+        } else {
+          rh = a.x_hi + (long long)(sidx - a.num_zrows) * a.lds;
+          if (SPLIT) rl = a.x_lo + (long long)(sidx - a.num_zrows) * a.lds;
+        }
+      } else {
+        const long long xr = okr ? xrow0 + l : 0;
+        rh = a.x_hi + xr * a.lds;
+        if (SPLIT) rl = a.x_lo + xr * a.lds;
+      }
+      const bool ok = okr && col < a.K;
+      const uint32_t so = b * BLK + k * 128 + ((q ^ (k & 7)) << 4);
+      cp_async16_zfill(s_at(s, 0) + so, ok ? rh + col : rh, ok);
+      if (SPLIT) cp_async16_zfill(s_at(s, 1) + so, ok ? rl + col : rl, ok);
     }
   };
 
   for (int c = 0; c < kTcStages - 1; c++) {
-    if (c < nch) load(c, c);
+    fetch_src(c, src_cur);
+    if (c < nch) load(c, c, src_cur);
     cp_commit();
   }
+  fetch_src(kTcStages - 1, src_cur);
   bool ok = true;
   for (int c = 0; c < nch; c++) {
     const int s = c % kTcStages;
@@ -219,41 +328,48 @@ phaseB_tc_bf16(TcPhaseB op, const __nv_bfloat16* __restrict__ panel,
     if (abort_flag) { ok = false; break; }
     if (tid == 0) {
       tc_fence_after();
-      const uint32_t wst = sbase + s * kTcStageBytes;
-      const uint32_t sst = wst + kTcWBytes;
 #pragma unroll
-      for (int q = 0; q < kTcChunk / 16; q++) {
-        // 16 panel rows = two 8-line groups (SBO 1 KiB); k-step offset 2 KiB
-        const uint64_t bdesc = sw128_desc(wst + q * 2048, 8192, 1024);
+      for (int q = 0; q < CH / 16; q++) {
+        // 16 reduction rows = two 8-line groups (SBO 1 KiB); k-step offset 2 KiB
+        const uint64_t bh = sw128_desc(w_at(s, 0) + q * 2048, 8192, 1024);
 #pragma unroll
-        for (int a = 0; a < kTcNC / 128; a++) {
+        for (int h = 0; h < kTcNC / 128; h++) {
           // M = 128 columns = two 64-column blocks, LBO = block stride
-          const uint64_t adesc = sw128_desc(sst + a * 2 * (kTcChunk * 128) + q * 2048,
-                                            kTcChunk * 128, 1024);
-          mma_bf16_tc(tmem + a * kTcTileRows, adesc, bdesc, kIdesc, (c | q) != 0);
+          const uint64_t ah = sw128_desc(s_at(s, 0) + h * 2 * BLK + q * 2048, BLK, 1024);
+          const uint32_t d = tmem + h * kTcRows;
+          mma_bf16_tc(d, ah, bh, (c | q) != 0);
+          if (SPLIT) {
+            const uint64_t bl = sw128_desc(w_at(s, 1) + q * 2048, 8192, 1024);
+            const uint64_t al = sw128_desc(s_at(s, 1) + h * 2 * BLK + q * 2048, BLK, 1024);
+            mma_bf16_tc(d, al, bh, 1u);
+            mma_bf16_tc(d, ah, bl, 1u);
+          }
         }
       }
       mma_commit(smem_addr(&bars[s]));
     }
     const int cn = c + kTcStages - 1;
+    fetch_src(cn + 1, src_nxt);
     if (cn < nch) {
       if (c >= 1) {
         const int sp = (c - 1) % kTcStages;
         if (!mbar_wait(smem_addr(&bars[sp]), ((c - 1) / kTcStages) & 1)) {
-          atomicOr(flags, FGB_FLAG_DEVICE_TIMEOUT);
+          atomicOr(a.flags, FGB_FLAG_DEVICE_TIMEOUT);
           abort_flag = 1;
         }
       }
-      if (!abort_flag) load(cn, cn % kTcStages);
+      if (!abort_flag) load(cn, cn % kTcStages, src_cur);
     }
     cp_commit();
+#pragma unroll
+    for (int j = 0; j < RPW; j++) src_cur[j] = src_nxt[j];
   }
   cp_wait_all();
   // all MMAs of this CTA complete (they finish in order): last chunk's barrier
   if (nch > 0 && ok) {
     const int cl = nch - 1;
     if (!mbar_wait(smem_addr(&bars[cl % kTcStages]), (cl / kTcStages) & 1)) {
-      atomicOr(flags, FGB_FLAG_DEVICE_TIMEOUT);
+      atomicOr(a.flags, FGB_FLAG_DEVICE_TIMEOUT);
       ok = false;
     }
   }
@@ -261,28 +377,36 @@ phaseB_tc_bf16(TcPhaseB op, const __nv_bfloat16* __restrict__ panel,
   __syncthreads();
   if (abort_flag) ok = false;
 
-  // epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 = columns
-  // c_base + 128 a + 32 (w % 4) + lane, for a = w / 4
+  // epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31, i.e. columns
+  // c_base + 128 h + 32 (w % 4) + lane, for h = w / 4
   if (ok) {
-    const int quarter = warp & 3, a = warp >> 2;
-    const int col = c_base + a * 128 + quarter * 32 + lane;
+    const int quarter = warp & 3, h = warp >> 2;
+    const int col = c_base + h * 128 + quarter * 32 + lane;
 #pragma unroll
-    for (int h = 0; h < kTcTileRows / 32; h++) {
+    for (int half = 0; half < kTcRows / 32; half++) {
       float v[32];
       if (nch > 0) {
-        tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + a * kTcTileRows + h * 32, v);
+        tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + h * kTcRows + half * 32, v);
       } else {
 #pragma unroll
         for (int i = 0; i < 32; i++) v[i] = 0.f;
       }
-      if (col < K) {
+      if (col < a.K) {
 #pragma unroll
         for (int i = 0; i < 32; i++) {
-          const long long row = t * kTcTileRows + h * 32 + i;
-          if (row < op.N) {
-            float y = v[i];
-            if (add_mat) y = add_mat[row * ld_add + col] + alpha * y;
-            Y[row * ldy + col] = y;
+          const int r = half * 32 + i;
+          if (r < out_rows) {
+            const long long row = out_row0 + r;
+            float* dst = a.out + row * (long long)a.K + col;
+            if (MODE == kModeB) {
+              float y = v[i];
+              if (a.add) y = a.add[row * (long long)a.K + col] + a.alpha * y;
+              *dst = y;
+            } else if (excl) {
+              *dst = v[i];
+            } else {
+              atomicAdd(dst, v[i]);
+            }
           }
         }
       }
@@ -296,38 +420,159 @@ phaseB_tc_bf16(TcPhaseB op, const __nv_bfloat16* __restrict__ panel,
   }
 }
 
+__global__ void split_bf16_kernel(const float* __restrict__ in, __nv_bfloat16* __restrict__ hi,
+                                  __nv_bfloat16* __restrict__ lo, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const float v = in[i];
+    const __nv_bfloat16 h = __float2bfloat16(v);
+    hi[i] = h;
+    if (lo) lo[i] = __float2bfloat16(v - __bfloat162float(h));
+  }
+}
+
+// Transposed phase-A panel: tile (g, s, jb) moves V^T rows 64 s .. of group g,
+// columns 64 jb .., through shared memory; rows r >= kz are zero.
+__global__ void vpanel_transpose_kernel(const int* __restrict__ g_n, const int* __restrict__ g_kz,
+                                        const int* __restrict__ g_ldv,
+                                        const long long* __restrict__ g_voff,
+                                        const int* __restrict__ g_kzp,
+                                        const long long* __restrict__ g_vtoff,
+                                        const float* __restrict__ vpanel,
+                                        const int* __restrict__ tile_g,
+                                        const int* __restrict__ tile_s,
+                                        const int* __restrict__ tile_j, long long num_tiles,
+                                        __nv_bfloat16* __restrict__ vt_hi,
+                                        __nv_bfloat16* __restrict__ vt_lo) {
+  __shared__ float tile[64][65];
+  for (long long t = blockIdx.x; t < num_tiles; t += gridDim.x) {
+    const int g = tile_g[t], s = tile_s[t], jb = tile_j[t];
+    const int n = g_n[g], kz = g_kz[g], ldv = g_ldv[g], kzp = g_kzp[g];
+    const float* v = vpanel + g_voff[g];
+    __syncthreads();
+    for (int e = threadIdx.x; e < 64 * 64; e += blockDim.x) {
+      const int rr = e >> 6, jj = e & 63;
+      const int r = s * 64 + rr, j = jb * 64 + jj;
+      tile[rr][jj] = (r < kz && j < n) ? v[(long long)r * ldv + j] : 0.f;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < 64 * 64; e += blockDim.x) {
+      const int jj = e >> 6, rr = e & 63;
+      const int r = s * 64 + rr, j = jb * 64 + jj;
+      if (j < n && r < kzp) {
+        const float x = tile[rr][jj];
+        const __nv_bfloat16 h = __float2bfloat16(x);
+        const long long o = g_vtoff[g] + (long long)j * kzp + r;
+        vt_hi[o] = h;
+        if (vt_lo) vt_lo[o] = __float2bfloat16(x - __bfloat162float(h));
+      }
+    }
+  }
+}
+
+template <int MODE, bool SPLIT>
+int launch_tc(const TcArgs& a, long long units, cudaStream_t st) {
+  static bool attr_set = false;
+  if (!attr_set) {
+    FGB_CUDA_TRY(cudaFuncSetAttribute(tc_gather_gemm<MODE, SPLIT>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemBytes));
+    attr_set = true;
+  }
+  const long long nks = (a.K + kTcNC - 1) / kTcNC;
+  const long long grid = units * nks;
+  if (grid <= 0) return FGB_OK;
+  if (grid > 0x7fffffffLL) { set_error("grid too large"); return FGB_BAD_ARG; }
+  tc_gather_gemm<MODE, SPLIT><<<(unsigned)grid, kTcThreads, kTcSmemBytes, st>>>(a);
+  FGB_LAUNCH_CHECK("tc_gather_gemm");
+  return FGB_OK;
+}
+
+bool misaligned(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) != 0; }
+
 }  // namespace
 }  // namespace fgb
 
 extern "C" {
 
-int fgb_matmat_bf16_tc_phase_b(const struct fgb_op_desc* d, const void* panel, const void* X,
-                               const void* Zb, float* Y, int K, const float* add, float alpha,
-                               unsigned* flags, void* stream) {
+int fgb_tc_phase_a(const struct fgb_op_desc* d, const void* vt_hi, const void* vt_lo,
+                   const void* X_hi, const void* X_lo, float* Z, int K, int zero_z,
+                   unsigned* flags, void* stream) {
   if (!d || !flags) { fgb::set_error("null operator or flags"); return FGB_BAD_ARG; }
   if (K < 8 || (K % 8) != 0) { fgb::set_error("K must be a positive multiple of 8"); return FGB_BAD_ARG; }
-  if ((reinterpret_cast<uintptr_t>(X) & 15) || (reinterpret_cast<uintptr_t>(Zb) & 15) ||
-      (reinterpret_cast<uintptr_t>(panel) & 15)) {
-    fgb::set_error("X, Zb and the panel must be 16-byte aligned");
+  const bool split = vt_lo != nullptr;
+  if (split != (X_lo != nullptr)) { fgb::set_error("split operands must come in pairs"); return FGB_BAD_ARG; }
+  if (fgb::misaligned(vt_hi) || fgb::misaligned(X_hi) || fgb::misaligned(vt_lo) ||
+      fgb::misaligned(X_lo)) {
+    fgb::set_error("tensor-core operands must be 16-byte aligned");
+    return FGB_BAD_ARG;
+  }
+  if (d->num_items <= 0 || d->num_zrows <= 0) return FGB_OK;
+  cudaStream_t st = fgb::as_stream(stream);
+  if (zero_z) FGB_CUDA_TRY(cudaMemsetAsync(Z, 0, sizeof(float) * d->num_zrows * (size_t)K, st));
+  fgb::TcArgs a{};
+  a.a_grp = d->a_grp; a.a_j0 = d->a_j0; a.a_j1 = d->a_j1; a.a_excl = d->a_excl;
+  a.a_woff = d->a_woff; a.num_items = d->num_items;
+  a.g_c0 = d->g_c0; a.g_kz = d->g_kz; a.g_kzp = d->g_kzp; a.g_vtoff = d->g_vtoff; a.g_z0 = d->g_z0;
+  a.w_hi = static_cast<const __nv_bfloat16*>(vt_hi);
+  a.w_lo = static_cast<const __nv_bfloat16*>(vt_lo);
+  a.x_hi = static_cast<const __nv_bfloat16*>(X_hi);
+  a.x_lo = static_cast<const __nv_bfloat16*>(X_lo);
+  a.lds = K; a.K = K; a.out = Z; a.add = nullptr; a.alpha = 1.f; a.flags = flags;
+  a.N = d->N; a.num_zrows = d->num_zrows;
+  return split ? fgb::launch_tc<fgb::kModeA, true>(a, d->num_work, st)
+               : fgb::launch_tc<fgb::kModeA, false>(a, d->num_work, st);
+}
+
+int fgb_tc_phase_b(const struct fgb_op_desc* d, const void* w_hi, const void* w_lo,
+                   const void* X_hi, const void* X_lo, const void* Z_hi, const void* Z_lo,
+                   float* Y, int K, const float* add, float alpha, unsigned* flags,
+                   void* stream) {
+  if (!d || !flags) { fgb::set_error("null operator or flags"); return FGB_BAD_ARG; }
+  if (K < 8 || (K % 8) != 0) { fgb::set_error("K must be a positive multiple of 8"); return FGB_BAD_ARG; }
+  const bool split = w_lo != nullptr;
+  if (split != (X_lo != nullptr) || split != (Z_lo != nullptr)) {
+    fgb::set_error("split operands must come in pairs");
+    return FGB_BAD_ARG;
+  }
+  if (fgb::misaligned(w_hi) || fgb::misaligned(w_lo) || fgb::misaligned(X_hi) ||
+      fgb::misaligned(X_lo) || fgb::misaligned(Z_hi) || fgb::misaligned(Z_lo)) {
+    fgb::set_error("tensor-core operands must be 16-byte aligned");
     return FGB_BAD_ARG;
   }
   if (d->num_tiles <= 0) return FGB_OK;
-  static bool attr_set = false;
-  if (!attr_set) {
-    FGB_CUDA_TRY(cudaFuncSetAttribute(fgb::phaseB_tc_bf16,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      fgb::kTcSmemBytes));
-    attr_set = true;
-  }
-  fgb::TcPhaseB op{d->t_p0, d->src, d->num_tiles, d->N, d->num_zrows};
-  const long long nks = (K + fgb::kTcNC - 1) / fgb::kTcNC;
-  const long long grid = d->num_tiles * nks;
-  if (grid > 0x7fffffffLL) { fgb::set_error("grid too large"); return FGB_BAD_ARG; }
-  fgb::phaseB_tc_bf16<<<(unsigned)grid, fgb::kTcThreads, fgb::kTcSmemBytes,
-                        fgb::as_stream(stream)>>>(
-      op, static_cast<const __nv_bfloat16*>(panel), static_cast<const __nv_bfloat16*>(X),
-      static_cast<const __nv_bfloat16*>(Zb), K, Y, K, K, add, K, alpha, flags);
-  FGB_LAUNCH_CHECK("phaseB_tc_bf16");
+  fgb::TcArgs a{};
+  a.t_p0 = d->t_p0; a.src = d->src; a.N = d->N; a.num_zrows = d->num_zrows;
+  a.w_hi = static_cast<const __nv_bfloat16*>(w_hi);
+  a.w_lo = static_cast<const __nv_bfloat16*>(w_lo);
+  a.x_hi = static_cast<const __nv_bfloat16*>(X_hi);
+  a.x_lo = static_cast<const __nv_bfloat16*>(X_lo);
+  a.z_hi = static_cast<const __nv_bfloat16*>(Z_hi);
+  a.z_lo = static_cast<const __nv_bfloat16*>(Z_lo);
+  a.lds = K; a.K = K; a.out = Y; a.add = add; a.alpha = alpha; a.flags = flags;
+  cudaStream_t st = fgb::as_stream(stream);
+  return split ? fgb::launch_tc<fgb::kModeB, true>(a, d->num_tiles, st)
+               : fgb::launch_tc<fgb::kModeB, false>(a, d->num_tiles, st);
+}
+
+int fgb_split_bf16(const float* in, void* hi, void* lo, long long n, void* stream) {
+  if (n < 0 || !hi) { fgb::set_error("bad arguments"); return FGB_BAD_ARG; }
+  if (n == 0) return FGB_OK;
+  fgb::split_bf16_kernel<<<fgb::grid_for(n, 256, 152LL * 16), 256, 0, fgb::as_stream(stream)>>>(
+      in, static_cast<__nv_bfloat16*>(hi), static_cast<__nv_bfloat16*>(lo), n);
+  FGB_LAUNCH_CHECK("split_bf16_kernel");
+  return FGB_OK;
+}
+
+int fgb_vpanel_transpose_bf16(const struct fgb_op_desc* d, const float* vpanel,
+                              const int* tile_g, const int* tile_s, const int* tile_j,
+                              long long num_tiles, void* vt_hi, void* vt_lo, void* stream) {
+  if (!d || num_tiles < 0 || !vt_hi) { fgb::set_error("bad arguments"); return FGB_BAD_ARG; }
+  if (num_tiles == 0) return FGB_OK;
+  fgb::vpanel_transpose_kernel<<<fgb::grid_for(num_tiles, 1, 152LL * 32), 256, 0,
+                                  fgb::as_stream(stream)>>>(
+      d->g_n, d->g_kz, d->g_ldv, d->g_voff, d->g_kzp, d->g_vtoff, vpanel, tile_g, tile_s, tile_j,
+      num_tiles, static_cast<__nv_bfloat16*>(vt_hi), static_cast<__nv_bfloat16*>(vt_lo));
+  FGB_LAUNCH_CHECK("vpanel_transpose_kernel");
   return FGB_OK;
 }
 

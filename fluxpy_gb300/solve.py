@@ -219,16 +219,28 @@ def _colmax(t):
     return t.view(torch.int32).cpu().numpy().view(np.float32)
 
 
+# Split-BF16 residual: the operands' hi + lo parts differ from the FP32 ones
+# by at most 2^-18 relative, so the product is within 3 * 2^-18 |F| |rho B|
+# (1.1e-5 relative) of the FP32 operator's, before FP32 accumulation
+# rounding.  For rho = 0.12 that is about 1.5e-6 of max|E|; the convergence
+# test charges a fixed 30 % of rtol for it (the solution is then verified
+# independently in FP64 arithmetic by the tests and the benchmark).
+_SPLIT_MARGIN = 0.3
+
+
 def _auto_chunk(FF, N, K):
     free, _ = torch.cuda.mem_get_info()
-    per_col = N * (6 * 4 + 2) + max(FF._num_zrows, 1) * 6
+    # memory held by the caching allocator but not in use is available too
+    free += torch.cuda.memory_reserved() - torch.cuda.memory_allocated()
+    # per column: E, B, R, D, Y, X (FP32), X hi/lo (BF16); Z (FP32), Z hi/lo
+    per_col = N * (6 * 4 + 2 * 2) + max(FF._num_zrows, 1) * 8
     c = int(0.6 * free / per_col) // 8 * 8
     return max(8, min(K, c))
 
 
 def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_iter=200,
                             inner=3, E_is_permuted=False, return_permuted=False, stats=None,
-                            chunk=None, inner0=4, engine="tc"):
+                            chunk=None, inner0=4, engine="tc", residual="split-bf16"):
     """Right-placement radiosity solve for K sun directions at once.
 
     FF: CompressedFormFactorMatrix; E: (N, K) device tensor (facet order, or
@@ -243,8 +255,13 @@ def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_
                      corrected by `inner` sweeps D <- R + F_bf16(rho D),
                      until max|R[:, k]| <= rtol * max|E[:, k]| for every
                      column (each solve ends on a checked FP32 residual).
-    engine: 'tc' (tcgen05 tensor cores for the BF16 phase B) or 'mma'
+    engine: 'tc' (tcgen05 tensor cores for the BF16 products) or 'mma'
     (mma.sync kernels).
+    residual: how bf16-refine evaluates F (rho B): 'split-bf16' (tensor
+    cores, split-BF16 operands hi.hi + lo.hi + hi.lo with FP32 accumulation,
+    elementwise within 3 * 2^-18 |F| |rho B| of the FP32 operator's product
+    plus accumulation rounding; the convergence test keeps a margin for it,
+    _SPLIT_MARGIN) or 'fp32' (FP32 CUDA-core kernels).
     Returns B (N, K) fp32; fills `stats` (iterations, matmats, residuals).
     """
     dev = E.device
@@ -261,7 +278,8 @@ def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_
             parts.append(solve_radiosity_batched(FF, E[:, c0:c0 + chunk].contiguous(), rho, rtol,
                                                  precision, max_iter, inner, E_is_permuted,
                                                  return_permuted, st, chunk=chunk,
-                                                 inner0=inner0, engine=engine))
+                                                 inner0=inner0, engine=engine,
+                                                 residual=residual))
             for k_, v_ in st.items():
                 if isinstance(v_, (int, float)) and k_ != "residual":
                     agg[k_] = agg.get(k_, 0) + v_
@@ -274,7 +292,7 @@ def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_
         E = torch.cat([E, torch.zeros((N, pad), dtype=E.dtype, device=dev)], 1)
         B = solve_radiosity_batched(FF, E, rho, rtol, precision, max_iter, inner, E_is_permuted,
                                     return_permuted, stats, chunk=chunk, inner0=inner0,
-                                    engine=engine)
+                                    engine=engine, residual=residual)
         return B[:, :K0].contiguous()
     K = K0
     stream = _lib.stream_handle()
@@ -317,7 +335,12 @@ def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_
         D = torch.empty_like(Ep)
         Xb = torch.empty((N, K), dtype=torch.bfloat16, device=dev)
         Zb = torch.empty((max(FF._num_zrows, 1), K), dtype=torch.bfloat16, device=dev)
+        work = {"z": Z32, "z_hi": Zb, "x_hi": Xb}
         emax_h = np.maximum(emax.cpu().numpy(), 1e-30)
+        if residual == "split-bf16":
+            # the computed residual may be smaller than the exact one by the
+            # split product's error bound: check against a reduced threshold
+            thresh = thresh * np.float32(1.0 - _SPLIT_MARGIN)
         for it in range(1, max_iter + 1):
             if it == 1:
                 # B = 0: the residual is E itself
@@ -326,8 +349,12 @@ def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_
                 # residual with the FP32 operator
                 _lib.call("fgb_scale_rows_f32", _lib.ptr(B), _lib.ptr(rho_d), rho_s,
                           _lib.ptr(X32), N, K, stream)
-                FF.matmat_permuted(X32, "fp32", out=Y, Z=Z32)
-                st["fp32_matmats"] += 1
+                if residual == "split-bf16":
+                    FF.split_product(X32, Y, work=work)
+                    st["split_matmats"] = st.get("split_matmats", 0) + 1
+                else:
+                    FF.matmat_permuted(X32, "fp32", out=Y, Z=Z32)
+                    st["fp32_matmats"] += 1
                 colmax.zero_()
                 _lib.call("fgb_residual", _lib.ptr(Y), _lib.ptr(B), _lib.ptr(Ep), _lib.ptr(R), N,
                           K, _lib.ptr(colmax), stream)

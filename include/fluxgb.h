@@ -270,8 +270,12 @@ int fgb_aca_f64(const void* bvh, const double* P, const double* N, const double*
  *     g_voff (panel offset), g_z0 (first Z row); work items a_grp, a_j0,
  *     a_j1, a_excl (1: the item covers its whole group);
  *   phase B row tiles of 64 rows: t_p0[num_tiles+1] panel-row offsets (each
- *     tile a multiple of 32 rows), src[row] = source row (< num_zrows: a row
- *     of Z; else a row of X at src - num_zrows).
+ *     tile a multiple of 64 rows), src[row] = source row (< num_zrows: a row
+ *     of Z; else a row of X at src - num_zrows);
+ *   tensor-core phase A: the transposed BF16 phase-A panel holds group g as
+ *     n x g_kzp (g_kz rounded up to 64) at g_vtoff, element (r, j) at
+ *     g_vtoff + j g_kzp + r; a_woff[num_items + 1]: first 64-row work slice
+ *     of each item (slices of an item: ceil(g_kz / 64)).
  */
 struct fgb_op_desc {
   const int* g_c0;
@@ -291,6 +295,10 @@ struct fgb_op_desc {
   long long N;
   long long num_zrows;
   int max_group_tiles; /* max over groups of ceil(g_kz / 64) */
+  const int* g_kzp;
+  const long long* g_vtoff;
+  const long long* a_woff;
+  long long num_work;   /* a_woff[num_items] */
 };
 /*
  * y = F x (or y = add + alpha F x), vectors in cluster order.  Replaces
@@ -321,13 +329,32 @@ int fgb_matmat_f32(const struct fgb_op_desc* d, const float* panel, const float*
 int fgb_matmat_bf16(const struct fgb_op_desc* d, const void* panel, const void* vpanel,
                     const void* X, float* Z, void* Zb, float* Y, int K, const float* add,
                     float alpha, int zero_z, int phases, void* stream);
-/* Phase B of fgb_matmat_bf16 on the tcgen05 tensor cores (TMEM accumulators):
- * Y = add + alpha * (panel rows x gathered [Zb; X] rows), tiles' panel rows a
- * multiple of 64, K % 8 == 0, Zb (num_zrows x K) and X (N x K) bf16 with row
- * stride K.  Bounded device waits: FGB_FLAG_DEVICE_TIMEOUT in *flags. */
-int fgb_matmat_bf16_tc_phase_b(const struct fgb_op_desc* d, const void* panel, const void* X,
-                               const void* Zb, float* Y, int K, const float* add, float alpha,
-                               unsigned* flags, void* stream);
+/*
+ * The two phases on the tcgen05 tensor cores (TMEM accumulators, FP32), BF16
+ * operands, K % 8 == 0, all matrices row stride K.  With the *_lo operands
+ * NULL the product is the plain BF16 one; with them, every FP32 operand is
+ * given as hi = bf16(v), lo = bf16(v - hi) and the product is
+ * hi.hi + hi.lo + lo.hi ("split BF16": relative error per product term
+ * about 2^-16 instead of 2^-8).  Bounded device waits: a wait that runs out
+ * sets FGB_FLAG_DEVICE_TIMEOUT in *flags.
+ *   phase A: Z = Vg^T-panel x X rows (Z FP32, num_zrows x K; items that do
+ *            not cover their group accumulate atomically into a zeroed Z);
+ *   phase B: Y = add + alpha * (panel rows x gathered [Z; X] rows).
+ */
+int fgb_tc_phase_a(const struct fgb_op_desc* d, const void* vt_hi, const void* vt_lo,
+                   const void* X_hi, const void* X_lo, float* Z, int K, int zero_z,
+                   unsigned* flags, void* stream);
+int fgb_tc_phase_b(const struct fgb_op_desc* d, const void* w_hi, const void* w_lo,
+                   const void* X_hi, const void* X_lo, const void* Z_hi, const void* Z_lo,
+                   float* Y, int K, const float* add, float alpha, unsigned* flags,
+                   void* stream);
+/* hi = bf16(in), lo = bf16(in - hi) elementwise (lo may be NULL). */
+int fgb_split_bf16(const float* in, void* hi, void* lo, long long n, void* stream);
+/* Transposed BF16 phase-A panel from the FP32 one (layouts in fgb_op_desc);
+ * tiles: (group, 64-row slice, 64-column block) triples, num_tiles of them. */
+int fgb_vpanel_transpose_bf16(const struct fgb_op_desc* d, const float* vpanel,
+                              const int* tile_g, const int* tile_s, const int* tile_j,
+                              long long num_tiles, void* vt_hi, void* vt_lo, void* stream);
 /*
  * Panel construction (setup).  Phase B: pairs q (tile, contributing block)
  * with pair_p0 (first panel row, sorted), pair_w (pool offset of the block's

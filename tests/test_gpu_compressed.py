@@ -160,26 +160,38 @@ def test_batched_solvers_reach_rtol():
     dirs = terrain.random_sun_directions(64, seed=2)
     E = sm.get_direct_irradiance_batch(1365.0, dirs, out_dtype=torch.float32)
     assert E.shape == (sm.num_faces, 64)
-    for prec in ("fp32", "bf16-refine"):
+    cases = [("fp32", "tc", "fp32", 2e-5), ("bf16-refine", "tc", "split-bf16", 1e-5),
+             ("bf16-refine", "tc", "fp32", 1e-5), ("bf16-refine", "mma", "fp32", 1e-5)]
+    for prec, eng, res, bound in cases:
         st = {}
-        B = solve_radiosity_batched(FF, E, 0.12, rtol=1e-5, precision=prec, stats=st)
-        # residual with the operator in FP64 arithmetic
+        B = solve_radiosity_batched(FF, E, 0.12, rtol=1e-5, precision=prec, stats=st,
+                                    engine=eng, residual=res)
+        # residual with the operator in FP64 arithmetic; the plain Jacobi
+        # path stops on its update size (as the reference does), the
+        # refinement on the residual itself
         Bp = FF.permute(B.double())
         FBp = FF.matmat_permuted(Bp[:, :8].contiguous() * 0.12, "fp64")
         Ep = FF.permute(E.double())[:, :8]
         R = Ep - (Bp[:, :8] - FBp)
         rel = (R.abs().amax(0) / Ep.abs().amax(0).clamp_min(1e-30)).max().item()
-        assert rel <= 2e-5, (prec, rel, st)
+        assert rel <= bound, (prec, eng, res, rel, st)
 
 
-@pytest.mark.parametrize("K", [256, 200, 1024])
-def test_tensor_core_phase_b_matches_mma(K):
-    """The tcgen05 phase-B kernel against the mma.sync kernels on the same
-    BF16 operands (FP32 accumulation in both: only the summation order
-    differs), and both against the FP64 product."""
+@pytest.fixture(scope="module")
+def terrain_op():
     sm = _terrain_case(64)
     FF = CompressedFormFactorMatrix(sm, tol=1e-5, min_size=4096, dtype=np.float32,
                                     RootBlock=FormFactorOctreeBlock)
+    return sm, FF
+
+
+@pytest.mark.parametrize("K", [256, 200, 1024])
+def test_tensor_core_product_matches_mma(terrain_op, K):
+    """The tcgen05 kernels (both phases) against the mma.sync kernels on the
+    same BF16 operands (FP32 accumulation in both: only the summation order
+    differs, and with it a rare last-bit rounding of the BF16 copy of Z), and
+    both against the FP64 product."""
+    sm, FF = terrain_op
     N = sm.num_faces
     g = torch.Generator(device="cuda").manual_seed(K)
     Xp = torch.rand((N, K), device="cuda", generator=g)
@@ -197,8 +209,35 @@ def test_tensor_core_phase_b_matches_mma(K):
     assert torch.isfinite(outs["tc"]).all()
     ref = (outs["mma"] - add).abs().max().item()
     d = (outs["tc"] - outs["mma"]).abs().max().item()
-    assert d <= 1e-5 * max(ref, 1e-30) + 1e-6, (d, ref)
+    assert d <= 2e-3 * ref, (d, ref)
     # against FP64 (BF16 rounding of operator and sources)
     Y64 = FF.matmat_permuted(Xp[:, :4].double().contiguous(), "fp64")
     yt = (outs["tc"][:, :4].double() - add[:, :4].double()) / 0.5
     assert (yt - Y64).abs().max().item() <= 2e-2 * Y64.abs().max().item()
+
+
+@pytest.mark.parametrize("K", [64, 264])
+def test_split_bf16_product_accuracy(terrain_op, K):
+    """Split-BF16 tensor-core product of the FP32 operator against the same
+    operator applied in FP64 arithmetic: within a few 1e-6 of max |F x|, like
+    the FP32 CUDA-core product."""
+    sm, FF = terrain_op
+    N = sm.num_faces
+    g = torch.Generator(device="cuda").manual_seed(K + 1)
+    X = torch.rand((N, K), device="cuda", generator=g)
+    Y = torch.full((N, K), float("nan"), device="cuda")
+    FF.split_product(X, Y)
+    FF.check_device_flags()
+    Y32 = FF.matmat_permuted(X, "fp32")
+    for c in (0, K // 2, K - 1):
+        y64 = FF.matvec_permuted(X[:, c].double().contiguous(), "fp32-fp64")
+        ref = y64.abs().max().item()
+        e_split = (Y[:, c].double() - y64).abs().max().item() / ref
+        e_fp32 = (Y32[:, c].double() - y64).abs().max().item() / ref
+        assert e_split <= 5e-6, (c, e_split, e_fp32)
+        assert e_fp32 <= 5e-6, (c, e_split, e_fp32)
+    # with add / alpha
+    add = torch.rand((N, K), device="cuda", generator=g)
+    Y2 = torch.empty_like(Y)
+    FF.split_product(X, Y2, add=add, alpha=-0.25)
+    assert torch.allclose(Y2, add - 0.25 * Y, rtol=0, atol=1e-5 * Y.abs().max().item())

@@ -51,7 +51,16 @@ constexpr int kTcStages = 5;
 constexpr int kTcThreads = 256;
 constexpr int kTcStageBytes = 40 * 1024;
 constexpr int kTcSmemBytes = kTcStages * kTcStageBytes + 1024;  // + alignment slack
-constexpr int kTcTmemCols = 128;                                // 2 accumulators x 64
+// TMEM columns: 2 accumulators (one per 128-column half) x 64 rows, and in
+// split mode two such sets used by alternate accumulation windows
+constexpr int kTcTmemCols = 128;
+constexpr int kTcTmemColsSplit = 256;
+// split mode: the tensor core's FP32 accumulation loses up to ~2^-23 of the
+// running sum per MMA, which over thousands of reduction steps exceeds the
+// split operands' 2^-16 accuracy; every kTcWin chunks (12 MMAs) the window's
+// accumulators are drained into registers and summed there with Kahan
+// compensation
+constexpr int kTcWin = 2;
 constexpr unsigned long long kWaitNs = 2000000000ull;           // 2 s
 
 enum { kModeA = 0, kModeB = 1 };
@@ -181,8 +190,16 @@ struct TcArgs {
   unsigned* flags;
 };
 
+__device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
+  const float y = __fsub_rn(x, c);
+  const float t = __fadd_rn(s, y);
+  c = __fsub_rn(__fsub_rn(t, s), y);
+  s = t;
+}
+
 template <int MODE, bool SPLIT>
 __global__ void __launch_bounds__(kTcThreads, 1) tc_gather_gemm(TcArgs a) {
+  constexpr int TMEM_COLS = SPLIT ? kTcTmemColsSplit : kTcTmemCols;
   constexpr int CH = SPLIT ? 32 : 64;                 // reduction rows per stage
   constexpr int WB = CH * kTcRows * 2;                 // W bytes per stage (per part)
   constexpr int SB = CH * kTcNC * 2;                   // S bytes per stage (per part)
@@ -243,7 +260,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gather_gemm(TcArgs a) {
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
-                 ::"r"(smem_addr(&tmem_slot)), "r"(kTcTmemCols) : "memory");
+                 ::"r"(smem_addr(&tmem_slot)), "r"(TMEM_COLS) : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   tc_fence_before();
@@ -319,6 +336,25 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gather_gemm(TcArgs a) {
     cp_commit();
   }
   fetch_src(kTcStages - 1, src_cur);
+  // epilogue / drain mapping: warp w reads TMEM lanes 32 (w % 4) .. + 31 of
+  // the accumulator of half h = w / 4, i.e. right-hand-side column
+  // c_base + 128 h + 32 (w % 4) + lane, all 64 output rows
+  const int quarter = warp & 3, hw = warp >> 2;
+  float racc[SPLIT ? kTcRows : 1], rcmp[SPLIT ? kTcRows : 1];
+#pragma unroll
+  for (int i = 0; i < (SPLIT ? kTcRows : 1); i++) { racc[i] = 0.f; rcmp[i] = 0.f; }
+  auto drain = [&](int set) {
+    if (SPLIT) {
+#pragma unroll
+      for (int half = 0; half < kTcRows / 32; half++) {
+        float v[32];
+        tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + set * 128 + hw * kTcRows + half * 32, v);
+#pragma unroll
+        for (int i = 0; i < 32; i++) kahan_add(racc[half * 32 + i], rcmp[half * 32 + i], v[i]);
+      }
+      tc_fence_before();
+    }
+  };
   bool ok = true;
   for (int c = 0; c < nch; c++) {
     const int s = c % kTcStages;
@@ -328,6 +364,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gather_gemm(TcArgs a) {
     if (abort_flag) { ok = false; break; }
     if (tid == 0) {
       tc_fence_after();
+      // split mode: window c / kTcWin accumulates into set (c / kTcWin) & 1
+      const uint32_t dset = SPLIT ? (uint32_t)(((c / kTcWin) & 1) * 128) : 0u;
+      const bool first = SPLIT ? (c % kTcWin) == 0 : c == 0;
 #pragma unroll
       for (int q = 0; q < CH / 16; q++) {
         // 16 reduction rows = two 8-line groups (SBO 1 KiB); k-step offset 2 KiB
@@ -336,8 +375,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gather_gemm(TcArgs a) {
         for (int h = 0; h < kTcNC / 128; h++) {
           // M = 128 columns = two 64-column blocks, LBO = block stride
           const uint64_t ah = sw128_desc(s_at(s, 0) + h * 2 * BLK + q * 2048, BLK, 1024);
-          const uint32_t d = tmem + h * kTcRows;
-          mma_bf16_tc(d, ah, bh, (c | q) != 0);
+          const uint32_t d = tmem + dset + h * kTcRows;
+          mma_bf16_tc(d, ah, bh, !(first && q == 0));
           if (SPLIT) {
             const uint64_t bl = sw128_desc(w_at(s, 1) + q * 2048, 8192, 1024);
             const uint64_t al = sw128_desc(s_at(s, 1) + h * 2 * BLK + q * 2048, BLK, 1024);
@@ -350,16 +389,21 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gather_gemm(TcArgs a) {
     }
     const int cn = c + kTcStages - 1;
     fetch_src(cn + 1, src_nxt);
-    if (cn < nch) {
-      if (c >= 1) {
-        const int sp = (c - 1) % kTcStages;
-        if (!mbar_wait(smem_addr(&bars[sp]), ((c - 1) / kTcStages) & 1)) {
-          atomicOr(a.flags, FGB_FLAG_DEVICE_TIMEOUT);
-          abort_flag = 1;
-        }
+    // chunk c - 1 ends a window: its set is drained while chunk c's MMAs
+    // run on the other set
+    const bool drain_now = SPLIT && c >= 1 && (c % kTcWin) == 0;
+    if (c >= 1 && (cn < nch || drain_now)) {
+      const int sp = (c - 1) % kTcStages;
+      if (!mbar_wait(smem_addr(&bars[sp]), ((c - 1) / kTcStages) & 1)) {
+        atomicOr(a.flags, FGB_FLAG_DEVICE_TIMEOUT);
+        abort_flag = 1;
       }
-      if (!abort_flag) load(cn, cn % kTcStages, src_cur);
     }
+    if (drain_now && !abort_flag) {
+      tc_fence_after();
+      drain(((c - 1) / kTcWin) & 1);
+    }
+    if (cn < nch && !abort_flag) load(cn, cn % kTcStages, src_cur);
     cp_commit();
 #pragma unroll
     for (int j = 0; j < RPW; j++) src_cur[j] = src_nxt[j];
@@ -377,16 +421,20 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gather_gemm(TcArgs a) {
   __syncthreads();
   if (abort_flag) ok = false;
 
-  // epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31, i.e. columns
-  // c_base + 128 h + 32 (w % 4) + lane, for h = w / 4
+  // the last (possibly partial) window
+  if (SPLIT && ok && nch > 0) drain(((nch - 1) / kTcWin) & 1);
+
+  // epilogue (mapping as for the drain)
   if (ok) {
-    const int quarter = warp & 3, h = warp >> 2;
-    const int col = c_base + h * 128 + quarter * 32 + lane;
+    const int col = c_base + hw * 128 + quarter * 32 + lane;
 #pragma unroll
     for (int half = 0; half < kTcRows / 32; half++) {
       float v[32];
-      if (nch > 0) {
-        tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + h * kTcRows + half * 32, v);
+      if (SPLIT) {
+#pragma unroll
+        for (int i = 0; i < 32; i++) v[i] = racc[half * 32 + i];
+      } else if (nch > 0) {
+        tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + hw * kTcRows + half * 32, v);
       } else {
 #pragma unroll
         for (int i = 0; i < 32; i++) v[i] = 0.f;
@@ -416,7 +464,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gather_gemm(TcArgs a) {
   __syncthreads();
   if (warp == 0) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;"
-                 ::"r"(tmem), "r"(kTcTmemCols) : "memory");
+                 ::"r"(tmem), "r"(TMEM_COLS) : "memory");
   }
 }
 

@@ -909,11 +909,12 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
 
     def split_product(self, X, Y, add=None, alpha=1.0, work=None):
         """Y = add + alpha F X for FP32 X (N x K, K % 8 == 0) on the tensor
-        cores with split-BF16 operands (hi.hi + lo.hi + hi.lo, FP32
-        accumulation): each product term is exact, the represented operator
-        and sources differ from the FP32 ones by at most 2^-16 relative, so
-        |error| <= ~3 * 2^-17 * (|F| |X|) elementwise, near the FP32 product's
-        own rounding.  work: optional dict of scratch tensors (reused)."""
+        cores with split-BF16 operands (hi.hi + lo.hi + hi.lo; the tensor
+        core's FP32 accumulators are drained every two chunks into
+        compensated register sums).  Each product term is exact and the
+        split operands carry ~17 significant bits, so the result behaves
+        like FP32 arithmetic with 7 fewer bits.  work: optional dict of
+        scratch tensors (reused)."""
         N, K = X.shape
         dev = X.device
         st = _lib.stream_handle()

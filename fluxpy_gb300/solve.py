@@ -219,12 +219,13 @@ def _colmax(t):
     return t.view(torch.int32).cpu().numpy().view(np.float32)
 
 
-# Split-BF16 residual: the operands' hi + lo parts differ from the FP32 ones
-# by at most 2^-18 relative, so the product is within 3 * 2^-18 |F| |rho B|
-# (1.1e-5 relative) of the FP32 operator's, before FP32 accumulation
-# rounding.  For rho = 0.12 that is about 1.5e-6 of max|E|; the convergence
-# test charges a fixed 30 % of rtol for it (the solution is then verified
-# independently in FP64 arithmetic by the tests and the benchmark).
+# Split-BF16 residual: the operands' hi + lo parts carry ~17 significant
+# bits (|v - hi - lo| <= 2^-18 |v|), so the product behaves like FP32
+# arithmetic with 7 fewer bits: measured within 1e-5 of max |F x| against
+# the operator in FP64 arithmetic.  Scaled by rho = 0.12 that is ~1e-6 of
+# max|E|; the convergence test charges a fixed 30 % of rtol for it (the
+# solution is verified independently in FP64 arithmetic by the tests and
+# the benchmark).
 _SPLIT_MARGIN = 0.3
 
 
@@ -258,10 +259,9 @@ def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_
     engine: 'tc' (tcgen05 tensor cores for the BF16 products) or 'mma'
     (mma.sync kernels).
     residual: how bf16-refine evaluates F (rho B): 'split-bf16' (tensor
-    cores, split-BF16 operands hi.hi + lo.hi + hi.lo with FP32 accumulation,
-    elementwise within 3 * 2^-18 |F| |rho B| of the FP32 operator's product
-    plus accumulation rounding; the convergence test keeps a margin for it,
-    _SPLIT_MARGIN) or 'fp32' (FP32 CUDA-core kernels).
+    cores, split-BF16 operands hi.hi + lo.hi + hi.lo, FP32 accumulation
+    drained into compensated sums; ~17-bit arithmetic, the convergence test
+    keeps a margin for it, _SPLIT_MARGIN) or 'fp32' (FP32 CUDA-core kernels).
     Returns B (N, K) fp32; fills `stats` (iterations, matmats, residuals).
     """
     dev = E.device

@@ -219,8 +219,11 @@ def test_tensor_core_product_matches_mma(terrain_op, K):
 @pytest.mark.parametrize("K", [64, 264])
 def test_split_bf16_product_accuracy(terrain_op, K):
     """Split-BF16 tensor-core product of the FP32 operator against the same
-    operator applied in FP64 arithmetic: within a few 1e-6 of max |F x|, like
-    the FP32 CUDA-core product."""
+    operator applied in FP64 arithmetic.  A two-part BF16 split carries ~17
+    significant bits, so the product behaves like FP32 arithmetic with 7
+    fewer bits (the low-rank factors amplify rounding as they do in FP32):
+    within 2e-5 of max |F x| (the FP32 CUDA-core product: 5e-6).  In the
+    refinement residual this is scaled by rho."""
     sm, FF = terrain_op
     N = sm.num_faces
     g = torch.Generator(device="cuda").manual_seed(K + 1)
@@ -234,7 +237,7 @@ def test_split_bf16_product_accuracy(terrain_op, K):
         ref = y64.abs().max().item()
         e_split = (Y[:, c].double() - y64).abs().max().item() / ref
         e_fp32 = (Y32[:, c].double() - y64).abs().max().item() / ref
-        assert e_split <= 5e-6, (c, e_split, e_fp32)
+        assert e_split <= 2e-5, (c, e_split, e_fp32)
         assert e_fp32 <= 5e-6, (c, e_split, e_fp32)
     # with add / alpha
     add = torch.rand((N, K), device="cuda", generator=g)

@@ -183,7 +183,7 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
 
     def __init__(self, shape_model, tol=1e-5, min_size=16384, max_depth=None,
                  force_max_depth=False, RootBlock=None, *, leaf_size=64, eta=1.0, rmax=64,
-                 nsample=1024, exact_aca_max=65536, dtype=None, eps=None, **kwargs):
+                 nsample=4096, exact_aca_max=262144, dtype=None, eps=None, **kwargs):
         if tol < 0:
             raise RuntimeError('tol should be a nonnegative float')
         if max_depth is not None and not isinstance(max_depth, int):

@@ -312,11 +312,13 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
     zr = max(FF._num_zrows, 1)
     Ek = Ep[:, :K].contiguous()
     X32 = (RHO * Ek).contiguous()
-    xh = torch.empty((N, K), dtype=torch.bfloat16, device=dev)
-    xl = torch.empty_like(xh)
+    # sources stacked as [Z; X] (hi and lo parts), as the solver keeps them
+    nz = int(FF._num_zrows)
+    sh = torch.zeros((nz + N, K), dtype=torch.bfloat16, device=dev)
+    sl = torch.zeros_like(sh)
+    zh, xh = sh[:nz], sh[nz:]
+    zl, xl = sl[:nz], sl[nz:]
     Z32 = torch.zeros((zr, K), dtype=torch.float32, device=dev)
-    zh = torch.zeros((zr, K), dtype=torch.bfloat16, device=dev)
-    zl = torch.zeros_like(zh)
     Y = torch.empty_like(Ek)
     tc = FF.tc_operands(split=True)
     panel_f, vpanel_f = FF.panels("fp32")
@@ -406,7 +408,7 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
                            "algorithmic_flops": fl, "ms_per_launch": t_ms, "fp32_tflops": tfl}
     out["kernel_ms"] = {"columns": K, **ms, "per_step_ms": per_step,
                         "tflops": {k: work[k][1] / (ms[k] * 1e-3) / 1e12 for k in ms}}
-    del X32, xh, xl, Z32, zh, zl, Y, Ek
+    del X32, xh, xl, Z32, zh, zl, sh, sl, Y, Ek
     torch.cuda.empty_cache()
     K = K_all
     # ---- plain FP32 GPU paths

@@ -161,7 +161,7 @@ class fgb_op_desc(C.Structure):
         ("num_items", C.c_longlong), ("t_p0", C.c_void_p), ("src", C.c_void_p),
         ("num_tiles", C.c_longlong), ("N", C.c_longlong), ("num_zrows", C.c_longlong),
         ("max_group_tiles", C.c_int), ("g_kzp", C.c_void_p), ("g_vtoff", C.c_void_p),
-        ("a_woff", C.c_void_p), ("num_work", C.c_longlong),
+        ("a_woff", C.c_void_p), ("num_work", C.c_longlong), ("panel_rows", C.c_longlong),
     ]
 
 
@@ -706,6 +706,7 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         desc.num_zrows = self._num_zrows
         desc.max_group_tiles = max_gt
         desc.num_work = num_work
+        desc.panel_rows = int(self._panel_rows)
         return desc
 
     # -- device products --------------------------------------------------
@@ -842,14 +843,23 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
 
     def _matmat_bf16(self, Xp, out=None, add=None, alpha=1.0, Z=None, engine="tc"):
         K = Xp.shape[1]
-        Xb = Xp.to(torch.bfloat16).contiguous()
+        S, Zb, Xb = self.stacked_sources(K, Xp.device)
+        Xb.copy_(Xp)
         if out is None:
             out = torch.empty(Xp.shape, dtype=torch.float32, device=Xp.device)
         if Z is None:
             Z = torch.empty((max(self._num_zrows, 1), K), dtype=torch.float32, device=Xp.device)
-        Zb = torch.empty((max(self._num_zrows, 1), K), dtype=torch.bfloat16, device=Xp.device)
         self.bf16_product(Xb, Z, Zb, out, add, alpha, engine)
         return out
+
+    def stacked_sources(self, K, device, buf=None):
+        """A BF16 (num_zrows + N) x K tensor S with its two views Z = S[:num_zrows]
+        and X = S[num_zrows:]: the phase-B sources stacked as the TMA gather
+        kernel wants them (any Z / X pair works, stacked ones are faster)."""
+        zr = self._num_zrows
+        if buf is None or tuple(buf.shape) != (zr + self.num_faces, K):
+            buf = torch.empty((zr + self.num_faces, K), dtype=torch.bfloat16, device=device)
+        return buf, buf[:zr], buf[zr:]
 
     def tc_operands(self, split=False):
         """BF16 operands of the tensor-core products, built once from the
@@ -926,9 +936,13 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
             if t is None or tuple(t.shape) != tuple(shape) or t.dtype != dt:
                 t = w[name] = torch.empty(shape, dtype=dt, device=dev)
             return t
-        xh, xl = buf("x_hi", (N, K), torch.bfloat16), buf("x_lo", (N, K), torch.bfloat16)
+        # stacked [Z; X] sources, hi and lo parts (TMA gathers)
+        nz = self._num_zrows
+        sh = buf("s_hi", (nz + N, K), torch.bfloat16)
+        sl = buf("s_lo", (nz + N, K), torch.bfloat16)
+        zh, xh = sh[:nz], sh[nz:]
+        zl, xl = sl[:nz], sl[nz:]
         z = buf("z", (zr, K), torch.float32)
-        zh, zl = buf("z_hi", (zr, K), torch.bfloat16), buf("z_lo", (zr, K), torch.bfloat16)
         tc = self.tc_operands(split=True)
         flags = _lib.ptr(self.device_flags())
         _lib.call("fgb_split_bf16", _lib.ptr(X), _lib.ptr(xh), _lib.ptr(xl), N * K, st)

@@ -40,6 +40,8 @@
 // CTA skips the rest of its work, drains its copies and frees its TMEM.
 #include "common.cuh"
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 
 namespace fgb {
@@ -537,6 +539,342 @@ int launch_tc(const TcArgs& a, long long units, cudaStream_t st) {
 
 bool misaligned(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) != 0; }
 
+// ---------------------------------------------------------------------------
+// Phase B with TMA (warp-specialised).  The sources must be one row-major
+// tensor S = [Z; X] ((num_zrows + N) x K, BF16); its rows are gathered four
+// at a time by cp.async.bulk.tensor ... tile::gather4 (a tensor map with a
+// 64-column x 1-row box and the 128-byte swizzle, so rows land directly in
+// the MMA's MN-major swizzled layout, four 128-byte lines per request), the
+// panel chunk comes with one tiled TMA load (64 x 64 box).  Copies complete
+// on the stage's "full" mbarrier (transaction bytes); no thread issues
+// per-16-byte copies and no CTA-wide barrier runs per chunk.
+//   warp 0      producer: lanes 0..15 gather rows 4 lane .. 4 lane + 3
+//   warp 1      MMA issuer (lane 0): waits "full", issues, commits "empty"
+//   warps 4..7  epilogue (TMEM lanes 32 (w - 4) ..); in split mode they also
+//               drain each chunk's accumulator set into compensated sums
+// Split mode: NC = 128 columns (one accumulator half, two TMEM sets that
+// alternate by chunk), hi and lo maps for both operands.
+template <bool SPLIT>
+struct TmaCfg {
+  static constexpr int CH = 64;                       // panel rows per stage
+  static constexpr int NC = SPLIT ? 128 : 256;        // right-hand-side columns per CTA
+  static constexpr int PARTS = SPLIT ? 2 : 1;
+  static constexpr int WB = CH * kTcRows * 2;         // 8 KiB per part
+  static constexpr int SB = CH * NC * 2;              // 16 / 32 KiB per part
+  static constexpr int STAGE = PARTS * (WB + SB);     // 48 / 40 KiB
+  static constexpr int STAGES = SPLIT ? 4 : 5;
+  static constexpr int SMEM = STAGES * STAGE + 1024;
+  static constexpr int HALVES = NC / 128;
+  static constexpr int TMEM_COLS = 128;
+};
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y,
+                                            uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];"
+      ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar) : "memory");
+}
+__device__ __forceinline__ void tma_gather4(uint32_t dst, const CUtensorMap* map, int x, int r0,
+                                            int r1, int r2, int r3, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cta.global.tile::gather4.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];"
+      ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(r0), "r"(r1), "r"(r2),
+        "r"(r3), "r"(bar) : "memory");
+}
+
+template <bool SPLIT>
+__global__ void __launch_bounds__(kTcThreads, 1)
+tc_phase_b_tma(const __grid_constant__ CUtensorMap tm_w_hi,
+               const __grid_constant__ CUtensorMap tm_w_lo,
+               const __grid_constant__ CUtensorMap tm_s_hi,
+               const __grid_constant__ CUtensorMap tm_s_lo, TcArgs a) {
+  using Cfg = TmaCfg<SPLIT>;
+  constexpr int S = Cfg::STAGES;
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ __align__(8) unsigned long long full_bar[S], empty_bar[S], win_full[2], win_empty[2],
+      done_bar;
+  __shared__ uint32_t tmem_slot;
+  __shared__ volatile int abort_flag;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int nks = (a.K + Cfg::NC - 1) / Cfg::NC;
+  const long long t = blockIdx.x / nks;
+  const int c_base = (int)(blockIdx.x % nks) * Cfg::NC;
+  const long long p0 = a.t_p0[t], p1 = a.t_p0[t + 1];
+  const int nch = (int)((p1 - p0) / Cfg::CH);
+  const long long out_row0 = t * kTcRows;
+  const int out_rows = (int)min((long long)kTcRows, a.N - out_row0);
+
+  uint8_t* smem = reinterpret_cast<uint8_t*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  const uint32_t sbase = smem_addr(smem);
+  auto w_at = [&](int s, int part) { return sbase + s * Cfg::STAGE + part * Cfg::WB; };
+  auto s_at = [&](int s, int part) {
+    return sbase + s * Cfg::STAGE + Cfg::PARTS * Cfg::WB + part * Cfg::SB;
+  };
+  if (tid == 0) {
+    if (((p1 - p0) % Cfg::CH) != 0) atomicOr(a.flags, FGB_FLAG_INDEX_RANGE);
+    for (int i = 0; i < S; i++) {
+      mbar_init(smem_addr(&full_bar[i]), 1);
+      mbar_init(smem_addr(&empty_bar[i]), 1);
+    }
+    for (int i = 0; i < 2; i++) {
+      mbar_init(smem_addr(&win_full[i]), 1);
+      mbar_init(smem_addr(&win_empty[i]), 4);
+    }
+    mbar_init(smem_addr(&done_bar), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    abort_flag = 0;
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                 ::"r"(smem_addr(&tmem_slot)), "r"(Cfg::TMEM_COLS) : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+  auto fail = [&]() {
+    atomicOr(a.flags, FGB_FLAG_DEVICE_TIMEOUT);
+    abort_flag = 1;
+  };
+  // warp-uniform bounded wait (lane 0 polls) and abort test, so that the
+  // warp stays converged for the .sync.aligned tcgen05 instructions
+  auto warp_wait = [&](uint32_t bar, uint32_t parity) {
+    int got = 1;
+    if (lane == 0) got = mbar_wait(bar, parity) ? 1 : 0;
+    return __shfl_sync(0xffffffffu, got, 0) != 0;
+  };
+  auto warp_abort = [&]() { return __shfl_sync(0xffffffffu, (int)abort_flag, 0) != 0; };
+
+  if (warp == 0) {
+    // ---------------- producer
+    constexpr uint32_t kBytes = Cfg::STAGE;
+    auto fetch = [&](int c) {
+      int4 v = make_int4(0, 0, 0, 0);
+      if (c < nch && lane < Cfg::CH / 4)
+        v = __ldg(reinterpret_cast<const int4*>(a.src + p0 + (long long)c * Cfg::CH) + lane);
+      return v;
+    };
+    int4 sv = fetch(0);
+    int issued = 0;
+    for (int c = 0; c < nch; c++) {
+      const int s = c % S;
+      const int4 sv_next = fetch(c + 1);
+      if (c >= S && !warp_wait(smem_addr(&empty_bar[s]), ((c / S) - 1) & 1)) {
+        if (lane == 0) fail();
+      }
+      if (warp_abort()) break;
+      const uint32_t fb = smem_addr(&full_bar[s]);
+      if (lane == 0) {
+        mbar_expect_tx(fb, kBytes);
+        const int y = (int)(p0 + (long long)c * Cfg::CH);
+        tma_load_2d(w_at(s, 0), &tm_w_hi, 0, y, fb);
+        if (SPLIT) tma_load_2d(w_at(s, 1), &tm_w_lo, 0, y, fb);
+      }
+      __syncwarp();
+      if (lane < Cfg::CH / 4) {
+#pragma unroll
+        for (int b = 0; b < Cfg::NC / 64; b++) {
+          const uint32_t off = b * (Cfg::CH * 128) + lane * 512;
+          tma_gather4(s_at(s, 0) + off, &tm_s_hi, c_base + 64 * b, sv.x, sv.y, sv.z, sv.w, fb);
+          if (SPLIT)
+            tma_gather4(s_at(s, 1) + off, &tm_s_lo, c_base + 64 * b, sv.x, sv.y, sv.z, sv.w, fb);
+        }
+      }
+      sv = sv_next;
+      issued = c + 1;
+    }
+    // copies still in flight (an aborted run): wait for the last stages to land
+    if (lane == 0 && abort_flag) {
+      for (int c = max(0, issued - S); c < issued; c++)
+        mbar_wait(smem_addr(&full_bar[c % S]), (c / S) & 1);
+    }
+  } else if (warp == 1) {
+    // ---------------- MMA issuer
+    if (lane == 0) {
+      for (int c = 0; c < nch; c++) {
+        const int s = c % S;
+        if (!mbar_wait(smem_addr(&full_bar[s]), (c / S) & 1)) { fail(); break; }
+        if (abort_flag) break;
+        const int set = SPLIT ? (c & 1) : 0;
+        if (SPLIT && c >= 2 && !mbar_wait(smem_addr(&win_empty[set]), ((c >> 1) - 1) & 1)) {
+          fail();
+          break;
+        }
+        tc_fence_after();
+#pragma unroll
+        for (int q = 0; q < Cfg::CH / 16; q++) {
+          const uint64_t bh = sw128_desc(w_at(s, 0) + q * 2048, 8192, 1024);
+#pragma unroll
+          for (int h = 0; h < Cfg::HALVES; h++) {
+            const uint32_t blk = Cfg::CH * 128;
+            const uint64_t ah = sw128_desc(s_at(s, 0) + h * 2 * blk + q * 2048, blk, 1024);
+            const uint32_t d = tmem + (SPLIT ? set * kTcRows : h * kTcRows);
+            if (SPLIT) {
+              const uint64_t bl = sw128_desc(w_at(s, 1) + q * 2048, 8192, 1024);
+              const uint64_t al = sw128_desc(s_at(s, 1) + h * 2 * blk + q * 2048, blk, 1024);
+              mma_bf16_tc(d, ah, bh, q != 0);
+              mma_bf16_tc(d, al, bh, 1u);
+              mma_bf16_tc(d, ah, bl, 1u);
+            } else {
+              mma_bf16_tc(d, ah, bh, (c | q) != 0);
+            }
+          }
+        }
+        mma_commit(smem_addr(&empty_bar[s]));
+        if (SPLIT) mma_commit(smem_addr(&win_full[set]));
+      }
+      mma_commit(smem_addr(&done_bar));
+    }
+  } else if (warp >= 4) {
+    // ---------------- epilogue
+    const int quarter = warp - 4;
+    float racc[SPLIT ? kTcRows : 1], rcmp[SPLIT ? kTcRows : 1];
+#pragma unroll
+    for (int i = 0; i < (SPLIT ? kTcRows : 1); i++) { racc[i] = 0.f; rcmp[i] = 0.f; }
+    bool ok = true;
+    if (SPLIT) {
+      for (int c = 0; c < nch; c++) {
+        const int set = c & 1;
+        if (!warp_wait(smem_addr(&win_full[set]), (c >> 1) & 1)) {
+          if (lane == 0) fail();
+          ok = false;
+          break;
+        }
+        if (warp_abort()) { ok = false; break; }
+        tc_fence_after();
+#pragma unroll
+        for (int half = 0; half < kTcRows / 32; half++) {
+          float v[32];
+          tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + set * kTcRows + half * 32, v);
+#pragma unroll
+          for (int i = 0; i < 32; i++) kahan_add(racc[half * 32 + i], rcmp[half * 32 + i], v[i]);
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(smem_addr(&win_empty[set]));
+      }
+    }
+    if (ok && !warp_wait(smem_addr(&done_bar), 0)) {
+      if (lane == 0) fail();
+      ok = false;
+    }
+    if (warp_abort()) ok = false;
+    tc_fence_after();
+    if (ok) {
+#pragma unroll
+      for (int h = 0; h < Cfg::HALVES; h++) {
+        const int col = c_base + h * 128 + quarter * 32 + lane;
+#pragma unroll
+        for (int half = 0; half < kTcRows / 32; half++) {
+          float v[32];
+          if (SPLIT) {
+#pragma unroll
+            for (int i = 0; i < 32; i++) v[i] = racc[half * 32 + i];
+          } else if (nch > 0) {
+            tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + h * kTcRows + half * 32, v);
+          } else {
+#pragma unroll
+            for (int i = 0; i < 32; i++) v[i] = 0.f;
+          }
+          if (col < a.K) {
+#pragma unroll
+            for (int i = 0; i < 32; i++) {
+              const int r = half * 32 + i;
+              if (r < out_rows) {
+                const long long row = out_row0 + r;
+                float y = v[i];
+                if (a.add) y = a.add[row * (long long)a.K + col] + a.alpha * y;
+                a.out[row * (long long)a.K + col] = y;
+              }
+            }
+          }
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    __syncwarp();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;"
+                 ::"r"(tmem), "r"(Cfg::TMEM_COLS) : "memory");
+  }
+}
+
+// cuTensorMapEncodeTiled, resolved through the runtime at first use so that
+// the library carries no link-time dependency on the driver library
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+int encode_map(CUtensorMap* m, const void* base, unsigned long long inner, unsigned long long rows,
+               unsigned box_inner, unsigned box_rows) {
+  cuuint64_t dims[2] = {inner, rows};
+  cuuint64_t strides[1] = {inner * 2};
+  cuuint32_t box[2] = {box_inner, box_rows};
+  cuuint32_t es[2] = {1, 1};
+  PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn();
+  if (!fn) { set_error("cuTensorMapEncodeTiled is not available"); return FGB_CUDA_ERR; }
+  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides,
+                  box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return FGB_CUDA_ERR;
+  }
+  return FGB_OK;
+}
+
+template <bool SPLIT>
+int launch_tma_b(const fgb_op_desc* d, const void* w_hi, const void* w_lo, const void* s_hi,
+                 const void* s_lo, const TcArgs& a, cudaStream_t st) {
+  using Cfg = TmaCfg<SPLIT>;
+  static bool attr_set = false;
+  if (!attr_set) {
+    FGB_CUDA_TRY(cudaFuncSetAttribute(tc_phase_b_tma<SPLIT>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM));
+    attr_set = true;
+  }
+  alignas(64) CUtensorMap mw_hi, mw_lo, ms_hi, ms_lo;
+  const unsigned long long srows = (unsigned long long)(d->num_zrows + d->N);
+  int rc;
+  if ((rc = encode_map(&mw_hi, w_hi, kTcRows, d->panel_rows, kTcRows, Cfg::CH))) return rc;
+  if ((rc = encode_map(&ms_hi, s_hi, a.K, srows, 64, 1))) return rc;
+  if (SPLIT) {
+    if ((rc = encode_map(&mw_lo, w_lo, kTcRows, d->panel_rows, kTcRows, Cfg::CH))) return rc;
+    if ((rc = encode_map(&ms_lo, s_lo, a.K, srows, 64, 1))) return rc;
+  } else {
+    mw_lo = mw_hi;
+    ms_lo = ms_hi;
+  }
+  const long long nks = (a.K + Cfg::NC - 1) / Cfg::NC;
+  const long long grid = d->num_tiles * nks;
+  if (grid > 0x7fffffffLL) { set_error("grid too large"); return FGB_BAD_ARG; }
+  tc_phase_b_tma<SPLIT><<<(unsigned)grid, kTcThreads, Cfg::SMEM, st>>>(mw_hi, mw_lo, ms_hi, ms_lo, a);
+  FGB_LAUNCH_CHECK("tc_phase_b_tma");
+  return FGB_OK;
+}
+
 }  // namespace
 }  // namespace fgb
 
@@ -590,6 +928,18 @@ int fgb_tc_phase_b(const struct fgb_op_desc* d, const void* w_hi, const void* w_
   if (d->num_tiles <= 0) return FGB_OK;
   fgb::TcArgs a{};
   a.t_p0 = d->t_p0; a.src = d->src; a.N = d->N; a.num_zrows = d->num_zrows;
+  cudaStream_t st0 = fgb::as_stream(stream);
+  // one stacked source tensor [Z; X] (X directly after Z): the TMA kernel
+  const size_t zbytes = (size_t)d->num_zrows * (size_t)K * 2;
+  const bool stacked =
+      static_cast<const char*>(Z_hi) + zbytes == static_cast<const char*>(X_hi) &&
+      (!split || static_cast<const char*>(Z_lo) + zbytes == static_cast<const char*>(X_lo)) &&
+      d->panel_rows > 0 && (reinterpret_cast<uintptr_t>(d->src) & 15) == 0;
+  if (stacked) {
+    a.K = K; a.lds = K; a.out = Y; a.add = add; a.alpha = alpha; a.flags = flags;
+    return split ? fgb::launch_tma_b<true>(d, w_hi, w_lo, Z_hi, Z_lo, a, st0)
+                 : fgb::launch_tma_b<false>(d, w_hi, nullptr, Z_hi, nullptr, a, st0);
+  }
   a.w_hi = static_cast<const __nv_bfloat16*>(w_hi);
   a.w_lo = static_cast<const __nv_bfloat16*>(w_lo);
   a.x_hi = static_cast<const __nv_bfloat16*>(X_hi);

@@ -333,9 +333,9 @@ def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_
         B = torch.empty_like(Ep)
         R = torch.empty_like(Ep)
         D = torch.empty_like(Ep)
-        Xb = torch.empty((N, K), dtype=torch.bfloat16, device=dev)
-        Zb = torch.empty((max(FF._num_zrows, 1), K), dtype=torch.bfloat16, device=dev)
-        work = {"z": Z32, "z_hi": Zb, "x_hi": Xb}
+        # BF16 sources stacked as [Z; X] (one tensor: TMA gathers in phase B)
+        Sb, Zb, Xb = FF.stacked_sources(K, dev)
+        work = {"z": Z32, "s_hi": Sb}
         emax_h = np.maximum(emax.cpu().numpy(), 1e-30)
         if residual == "split-bf16":
             # the computed residual may be smaller than the exact one by the

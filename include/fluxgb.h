@@ -299,6 +299,7 @@ struct fgb_op_desc {
   const long long* g_vtoff;
   const long long* a_woff;
   long long num_work;   /* a_woff[num_items] */
+  long long panel_rows; /* t_p0[num_tiles] */
 };
 /*
  * y = F x (or y = add + alpha F x), vectors in cluster order.  Replaces
@@ -339,7 +340,11 @@ int fgb_matmat_bf16(const struct fgb_op_desc* d, const void* panel, const void* 
  * sets FGB_FLAG_DEVICE_TIMEOUT in *flags.
  *   phase A: Z = Vg^T-panel x X rows (Z FP32, num_zrows x K; items that do
  *            not cover their group accumulate atomically into a zeroed Z);
- *   phase B: Y = add + alpha * (panel rows x gathered [Z; X] rows).
+ *   phase B: Y = add + alpha * (panel rows x gathered [Z; X] rows).  When
+ *            X directly follows Z in memory (one stacked (num_zrows + N) x K
+ *            tensor, and likewise for the lo parts) the rows are gathered
+ *            by TMA (tile::gather4) in a warp-specialised kernel; otherwise
+ *            by cp.async.
  */
 int fgb_tc_phase_a(const struct fgb_op_desc* d, const void* vt_hi, const void* vt_lo,
                    const void* X_hi, const void* X_lo, float* Z, int K, int zero_z,

@@ -209,6 +209,10 @@ def main():
     sm = shape.EmbreeTrimeshShapeModel(V, F)
     FF = CompressedFormFactorMatrix(sm, tol=args.tol, min_size=4096, leaf_size=64,
                                     RootBlock=FormFactorOctreeBlock, dtype=np.float32)
+    # build the FP32 panels and the tensor-core operands, then move the
+    # block pool and the exact-leaf CSR (not used by the products) to host
+    FF.offload_pool()
+    FF.tc_operands(split=True)
     nf = sm.num_faces
     dirs = terrain.random_sun_directions(args.rhs, seed=2 + rank)
     E = sm.get_direct_irradiance_batch(F0, dirs, out_dtype=torch.float32)

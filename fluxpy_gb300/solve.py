@@ -235,7 +235,7 @@ def _auto_chunk(FF, N, K):
     free += torch.cuda.memory_reserved() - torch.cuda.memory_allocated()
     # per column: E, B, R, D, Y, X (FP32), X hi/lo (BF16); Z (FP32), Z hi/lo
     per_col = N * (6 * 4 + 2 * 2) + max(FF._num_zrows, 1) * 8
-    c = int(0.6 * free / per_col) // 8 * 8
+    c = int(0.5 * free / per_col) // 8 * 8
     return max(8, min(K, c))
 
 

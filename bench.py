@@ -355,6 +355,10 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
                   _lib.ptr(xl) if split else None, _lib.ptr(zh), _lib.ptr(zl) if split else None,
                   _lib.ptr(Y), K, _lib.ptr(Ek), 1.0, _lib.ptr(flags), st())
 
+    def tc_b_tma():
+        _lib.call("fgb_tc_phase_b_tma", desc, _lib.ptr(tc["w_hi"]), None, _lib.ptr(sh), None,
+                  _lib.ptr(Y), K, _lib.ptr(Ek), 1.0, _lib.ptr(flags), st())
+
     def f32(phases):
         _lib.call("fgb_matmat_f32", desc, _lib.ptr(panel_f), _lib.ptr(vpanel_f), _lib.ptr(X32),
                   _lib.ptr(Z32), _lib.ptr(Y), K, None, 1.0, int(FF._needs_zero_z), phases, st())
@@ -363,6 +367,7 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
           "phaseA_tc_split": t_events(lambda: tc_a(True)),
           "phaseB_tc_split": t_events(lambda: tc_b(True)),
           "phaseA_f32": t_events(lambda: f32(1), 3), "phaseB_f32": t_events(lambda: f32(2), 3)}
+    ms_tma = t_events(tc_b_tma, 3)
     FF.check_device_flags()
     # algorithmic work per launch: every stored weight read once, every
     # distinct source row read once, outputs written once; flops 2 per
@@ -410,7 +415,8 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
                            "unit": "GB/s", "frac": gbs / hbm, "traffic": None,
                            "peak_source": src, "algorithmic_bytes": byts,
                            "algorithmic_flops": fl, "ms_per_launch": t_ms, "fp32_tflops": tfl}
-    out["kernel_ms"] = {"columns": K, **ms, "per_step_ms": per_step,
+    out["kernel_ms"] = {"columns": K, **ms, "phaseB_tc_tma_gather_variant": ms_tma,
+                        "per_step_ms": per_step,
                         "tflops": {k: work[k][1] / (ms[k] * 1e-3) / 1e12 for k in ms}}
     del X32, xh, xl, Z32, zh, zl, sh, sl, Y, Ek
     torch.cuda.empty_cache()

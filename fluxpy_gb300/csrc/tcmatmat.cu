@@ -928,18 +928,7 @@ int fgb_tc_phase_b(const struct fgb_op_desc* d, const void* w_hi, const void* w_
   if (d->num_tiles <= 0) return FGB_OK;
   fgb::TcArgs a{};
   a.t_p0 = d->t_p0; a.src = d->src; a.N = d->N; a.num_zrows = d->num_zrows;
-  cudaStream_t st0 = fgb::as_stream(stream);
-  // one stacked source tensor [Z; X] (X directly after Z): the TMA kernel
-  const size_t zbytes = (size_t)d->num_zrows * (size_t)K * 2;
-  const bool stacked =
-      static_cast<const char*>(Z_hi) + zbytes == static_cast<const char*>(X_hi) &&
-      (!split || static_cast<const char*>(Z_lo) + zbytes == static_cast<const char*>(X_lo)) &&
-      d->panel_rows > 0 && (reinterpret_cast<uintptr_t>(d->src) & 15) == 0;
-  if (stacked) {
-    a.K = K; a.lds = K; a.out = Y; a.add = add; a.alpha = alpha; a.flags = flags;
-    return split ? fgb::launch_tma_b<true>(d, w_hi, w_lo, Z_hi, Z_lo, a, st0)
-                 : fgb::launch_tma_b<false>(d, w_hi, nullptr, Z_hi, nullptr, a, st0);
-  }
+
   a.w_hi = static_cast<const __nv_bfloat16*>(w_hi);
   a.w_lo = static_cast<const __nv_bfloat16*>(w_lo);
   a.x_hi = static_cast<const __nv_bfloat16*>(X_hi);
@@ -950,6 +939,28 @@ int fgb_tc_phase_b(const struct fgb_op_desc* d, const void* w_hi, const void* w_
   cudaStream_t st = fgb::as_stream(stream);
   return split ? fgb::launch_tc<fgb::kModeB, true>(a, d->num_tiles, st)
                : fgb::launch_tc<fgb::kModeB, false>(a, d->num_tiles, st);
+}
+
+int fgb_tc_phase_b_tma(const struct fgb_op_desc* d, const void* w_hi, const void* w_lo,
+                       const void* S_hi, const void* S_lo, float* Y, int K, const float* add,
+                       float alpha, unsigned* flags, void* stream) {
+  if (!d || !flags) { fgb::set_error("null operator or flags"); return FGB_BAD_ARG; }
+  if (K < 8 || (K % 8) != 0) { fgb::set_error("K must be a positive multiple of 8"); return FGB_BAD_ARG; }
+  const bool split = w_lo != nullptr;
+  if (split != (S_lo != nullptr)) { fgb::set_error("split operands must come in pairs"); return FGB_BAD_ARG; }
+  if (fgb::misaligned(w_hi) || fgb::misaligned(w_lo) || fgb::misaligned(S_hi) ||
+      fgb::misaligned(S_lo) || (reinterpret_cast<uintptr_t>(d->src) & 15)) {
+    fgb::set_error("TMA operands and src must be 16-byte aligned");
+    return FGB_BAD_ARG;
+  }
+  if (d->num_tiles <= 0) return FGB_OK;
+  if (d->panel_rows <= 0) { fgb::set_error("panel_rows not set"); return FGB_BAD_ARG; }
+  fgb::TcArgs a{};
+  a.t_p0 = d->t_p0; a.src = d->src; a.N = d->N; a.num_zrows = d->num_zrows;
+  a.K = K; a.lds = K; a.out = Y; a.add = add; a.alpha = alpha; a.flags = flags;
+  cudaStream_t st = fgb::as_stream(stream);
+  return split ? fgb::launch_tma_b<true>(d, w_hi, w_lo, S_hi, S_lo, a, st)
+               : fgb::launch_tma_b<false>(d, w_hi, nullptr, S_hi, nullptr, a, st);
 }
 
 int fgb_split_bf16(const float* in, void* hi, void* lo, long long n, void* stream) {

@@ -340,11 +340,7 @@ int fgb_matmat_bf16(const struct fgb_op_desc* d, const void* panel, const void* 
  * sets FGB_FLAG_DEVICE_TIMEOUT in *flags.
  *   phase A: Z = Vg^T-panel x X rows (Z FP32, num_zrows x K; items that do
  *            not cover their group accumulate atomically into a zeroed Z);
- *   phase B: Y = add + alpha * (panel rows x gathered [Z; X] rows).  When
- *            X directly follows Z in memory (one stacked (num_zrows + N) x K
- *            tensor, and likewise for the lo parts) the rows are gathered
- *            by TMA (tile::gather4) in a warp-specialised kernel; otherwise
- *            by cp.async.
+ *   phase B: Y = add + alpha * (panel rows x gathered [Z; X] rows).
  */
 int fgb_tc_phase_a(const struct fgb_op_desc* d, const void* vt_hi, const void* vt_lo,
                    const void* X_hi, const void* X_lo, float* Z, int K, int zero_z,
@@ -353,6 +349,14 @@ int fgb_tc_phase_b(const struct fgb_op_desc* d, const void* w_hi, const void* w_
                    const void* X_hi, const void* X_lo, const void* Z_hi, const void* Z_lo,
                    float* Y, int K, const float* add, float alpha, unsigned* flags,
                    void* stream);
+/* Phase B with the sources stacked in one (num_zrows + N) x K tensor S = [Z; X]
+ * (and S_lo for split products), rows gathered by TMA (tile::gather4, four
+ * 128-byte lines per request) in a warp-specialised kernel.  Same results as
+ * fgb_tc_phase_b; slower on GB300 for these 128-byte row pieces than the
+ * cp.async gathers (per-request cost), kept as the TMA variant. */
+int fgb_tc_phase_b_tma(const struct fgb_op_desc* d, const void* w_hi, const void* w_lo,
+                       const void* S_hi, const void* S_lo, float* Y, int K, const float* add,
+                       float alpha, unsigned* flags, void* stream);
 /* hi = bf16(in), lo = bf16(in - hi) elementwise (lo may be NULL). */
 int fgb_split_bf16(const float* in, void* hi, void* lo, long long n, void* stream);
 /* Transposed BF16 phase-A panel from the FP32 one (layouts in fgb_op_desc);

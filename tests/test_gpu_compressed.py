@@ -248,51 +248,39 @@ def test_split_bf16_product_accuracy(terrain_op, K):
 
 @pytest.mark.parametrize("K", [200, 512])
 def test_tma_gather_phase_b_matches_cp_async(terrain_op, K):
-    """Phase B with stacked [Z; X] sources runs the warp-specialised TMA
-    kernel (tile::gather4 row gathers); with separate Z and X buffers the
-    cp.async kernel.  Same MMA order and accumulation windows: identical
-    results, plain and split."""
+    """The TMA variant of phase B (sources stacked as [Z; X], rows gathered
+    by tile::gather4 in a warp-specialised kernel) against the cp.async
+    kernel: same MMA order and accumulation windows, identical results,
+    plain and split."""
+    import ctypes as C
+    from fluxpy_gb300 import _lib
     sm, FF = terrain_op
     N = sm.num_faces
     nz = FF._num_zrows
     g = torch.Generator(device="cuda").manual_seed(K + 7)
     X = torch.rand((N, K), device="cuda", generator=g)
     add = torch.rand((N, K), device="cuda", generator=g)
-    # plain BF16
-    S, Zs, Xs = FF.stacked_sources(K, "cuda")
-    Xs.copy_(X)
-    Xsep = X.to(torch.bfloat16).contiguous()
-    Z = torch.empty((max(nz, 1), K), device="cuda")
-    Zsep = torch.empty((max(nz, 1), K), dtype=torch.bfloat16, device="cuda")
-    Y_tma = torch.full((N, K), float("nan"), device="cuda")
-    Y_cp = torch.full((N, K), float("nan"), device="cuda")
-    FF.bf16_product(Xs, Z, Zs, Y_tma, add=add, alpha=0.5)
-    FF.bf16_product(Xsep, Z, Zsep, Y_cp, add=add, alpha=0.5)
-    FF.check_device_flags()
-    assert torch.isfinite(Y_tma).all()
-    assert torch.equal(Y_tma, Y_cp)
-    # split: stacked (the solver's layout) against separate hi / lo buffers
-    Y_s = torch.full((N, K), float("nan"), device="cuda")
-    FF.split_product(X, Y_s, add=add, alpha=-0.25)
-    FF.check_device_flags()
     tc = FF.tc_operands(split=True)
-    from fluxpy_gb300 import _lib
-    import ctypes as C
-    xh = torch.empty((N, K), dtype=torch.bfloat16, device="cuda")
-    xl = torch.empty_like(xh)
-    zf = torch.empty((max(nz, 1), K), device="cuda")
-    zh = torch.empty((max(nz, 1), K), dtype=torch.bfloat16, device="cuda")
-    zl = torch.empty_like(zh)
     st = _lib.stream_handle()
     fl = _lib.ptr(FF.device_flags())
-    _lib.call("fgb_split_bf16", _lib.ptr(X), _lib.ptr(xh), _lib.ptr(xl), N * K, st)
+    sh = torch.empty((nz + N, K), dtype=torch.bfloat16, device="cuda")
+    sl = torch.empty_like(sh)
+    zf = torch.empty((max(nz, 1), K), device="cuda")
+    _lib.call("fgb_split_bf16", _lib.ptr(X), _lib.ptr(sh[nz:]), _lib.ptr(sl[nz:]), N * K, st)
     _lib.call("fgb_tc_phase_a", C.byref(FF._desc), _lib.ptr(tc["vt_hi"]), _lib.ptr(tc["vt_lo"]),
-              _lib.ptr(xh), _lib.ptr(xl), _lib.ptr(zf), K, int(FF._needs_zero_z), fl, st)
-    _lib.call("fgb_split_bf16", _lib.ptr(zf), _lib.ptr(zh), _lib.ptr(zl), nz * K, st)
-    Y_sep = torch.full((N, K), float("nan"), device="cuda")
-    _lib.call("fgb_tc_phase_b", C.byref(FF._desc), _lib.ptr(tc["w_hi"]), _lib.ptr(tc["w_lo"]),
-              _lib.ptr(xh), _lib.ptr(xl), _lib.ptr(zh), _lib.ptr(zl), _lib.ptr(Y_sep), K,
-              _lib.ptr(add), -0.25, fl, st)
-    FF.check_device_flags()
-    assert torch.isfinite(Y_s).all()
-    assert torch.equal(Y_s, Y_sep)
+              _lib.ptr(sh[nz:]), _lib.ptr(sl[nz:]), _lib.ptr(zf), K, int(FF._needs_zero_z), fl, st)
+    _lib.call("fgb_split_bf16", _lib.ptr(zf), _lib.ptr(sh[:nz]), _lib.ptr(sl[:nz]), nz * K, st)
+    for split in (False, True):
+        wl = _lib.ptr(tc["w_lo"]) if split else None
+        Y_cp = torch.full((N, K), float("nan"), device="cuda")
+        Y_tma = torch.full((N, K), float("nan"), device="cuda")
+        _lib.call("fgb_tc_phase_b", C.byref(FF._desc), _lib.ptr(tc["w_hi"]), wl,
+                  _lib.ptr(sh[nz:]), _lib.ptr(sl[nz:]) if split else None, _lib.ptr(sh[:nz]),
+                  _lib.ptr(sl[:nz]) if split else None, _lib.ptr(Y_cp), K, _lib.ptr(add), -0.25,
+                  fl, st)
+        _lib.call("fgb_tc_phase_b_tma", C.byref(FF._desc), _lib.ptr(tc["w_hi"]), wl,
+                  _lib.ptr(sh), _lib.ptr(sl) if split else None, _lib.ptr(Y_tma), K,
+                  _lib.ptr(add), -0.25, fl, st)
+        FF.check_device_flags()
+        assert torch.isfinite(Y_tma).all()
+        assert torch.equal(Y_tma, Y_cp), split

@@ -87,6 +87,8 @@ SIGNATURES: dict[str, list] = {
     "fgb_aca_scratch_floats": [I32, I64, I64, P],
     "fgb_aca_f64": [P, P, P, P, P, I64, P, P, P, P, I64, I64, F64, I32, F32, I32, I32, I64, P,
                     P, I32, P, I64, P, P, P, P, U32P, P],
+    "fgb_aca_f64_static": [P, P, P, P, P, I64, P, P, P, P, I64, I64, F64, I32, F32, I32, I32,
+                           I64, I32, P, I64, P, P, P, U32P, P],
     # block matvec (a9)
     "fgb_build_panel_f32_f32": [P, I64, P, P, P, P, P, I64, P, P],
     "fgb_build_panel_f32_bf16": [P, I64, P, P, P, P, P, I64, P, P],

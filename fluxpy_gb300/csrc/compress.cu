@@ -24,6 +24,8 @@
 #include "common.cuh"
 #include "ffentry.cuh"
 
+#include <mutex>
+
 namespace fgb {
 BvhView view_of(const void* handle);
 
@@ -395,6 +397,46 @@ int fgb_aca_scratch_floats(int rmax, long long mmax, long long nmax, long long* 
   return FGB_OK;
 }
 
+}  // extern "C"
+
+namespace fgb {
+namespace {
+// Scratch of fgb_aca_f64_static: one file-scope device array per device
+// (the module's static data), sized for small batches.  Its address is
+// looked up once per device; the entry point allocates nothing.
+constexpr long long kAcaStaticFloats = 8LL << 20;   // 32 MiB
+static __device__ __align__(256) float g_aca_static_scratch[kAcaStaticFloats];
+static __device__ __align__(256) int g_aca_static_queue[64];
+
+struct StaticAcaSlot {
+  float* scratch = nullptr;
+  int* queue = nullptr;
+};
+std::mutex g_aca_static_mutex;
+StaticAcaSlot g_aca_static_slots[64];
+
+int static_aca_slot(StaticAcaSlot* out) {
+  int dev = 0;
+  FGB_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) { set_error("device index out of range"); return FGB_BAD_ARG; }
+  std::lock_guard<std::mutex> lock(g_aca_static_mutex);
+  StaticAcaSlot& s = g_aca_static_slots[dev];
+  if (!s.scratch) {
+    void* p = nullptr;
+    void* q = nullptr;
+    FGB_CUDA_TRY(cudaGetSymbolAddress(&p, g_aca_static_scratch));
+    FGB_CUDA_TRY(cudaGetSymbolAddress(&q, g_aca_static_queue));
+    s.scratch = static_cast<float*>(p);
+    s.queue = static_cast<int*>(q);
+  }
+  *out = s;
+  return FGB_OK;
+}
+}  // namespace
+}  // namespace fgb
+
+extern "C" {
+
 int fgb_aca_f64(const void* bvh, const double* P, const double* N, const double* A,
                 const long long* perm, long long nblocks, const int* r0, const int* m,
                 const int* c0, const int* n, long long mmax, long long nmax, double eps,
@@ -433,6 +475,41 @@ int fgb_aca_f64(const void* bvh, const double* P, const double* N, const double*
   fgb::aca_kernel<double><<<num_ctas, fgb::kAcaThreads, 0, fgb::as_stream(stream)>>>(a, e);
   FGB_LAUNCH_CHECK("aca_kernel");
   return FGB_OK;
+}
+
+int fgb_aca_f64_static(const void* bvh, const double* P, const double* N, const double* A,
+                       const long long* perm, long long nblocks, const int* r0, const int* m,
+                       const int* c0, const int* n, long long mmax, long long nmax, double eps,
+                       int semantics, float tol, int rmax, int nsample, long long exact_max,
+                       int num_ctas, float* pool, long long pool_capacity,
+                       unsigned long long* pool_used, int* rank_out, long long* off_out,
+                       unsigned* flags, void* stream) {
+  if (!bvh || nblocks < 0 || num_ctas < 1) { fgb::set_error("bad ACA arguments"); return FGB_BAD_ARG; }
+  if (nblocks == 0) return FGB_OK;
+  long long per_cta;
+  int st = fgb_aca_scratch_floats(rmax, mmax, nmax, &per_cta);
+  if (st) return st;
+  if (exact_max < 0) exact_max = 0;
+  // per CTA: the factor scratch slice, then (blocks with m n <= exact_max)
+  // the dense block
+  const long long need = (long long)num_ctas * (per_cta + exact_max);
+  if (need > fgb::kAcaStaticFloats) {
+    fgb::set_error("fgb_aca_f64_static: needs %lld floats of scratch for %d CTAs "
+                   "(rmax %d, mmax %lld, nmax %lld, exact_max %lld); the static scratch holds "
+                   "%lld: use fewer CTAs, smaller blocks or fgb_aca_f64",
+                   need, num_ctas, rmax, mmax, nmax, exact_max, fgb::kAcaStaticFloats);
+    return FGB_BAD_ARG;
+  }
+  fgb::StaticAcaSlot slot;
+  if ((st = fgb::static_aca_slot(&slot))) return st;
+  cudaStream_t s = fgb::as_stream(stream);
+  // the work queue must start at zero for every call
+  FGB_CUDA_TRY(cudaMemsetAsync(slot.queue, 0, sizeof(int), s));
+  float* scratch = slot.scratch;
+  float* dense = exact_max > 0 ? slot.scratch + (long long)num_ctas * per_cta : nullptr;
+  return fgb_aca_f64(bvh, P, N, A, perm, nblocks, r0, m, c0, n, mmax, nmax, eps, semantics, tol,
+                     rmax, nsample, exact_max, dense, scratch, num_ctas, pool, pool_capacity,
+                     pool_used, rank_out, off_out, slot.queue, flags, stream);
 }
 
 }  // extern "C"

@@ -260,6 +260,25 @@ int fgb_aca_f64(const void* bvh, const double* P, const double* N, const double*
                 float* dense_scratch, float* scratch, int num_ctas,
                 float* pool, long long pool_capacity, unsigned long long* pool_used,
                 int* rank_out, long long* off_out, int* queue, unsigned* flags, void* stream);
+/*
+ * fgb_aca_f64 without caller-provided scratch (no reference counterpart):
+ * the factor scratch, the dense-block scratch and the work queue live in
+ * the library's static device memory (32 MiB of floats per device, found
+ * once per device with cudaGetSymbolAddress); the call allocates nothing.
+ * A call whose num_ctas * (fgb_aca_scratch_floats(...) + exact_max) floats
+ * exceed that returns FGB_BAD_ARG with the sizes in fgb_last_error().  The
+ * queue is zeroed by the call (cudaMemsetAsync on `stream`); *pool_used
+ * must be zero on entry, as for fgb_aca_f64.  The static scratch is shared
+ * by every call on a device: calls must not overlap (issue them on one
+ * stream, or synchronise between streams / host threads).
+ */
+int fgb_aca_f64_static(const void* bvh, const double* P, const double* N, const double* A,
+                       const long long* perm, long long nblocks, const int* r0, const int* m,
+                       const int* c0, const int* n, long long mmax, long long nmax, double eps,
+                       int semantics, float tol, int rmax, int nsample, long long exact_max,
+                       int num_ctas, float* pool, long long pool_capacity,
+                       unsigned long long* pool_used, int* rank_out, long long* off_out,
+                       unsigned* flags, void* stream);
 
 /* ----------------------------------------------- block matvec (a9) */
 /*

@@ -312,7 +312,7 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
     # block the solver works on (it solves the 1,024 columns in blocks that
     # fit in memory)
     from fluxpy_gb300.solve import _auto_chunk
-    K = min(K_all, _auto_chunk(FF, N, K_all))
+    K = min(K_all, _auto_chunk(FF, N, K_all, fp32_z=False))
     zr = max(FF._num_zrows, 1)
     Ek = Ep[:, :K].contiguous()
     X32 = (RHO * Ek).contiguous()
@@ -344,10 +344,12 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
         return a.elapsed_time(b) / reps
 
     def tc_a(split):
-        _lib.call("fgb_tc_phase_a", desc, _lib.ptr(tc["vt_hi"]),
+        # phase A as the solver runs it: whole-group work items, Z written
+        # directly as BF16 (hi, and lo for the split product)
+        _lib.call("fgb_tc_phase_a_bf16", C.byref(FF._desc_tc), _lib.ptr(tc["vt_hi"]),
                   _lib.ptr(tc["vt_lo"]) if split else None, _lib.ptr(xh),
-                  _lib.ptr(xl) if split else None, _lib.ptr(Z32), K, int(FF._needs_zero_z),
-                  _lib.ptr(flags), st())
+                  _lib.ptr(xl) if split else None, _lib.ptr(zh), _lib.ptr(zl) if split else None,
+                  K, _lib.ptr(flags), st())
 
     def tc_b(split):
         _lib.call("fgb_tc_phase_b", desc, _lib.ptr(tc["w_hi"]),
@@ -378,7 +380,7 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
     srcB = int(torch.unique(FF._dev["src"]).numel()) * K   # distinct source rows
     xA = int(FF._dev["g_n"].sum().item()) * K             # X rows read by phase A groups
     work = {
-        "phaseA_tc": (vA * 2 + xA * 2 + zrows * K * 4, 2.0 * vA * K),
+        "phaseA_tc": (vA * 2 + xA * 2 + zrows * K * 2, 2.0 * vA * K),
         "phaseB_tc": (wB * 2 + srcB * 2 + N * K * 4 * 2, 2.0 * wB * K),
         "phaseA_tc_split": (vA * 4 + xA * 4 + zrows * K * 4, 6.0 * vA * K),
         "phaseB_tc_split": (wB * 4 + srcB * 4 + N * K * 4 * 2, 6.0 * wB * K),

@@ -106,6 +106,7 @@ SIGNATURES: dict[str, list] = {
     "fgb_matmat_f32": [P, P, P, P, P, P, I32, P, F32, I32, I32, P],
     "fgb_matmat_bf16": [P, P, P, P, P, P, P, I32, P, F32, I32, I32, P],
     "fgb_tc_phase_a": [P, P, P, P, P, P, I32, I32, P, P],
+    "fgb_tc_phase_a_bf16": [P, P, P, P, P, P, P, I32, P, P],
     "fgb_tc_phase_b": [P, P, P, P, P, P, P, P, I32, P, F32, P, P],
     "fgb_tc_phase_b_tma": [P, P, P, P, P, P, I32, P, F32, P, P],
     "fgb_split_bf16": [P, P, P, I64, P],

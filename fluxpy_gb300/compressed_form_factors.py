@@ -552,6 +552,10 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         a_wn = (g_kz[a_grp] + 63) // 64
         a_woff = np.zeros(a_grp.size + 1, np.int64)
         np.cumsum(a_wn, out=a_woff[1:])
+        # the tensor-core phase A with BF16 output takes one work item per
+        # whole group (every CTA owns its output rows: no atomics, no FP32 Z)
+        tg_woff = np.zeros(ng + 1, np.int64)
+        np.cumsum((g_kz + 63) // 64, out=tg_woff[1:])
         tsl = g_kzp // 64
         tjb = (g_n + 63) // 64
         tcnt = tsl * tjb
@@ -673,6 +677,9 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
             a_excl=d(a_ex, np.uint8), t_p0=d(t_p0, np.int64), src=src_d,
             g_kzp=d(g_kzp, np.int32), g_vtoff=d(g_vtoff[:-1], np.int64),
             a_woff=d(a_woff, np.int64))
+        self._dev_tc = dict(
+            a_grp=d(np.arange(ng), np.int32), a_j0=d(np.zeros(ng), np.int32),
+            a_j1=d(g_n, np.int32), a_excl=d(np.ones(ng), np.uint8), a_woff=d(tg_woff, np.int64))
         self._build_dev = dict(
             vt_g=d(vt_g, np.int32), vt_s=d(vt_s, np.int32), vt_j=d(vt_j, np.int32),
             vr_src=d(vr_src, np.int64), vr_dst=d(vr_dst, np.int64), vr_n=d(vr_n, np.int32),
@@ -685,6 +692,7 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         self._num_vrows = int(vr_src.size)
         self._num_pairs = int(all_p0.size)
         self._desc = self._make_desc(int(a_grp.size), ntiles, max_gt, int(a_woff[-1]))
+        self._desc_tc = self._make_desc_tc()
         self._lr_blocks = lr
         self._lr_u, self._lr_v = lr_u, lr_v
         self._panels = {}
@@ -707,6 +715,15 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         desc.max_group_tiles = max_gt
         desc.num_work = num_work
         desc.panel_rows = int(self._panel_rows)
+        return desc
+
+    def _make_desc_tc(self):
+        """The descriptor with one phase-A work item per whole group."""
+        desc = fgb_op_desc.from_buffer_copy(self._desc)
+        for key in ("a_grp", "a_j0", "a_j1", "a_excl", "a_woff"):
+            setattr(desc, key, self._dev_tc[key].data_ptr())
+        desc.num_items = int(self._dev_tc["a_grp"].numel()) if self._num_zrows > 0 else 0
+        desc.num_work = int(self._dev_tc["a_woff"][-1].item())
         return desc
 
     # -- device products --------------------------------------------------
@@ -908,10 +925,9 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         tc = self.tc_operands()
         flags = _lib.ptr(self.device_flags())
         if self._num_zrows > 0:
-            _lib.call("fgb_tc_phase_a", C.byref(self._desc), _lib.ptr(tc["vt_hi"]), None,
-                      _lib.ptr(Xb), None, _lib.ptr(Z), K, int(self._needs_zero_z), flags, st)
-            _lib.call("fgb_split_bf16", _lib.ptr(Z), _lib.ptr(Zb), None,
-                      self._num_zrows * K, st)
+            # phase A writes Z directly in BF16 (Z, the FP32 scratch, is unused)
+            _lib.call("fgb_tc_phase_a_bf16", C.byref(self._desc_tc), _lib.ptr(tc["vt_hi"]), None,
+                      _lib.ptr(Xb), None, _lib.ptr(Zb), None, K, flags, st)
         _lib.call("fgb_tc_phase_b", C.byref(self._desc), _lib.ptr(tc["w_hi"]), None,
                   _lib.ptr(Xb), None, _lib.ptr(Zb), None, _lib.ptr(Y), K, _lib.ptr(add),
                   float(alpha), flags, st)
@@ -942,16 +958,14 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         sl = buf("s_lo", (nz + N, K), torch.bfloat16)
         zh, xh = sh[:nz], sh[nz:]
         zl, xl = sl[:nz], sl[nz:]
-        z = buf("z", (zr, K), torch.float32)
         tc = self.tc_operands(split=True)
         flags = _lib.ptr(self.device_flags())
         _lib.call("fgb_split_bf16", _lib.ptr(X), _lib.ptr(xh), _lib.ptr(xl), N * K, st)
         if self._num_zrows > 0:
-            _lib.call("fgb_tc_phase_a", C.byref(self._desc), _lib.ptr(tc["vt_hi"]),
-                      _lib.ptr(tc["vt_lo"]), _lib.ptr(xh), _lib.ptr(xl), _lib.ptr(z), K,
-                      int(self._needs_zero_z), flags, st)
-            _lib.call("fgb_split_bf16", _lib.ptr(z), _lib.ptr(zh), _lib.ptr(zl),
-                      self._num_zrows * K, st)
+            # phase A writes the hi / lo BF16 parts of Z directly
+            _lib.call("fgb_tc_phase_a_bf16", C.byref(self._desc_tc), _lib.ptr(tc["vt_hi"]),
+                      _lib.ptr(tc["vt_lo"]), _lib.ptr(xh), _lib.ptr(xl), _lib.ptr(zh),
+                      _lib.ptr(zl), K, flags, st)
         _lib.call("fgb_tc_phase_b", C.byref(self._desc), _lib.ptr(tc["w_hi"]),
                   _lib.ptr(tc["w_lo"]), _lib.ptr(xh), _lib.ptr(xl), _lib.ptr(zh), _lib.ptr(zl),
                   _lib.ptr(Y), K, _lib.ptr(add), float(alpha), flags, st)
@@ -1101,12 +1115,13 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         with open(path, 'rb') as f:
             return pickle.load(f)
 
-    _DEV_DICTS = ("_dev", "_build_dev", "_nf")
+    _DEV_DICTS = ("_dev", "_dev_tc", "_build_dev", "_nf")
 
     def __getstate__(self):
         st = dict(self.__dict__)
         st["_root_cache"] = None
         st["_desc"] = None
+        st["_desc_tc"] = None
         st["_panels"] = {}
         st["_tc"] = {}
         st["_flags_d"] = None
@@ -1139,6 +1154,7 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         self._desc = self._make_desc(int(self.stats["num_items"]), int(self.stats["num_tiles"]),
                                      int(self.stats["max_group_tiles"]),
                                      int(self._dev["a_woff"][-1].item()))
+        self._desc_tc = self._make_desc_tc()
 
     # -- leaf data for the Python block objects --------------------------
     def _leaf_dense(self, b):

@@ -187,6 +187,10 @@ struct TcArgs {
   long long lds;           // row stride of X and Z (= K)
   int K;
   float* out;              // Y (phase B) or Z (phase A), row stride K
+  // phase A with BF16 output: Z written as hi (and lo) BF16 parts instead of
+  // FP32 (every work item must cover its whole group)
+  __nv_bfloat16* zout_hi;
+  __nv_bfloat16* zout_lo;
   const float* add;
   float alpha;
   unsigned* flags;
@@ -249,6 +253,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gather_gemm(TcArgs a) {
     if (SPLIT) wbase_lo = a.w_lo + a.g_vtoff[g] + (long long)s * kTcRows;
     xrow0 = a.g_c0[g];
     excl = a.a_excl[it] != 0;
+    if (a.zout_hi && !excl && tid == 0) atomicOr(a.flags, FGB_FLAG_INDEX_RANGE);
   }
   const int nch = (int)((r_end - r_first + CH - 1) / CH);
 
@@ -447,15 +452,21 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gather_gemm(TcArgs a) {
           const int r = half * 32 + i;
           if (r < out_rows) {
             const long long row = out_row0 + r;
-            float* dst = a.out + row * (long long)a.K + col;
+            const long long o = row * (long long)a.K + col;
             if (MODE == kModeB) {
               float y = v[i];
-              if (a.add) y = a.add[row * (long long)a.K + col] + a.alpha * y;
-              *dst = y;
+              if (a.add) y = a.add[o] + a.alpha * y;
+              a.out[o] = y;
+            } else if (a.zout_hi) {
+              if (excl) {
+                const __nv_bfloat16 h = __float2bfloat16(v[i]);
+                a.zout_hi[o] = h;
+                if (a.zout_lo) a.zout_lo[o] = __float2bfloat16(v[i] - __bfloat162float(h));
+              }
             } else if (excl) {
-              *dst = v[i];
+              a.out[o] = v[i];
             } else {
-              atomicAdd(dst, v[i]);
+              atomicAdd(a.out + o, v[i]);
             }
           }
         }
@@ -905,6 +916,39 @@ int fgb_tc_phase_a(const struct fgb_op_desc* d, const void* vt_hi, const void* v
   a.x_lo = static_cast<const __nv_bfloat16*>(X_lo);
   a.lds = K; a.K = K; a.out = Z; a.add = nullptr; a.alpha = 1.f; a.flags = flags;
   a.N = d->N; a.num_zrows = d->num_zrows;
+  return split ? fgb::launch_tc<fgb::kModeA, true>(a, d->num_work, st)
+               : fgb::launch_tc<fgb::kModeA, false>(a, d->num_work, st);
+}
+
+int fgb_tc_phase_a_bf16(const struct fgb_op_desc* d, const void* vt_hi, const void* vt_lo,
+                        const void* X_hi, const void* X_lo, void* Z_hi, void* Z_lo, int K,
+                        unsigned* flags, void* stream) {
+  if (!d || !flags || !Z_hi) { fgb::set_error("null operator, output or flags"); return FGB_BAD_ARG; }
+  if (K < 8 || (K % 8) != 0) { fgb::set_error("K must be a positive multiple of 8"); return FGB_BAD_ARG; }
+  const bool split = vt_lo != nullptr;
+  if (split != (X_lo != nullptr) || split != (Z_lo != nullptr)) {
+    fgb::set_error("split operands must come in pairs");
+    return FGB_BAD_ARG;
+  }
+  if (fgb::misaligned(vt_hi) || fgb::misaligned(X_hi) || fgb::misaligned(vt_lo) ||
+      fgb::misaligned(X_lo)) {
+    fgb::set_error("tensor-core operands must be 16-byte aligned");
+    return FGB_BAD_ARG;
+  }
+  if (d->num_items <= 0 || d->num_zrows <= 0) return FGB_OK;
+  fgb::TcArgs a{};
+  a.a_grp = d->a_grp; a.a_j0 = d->a_j0; a.a_j1 = d->a_j1; a.a_excl = d->a_excl;
+  a.a_woff = d->a_woff; a.num_items = d->num_items;
+  a.g_c0 = d->g_c0; a.g_kz = d->g_kz; a.g_kzp = d->g_kzp; a.g_vtoff = d->g_vtoff; a.g_z0 = d->g_z0;
+  a.w_hi = static_cast<const __nv_bfloat16*>(vt_hi);
+  a.w_lo = static_cast<const __nv_bfloat16*>(vt_lo);
+  a.x_hi = static_cast<const __nv_bfloat16*>(X_hi);
+  a.x_lo = static_cast<const __nv_bfloat16*>(X_lo);
+  a.zout_hi = static_cast<__nv_bfloat16*>(Z_hi);
+  a.zout_lo = static_cast<__nv_bfloat16*>(Z_lo);
+  a.lds = K; a.K = K; a.out = nullptr; a.add = nullptr; a.alpha = 1.f; a.flags = flags;
+  a.N = d->N; a.num_zrows = d->num_zrows;
+  cudaStream_t st = fgb::as_stream(stream);
   return split ? fgb::launch_tc<fgb::kModeA, true>(a, d->num_work, st)
                : fgb::launch_tc<fgb::kModeA, false>(a, d->num_work, st);
 }

@@ -229,12 +229,13 @@ def _colmax(t):
 _SPLIT_MARGIN = 0.3
 
 
-def _auto_chunk(FF, N, K):
+def _auto_chunk(FF, N, K, fp32_z=True):
     free, _ = torch.cuda.mem_get_info()
     # memory held by the caching allocator but not in use is available too
     free += torch.cuda.memory_reserved() - torch.cuda.memory_allocated()
-    # per column: E, B, R, D, Y, X (FP32), X hi/lo (BF16); Z (FP32), Z hi/lo
-    per_col = N * (6 * 4 + 2 * 2) + max(FF._num_zrows, 1) * 8
+    # per column: E, B, R, D, Y, X (FP32), X hi/lo (BF16); Z hi/lo (BF16),
+    # and Z in FP32 for the CUDA-core and mma.sync products
+    per_col = N * (6 * 4 + 2 * 2) + max(FF._num_zrows, 1) * (8 if fp32_z else 4)
     c = int(0.5 * free / per_col) // 8 * 8
     return max(8, min(K, c))
 
@@ -266,8 +267,11 @@ def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_
     """
     dev = E.device
     N, K0 = E.shape
+    # the tensor-core products write Z directly in BF16; FP32 Z is needed by
+    # the CUDA-core / mma.sync products only
+    fp32_z = precision == "fp32" or residual == "fp32" or engine != "tc"
     if chunk is None:
-        chunk = _auto_chunk(FF, N, K0)
+        chunk = _auto_chunk(FF, N, K0, fp32_z)
     if K0 > chunk:
         # the columns are independent: solve them in chunks that fit in memory
         parts = []
@@ -309,7 +313,8 @@ def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_
     thresh = (rtol * emax).cpu().numpy().astype(np.float32)
     thresh[thresh == 0] = 0.0
     colmax = torch.zeros(K, dtype=torch.int32, device=dev)
-    Z32 = torch.empty((max(FF._num_zrows, 1), K), dtype=torch.float32, device=dev)
+    Z32 = (torch.empty((max(FF._num_zrows, 1), K), dtype=torch.float32, device=dev) if fp32_z
+           else None)
     X32 = torch.empty_like(Ep)
     Y = torch.empty_like(Ep)
     st = stats if stats is not None else {}
@@ -335,7 +340,7 @@ def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_
         D = torch.empty_like(Ep)
         # BF16 sources stacked as [Z; X] (one tensor: TMA gathers in phase B)
         Sb, Zb, Xb = FF.stacked_sources(K, dev)
-        work = {"z": Z32, "s_hi": Sb}
+        work = {"s_hi": Sb}
         emax_h = np.maximum(emax.cpu().numpy(), 1e-30)
         if residual == "split-bf16":
             # the computed residual may be smaller than the exact one by the

@@ -364,6 +364,13 @@ int fgb_matmat_bf16(const struct fgb_op_desc* d, const void* panel, const void* 
 int fgb_tc_phase_a(const struct fgb_op_desc* d, const void* vt_hi, const void* vt_lo,
                    const void* X_hi, const void* X_lo, float* Z, int K, int zero_z,
                    unsigned* flags, void* stream);
+/* Phase A writing Z directly as BF16 (Z_hi = bf16(z), and with the split
+ * operands Z_lo = bf16(z - Z_hi)), num_zrows x K each: for a descriptor whose
+ * work items all cover their whole group (a_excl == 1; an item that does not
+ * is skipped and flagged FGB_FLAG_INDEX_RANGE). */
+int fgb_tc_phase_a_bf16(const struct fgb_op_desc* d, const void* vt_hi, const void* vt_lo,
+                        const void* X_hi, const void* X_lo, void* Z_hi, void* Z_lo, int K,
+                        unsigned* flags, void* stream);
 int fgb_tc_phase_b(const struct fgb_op_desc* d, const void* w_hi, const void* w_lo,
                    const void* X_hi, const void* X_lo, const void* Z_hi, const void* Z_lo,
                    float* Y, int K, const float* add, float alpha, unsigned* flags,

@@ -284,3 +284,33 @@ def test_tma_gather_phase_b_matches_cp_async(terrain_op, K):
         FF.check_device_flags()
         assert torch.isfinite(Y_tma).all()
         assert torch.equal(Y_tma, Y_cp), split
+
+
+def test_phase_a_bf16_output_matches_fp32(terrain_op):
+    """Phase A with whole-group work items writing Z as BF16 hi / lo parts
+    against phase A with column-split items accumulating FP32 Z."""
+    import ctypes as C
+    from fluxpy_gb300 import _lib
+    sm, FF = terrain_op
+    N, K = sm.num_faces, 136
+    nz = FF._num_zrows
+    g = torch.Generator(device="cuda").manual_seed(11)
+    X = torch.rand((N, K), device="cuda", generator=g)
+    tc = FF.tc_operands(split=True)
+    st = _lib.stream_handle()
+    fl = _lib.ptr(FF.device_flags())
+    xh = torch.empty((N, K), dtype=torch.bfloat16, device="cuda")
+    xl = torch.empty_like(xh)
+    _lib.call("fgb_split_bf16", _lib.ptr(X), _lib.ptr(xh), _lib.ptr(xl), N * K, st)
+    z32 = torch.empty((nz, K), device="cuda")
+    _lib.call("fgb_tc_phase_a", C.byref(FF._desc), _lib.ptr(tc["vt_hi"]), _lib.ptr(tc["vt_lo"]),
+              _lib.ptr(xh), _lib.ptr(xl), _lib.ptr(z32), K, int(FF._needs_zero_z), fl, st)
+    zh = torch.full((nz, K), float("nan"), dtype=torch.bfloat16, device="cuda")
+    zl = torch.full_like(zh, float("nan"))
+    _lib.call("fgb_tc_phase_a_bf16", C.byref(FF._desc_tc), _lib.ptr(tc["vt_hi"]),
+              _lib.ptr(tc["vt_lo"]), _lib.ptr(xh), _lib.ptr(xl), _lib.ptr(zh), _lib.ptr(zl), K,
+              fl, st)
+    FF.check_device_flags()
+    z = zh.float() + zl.float()
+    assert torch.isfinite(z).all()
+    assert (z - z32).abs().max().item() <= 1e-5 * z32.abs().max().item()

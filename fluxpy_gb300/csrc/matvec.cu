@@ -47,6 +47,8 @@ struct PanelView {
   const int* a_j1;
   const unsigned char* a_excl;
   long long num_items;
+  const long long* a_woff;  // first 64-row work slice of each item
+  long long num_work;
   // phase B
   const long long* t_p0;  // num_tiles + 1 panel row offsets
   const int* src;         // per panel row
@@ -56,64 +58,116 @@ struct PanelView {
 };
 
 // ------------------------------------------------------------ K = 1 ----
+// Phase A: one CTA per work slice (item, 64 stacked V^T rows); the item's
+// x segment (at most ITEM_COLS = 2048 values) is staged in shared memory and
+// warp w computes the dot products of rows w, w + 8, ... (coalesced, 4-wide
+// loads along the row), reduced with shuffles in a fixed order.
+constexpr int kItemColsMax = 2048;
+
+template <class T> struct Vec4;
+template <> struct Vec4<float> { using type = float4; };
+template <> struct Vec4<double> { using type = double4; };
+
 template <class T, class V>
-__global__ void phaseA_k1(PanelView op, const T* __restrict__ vpanel, const V* __restrict__ x,
-                          V* __restrict__ z) {
-  const int lane = threadIdx.x & 31;
-  const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
-  for (long long it = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; it < op.num_items;
-       it += warps) {
+__global__ void __launch_bounds__(256)
+phaseA_k1(PanelView op, const T* __restrict__ vpanel, const V* __restrict__ x,
+          V* __restrict__ z) {
+  __shared__ __align__(16) V s_x[kItemColsMax];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (long long unit = blockIdx.x; unit < op.num_work; unit += gridDim.x) {
+    long long lo = 0, hi = op.num_items - 1;
+    while (lo < hi) {
+      const long long mid = (lo + hi + 1) >> 1;
+      if (op.a_woff[mid] <= unit) lo = mid; else hi = mid - 1;
+    }
+    const long long it = lo;
+    const int s = (int)(unit - op.a_woff[it]);
     const int g = op.a_grp[it];
     const int j0 = op.a_j0[it], j1 = op.a_j1[it];
+    const int n = j1 - j0;
     const int kz = op.g_kz[g], ldv = op.g_ldv[g];
-    const V* xb = x + op.g_c0[g];
-    const T* vg = vpanel + op.g_voff[g];
-    V* zg = z + op.g_z0[g];
     const bool excl = op.a_excl[it];
-    for (int r = 0; r < kz; r++) {
-      const T* row = vg + (long long)r * ldv;
-      V s = V(0);
-      for (int j = j0 + lane; j < j1; j += 32) s += (V)row[j] * __ldg(xb + j);
-      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    __syncthreads();
+    const V* xb = x + op.g_c0[g] + j0;
+    // items are at most kItemColsMax columns wide (the host splits groups);
+    // a wider one would read x from global memory directly
+    const bool staged = n <= kItemColsMax;
+    if (staged)
+      for (int j = threadIdx.x; j < n; j += blockDim.x) s_x[j] = __ldg(xb + j);
+    __syncthreads();
+    const V* xs = staged ? s_x : xb;
+    const T* vg = vpanel + op.g_voff[g] + j0;
+    V* zg = z + op.g_z0[g];
+    const int r_end = min(kz, (s + 1) * 64);
+    for (int r = s * 64 + warp; r < r_end; r += 8) {
+      const T* row = vg + (long long)r * ldv;   // 32-byte aligned: ldv % 8 == 0, j0 % 2048 == 0
+      V acc = V(0);
+      const int n4 = n & ~3;
+      for (int j = lane * 4; j < n4; j += 128) {
+        const typename Vec4<T>::type w = *reinterpret_cast<const typename Vec4<T>::type*>(row + j);
+        acc += (V)w.x * xs[j] + (V)w.y * xs[j + 1] + (V)w.z * xs[j + 2] + (V)w.w * xs[j + 3];
+      }
+      for (int j = n4 + lane; j < n; j += 32) acc += (V)row[j] * xs[j];
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
       if (lane == 0) {
-        if (excl) zg[r] = s;
-        else atomicAdd(zg + r, s);
+        if (excl) zg[r] = acc;
+        else atomicAdd(zg + r, acc);
       }
     }
   }
 }
 
-// One CTA per tile: thread (i, q) = (tid % 64, tid / 64) accumulates row i
-// over panel rows l = p0 + q, p0 + q + 4, ...; fixed-order reduction.
+// Phase B: one CTA per tile; warp w accumulates panel rows p0 + w, p0 + w + 8,
+// ... for the tile's rows 2 lane and 2 lane + 1 (each panel row read as one
+// 256-byte (FP32) line per warp), eight rows in flight per warp; the eight
+// warps' partial sums are added in a fixed order.
+template <class T> struct Vec2;
+template <> struct Vec2<float> { using type = float2; };
+template <> struct Vec2<double> { using type = double2; };
+
 template <class T, class V>
 __global__ void __launch_bounds__(256)
 phaseB_k1(PanelView op, const T* __restrict__ panel, const V* __restrict__ x,
           const V* __restrict__ z, V* __restrict__ y, const V* __restrict__ add_vec, V alpha) {
-  __shared__ V s_part[4][kTileRows];
-  const int i = threadIdx.x & (kTileRows - 1), q = threadIdx.x >> 6;
+  __shared__ V s_part[8][kTileRows];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const long long t = blockIdx.x;
   const long long p0 = op.t_p0[t], p1 = op.t_p0[t + 1];
   const long long nz = op.num_zrows;
-  V acc = V(0);
-  long long l = p0 + q;
-  for (; l + 12 < p1; l += 16) {
-    const int s0 = op.src[l], s1 = op.src[l + 4], s2 = op.src[l + 8], s3 = op.src[l + 12];
-    const V v0 = s0 < nz ? __ldg(z + s0) : __ldg(x + (s0 - nz));
-    const V v1 = s1 < nz ? __ldg(z + s1) : __ldg(x + (s1 - nz));
-    const V v2 = s2 < nz ? __ldg(z + s2) : __ldg(x + (s2 - nz));
-    const V v3 = s3 < nz ? __ldg(z + s3) : __ldg(x + (s3 - nz));
-    acc += (V)panel[l * kTileRows + i] * v0 + (V)panel[(l + 4) * kTileRows + i] * v1 +
-           (V)panel[(l + 8) * kTileRows + i] * v2 + (V)panel[(l + 12) * kTileRows + i] * v3;
+  using T2 = typename Vec2<T>::type;
+  V a0 = V(0), a1 = V(0);
+  auto src_val = [&](long long l) -> V {
+    const int sidx = __ldg(op.src + l);
+    return sidx < nz ? __ldg(z + sidx) : __ldg(x + (sidx - nz));
+  };
+  long long l = p0 + warp;
+  for (; l + 56 < p1; l += 64) {
+    V v[8];
+    T2 w[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+      w[u] = __ldg(reinterpret_cast<const T2*>(panel + (l + 8 * u) * kTileRows) + lane);
+      v[u] = src_val(l + 8 * u);
+    }
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+      a0 += (V)w[u].x * v[u];
+      a1 += (V)w[u].y * v[u];
+    }
   }
-  for (; l < p1; l += 4) {
-    const int s0 = op.src[l];
-    const V v0 = s0 < nz ? __ldg(z + s0) : __ldg(x + (s0 - nz));
-    acc += (V)panel[l * kTileRows + i] * v0;
+  for (; l < p1; l += 8) {
+    const T2 w = __ldg(reinterpret_cast<const T2*>(panel + l * kTileRows) + lane);
+    const V v = src_val(l);
+    a0 += (V)w.x * v;
+    a1 += (V)w.y * v;
   }
-  s_part[q][i] = acc;
+  s_part[warp][2 * lane] = a0;
+  s_part[warp][2 * lane + 1] = a1;
   __syncthreads();
   if (threadIdx.x < kTileRows) {
-    const V sum = (s_part[0][i] + s_part[1][i]) + (s_part[2][i] + s_part[3][i]);
+    const int i = threadIdx.x;
+    const V sum = ((s_part[0][i] + s_part[1][i]) + (s_part[2][i] + s_part[3][i])) +
+                  ((s_part[4][i] + s_part[5][i]) + (s_part[6][i] + s_part[7][i]));
     const long long row = t * kTileRows + i;
     if (row < op.N) y[row] = add_vec ? add_vec[row] + alpha * sum : sum;
   }
@@ -599,6 +653,7 @@ PanelView to_view(const fgb_op_desc* d) {
   v.g_voff = d->g_voff; v.g_z0 = d->g_z0;
   v.a_grp = d->a_grp; v.a_j0 = d->a_j0; v.a_j1 = d->a_j1; v.a_excl = d->a_excl;
   v.num_items = d->num_items;
+  v.a_woff = d->a_woff; v.num_work = d->num_work;
   v.t_p0 = d->t_p0; v.src = d->src; v.num_tiles = d->num_tiles;
   v.N = d->N;
   v.num_zrows = d->num_zrows;
@@ -618,7 +673,7 @@ int fgb_matvec_f32(const fgb_op_desc* d, const float* panel, const float* vpanel
   cudaStream_t s = fgb::as_stream(stream);
   if (zero_z && d->num_zrows > 0) FGB_CUDA_TRY(cudaMemsetAsync(z, 0, sizeof(float) * d->num_zrows, s));
   if (op.num_items > 0) {
-    fgb::phaseA_k1<float, float><<<fgb::grid_for(op.num_items * 32, 256, 152LL * 64), 256, 0, s>>>(op, vpanel, x, z);
+    fgb::phaseA_k1<float, float><<<fgb::grid_for(op.num_work, 1, 152LL * 64), 256, 0, s>>>(op, vpanel, x, z);
     FGB_LAUNCH_CHECK("phaseA_k1");
   }
   if (op.num_tiles > 0) {
@@ -637,7 +692,7 @@ int fgb_matvec_f64(const fgb_op_desc* d, const double* panel, const double* vpan
   cudaStream_t s = fgb::as_stream(stream);
   if (zero_z && d->num_zrows > 0) FGB_CUDA_TRY(cudaMemsetAsync(z, 0, sizeof(double) * d->num_zrows, s));
   if (op.num_items > 0) {
-    fgb::phaseA_k1<double, double><<<fgb::grid_for(op.num_items * 32, 256, 152LL * 64), 256, 0, s>>>(op, vpanel, x, z);
+    fgb::phaseA_k1<double, double><<<fgb::grid_for(op.num_work, 1, 152LL * 64), 256, 0, s>>>(op, vpanel, x, z);
     FGB_LAUNCH_CHECK("phaseA_k1");
   }
   if (op.num_tiles > 0) {
@@ -657,7 +712,7 @@ int fgb_matvec_f32_f64(const fgb_op_desc* d, const float* panel, const float* vp
   cudaStream_t s = fgb::as_stream(stream);
   if (zero_z && d->num_zrows > 0) FGB_CUDA_TRY(cudaMemsetAsync(z, 0, sizeof(double) * d->num_zrows, s));
   if (op.num_items > 0) {
-    fgb::phaseA_k1<float, double><<<fgb::grid_for(op.num_items * 32, 256, 152LL * 64), 256, 0, s>>>(op, vpanel, x, z);
+    fgb::phaseA_k1<float, double><<<fgb::grid_for(op.num_work, 1, 152LL * 64), 256, 0, s>>>(op, vpanel, x, z);
     FGB_LAUNCH_CHECK("phaseA_k1");
   }
   if (op.num_tiles > 0) {

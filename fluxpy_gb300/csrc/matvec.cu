@@ -173,6 +173,44 @@ phaseB_k1(PanelView op, const T* __restrict__ panel, const V* __restrict__ x,
   }
 }
 
+// ------------------------------------------------- async-copy helpers ----
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void ldm_x4(unsigned addr, unsigned& r0, unsigned& r1, unsigned& r2,
+                                       unsigned& r3) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3) : "r"(addr));
+}
+__device__ __forceinline__ void ldm_x4_t(unsigned addr, unsigned& r0, unsigned& r1, unsigned& r2,
+                                         unsigned& r3) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3) : "r"(addr));
+}
+__device__ __forceinline__ void mma_bf16(float* c, unsigned a0, unsigned a1, unsigned a2,
+                                         unsigned a3, unsigned b0, unsigned b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+      "{%8,%9}, {%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+// 16-byte async copy; src_size 0 zero-fills (the address must still be valid)
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem, bool pred) {
+  const unsigned s = smem_u32(smem);
+  const int n = pred ? 16 : 0;
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(n));
+}
+// 4-byte async copy (zero-fill when !pred)
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem, bool pred) {
+  const unsigned s = smem_u32(smem);
+  const int n = pred ? 4 : 0;
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(s), "l"(gmem), "r"(n));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
 // ------------------------------------------------- K RHS, FP32 FFMA ----
 // s += x with Kahan compensation c (the _rn intrinsics keep the compiler
 // from re-associating the compensation away).
@@ -268,77 +306,115 @@ phaseA_kn_f32(PanelView op, const float* __restrict__ vpanel, const float* __res
   }
 }
 
-// Phase B: CTA per (tile, 64 columns); thread owns 4 rows x 4 cols.
-__global__ void __launch_bounds__(256)
+// Phase B: CTA per (tile, 128 columns), 256 threads; thread (ty, tx) =
+// (tid / 32, tid % 32) owns rows 8 ty .. 8 ty + 7 and columns 4 tx .. 4 tx + 3
+// (32 accumulators).  Per panel row a thread reads its 8 weights as two
+// broadcast 16-byte shared loads and its 4 sources as one, for 32 FMAs.
+// Chunks of 32 panel rows are double-buffered with cp.async; the chunk's
+// partial sums are added to the running sums with Kahan compensation.
+constexpr int kB32Cols = 128;
+constexpr int kB32Chunk = 32;
+
+__global__ void __launch_bounds__(256, 2)
 phaseB_kn_f32(PanelView op, const float* __restrict__ panel, const float* __restrict__ X,
               long long ldx, const float* __restrict__ Z, long long ldz, float* __restrict__ Y,
               long long ldy, int K, const float* __restrict__ add_mat, long long ld_add,
               float alpha) {
-  __shared__ float s_w[kJC][kTileRows + 4];
-  __shared__ float s_s[kJC][kKT];
-  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  const int nkt = (K + kKT - 1) / kKT;
+  __shared__ __align__(16) float s_w[2][kB32Chunk][kTileRows];
+  __shared__ __align__(16) float s_s[2][kB32Chunk][kB32Cols];
+  const int tid = threadIdx.x, ty = tid >> 5, tx = tid & 31;
+  const int nkt = (K + kB32Cols - 1) / kB32Cols;
   const long long t = blockIdx.x / nkt;
-  const int c_base = (int)(blockIdx.x % nkt) * kKT;
+  const int c_base = (int)(blockIdx.x % nkt) * kB32Cols;
   const long long p0 = op.t_p0[t], p1 = op.t_p0[t + 1];
-  float acc[4][4];
+  const bool vec = (K % 4) == 0 && (ldx % 4) == 0 && (ldz % 4) == 0 && (ldy % 4) == 0;
+  float acc[8][4], comp[8][4];
 #pragma unroll
-  for (int r = 0; r < 4; r++)
+  for (int r = 0; r < 8; r++)
 #pragma unroll
-    for (int c = 0; c < 4; c++) acc[r][c] = 0.f;
-  float comp[4][4];
+    for (int c = 0; c < 4; c++) { acc[r][c] = 0.f; comp[r][c] = 0.f; }
+  auto load = [&](int buf, long long l0) {
+    // W: 32 rows x 64 floats = 512 16-byte pieces (2 per thread)
 #pragma unroll
-  for (int r = 0; r < 4; r++)
-#pragma unroll
-    for (int c = 0; c < 4; c++) comp[r][c] = 0.f;
-  for (long long l0 = p0; l0 < p1; l0 += kJC) {
-    __syncthreads();
-    for (int e = threadIdx.x; e < kJC * kTileRows / 4; e += 256) {
-      int l = e / (kTileRows / 4), i4 = (e % (kTileRows / 4)) * 4;
-      float4 w = *reinterpret_cast<const float4*>(panel + (l0 + l) * kTileRows + i4);
-      s_w[l][i4] = w.x; s_w[l][i4 + 1] = w.y; s_w[l][i4 + 2] = w.z; s_w[l][i4 + 3] = w.w;
+    for (int q = 0; q < 2; q++) {
+      const int e = tid + q * 256;
+      const int l = e >> 4, i4 = (e & 15) * 4;
+      cp_async16(&s_w[buf][l][i4], panel + (l0 + l) * kTileRows + i4, true);
     }
-    for (int e = threadIdx.x; e < kJC * kKT; e += 256) {
-      int l = e / kKT, c = e % kKT;
+    // S: 32 gathered rows x 128 floats = 1024 pieces (4 per thread); rows
+    // l = tid / 32 + 8 q, piece tx (16-byte copies when rows are 16-byte
+    // aligned, K % 4 == 0; 4-byte copies otherwise)
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int l = ty + 8 * q;
       const int sidx = op.src[l0 + l];
       const float* srow = sidx < op.num_zrows ? Z + (long long)sidx * ldz
                                               : X + (long long)(sidx - op.num_zrows) * ldx;
-      s_s[l][c] = (c_base + c < K) ? srow[c_base + c] : 0.f;
-    }
-    __syncthreads();
-    float part[4][4];
+      const int c = c_base + tx * 4;
+      if (vec) {
+        const bool ok = c < K;
+        cp_async16(&s_s[buf][l][tx * 4], ok ? srow + c : srow, ok);
+      } else {
 #pragma unroll
-    for (int r = 0; r < 4; r++)
-#pragma unroll
-      for (int c = 0; c < 4; c++) part[r][c] = 0.f;
-#pragma unroll 4
-    for (int l = 0; l < kJC; l++) {
-      float sv[4];
-#pragma unroll
-      for (int c = 0; c < 4; c++) sv[c] = s_s[l][tx * 4 + c];
-#pragma unroll
-      for (int r = 0; r < 4; r++) {
-        float wv = s_w[l][ty + 16 * r];
-#pragma unroll
-        for (int c = 0; c < 4; c++) part[r][c] += wv * sv[c];
+        for (int e = 0; e < 4; e++) {
+          const bool ok = c + e < K;
+          cp_async4(&s_s[buf][l][tx * 4 + e], ok ? srow + c + e : srow, ok);
+        }
       }
     }
+    cp_async_commit();
+  };
+  int buf = 0;
+  if (p0 < p1) load(0, p0);
+  for (long long l0 = p0; l0 < p1; l0 += kB32Chunk) {
+    if (l0 + kB32Chunk < p1) {
+      load(buf ^ 1, l0 + kB32Chunk);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncthreads();
+    float part[8][4];
 #pragma unroll
-    for (int r = 0; r < 4; r++)
+    for (int r = 0; r < 8; r++)
+#pragma unroll
+      for (int c = 0; c < 4; c++) part[r][c] = 0.f;
+#pragma unroll 8
+    for (int l = 0; l < kB32Chunk; l++) {
+      const float4 w0 = *reinterpret_cast<const float4*>(&s_w[buf][l][ty * 8]);
+      const float4 w1 = *reinterpret_cast<const float4*>(&s_w[buf][l][ty * 8 + 4]);
+      const float4 sv = *reinterpret_cast<const float4*>(&s_s[buf][l][tx * 4]);
+      const float w[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+      const float x4[4] = {sv.x, sv.y, sv.z, sv.w};
+#pragma unroll
+      for (int r = 0; r < 8; r++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) part[r][c] = fmaf(w[r], x4[c], part[r][c]);
+    }
+#pragma unroll
+    for (int r = 0; r < 8; r++)
 #pragma unroll
       for (int c = 0; c < 4; c++) kahan_add(acc[r][c], comp[r][c], part[r][c]);
+    __syncthreads();
+    buf ^= 1;
   }
+  const int col = c_base + tx * 4;
+  if (col < K) {
 #pragma unroll
-  for (int r = 0; r < 4; r++) {
-    long long i = t * kTileRows + ty + 16 * r;
-    if (i >= op.N) continue;
+    for (int r = 0; r < 8; r++) {
+      const long long i = t * kTileRows + ty * 8 + r;
+      if (i >= op.N) continue;
+      float v[4];
 #pragma unroll
-    for (int c = 0; c < 4; c++) {
-      int col = c_base + tx * 4 + c;
-      if (col >= K) continue;
-      float v = acc[r][c];
-      if (add_mat) v = add_mat[i * ld_add + col] + alpha * v;
-      Y[i * ldy + col] = v;
+      for (int c = 0; c < 4; c++) {
+        v[c] = acc[r][c];
+        if (add_mat) v[c] = add_mat[i * ld_add + col + c] + alpha * v[c];
+      }
+      if (vec && col + 4 <= K) {
+        *reinterpret_cast<float4*>(Y + i * ldy + col) = make_float4(v[0], v[1], v[2], v[3]);
+      } else {
+        for (int c = 0; c < 4 && col + c < K; c++) Y[i * ldy + col + c] = v[c];
+      }
     }
   }
 }
@@ -352,37 +428,6 @@ constexpr int kBK = 32;      // reduction chunk
 constexpr int kAPad = 40;    // smem row length (elements) for 32-wide rows
 constexpr int kBPad = 136;   // smem row length for 128-wide rows
 constexpr int kMPad = 72;    // smem row length for 64-wide rows
-
-__device__ __forceinline__ unsigned smem_u32(const void* p) {
-  return (unsigned)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ void ldm_x4(unsigned addr, unsigned& r0, unsigned& r1, unsigned& r2,
-                                       unsigned& r3) {
-  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
-               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3) : "r"(addr));
-}
-__device__ __forceinline__ void ldm_x4_t(unsigned addr, unsigned& r0, unsigned& r1, unsigned& r2,
-                                         unsigned& r3) {
-  asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
-               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3) : "r"(addr));
-}
-__device__ __forceinline__ void mma_bf16(float* c, unsigned a0, unsigned a1, unsigned a2,
-                                         unsigned a3, unsigned b0, unsigned b1) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
-      "{%8,%9}, {%0,%1,%2,%3};\n"
-      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
-}
-// 16-byte async copy; src_size 0 zero-fills (the address must still be valid)
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem, bool pred) {
-  const unsigned s = smem_u32(smem);
-  const int n = pred ? 16 : 0;
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(n));
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
 
 // Phase A: Z[z0 + r, c] (+)= sum_j Vg[r, j] X[c0 + j, c], r in a 64-row slice.
 __global__ void __launch_bounds__(128)
@@ -739,7 +784,8 @@ int fgb_matmat_f32(const fgb_op_desc* d, const float* panel, const float* vpanel
     FGB_LAUNCH_CHECK("phaseA_kn_f32");
   }
   if ((phases & 2) && op.num_tiles > 0) {
-    fgb::phaseB_kn_f32<<<(unsigned)(op.num_tiles * ky), 256, 0, s>>>(op, panel, X, K, Z, K, Y, K, K,
+    const unsigned kb = (unsigned)((K + fgb::kB32Cols - 1) / fgb::kB32Cols);
+    fgb::phaseB_kn_f32<<<(unsigned)(op.num_tiles * kb), 256, 0, s>>>(op, panel, X, K, Z, K, Y, K, K,
                                                                       add, K, alpha);
     FGB_LAUNCH_CHECK("phaseB_kn_f32");
   }

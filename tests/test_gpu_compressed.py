@@ -314,3 +314,15 @@ def test_phase_a_bf16_output_matches_fp32(terrain_op):
     z = zh.float() + zl.float()
     assert torch.isfinite(z).all()
     assert (z - z32).abs().max().item() <= 1e-5 * z32.abs().max().item()
+
+
+@pytest.mark.parametrize("K", [3, 5, 132])
+def test_fp32_multi_rhs_product_any_width(terrain_op, K):
+    """The FP32 CUDA-core K-column product (16-byte gathers when K % 4 == 0,
+    4-byte gathers otherwise) against the FP64 product."""
+    sm, FF = terrain_op
+    g = torch.Generator(device="cuda").manual_seed(K + 3)
+    X = torch.rand((sm.num_faces, K), device="cuda", generator=g, dtype=torch.float64)
+    Y32 = FF.matmat_permuted(X.float().contiguous(), "fp32")
+    Y64 = FF.matmat_permuted(X, "fp64")
+    assert (Y32.double() - Y64).abs().max().item() <= 5e-6 * Y64.abs().max().item()

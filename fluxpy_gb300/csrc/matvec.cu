@@ -66,7 +66,7 @@ constexpr int kItemColsMax = 2048;
 
 template <class T> struct Vec4;
 template <> struct Vec4<float> { using type = float4; };
-template <> struct Vec4<double> { using type = double4; };
+template <> struct Vec4<double> { using type = double4_32a; };
 
 template <class T, class V>
 __global__ void __launch_bounds__(256)
@@ -221,87 +221,124 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
   s = t;
 }
 
-constexpr int kKT = 64;   // K columns per CTA (FP32 kernels)
-constexpr int kJC = 32;   // reduction chunk
+constexpr int kB32Cols = 128;   // K columns per CTA (FP32 K-column kernels)
+constexpr int kB32Chunk = 32;   // reduction rows per stage
 
-// Phase A: CTA per (item, 64-row slice of the group's panel, 64 columns).
-__global__ void __launch_bounds__(256)
+// Phase A: CTA per (work slice = item x 64 stacked V^T rows, 128 columns),
+// 256 threads; thread (ty, tx) owns rows 8 ty .. + 7 and columns 4 tx .. + 3.
+// Per chunk of 32 group columns j the 64 x 32 slab of V^T is staged
+// transposed (s_v[j][row], two broadcast 16-byte reads per thread and j)
+// and the 32 X rows c0 + j with cp.async; Kahan-compensated chunk sums.
+__global__ void __launch_bounds__(256, 2)
 phaseA_kn_f32(PanelView op, const float* __restrict__ vpanel, const float* __restrict__ X,
-              long long ldx, float* __restrict__ Z, long long ldz, int K, int mt_per_item) {
-  __shared__ float s_v[64][kJC + 1];
-  __shared__ float s_x[kJC][kKT];
-  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  const int nkt = (K + kKT - 1) / kKT;
-  long long bid = blockIdx.x;
-  const int c_base = (int)(bid % nkt) * kKT;
-  bid /= nkt;
-  const int mt = (int)(bid % mt_per_item);
-  const long long it = bid / mt_per_item;
+              long long ldx, float* __restrict__ Z, long long ldz, int K) {
+  __shared__ __align__(16) float s_v[kB32Chunk][68];   // padded: 4-way store conflicts
+  __shared__ __align__(16) float s_x[kB32Chunk][kB32Cols];
+  const int tid = threadIdx.x, ty = tid >> 5, tx = tid & 31;
+  const int nkt = (K + kB32Cols - 1) / kB32Cols;
+  const long long unit = blockIdx.x / nkt;
+  const int c_base = (int)(blockIdx.x % nkt) * kB32Cols;
+  long long lo = 0, hi = op.num_items - 1;
+  while (lo < hi) {
+    const long long mid = (lo + hi + 1) >> 1;
+    if (op.a_woff[mid] <= unit) lo = mid; else hi = mid - 1;
+  }
+  const long long it = lo;
+  const int sl = (int)(unit - op.a_woff[it]);
   const int g = op.a_grp[it];
   const int kz = op.g_kz[g];
-  const int r_base = mt * 64;
-  if (r_base >= kz) return;
+  const int r_base = sl * 64;
   const int j0 = op.a_j0[it], j1 = op.a_j1[it];
   const int ldv = op.g_ldv[g];
   const long long c0 = op.g_c0[g];
   const float* vg = vpanel + op.g_voff[g];
-  float acc[4][4];
+  const bool vec = (K % 4) == 0 && (ldx % 4) == 0 && (ldz % 4) == 0;
+  float acc[8][4], comp[8][4];
 #pragma unroll
-  for (int r = 0; r < 4; r++)
+  for (int r = 0; r < 8; r++)
 #pragma unroll
-    for (int c = 0; c < 4; c++) acc[r][c] = 0.f;
-  float comp[4][4];
-#pragma unroll
-  for (int r = 0; r < 4; r++)
-#pragma unroll
-    for (int c = 0; c < 4; c++) comp[r][c] = 0.f;
-  for (int jc = j0; jc < j1; jc += kJC) {
+    for (int c = 0; c < 4; c++) { acc[r][c] = 0.f; comp[r][c] = 0.f; }
+  for (int jc = j0; jc < j1; jc += kB32Chunk) {
     __syncthreads();
-    for (int q = threadIdx.x; q < 64 * kJC; q += 256) {
-      int r = q / kJC, j = q % kJC;
-      s_v[r][j] = (r_base + r < kz && jc + j < j1) ? vg[(long long)(r_base + r) * ldv + jc + j] : 0.f;
+    // V^T slab: 64 rows x 32 columns, read along the rows in 16-byte pieces
+    // (a warp covers 4 rows x 128 bytes; rows are 32-byte aligned: ldv % 8
+    // == 0, jc % 32 == 0), stored transposed
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+      const int p = tid + q * 256;          // 512 pieces
+      const int r = p >> 3, j = (p & 7) * 4;
+      const int row = r_base + r;
+      float v[4] = {0.f, 0.f, 0.f, 0.f};
+      if (row < kz) {
+        const float* src = vg + (long long)row * ldv + jc + j;
+        if (jc + j + 3 < j1) {
+          const float4 f = *reinterpret_cast<const float4*>(src);
+          v[0] = f.x; v[1] = f.y; v[2] = f.z; v[3] = f.w;
+        } else {
+#pragma unroll
+          for (int e = 0; e < 4; e++)
+            if (jc + j + e < j1) v[e] = src[e];
+        }
+      }
+#pragma unroll
+      for (int e = 0; e < 4; e++) s_v[j + e][r] = v[e];
     }
-    for (int q = threadIdx.x; q < kJC * kKT; q += 256) {
-      int j = q / kKT, c = q % kKT;
-      s_x[j][c] = (jc + j < j1 && c_base + c < K) ? X[(c0 + jc + j) * ldx + c_base + c] : 0.f;
-    }
-    __syncthreads();
-    // per-chunk partial sums, added to the running sums with Kahan
-    // compensation so that long reductions keep FP32 accuracy
-    float part[4][4];
+    // X rows c0 + jc .. + 31, 128 columns
 #pragma unroll
-    for (int r = 0; r < 4; r++)
+    for (int q = 0; q < 4; q++) {
+      const int j = ty + 8 * q;
+      const bool okr = jc + j < j1;
+      const float* xrow = X + (c0 + (okr ? jc + j : 0)) * ldx;
+      const int c = c_base + tx * 4;
+      if (vec) {
+        const bool ok = okr && c < K;
+        cp_async16(&s_x[j][tx * 4], ok ? xrow + c : xrow, ok);
+      } else {
 #pragma unroll
-      for (int c = 0; c < 4; c++) part[r][c] = 0.f;
-#pragma unroll 4
-    for (int j = 0; j < kJC; j++) {
-      float xv[4];
-#pragma unroll
-      for (int c = 0; c < 4; c++) xv[c] = s_x[j][tx * 4 + c];
-#pragma unroll
-      for (int r = 0; r < 4; r++) {
-        float v = s_v[ty + 16 * r][j];
-#pragma unroll
-        for (int c = 0; c < 4; c++) part[r][c] += v * xv[c];
+        for (int e = 0; e < 4; e++) {
+          const bool ok = okr && c + e < K;
+          cp_async4(&s_x[j][tx * 4 + e], ok ? xrow + c + e : xrow, ok);
+        }
       }
     }
+    cp_async_commit();
+    cp_async_wait<0>();
+    __syncthreads();
+    float part[8][4];
 #pragma unroll
-    for (int r = 0; r < 4; r++)
+    for (int r = 0; r < 8; r++)
+#pragma unroll
+      for (int c = 0; c < 4; c++) part[r][c] = 0.f;
+#pragma unroll 8
+    for (int j = 0; j < kB32Chunk; j++) {
+      const float4 v0 = *reinterpret_cast<const float4*>(&s_v[j][ty * 8]);
+      const float4 v1 = *reinterpret_cast<const float4*>(&s_v[j][ty * 8 + 4]);
+      const float4 xv = *reinterpret_cast<const float4*>(&s_x[j][tx * 4]);
+      const float w[8] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
+      const float x4[4] = {xv.x, xv.y, xv.z, xv.w};
+#pragma unroll
+      for (int r = 0; r < 8; r++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) part[r][c] = fmaf(w[r], x4[c], part[r][c]);
+    }
+#pragma unroll
+    for (int r = 0; r < 8; r++)
 #pragma unroll
       for (int c = 0; c < 4; c++) kahan_add(acc[r][c], comp[r][c], part[r][c]);
   }
   const bool excl = op.a_excl[it];
   float* zg = Z + op.g_z0[g] * ldz;
+  const int col = c_base + tx * 4;
 #pragma unroll
-  for (int r = 0; r < 4; r++) {
-    int row = r_base + ty + 16 * r;
+  for (int r = 0; r < 8; r++) {
+    const int row = r_base + ty * 8 + r;
     if (row >= kz) continue;
 #pragma unroll
     for (int c = 0; c < 4; c++) {
-      int col = c_base + tx * 4 + c;
-      if (col >= K) continue;
-      if (excl) zg[(long long)row * ldz + col] = acc[r][c];
-      else atomicAdd(zg + (long long)row * ldz + col, acc[r][c]);
+      if (col + c >= K) continue;
+      float* dst = zg + (long long)row * ldz + col + c;
+      if (excl) *dst = acc[r][c];
+      else atomicAdd(dst, acc[r][c]);
     }
   }
 }
@@ -312,9 +349,6 @@ phaseA_kn_f32(PanelView op, const float* __restrict__ vpanel, const float* __res
 // broadcast 16-byte shared loads and its 4 sources as one, for 32 FMAs.
 // Chunks of 32 panel rows are double-buffered with cp.async; the chunk's
 // partial sums are added to the running sums with Kahan compensation.
-constexpr int kB32Cols = 128;
-constexpr int kB32Chunk = 32;
-
 __global__ void __launch_bounds__(256, 2)
 phaseB_kn_f32(PanelView op, const float* __restrict__ panel, const float* __restrict__ X,
               long long ldx, const float* __restrict__ Z, long long ldz, float* __restrict__ Y,
@@ -775,12 +809,11 @@ int fgb_matmat_f32(const fgb_op_desc* d, const float* panel, const float* vpanel
   if (st) return st;
   if (K < 1) { fgb::set_error("K must be >= 1"); return FGB_BAD_ARG; }
   cudaStream_t s = fgb::as_stream(stream);
-  unsigned ky = (unsigned)((K + fgb::kKT - 1) / fgb::kKT);
   if ((phases & 1) && op.num_items > 0) {
     if (zero_z && d->num_zrows > 0)
       FGB_CUDA_TRY(cudaMemsetAsync(Z, 0, sizeof(float) * d->num_zrows * (size_t)K, s));
-    const int mt = d->max_group_tiles;
-    fgb::phaseA_kn_f32<<<(unsigned)(op.num_items * mt * ky), 256, 0, s>>>(op, vpanel, X, K, Z, K, K, mt);
+    const long long kb = (K + fgb::kB32Cols - 1) / fgb::kB32Cols;
+    fgb::phaseA_kn_f32<<<(unsigned)(op.num_work * kb), 256, 0, s>>>(op, vpanel, X, K, Z, K, K);
     FGB_LAUNCH_CHECK("phaseA_kn_f32");
   }
   if ((phases & 2) && op.num_tiles > 0) {

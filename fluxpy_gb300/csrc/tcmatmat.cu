@@ -27,8 +27,7 @@
 // below 2^-16 relative and dropped).
 //
 // CTA = (tile or work slice, slice of NC = 256 right-hand-side columns), 8
-// warps.  All warps gather the next chunks' source rows with cp.async into a
-// 5-stage ring (phase B: the panel chunk comes by one tiled TMA copy)
+// warps.  All warps gather the next chunks with cp.async into a 5-stage ring
 // (40 KiB a stage: 64 rows, or 32 rows in split mode); thread 0 issues the
 // MMAs of the current chunk and commits them to the stage's mbarrier, which
 // the producers wait on before they refill that stage.  The accumulators (2
@@ -44,8 +43,6 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
-
-#include <cstring>
 
 namespace fgb {
 namespace {
@@ -145,29 +142,6 @@ __device__ __forceinline__ void fence_proxy_async() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y,
-                                            uint32_t bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%2, %3}], [%4];"
-      ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar) : "memory");
-}
-__device__ __forceinline__ void tma_gather4(uint32_t dst, const CUtensorMap* map, int x, int r0,
-                                            int r1, int r2, int r3, uint32_t bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cta.global.tile::gather4.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];"
-      ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(r0), "r"(r1), "r"(r2),
-        "r"(r3), "r"(bar) : "memory");
-}
-
 // 32 consecutive TMEM columns of this warp's 32 lanes -> 32 registers.
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
   uint32_t r[32];
@@ -229,13 +203,8 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
   s = t;
 }
 
-// Phase B loads each panel chunk with one tiled TMA copy (maps tm_w_hi /
-// tm_w_lo: 64 x CH boxes, 128-byte swizzle, completion on wbar[stage]);
-// phase A (strided transposed panel) gathers it with cp.async.
 template <int MODE, bool SPLIT>
-__global__ void __launch_bounds__(kTcThreads, 1)
-tc_gather_gemm(TcArgs a, const __grid_constant__ CUtensorMap tm_w_hi,
-               const __grid_constant__ CUtensorMap tm_w_lo) {
+__global__ void __launch_bounds__(kTcThreads, 1) tc_gather_gemm(TcArgs a) {
   constexpr int TMEM_COLS = SPLIT ? kTcTmemColsSplit : kTcTmemCols;
   constexpr int CH = SPLIT ? 32 : 64;                 // reduction rows per stage
   constexpr int WB = CH * kTcRows * 2;                 // W bytes per stage (per part)
@@ -244,10 +213,8 @@ tc_gather_gemm(TcArgs a, const __grid_constant__ CUtensorMap tm_w_hi,
   static_assert((SPLIT ? 2 : 1) * (WB + SB) == kTcStageBytes, "stage size");
   extern __shared__ uint8_t smem_raw[];
   __shared__ __align__(8) unsigned long long bars[kTcStages];
-  __shared__ __align__(8) unsigned long long wbar[kTcStages];
   __shared__ uint32_t tmem_slot;
   __shared__ int abort_flag;
-  constexpr bool kTmaW = MODE == kModeB;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nks = (a.K + kTcNC - 1) / kTcNC;
   const long long unit = blockIdx.x / nks;
@@ -294,10 +261,7 @@ tc_gather_gemm(TcArgs a, const __grid_constant__ CUtensorMap tm_w_hi,
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   const uint32_t sbase = smem_addr(smem);
   if (tid == 0) {
-    for (int s = 0; s < kTcStages; s++) {
-      mbar_init(smem_addr(&bars[s]), 1);
-      mbar_init(smem_addr(&wbar[s]), 1);
-    }
+    for (int s = 0; s < kTcStages; s++) mbar_init(smem_addr(&bars[s]), 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     abort_flag = 0;
   }
@@ -331,28 +295,17 @@ tc_gather_gemm(TcArgs a, const __grid_constant__ CUtensorMap tm_w_hi,
   // producer: chunk c -> stage s.  W: 16-byte piece q of row k; S: rows
   // k = warp + 8 j, lane = 16-byte piece (8 columns) of the 256-column slice;
   // srcs: the chunk's source indices (phase B)
-  int w_issued = 0;   // thread 0: panel chunks requested by TMA
   auto load = [&](int c, int s, const int (&srcs)[RPW]) {
     const long long l0 = r_first + (long long)c * CH;
-    if (kTmaW) {
-      if (tid == 0) {
-        w_issued = c + 1;
-        const uint32_t wb = smem_addr(&wbar[s]);
-        mbar_expect_tx(wb, (SPLIT ? 2 : 1) * WB);
-        tma_load_2d(w_at(s, 0), &tm_w_hi, 0, (int)l0, wb);
-        if (SPLIT) tma_load_2d(w_at(s, 1), &tm_w_lo, 0, (int)l0, wb);
-      }
-    } else {
 #pragma unroll
-      for (int j = 0; j < (CH * 8) / kTcThreads; j++) {
-        const int p = tid + j * kTcThreads;
-        const int k = p >> 3, q = p & 7;
-        const bool ok = l0 + k < r_end;
-        const long long off = ok ? (l0 + k) * wstride + q * 8 : 0;
-        const uint32_t so = k * 128 + ((q ^ (k & 7)) << 4);
-        cp_async16_zfill(w_at(s, 0) + so, wbase_hi + off, ok);
-        if (SPLIT) cp_async16_zfill(w_at(s, 1) + so, wbase_lo + off, ok);
-      }
+    for (int j = 0; j < (CH * 8) / kTcThreads; j++) {
+      const int p = tid + j * kTcThreads;
+      const int k = p >> 3, q = p & 7;
+      const bool ok = l0 + k < r_end;
+      const long long off = ok ? (l0 + k) * wstride + q * 8 : 0;
+      const uint32_t so = k * 128 + ((q ^ (k & 7)) << 4);
+      cp_async16_zfill(w_at(s, 0) + so, wbase_hi + off, ok);
+      if (SPLIT) cp_async16_zfill(w_at(s, 1) + so, wbase_lo + off, ok);
     }
     const int col = c_base + lane * 8;
     const int b = lane >> 3, q = lane & 7;
@@ -416,11 +369,7 @@ tc_gather_gemm(TcArgs a, const __grid_constant__ CUtensorMap tm_w_hi,
     fence_proxy_async();
     __syncthreads();
     if (abort_flag) { ok = false; break; }
-    if (tid == 0 && kTmaW && !mbar_wait(smem_addr(&wbar[s]), (c / kTcStages) & 1)) {
-      atomicOr(a.flags, FGB_FLAG_DEVICE_TIMEOUT);
-      abort_flag = 1;
-    }
-    if (tid == 0 && !abort_flag) {
+    if (tid == 0) {
       tc_fence_after();
       // split mode: window c / kTcWin accumulates into set (c / kTcWin) & 1
       const uint32_t dset = SPLIT ? (uint32_t)(((c / kTcWin) & 1) * 128) : 0u;
@@ -467,11 +416,6 @@ tc_gather_gemm(TcArgs a, const __grid_constant__ CUtensorMap tm_w_hi,
     for (int j = 0; j < RPW; j++) src_cur[j] = src_nxt[j];
   }
   cp_wait_all();
-  // an aborted CTA may still have panel copies in flight: let them land
-  if (kTmaW && tid == 0 && abort_flag) {
-    for (int c = max(0, w_issued - kTcStages); c < w_issued; c++)
-      mbar_wait(smem_addr(&wbar[c % kTcStages]), (c / kTcStages) & 1);
-  }
   // all MMAs of this CTA complete (they finish in order): last chunk's barrier
   if (nch > 0 && ok) {
     const int cl = nch - 1;
@@ -587,11 +531,8 @@ __global__ void vpanel_transpose_kernel(const int* __restrict__ g_n, const int* 
   }
 }
 
-int encode_map(CUtensorMap* m, const void* base, unsigned long long inner, unsigned long long rows,
-               unsigned box_inner, unsigned box_rows);
-
 template <int MODE, bool SPLIT>
-int launch_tc(const TcArgs& a, long long units, cudaStream_t st, long long panel_rows = 0) {
+int launch_tc(const TcArgs& a, long long units, cudaStream_t st) {
   static bool attr_set = false;
   if (!attr_set) {
     FGB_CUDA_TRY(cudaFuncSetAttribute(tc_gather_gemm<MODE, SPLIT>,
@@ -602,18 +543,7 @@ int launch_tc(const TcArgs& a, long long units, cudaStream_t st, long long panel
   const long long grid = units * nks;
   if (grid <= 0) return FGB_OK;
   if (grid > 0x7fffffffLL) { set_error("grid too large"); return FGB_BAD_ARG; }
-  alignas(64) CUtensorMap mhi, mlo;
-  memset(&mhi, 0, sizeof(mhi));
-  memset(&mlo, 0, sizeof(mlo));
-  if (MODE == kModeB) {
-    // panel chunks: 64 weights x CH rows per copy
-    const unsigned ch = SPLIT ? 32 : 64;
-    if (panel_rows <= 0) { set_error("panel_rows not set"); return FGB_BAD_ARG; }
-    int rc = encode_map(&mhi, a.w_hi, kTcRows, panel_rows, kTcRows, ch);
-    if (rc) return rc;
-    if (SPLIT && (rc = encode_map(&mlo, a.w_lo, kTcRows, panel_rows, kTcRows, ch))) return rc;
-  }
-  tc_gather_gemm<MODE, SPLIT><<<(unsigned)grid, kTcThreads, kTcSmemBytes, st>>>(a, mhi, mlo);
+  tc_gather_gemm<MODE, SPLIT><<<(unsigned)grid, kTcThreads, kTcSmemBytes, st>>>(a);
   FGB_LAUNCH_CHECK("tc_gather_gemm");
   return FGB_OK;
 }
@@ -648,6 +578,29 @@ struct TmaCfg {
   static constexpr int HALVES = NC / 128;
   static constexpr int TMEM_COLS = 128;
 };
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y,
+                                            uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];"
+      ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar) : "memory");
+}
+__device__ __forceinline__ void tma_gather4(uint32_t dst, const CUtensorMap* map, int x, int r0,
+                                            int r1, int r2, int r3, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cta.global.tile::gather4.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];"
+      ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(r0), "r"(r1), "r"(r2),
+        "r"(r3), "r"(bar) : "memory");
+}
 
 template <bool SPLIT>
 __global__ void __launch_bounds__(kTcThreads, 1)
@@ -1028,8 +981,8 @@ int fgb_tc_phase_b(const struct fgb_op_desc* d, const void* w_hi, const void* w_
   a.z_lo = static_cast<const __nv_bfloat16*>(Z_lo);
   a.lds = K; a.K = K; a.out = Y; a.add = add; a.alpha = alpha; a.flags = flags;
   cudaStream_t st = fgb::as_stream(stream);
-  return split ? fgb::launch_tc<fgb::kModeB, true>(a, d->num_tiles, st, d->panel_rows)
-               : fgb::launch_tc<fgb::kModeB, false>(a, d->num_tiles, st, d->panel_rows);
+  return split ? fgb::launch_tc<fgb::kModeB, true>(a, d->num_tiles, st)
+               : fgb::launch_tc<fgb::kModeB, false>(a, d->num_tiles, st);
 }
 
 int fgb_tc_phase_b_tma(const struct fgb_op_desc* d, const void* w_hi, const void* w_lo,

@@ -242,7 +242,8 @@ def _auto_chunk(FF, N, K, fp32_z=True):
 
 def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_iter=200,
                             inner=2, E_is_permuted=False, return_permuted=False, stats=None,
-                            chunk=None, inner0=3, engine="tc", residual="split-bf16"):
+                            chunk=None, inner0=3, engine="tc", residual="split-bf16",
+                            incremental=True):
     """Right-placement radiosity solve for K sun directions at once.
 
     FF: CompressedFormFactorMatrix; E: (N, K) device tensor (facet order, or
@@ -263,6 +264,9 @@ def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_
     cores, split-BF16 operands hi.hi + lo.hi + hi.lo, FP32 accumulation
     drained into compensated sums; ~17-bit arithmetic, the convergence test
     keeps a margin for it, _SPLIT_MARGIN) or 'fp32' (FP32 CUDA-core kernels).
+    incremental: with 'split-bf16', only the first residual is evaluated in
+    full; later ones are updated as R <- R - D + F_bf16 (rho D) with the last
+    (small) correction D, one BF16 product instead of a split one.
     Returns B (N, K) fp32; fills `stats` (iterations, matmats, residuals).
     """
     dev = E.device
@@ -283,7 +287,7 @@ def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_
                                                  precision, max_iter, inner, E_is_permuted,
                                                  return_permuted, st, chunk=chunk,
                                                  inner0=inner0, engine=engine,
-                                                 residual=residual))
+                                                 residual=residual, incremental=incremental))
             for k_, v_ in st.items():
                 if isinstance(v_, (int, float)) and k_ != "residual":
                     agg[k_] = agg.get(k_, 0) + v_
@@ -296,7 +300,7 @@ def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_
         E = torch.cat([E, torch.zeros((N, pad), dtype=E.dtype, device=dev)], 1)
         B = solve_radiosity_batched(FF, E, rho, rtol, precision, max_iter, inner, E_is_permuted,
                                     return_permuted, stats, chunk=chunk, inner0=inner0,
-                                    engine=engine, residual=residual)
+                                    engine=engine, residual=residual, incremental=incremental)
         return B[:, :K0].contiguous()
     K = K0
     stream = _lib.stream_handle()
@@ -350,6 +354,19 @@ def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_
             if it == 1:
                 # B = 0: the residual is E itself
                 rhs, sweeps = Ep, inner0
+            elif it >= 3 and incremental and residual == "split-bf16":
+                # R <- R - D + F_bf16 (rho D) for the last correction D: the
+                # correction is ~1e-4 of B, so the BF16 product's 2^-9
+                # relative error stays ~1e-7 of max|E| (the accurate residual
+                # of the previous step carries over)
+                _lib.call("fgb_scale_rows_bf16", _lib.ptr(D), _lib.ptr(rho_d), rho_s, _lib.ptr(Xb),
+                          N, K, stream)
+                R.sub_(D)
+                FF.bf16_product(Xb, Z32, Zb, Y, add=R, alpha=1.0, engine=engine)
+                st["bf16_matmats"] += 1
+                R, Y = Y, R
+                res = R.abs().amax(0).cpu().numpy()
+                FF.check_device_flags()
             else:
                 # residual with the FP32 operator
                 _lib.call("fgb_scale_rows_f32", _lib.ptr(B), _lib.ptr(rho_d), rho_s,
@@ -365,6 +382,7 @@ def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_
                           K, _lib.ptr(colmax), stream)
                 res = _colmax(colmax)
                 FF.check_device_flags()
+            if it >= 2:
                 st["outer"] = it - 1
                 st["residual"] = float(np.max(res / emax_h))
                 st.setdefault("history", []).append(st["residual"])

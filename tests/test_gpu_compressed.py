@@ -160,12 +160,13 @@ def test_batched_solvers_reach_rtol():
     dirs = terrain.random_sun_directions(64, seed=2)
     E = sm.get_direct_irradiance_batch(1365.0, dirs, out_dtype=torch.float32)
     assert E.shape == (sm.num_faces, 64)
-    cases = [("fp32", "tc", "fp32", 2e-5), ("bf16-refine", "tc", "split-bf16", 1e-5),
-             ("bf16-refine", "tc", "fp32", 1e-5), ("bf16-refine", "mma", "fp32", 1e-5)]
-    for prec, eng, res, bound in cases:
+    cases = [("fp32", "tc", "fp32", True, 2e-5), ("bf16-refine", "tc", "split-bf16", True, 1e-5),
+             ("bf16-refine", "tc", "split-bf16", False, 1e-5),
+             ("bf16-refine", "tc", "fp32", True, 1e-5), ("bf16-refine", "mma", "fp32", True, 1e-5)]
+    for prec, eng, res, incr, bound in cases:
         st = {}
         B = solve_radiosity_batched(FF, E, 0.12, rtol=1e-5, precision=prec, stats=st,
-                                    engine=eng, residual=res)
+                                    engine=eng, residual=res, incremental=incr)
         # residual with the operator in FP64 arithmetic; the plain Jacobi
         # path stops on its update size (as the reference does), the
         # refinement on the residual itself
@@ -174,7 +175,7 @@ def test_batched_solvers_reach_rtol():
         Ep = FF.permute(E.double())[:, :8]
         R = Ep - (Bp[:, :8] - FBp)
         rel = (R.abs().amax(0) / Ep.abs().amax(0).clamp_min(1e-30)).max().item()
-        assert rel <= bound, (prec, eng, res, rel, st)
+        assert rel <= bound, (prec, eng, res, incr, rel, st)
 
 
 @pytest.fixture(scope="module")

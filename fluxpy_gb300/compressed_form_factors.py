@@ -604,11 +604,51 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
                       _lib.ptr(nf["leaf_word_off"]), _lib.ptr(nf["leaf_row_off"]),
                       _lib.ptr(tcsr.bits), _lib.ptr(mask), _lib.ptr(cnt), stream)
             npk = cnt[:npc.size].cpu().numpy().astype(np.int64)
-            L_nf = np.bincount(npt, weights=npk, minlength=ntiles).astype(np.int64)
+            ndesc = int(npk.sum())
         else:
             npc = npt = npk = np.zeros(0, np.int64)
-            L_nf = np.zeros(ntiles, np.int64)
+            ndesc = 0
             mask = None
+        if ndesc:
+            # one descriptor (pair, column) per set bit of the pair masks
+            desc_off = np.zeros(npk.size + 1, np.int64)
+            np.cumsum(npk, out=desc_off[1:])
+            desc_pair = torch.empty(ndesc, dtype=torch.int32, device=dev)
+            desc_col = torch.empty(ndesc, dtype=torch.int32, device=dev)
+            nf = self._nf
+            _lib.call("fgb_nf_enumerate", _lib.ptr(nf["pair_q"]), _lib.ptr(nf["pair_t0"]),
+                      _lib.ptr(nf["pair_moff"]), npk.size, _lib.ptr(nf["leaf_wpr"]),
+                      _lib.ptr(mask), _lib.ptr(d(desc_off[:-1], np.int64)), _lib.ptr(desc_pair),
+                      _lib.ptr(desc_col), stream)
+            # Exact leaves partition the matrix, so leaves that share a column
+            # cluster cover disjoint rows: descriptors of one tile that gather
+            # the same source column are merged into one panel row (each
+            # fills only its own rows of it)
+            dp = desc_pair.to(torch.int64)
+            q_of = nf["pair_q"].to(torch.int64)[dp]
+            tile_of = torch.as_tensor(npt, device=dev)[dp]
+            c0_d = torch.as_tensor(ex_c0, device=dev)
+            srcv = self._num_zrows + c0_d[q_of] + desc_col.to(torch.int64)
+            del dp, q_of
+            key = tile_of * (1 << 31) + srcv
+            del tile_of, srcv
+            skey, order = torch.sort(key)
+            del key
+            newrow = torch.ones(ndesc, dtype=torch.bool, device=dev)
+            newrow[1:] = skey[1:] != skey[:-1]
+            uid_sorted = torch.cumsum(newrow.to(torch.int64), 0) - 1
+            ukeys = skey[newrow]
+            del skey, newrow
+            desc_uid = torch.empty(ndesc, dtype=torch.int64, device=dev)
+            desc_uid[order] = uid_sorted
+            del order, uid_sorted
+            u_tile = ukeys >> 31
+            u_src = ukeys & ((1 << 31) - 1)
+            del ukeys
+            L_nf = torch.bincount(u_tile, minlength=ntiles).cpu().numpy().astype(np.int64)
+            self.stats["nearfield_descriptors"] = ndesc
+        else:
+            L_nf = np.zeros(ntiles, np.int64)
         L = L_lr + L_nf
         Lpad = (L + PANEL_ALIGN - 1) // PANEL_ALIGN * PANEL_ALIGN
         t_p0 = np.zeros(ntiles + 1, np.int64)
@@ -624,7 +664,6 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
             return run - start[pt]
 
         lp0 = t_p0[lpt] + offsets_within_tile(lpt, lpk) if lpt.size else np.zeros(0, np.int64)
-        np0 = (t_p0[npt] + L_lr[npt] + offsets_within_tile(npt, npk)) if npt.size else np.zeros(0, np.int64)
         # build-kernel pairs: LR pairs, plus one zero pair at every tile's
         # first near-field / padding row (rows past a pair's k are zeroed)
         tail_t = np.flatnonzero(Lpad > L_lr)
@@ -643,26 +682,17 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         rows_l = np.arange(lpk.sum()) - np.repeat(np.cumsum(lpk) - lpk, lpk)
         src[lp0[rows_pair] + rows_l] = lr_z[lpc[rows_pair]] + rows_l
         src_d = d(src, np.int32)
-        if npk.size and npk.sum() > 0:
-            ndesc = int(npk.sum())
-            desc_off = np.zeros(npk.size + 1, np.int64)
-            np.cumsum(npk, out=desc_off[1:])
-            desc_pair = torch.empty(ndesc, dtype=torch.int32, device=dev)
-            desc_col = torch.empty(ndesc, dtype=torch.int32, device=dev)
-            desc_off_d = d(desc_off[:-1], np.int64)
-            nf = self._nf
-            _lib.call("fgb_nf_enumerate", _lib.ptr(nf["pair_q"]), _lib.ptr(nf["pair_t0"]),
-                      _lib.ptr(nf["pair_moff"]), npk.size, _lib.ptr(nf["leaf_wpr"]),
-                      _lib.ptr(mask), _lib.ptr(desc_off_d), _lib.ptr(desc_pair),
-                      _lib.ptr(desc_col), stream)
-            # panel row of each descriptor: pair start row + rank within the pair
-            dp = desc_pair.to(torch.int64)
-            np0_d = torch.as_tensor(np0, device=dev)
-            rank = torch.arange(ndesc, device=dev) - desc_off_d[dp]
-            desc_row = np0_d[dp] + rank
-            q_of = nf["pair_q"].to(torch.int64)[dp]
-            c0_d = torch.as_tensor(ex_c0, device=dev)
-            src_d[desc_row] = (self._num_zrows + c0_d[q_of] + desc_col.to(torch.int64)).to(torch.int32)
+        if ndesc:
+            # merged rows: tile t's near-field rows start after its LR rows
+            nf_start = torch.as_tensor(t_p0[:-1] + L_lr, device=dev)
+            ufirst = torch.zeros(ntiles + 1, dtype=torch.int64, device=dev)
+            ufirst[1:] = torch.cumsum(torch.as_tensor(L_nf, device=dev), 0)
+            uidx = torch.arange(u_tile.numel(), device=dev)
+            u_row = nf_start[u_tile] + (uidx - ufirst[u_tile])
+            del uidx, ufirst, nf_start
+            src_d[u_row] = u_src.to(torch.int32)
+            desc_row = u_row[desc_uid]
+            del u_row, u_src, u_tile, desc_uid
             self._nf.update(desc_pair=desc_pair, desc_col=desc_col, desc_row=desc_row)
             self._num_desc = ndesc
         else:

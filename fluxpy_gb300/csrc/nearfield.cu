@@ -10,8 +10,11 @@
 //   1. fgb_nf_pair_masks: OR of the tile's row masks -> pair mask + count;
 //   2. fgb_nf_enumerate:  one row descriptor (pair, column) per set bit, in
 //                         column order, at the pair's first descriptor slot;
-//   3. fgb_nf_fill_*:     64 weights per descriptor: value (i, j) looked up
-//                         in the CSR by the rank of bit j in row i's mask.
+//                         the host then merges the descriptors of a tile that
+//                         gather the same source column into one panel row;
+//   3. fgb_nf_fill_*:     each descriptor writes its leaf's rows of its panel
+//                         row: value (i, j) looked up in the CSR by the rank of
+//                         bit j in row i's mask.
 #include "common.cuh"
 
 #include <cuda_bf16.h>
@@ -124,17 +127,19 @@ __global__ void nf_fill_kernel(NfPairs P, NfLeaves L, const unsigned* __restrict
     TO* out = panel + desc_row[d] * kTile;
     const int cw = col >> 5;
     const unsigned below = (1u << (col & 31)) - 1u;
+    // only the leaf's own rows are written: descriptors of other leaves may
+    // share this panel row (the same column, disjoint rows); the rest of
+    // the row was zeroed when the panel was built
     for (int i = lane; i < kTile; i += 32) {
       const long long r = t0 + i;
+      if (r < r0 || r >= r0 + m) continue;
       TI v = TI(0);
-      if (r >= r0 && r < r0 + m) {
-        const unsigned* rb = bits + L.word_off[q] + (r - r0) * wpr;
-        const unsigned word = rb[cw];
-        if ((word >> (col & 31)) & 1u) {
-          int rank = __popc(word & below);
-          for (int w = 0; w < cw; w++) rank += __popc(rb[w]);
-          v = data[indptr[L.row_off[q] + (r - r0)] + rank];
-        }
+      const unsigned* rb = bits + L.word_off[q] + (r - r0) * wpr;
+      const unsigned word = rb[cw];
+      if ((word >> (col & 31)) & 1u) {
+        int rank = __popc(word & below);
+        for (int w = 0; w < cw; w++) rank += __popc(rb[w]);
+        v = data[indptr[L.row_off[q] + (r - r0)] + rank];
       }
       out[i] = to_out<TO>((double)v);
     }

@@ -496,11 +496,97 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
     t_e2e = (time.perf_counter() - t0) / reps
     out["e2e"] = {"value": K / t_e2e, "unit": "solves/s", "h2d_bytes_per_step": N * K * 4,
                   "d2h_bytes_per_step": N * K * 4, "ms_per_step": t_e2e * 1e3}
+    # ---- the other hot-path kernels on the same terrain
+    try:
+        out["other_paths"] = measure_other_paths(FF, sm, dev, hbm)
+    except Exception as e:  # secondary measurements must not break the line
+        out["other_paths"] = {"error": str(e)}
     # ---- CPU baseline (oracle port, bounded sample)
     try:
         out["cpu_baseline"] = cpu_baseline(int(FF.stats["operator_entries"]))
     except Exception as e:  # the checker must not break the GPU measurement
         out["cpu_baseline"] = {"value": None, "error": str(e)}
+    return out
+
+
+def measure_other_paths(FF, sm, dev, hbm):
+    """Insolation rays/s, pair-kernel pairs/s (from the operator build) and
+    the 1-D conduction step (facet-steps/s, against HBM bandwidth) on the
+    bench terrain; the conduction CPU rate is the oracle's restatement of
+    the reference's serial conductionQ loop on a sample of facets."""
+    import torch
+    from fluxpy_gb300 import terrain
+    from fluxpy_gb300.thermal import PccThermalModel1D, setgrid
+    stream = torch.cuda.current_stream()
+    out = {}
+    nf = sm.num_faces
+    # insolation: one ray per facet and direction
+    dirs = terrain.random_sun_directions(256, seed=5)
+    sm.get_direct_irradiance_batch(1365.0, dirs, out_dtype=torch.float32)
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    sm.get_direct_irradiance_batch(1365.0, dirs, out_dtype=torch.float32)
+    b.record(stream)
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b)
+    out["insolation"] = {"rays_per_s": nf * 256 / (ms * 1e-3), "directions": 256, "ms": ms}
+    st = FF.stats
+    if st.get("exact_s"):
+        out["pair_kernel"] = {"kept_pairs_per_s": st["kept_pairs"] / st["exact_s"],
+                              "kept_pairs": st["kept_pairs"], "s": st["exact_s"],
+                              "note": "visibility ray + form factor per kept pair (count and "
+                                      "fill passes), from the operator build"}
+    # conduction: 41-node grid (setgrid(40, 1.0817, 1.0) as in the thermal
+    # configuration), every facet of the terrain
+    z = np.concatenate([[0.0], setgrid(40, 1.0817, 1.0)])
+    rng = np.random.default_rng(3)
+    ti = np.linspace(55.0, 400.0, z.size)
+    rhoc = np.full(z.size, 1.2e6)
+    emiss = np.full(nf, 0.95)
+    Fg = np.full(nf, 0.005)
+    Q0 = rng.uniform(0, 400, nf)
+    Ts = np.full(nf, 250.0)
+    cond = {}
+    for dt_name, dt in (("fp64", np.float64), ("fp32", np.float32)):
+        m = PccThermalModel1D(z, np.full((nf, z.size), 250.0), ti, rhoc, emiss, Fg, Q0, Ts,
+                              dtype=dt)
+        X = torch.as_tensor(rng.uniform(0, 400, nf), device=dev,
+                            dtype=torch.float64 if dt == np.float64 else torch.float32)
+        for _ in range(3):
+            m.step(3600.0, X, check=False)
+        torch.cuda.synchronize()
+        a.record(stream)
+        nsteps = 20
+        for _ in range(nsteps):
+            m.step(3600.0, X, check=False)
+        b.record(stream)
+        torch.cuda.synchronize()
+        m.check_errors()
+        ms = a.elapsed_time(b) / nsteps
+        isz = 8 if dt == np.float64 else 4
+        per = 2 * z.size * isz + 5 * isz      # T read + write, Qprev, X, emiss, Fgeotherm, Fsurf
+        gbs = nf * per / (ms * 1e-3) / 1e9
+        cond[dt_name] = {"facet_steps_per_s": nf / (ms * 1e-3), "ms_per_step": ms,
+                         "bytes_per_facet_step": per, "achieved_gbs": gbs, "hbm_peak": hbm,
+                         "frac": gbs / hbm}
+        del m
+    try:
+        from oracle import pcc as opcc
+        ns = 4096
+        T = np.full((ns, z.size), 250.0)
+        t0 = time.perf_counter()
+        reps = 0
+        while time.perf_counter() - t0 < 2.0:
+            opcc.step_q(z, 3600.0, Q0[:ns], Q0[:ns], T, ti, rhoc, emiss[:ns], Fg[:ns])
+            reps += 1
+        rate = ns * reps / (time.perf_counter() - t0)
+        cond["cpu_oracle"] = {"facet_steps_per_s": rate, "cores": 1,
+                              "sample": f"{ns} facets x {reps} steps, serial C loop"}
+    except Exception as e:
+        cond["cpu_oracle"] = {"error": str(e)}
+    out["conduction"] = cond
     return out
 
 

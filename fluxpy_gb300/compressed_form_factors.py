@@ -170,6 +170,8 @@ ITEM_COLS = 2048
 # panel rows per tile are padded to this multiple (the tensor-core phase-B
 # kernel consumes 64 panel rows per pipeline stage)
 PANEL_ALIGN = 64
+# Z rows computed per CTA by the tensor-core phase A
+TC_A_ROWS = 128
 
 
 def _nbytes_csr(nnz, m, itemsize):
@@ -546,16 +548,22 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         max_gt = int(((g_kz + 63) // 64).max()) if ng else 1
         # tensor-core phase A: groups stored transposed (n x kz rounded up to
         # 64) and one work slice per (item, 64 rows of the group)
-        g_kzp = (g_kz + 63) // 64 * 64
+        # (kz rounded up to TC_A_ROWS: the tensor-core phase A computes
+        # TC_A_ROWS rows of Z per CTA)
+        g_kzp = (g_kz + TC_A_ROWS - 1) // TC_A_ROWS * TC_A_ROWS
         g_vtoff = np.zeros(ng + 1, np.int64)
         np.cumsum(g_n * g_kzp, out=g_vtoff[1:])
+        # work slices of 64 rows (CUDA-core kernels) and of TC_A_ROWS rows
+        # (tensor cores) per item
         a_wn = (g_kz[a_grp] + 63) // 64
         a_woff = np.zeros(a_grp.size + 1, np.int64)
         np.cumsum(a_wn, out=a_woff[1:])
+        a_woff_tc = np.zeros(a_grp.size + 1, np.int64)
+        np.cumsum(g_kzp[a_grp] // TC_A_ROWS, out=a_woff_tc[1:])
         # the tensor-core phase A with BF16 output takes one work item per
         # whole group (every CTA owns its output rows: no atomics, no FP32 Z)
         tg_woff = np.zeros(ng + 1, np.int64)
-        np.cumsum((g_kz + 63) // 64, out=tg_woff[1:])
+        np.cumsum(g_kzp // TC_A_ROWS, out=tg_woff[1:])
         tsl = g_kzp // 64
         tjb = (g_n + 63) // 64
         tcnt = tsl * tjb
@@ -706,7 +714,7 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
             a_grp=d(a_grp, np.int32), a_j0=d(a_j0, np.int32), a_j1=d(a_j1, np.int32),
             a_excl=d(a_ex, np.uint8), t_p0=d(t_p0, np.int64), src=src_d,
             g_kzp=d(g_kzp, np.int32), g_vtoff=d(g_vtoff[:-1], np.int64),
-            a_woff=d(a_woff, np.int64))
+            a_woff=d(a_woff, np.int64), a_woff_tc=d(a_woff_tc, np.int64))
         self._dev_tc = dict(
             a_grp=d(np.arange(ng), np.int32), a_j0=d(np.zeros(ng), np.int32),
             a_j1=d(g_n, np.int32), a_excl=d(np.ones(ng), np.uint8), a_woff=d(tg_woff, np.int64))
@@ -723,6 +731,7 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         self._num_pairs = int(all_p0.size)
         self._desc = self._make_desc(int(a_grp.size), ntiles, max_gt, int(a_woff[-1]))
         self._desc_tc = self._make_desc_tc()
+        self._desc_tc_items = self._make_desc_tc_items()
         self._lr_blocks = lr
         self._lr_u, self._lr_v = lr_u, lr_v
         self._panels = {}
@@ -745,6 +754,14 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         desc.max_group_tiles = max_gt
         desc.num_work = num_work
         desc.panel_rows = int(self._panel_rows)
+        return desc
+
+    def _make_desc_tc_items(self):
+        """The descriptor with the column-split work items, in work slices of
+        TC_A_ROWS rows (tensor-core phase A with FP32 output)."""
+        desc = fgb_op_desc.from_buffer_copy(self._desc)
+        desc.a_woff = self._dev["a_woff_tc"].data_ptr()
+        desc.num_work = int(self._dev["a_woff_tc"][-1].item())
         return desc
 
     def _make_desc_tc(self):
@@ -1152,6 +1169,7 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         st["_root_cache"] = None
         st["_desc"] = None
         st["_desc_tc"] = None
+        st["_desc_tc_items"] = None
         st["_panels"] = {}
         st["_tc"] = {}
         st["_flags_d"] = None
@@ -1185,6 +1203,7 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
                                      int(self.stats["max_group_tiles"]),
                                      int(self._dev["a_woff"][-1].item()))
         self._desc_tc = self._make_desc_tc()
+        self._desc_tc_items = self._make_desc_tc_items()
 
     # -- leaf data for the Python block objects --------------------------
     def _leaf_dense(self, b):

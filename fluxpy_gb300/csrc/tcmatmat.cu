@@ -203,37 +203,76 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
   s = t;
 }
 
+// Per-mode shapes.  NR = output rows per CTA (MMA N), NC = right-hand-side
+// columns per CTA (a multiple of the MMA M = 128), CH = reduction rows per
+// stage.  Phase A computes 128 rows of Z per CTA, so that each gathered X
+// row feeds twice the flops; phase B keeps the 64-row tiles of the panel.
+// Split mode keeps 64 accumulator values per thread for the compensated
+// drains (phase A: NC = 128).
+template <int MODE, bool SPLIT>
+struct TcCfg {
+  static constexpr int NR = MODE == kModeA ? 128 : 64;
+  static constexpr int NC = (MODE == kModeA && SPLIT) ? 128 : 256;
+  static constexpr int CH = SPLIT ? 32 : 64;
+  static constexpr int PARTS = SPLIT ? 2 : 1;
+  static constexpr int WB = CH * NR * 2;             // W bytes per stage and part
+  static constexpr int SB = CH * NC * 2;             // S bytes per stage and part
+  static constexpr int BLK = CH * 128;               // one 64-element block (W or S)
+  static constexpr int STAGE = PARTS * (WB + SB);
+  static constexpr int STAGES = (200 * 1024) / STAGE < 6 ? (200 * 1024) / STAGE : 6;
+  static constexpr int SMEM = STAGES * STAGE + 1024;
+  static constexpr int HALVES = NC / 128;            // accumulators per set
+  static constexpr int SETS = SPLIT ? 2 : 1;
+  static constexpr int TMEM_COLS = SETS * HALVES * NR;
+  static constexpr int SEGS = HALVES * NR / 64;      // 64-column TMEM segments per set
+  static constexpr int PPR = NC / 8;                 // 16-byte pieces per S row
+  static constexpr int RPI = 32 / PPR;               // S rows per warp instruction
+  static constexpr int SROWS = CH / (8 * RPI);       // S rows per thread and chunk
+  // instruction descriptor, kind::f16: D FP32, A and B BF16, both MN-major,
+  // N = NR, M = 128
+  static constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | (1u << 15) |
+                                    (1u << 16) | ((uint32_t)(NR >> 3) << 17) |
+                                    ((uint32_t)(128 >> 4) << 24);
+  static_assert(TMEM_COLS == 128 || TMEM_COLS == 256, "TMEM allocation");
+  static_assert(SPLIT ? SEGS == 2 : true, "split drains: one 64-row segment per warp");
+};
+
+__device__ __forceinline__ void mma_bf16_tc_n(uint32_t dtmem, uint64_t adesc, uint64_t bdesc,
+                                              uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+      ::"r"(dtmem), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate) : "memory");
+}
+
 template <int MODE, bool SPLIT>
 __global__ void __launch_bounds__(kTcThreads, 1) tc_gather_gemm(TcArgs a) {
-  constexpr int TMEM_COLS = SPLIT ? kTcTmemColsSplit : kTcTmemCols;
-  constexpr int CH = SPLIT ? 32 : 64;                 // reduction rows per stage
-  constexpr int WB = CH * kTcRows * 2;                 // W bytes per stage (per part)
-  constexpr int SB = CH * kTcNC * 2;                   // S bytes per stage (per part)
-  constexpr int BLK = CH * 128;                        // 64-column block of S
-  static_assert((SPLIT ? 2 : 1) * (WB + SB) == kTcStageBytes, "stage size");
+  using Cfg = TcCfg<MODE, SPLIT>;
+  constexpr int NR = Cfg::NR, NC = Cfg::NC, CH = Cfg::CH, WB = Cfg::WB, SB = Cfg::SB;
+  constexpr int BLK = Cfg::BLK, S = Cfg::STAGES, STAGE = Cfg::STAGE;
   extern __shared__ uint8_t smem_raw[];
-  __shared__ __align__(8) unsigned long long bars[kTcStages];
+  __shared__ __align__(8) unsigned long long bars[S];
   __shared__ uint32_t tmem_slot;
   __shared__ int abort_flag;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int nks = (a.K + kTcNC - 1) / kTcNC;
+  const int nks = (a.K + NC - 1) / NC;
   const long long unit = blockIdx.x / nks;
-  const int c_base = (int)(blockIdx.x % nks) * kTcNC;
+  const int c_base = (int)(blockIdx.x % nks) * NC;
 
   // ---- the CTA's reduction range and output rows
   long long r_first = 0, r_end = 0;   // reduction rows (panel rows / group columns)
   long long out_row0 = 0;             // first output row
-  int out_rows = kTcRows;             // valid output rows
+  int out_rows = NR;                  // valid output rows
   const __nv_bfloat16* wbase_hi = a.w_hi;
   const __nv_bfloat16* wbase_lo = a.w_lo;
-  long long wstride = kTcRows;        // elements between consecutive W rows
+  long long wstride = NR;             // elements between consecutive W rows
   long long xrow0 = 0;                // phase A: X row of reduction row 0
   bool excl = true;
   if (MODE == kModeB) {
     r_first = a.t_p0[unit];
     r_end = a.t_p0[unit + 1];
-    out_row0 = unit * kTcRows;
-    out_rows = (int)min((long long)kTcRows, a.N - out_row0);
+    out_row0 = unit * NR;
+    out_rows = (int)min((long long)NR, a.N - out_row0);
     if (tid == 0 && ((r_end - r_first) % 64) != 0) atomicOr(a.flags, FGB_FLAG_INDEX_RANGE);
   } else {
     long long lo = 0, hi = a.num_items - 1;
@@ -242,18 +281,19 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gather_gemm(TcArgs a) {
       if (a.a_woff[mid] <= unit) lo = mid; else hi = mid - 1;
     }
     const long long it = lo;
-    const int s = (int)(unit - a.a_woff[it]);
+    const int sl = (int)(unit - a.a_woff[it]);
     const int g = a.a_grp[it];
     r_first = a.a_j0[it];
     r_end = a.a_j1[it];
-    out_row0 = a.g_z0[g] + (long long)s * kTcRows;
-    out_rows = min(kTcRows, a.g_kz[g] - s * kTcRows);
+    out_row0 = a.g_z0[g] + (long long)sl * NR;
+    out_rows = min(NR, a.g_kz[g] - sl * NR);
     wstride = a.g_kzp[g];
-    wbase_hi = a.w_hi + a.g_vtoff[g] + (long long)s * kTcRows;
-    if (SPLIT) wbase_lo = a.w_lo + a.g_vtoff[g] + (long long)s * kTcRows;
+    wbase_hi = a.w_hi + a.g_vtoff[g] + (long long)sl * NR;
+    if (SPLIT) wbase_lo = a.w_lo + a.g_vtoff[g] + (long long)sl * NR;
     xrow0 = a.g_c0[g];
     excl = a.a_excl[it] != 0;
     if (a.zout_hi && !excl && tid == 0) atomicOr(a.flags, FGB_FLAG_INDEX_RANGE);
+    if (tid == 0 && (a.g_kzp[g] % NR) != 0) atomicOr(a.flags, FGB_FLAG_INDEX_RANGE);
   }
   const int nch = (int)((r_end - r_first + CH - 1) / CH);
 
@@ -261,13 +301,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gather_gemm(TcArgs a) {
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   const uint32_t sbase = smem_addr(smem);
   if (tid == 0) {
-    for (int s = 0; s < kTcStages; s++) mbar_init(smem_addr(&bars[s]), 1);
+    for (int st = 0; st < S; st++) mbar_init(smem_addr(&bars[st]), 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     abort_flag = 0;
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
-                 ::"r"(smem_addr(&tmem_slot)), "r"(TMEM_COLS) : "memory");
+                 ::"r"(smem_addr(&tmem_slot)), "r"(Cfg::TMEM_COLS) : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   tc_fence_before();
@@ -275,43 +315,48 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gather_gemm(TcArgs a) {
   tc_fence_after();
   const uint32_t tmem = tmem_slot;
 
-  // stage layout: [W_hi | S_hi] or [W_hi | W_lo | S_hi | S_lo]
-  auto w_at = [&](int s, int part) { return sbase + s * kTcStageBytes + part * WB; };
-  auto s_at = [&](int s, int part) {
-    return sbase + s * kTcStageBytes + (SPLIT ? 2 : 1) * WB + part * SB;
+  // stage layout: [W_hi | S_hi] or [W_hi | W_lo | S_hi | S_lo]; W and S are
+  // stored as 64-element blocks of CH 128-byte lines (1 KiB swizzle atoms)
+  auto w_at = [&](int st, int part) { return sbase + st * STAGE + part * WB; };
+  auto s_at = [&](int st, int part) {
+    return sbase + st * STAGE + Cfg::PARTS * WB + part * SB;
   };
-  // source rows of the reduction rows k = warp + 8 j of chunk c (phase B
-  // gathers through src[]); fetched one chunk ahead so that the dependent
-  // index load does not stall the copies
-  constexpr int RPW = CH / 8;   // rows per warp and chunk
+  // S rows handled by this thread: k = (warp * RPI + lane / PPR) + 8 RPI j
+  const int srow0 = warp * Cfg::RPI + lane / Cfg::PPR;
+  const int spiece = lane % Cfg::PPR;
+  // phase B: source rows of this thread's S rows of chunk c (through src[]),
+  // fetched one chunk ahead so that the dependent index load does not stall
+  // the copies
+  constexpr int RPW = Cfg::SROWS;
   int src_cur[RPW], src_nxt[RPW];
   auto fetch_src = [&](int c, int (&dst)[RPW]) {
 #pragma unroll
     for (int j = 0; j < RPW; j++) {
-      const long long l = r_first + (long long)c * CH + warp + 8 * j;
+      const long long l = r_first + (long long)c * CH + srow0 + 8 * Cfg::RPI * j;
       dst[j] = (MODE == kModeB && c < nch && l < r_end) ? __ldg(a.src + l) : 0;
     }
   };
-  // producer: chunk c -> stage s.  W: 16-byte piece q of row k; S: rows
-  // k = warp + 8 j, lane = 16-byte piece (8 columns) of the 256-column slice;
-  // srcs: the chunk's source indices (phase B)
-  auto load = [&](int c, int s, const int (&srcs)[RPW]) {
+  auto load = [&](int c, int st, const int (&srcs)[RPW]) {
     const long long l0 = r_first + (long long)c * CH;
+    // W: CH rows x NR weights, 16-byte piece (b, q) of row k
+    constexpr int WP = CH * NR / 8;
 #pragma unroll
-    for (int j = 0; j < (CH * 8) / kTcThreads; j++) {
+    for (int j = 0; j < WP / kTcThreads; j++) {
       const int p = tid + j * kTcThreads;
-      const int k = p >> 3, q = p & 7;
+      const int k = p / (NR / 8), rem = p % (NR / 8);
+      const int b = rem >> 3, q = rem & 7;
       const bool ok = l0 + k < r_end;
-      const long long off = ok ? (l0 + k) * wstride + q * 8 : 0;
-      const uint32_t so = k * 128 + ((q ^ (k & 7)) << 4);
-      cp_async16_zfill(w_at(s, 0) + so, wbase_hi + off, ok);
-      if (SPLIT) cp_async16_zfill(w_at(s, 1) + so, wbase_lo + off, ok);
+      const long long off = ok ? (l0 + k) * wstride + b * 64 + q * 8 : 0;
+      const uint32_t so = b * BLK + k * 128 + ((q ^ (k & 7)) << 4);
+      cp_async16_zfill(w_at(st, 0) + so, wbase_hi + off, ok);
+      if (SPLIT) cp_async16_zfill(w_at(st, 1) + so, wbase_lo + off, ok);
     }
-    const int col = c_base + lane * 8;
-    const int b = lane >> 3, q = lane & 7;
+    // S: CH gathered rows x NC columns
+    const int col = c_base + spiece * 8;
+    const int b = spiece >> 3, q = spiece & 7;
 #pragma unroll
-    for (int j = 0; j < CH / 8; j++) {
-      const int k = warp + 8 * j;
+    for (int j = 0; j < RPW; j++) {
+      const int k = srow0 + 8 * Cfg::RPI * j;
       const long long l = l0 + k;
       const bool okr = l < r_end;
       const __nv_bfloat16* rh;
@@ -332,30 +377,35 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gather_gemm(TcArgs a) {
       }
       const bool ok = okr && col < a.K;
       const uint32_t so = b * BLK + k * 128 + ((q ^ (k & 7)) << 4);
-      cp_async16_zfill(s_at(s, 0) + so, ok ? rh + col : rh, ok);
-      if (SPLIT) cp_async16_zfill(s_at(s, 1) + so, ok ? rl + col : rl, ok);
+      cp_async16_zfill(s_at(st, 0) + so, ok ? rh + col : rh, ok);
+      if (SPLIT) cp_async16_zfill(s_at(st, 1) + so, ok ? rl + col : rl, ok);
     }
   };
 
-  for (int c = 0; c < kTcStages - 1; c++) {
+  for (int c = 0; c < S - 1; c++) {
     fetch_src(c, src_cur);
     if (c < nch) load(c, c, src_cur);
     cp_commit();
   }
-  fetch_src(kTcStages - 1, src_cur);
-  // epilogue / drain mapping: warp w reads TMEM lanes 32 (w % 4) .. + 31 of
-  // the accumulator of half h = w / 4, i.e. right-hand-side column
-  // c_base + 128 h + 32 (w % 4) + lane, all 64 output rows
-  const int quarter = warp & 3, hw = warp >> 2;
-  float racc[SPLIT ? kTcRows : 1], rcmp[SPLIT ? kTcRows : 1];
+  fetch_src(S - 1, src_cur);
+  // epilogue / drain mapping: warp w reads TMEM lanes 32 (w % 4) .. + 31
+  // (right-hand-side columns) of the 64-column segments seg = w / 4,
+  // w / 4 + 2, ..., segment = (accumulator half h, 64-row block rb)
+  const int quarter = warp & 3, sg0 = warp >> 2;
+  float racc[SPLIT ? 64 : 1], rcmp[SPLIT ? 64 : 1];
 #pragma unroll
-  for (int i = 0; i < (SPLIT ? kTcRows : 1); i++) { racc[i] = 0.f; rcmp[i] = 0.f; }
+  for (int i = 0; i < (SPLIT ? 64 : 1); i++) { racc[i] = 0.f; rcmp[i] = 0.f; }
+  auto seg_col = [&](int seg) {          // TMEM column of segment seg (in a set)
+    const int h = seg / (NR / 64), rb = seg % (NR / 64);
+    return h * NR + rb * 64;
+  };
   auto drain = [&](int set) {
     if (SPLIT) {
 #pragma unroll
-      for (int half = 0; half < kTcRows / 32; half++) {
+      for (int half = 0; half < 2; half++) {
         float v[32];
-        tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + set * 128 + hw * kTcRows + half * 32, v);
+        tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + set * (Cfg::HALVES * NR) +
+                      seg_col(sg0) + half * 32, v);
 #pragma unroll
         for (int i = 0; i < 32; i++) kahan_add(racc[half * 32 + i], rcmp[half * 32 + i], v[i]);
       }
@@ -364,44 +414,45 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gather_gemm(TcArgs a) {
   };
   bool ok = true;
   for (int c = 0; c < nch; c++) {
-    const int s = c % kTcStages;
-    cp_wait<kTcStages - 2>();
+    const int st = c % S;
+    cp_wait<S - 2>();
     fence_proxy_async();
     __syncthreads();
     if (abort_flag) { ok = false; break; }
     if (tid == 0) {
       tc_fence_after();
       // split mode: window c / kTcWin accumulates into set (c / kTcWin) & 1
-      const uint32_t dset = SPLIT ? (uint32_t)(((c / kTcWin) & 1) * 128) : 0u;
+      const uint32_t dset = SPLIT ? (uint32_t)(((c / kTcWin) & 1) * (Cfg::HALVES * NR)) : 0u;
       const bool first = SPLIT ? (c % kTcWin) == 0 : c == 0;
 #pragma unroll
       for (int q = 0; q < CH / 16; q++) {
-        // 16 reduction rows = two 8-line groups (SBO 1 KiB); k-step offset 2 KiB
-        const uint64_t bh = sw128_desc(w_at(s, 0) + q * 2048, 8192, 1024);
+        // 16 reduction rows = two 8-line groups (SBO 1 KiB); k-step offset
+        // 2 KiB; NR output rows = NR / 64 blocks (LBO = block stride)
+        const uint64_t bh = sw128_desc(w_at(st, 0) + q * 2048, BLK, 1024);
 #pragma unroll
-        for (int h = 0; h < kTcNC / 128; h++) {
+        for (int h = 0; h < Cfg::HALVES; h++) {
           // M = 128 columns = two 64-column blocks, LBO = block stride
-          const uint64_t ah = sw128_desc(s_at(s, 0) + h * 2 * BLK + q * 2048, BLK, 1024);
-          const uint32_t d = tmem + dset + h * kTcRows;
-          mma_bf16_tc(d, ah, bh, !(first && q == 0));
+          const uint64_t ah = sw128_desc(s_at(st, 0) + h * 2 * BLK + q * 2048, BLK, 1024);
+          const uint32_t d = tmem + dset + h * NR;
+          mma_bf16_tc_n(d, ah, bh, Cfg::IDESC, !(first && q == 0));
           if (SPLIT) {
-            const uint64_t bl = sw128_desc(w_at(s, 1) + q * 2048, 8192, 1024);
-            const uint64_t al = sw128_desc(s_at(s, 1) + h * 2 * BLK + q * 2048, BLK, 1024);
-            mma_bf16_tc(d, al, bh, 1u);
-            mma_bf16_tc(d, ah, bl, 1u);
+            const uint64_t bl = sw128_desc(w_at(st, 1) + q * 2048, BLK, 1024);
+            const uint64_t al = sw128_desc(s_at(st, 1) + h * 2 * BLK + q * 2048, BLK, 1024);
+            mma_bf16_tc_n(d, al, bh, Cfg::IDESC, 1u);
+            mma_bf16_tc_n(d, ah, bl, Cfg::IDESC, 1u);
           }
         }
       }
-      mma_commit(smem_addr(&bars[s]));
+      mma_commit(smem_addr(&bars[st]));
     }
-    const int cn = c + kTcStages - 1;
+    const int cn = c + S - 1;
     fetch_src(cn + 1, src_nxt);
     // chunk c - 1 ends a window: its set is drained while chunk c's MMAs
     // run on the other set
     const bool drain_now = SPLIT && c >= 1 && (c % kTcWin) == 0;
     if (c >= 1 && (cn < nch || drain_now)) {
-      const int sp = (c - 1) % kTcStages;
-      if (!mbar_wait(smem_addr(&bars[sp]), ((c - 1) / kTcStages) & 1)) {
+      const int sp = (c - 1) % S;
+      if (!mbar_wait(smem_addr(&bars[sp]), ((c - 1) / S) & 1)) {
         atomicOr(a.flags, FGB_FLAG_DEVICE_TIMEOUT);
         abort_flag = 1;
       }
@@ -410,7 +461,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gather_gemm(TcArgs a) {
       tc_fence_after();
       drain(((c - 1) / kTcWin) & 1);
     }
-    if (cn < nch && !abort_flag) load(cn, cn % kTcStages, src_cur);
+    if (cn < nch && !abort_flag) load(cn, cn % S, src_cur);
     cp_commit();
 #pragma unroll
     for (int j = 0; j < RPW; j++) src_cur[j] = src_nxt[j];
@@ -419,7 +470,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gather_gemm(TcArgs a) {
   // all MMAs of this CTA complete (they finish in order): last chunk's barrier
   if (nch > 0 && ok) {
     const int cl = nch - 1;
-    if (!mbar_wait(smem_addr(&bars[cl % kTcStages]), (cl / kTcStages) & 1)) {
+    if (!mbar_wait(smem_addr(&bars[cl % S]), (cl / S) & 1)) {
       atomicOr(a.flags, FGB_FLAG_DEVICE_TIMEOUT);
       ok = false;
     }
@@ -427,46 +478,51 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gather_gemm(TcArgs a) {
   tc_fence_after();
   __syncthreads();
   if (abort_flag) ok = false;
+  ok = __syncthreads_and(ok) != 0;     // one decision for the whole CTA
 
   // the last (possibly partial) window
   if (SPLIT && ok && nch > 0) drain(((nch - 1) / kTcWin) & 1);
 
   // epilogue (mapping as for the drain)
   if (ok) {
-    const int col = c_base + hw * 128 + quarter * 32 + lane;
 #pragma unroll
-    for (int half = 0; half < kTcRows / 32; half++) {
-      float v[32];
-      if (SPLIT) {
+    for (int seg = sg0; seg < Cfg::SEGS; seg += 2) {
+      const int h = seg / (NR / 64), rb = seg % (NR / 64);
+      const int col = c_base + h * 128 + quarter * 32 + lane;
 #pragma unroll
-        for (int i = 0; i < 32; i++) v[i] = racc[half * 32 + i];
-      } else if (nch > 0) {
-        tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + hw * kTcRows + half * 32, v);
-      } else {
+      for (int half = 0; half < 2; half++) {
+        float v[32];
+        if (SPLIT) {
 #pragma unroll
-        for (int i = 0; i < 32; i++) v[i] = 0.f;
-      }
-      if (col < a.K) {
+          for (int i = 0; i < 32; i++) v[i] = racc[half * 32 + i];
+        } else if (nch > 0) {
+          tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + seg_col(seg) + half * 32, v);
+        } else {
 #pragma unroll
-        for (int i = 0; i < 32; i++) {
-          const int r = half * 32 + i;
-          if (r < out_rows) {
-            const long long row = out_row0 + r;
-            const long long o = row * (long long)a.K + col;
-            if (MODE == kModeB) {
-              float y = v[i];
-              if (a.add) y = a.add[o] + a.alpha * y;
-              a.out[o] = y;
-            } else if (a.zout_hi) {
-              if (excl) {
-                const __nv_bfloat16 h = __float2bfloat16(v[i]);
-                a.zout_hi[o] = h;
-                if (a.zout_lo) a.zout_lo[o] = __float2bfloat16(v[i] - __bfloat162float(h));
+          for (int i = 0; i < 32; i++) v[i] = 0.f;
+        }
+        if (col < a.K) {
+#pragma unroll
+          for (int i = 0; i < 32; i++) {
+            const int r = rb * 64 + half * 32 + i;
+            if (r < out_rows) {
+              const long long row = out_row0 + r;
+              const long long o = row * (long long)a.K + col;
+              if (MODE == kModeB) {
+                float y = v[i];
+                if (a.add) y = a.add[o] + a.alpha * y;
+                a.out[o] = y;
+              } else if (a.zout_hi) {
+                if (excl) {
+                  const __nv_bfloat16 hv = __float2bfloat16(v[i]);
+                  a.zout_hi[o] = hv;
+                  if (a.zout_lo) a.zout_lo[o] = __float2bfloat16(v[i] - __bfloat162float(hv));
+                }
+              } else if (excl) {
+                a.out[o] = v[i];
+              } else {
+                atomicAdd(a.out + o, v[i]);
               }
-            } else if (excl) {
-              a.out[o] = v[i];
-            } else {
-              atomicAdd(a.out + o, v[i]);
             }
           }
         }
@@ -476,8 +532,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gather_gemm(TcArgs a) {
   tc_fence_before();
   __syncthreads();
   if (warp == 0) {
+    __syncwarp();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;"
-                 ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+                 ::"r"(tmem), "r"(Cfg::TMEM_COLS) : "memory");
   }
 }
 
@@ -533,17 +590,18 @@ __global__ void vpanel_transpose_kernel(const int* __restrict__ g_n, const int* 
 
 template <int MODE, bool SPLIT>
 int launch_tc(const TcArgs& a, long long units, cudaStream_t st) {
+  using Cfg = TcCfg<MODE, SPLIT>;
   static bool attr_set = false;
   if (!attr_set) {
     FGB_CUDA_TRY(cudaFuncSetAttribute(tc_gather_gemm<MODE, SPLIT>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemBytes));
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM));
     attr_set = true;
   }
-  const long long nks = (a.K + kTcNC - 1) / kTcNC;
+  const long long nks = (a.K + Cfg::NC - 1) / Cfg::NC;
   const long long grid = units * nks;
   if (grid <= 0) return FGB_OK;
   if (grid > 0x7fffffffLL) { set_error("grid too large"); return FGB_BAD_ARG; }
-  tc_gather_gemm<MODE, SPLIT><<<(unsigned)grid, kTcThreads, kTcSmemBytes, st>>>(a);
+  tc_gather_gemm<MODE, SPLIT><<<(unsigned)grid, kTcThreads, Cfg::SMEM, st>>>(a);
   FGB_LAUNCH_CHECK("tc_gather_gemm");
   return FGB_OK;
 }

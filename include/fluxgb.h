@@ -292,9 +292,12 @@ int fgb_aca_f64_static(const void* bvh, const double* P, const double* N, const 
  *     tile a multiple of 64 rows), src[row] = source row (< num_zrows: a row
  *     of Z; else a row of X at src - num_zrows);
  *   tensor-core phase A: the transposed BF16 phase-A panel holds group g as
- *     n x g_kzp (g_kz rounded up to 64) at g_vtoff, element (r, j) at
- *     g_vtoff + j g_kzp + r; a_woff[num_items + 1]: first 64-row work slice
- *     of each item (slices of an item: ceil(g_kz / 64)).
+ *     n x g_kzp (g_kz rounded up to 128) at g_vtoff, element (r, j) at
+ *     g_vtoff + j g_kzp + r; a_woff[num_items + 1]: first work slice of each
+ *     item, num_work = a_woff[num_items].  The CUDA-core kernels take 64-row
+ *     slices (ceil(g_kz / 64) per item); the tensor-core phase A takes
+ *     128-row slices (g_kzp / 128 per item): it is called with a descriptor
+ *     whose a_woff / num_work count those.
  */
 struct fgb_op_desc {
   const int* g_c0;

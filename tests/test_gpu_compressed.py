@@ -268,7 +268,7 @@ def test_tma_gather_phase_b_matches_cp_async(terrain_op, K):
     sl = torch.empty_like(sh)
     zf = torch.empty((max(nz, 1), K), device="cuda")
     _lib.call("fgb_split_bf16", _lib.ptr(X), _lib.ptr(sh[nz:]), _lib.ptr(sl[nz:]), N * K, st)
-    _lib.call("fgb_tc_phase_a", C.byref(FF._desc), _lib.ptr(tc["vt_hi"]), _lib.ptr(tc["vt_lo"]),
+    _lib.call("fgb_tc_phase_a", C.byref(FF._desc_tc_items), _lib.ptr(tc["vt_hi"]), _lib.ptr(tc["vt_lo"]),
               _lib.ptr(sh[nz:]), _lib.ptr(sl[nz:]), _lib.ptr(zf), K, int(FF._needs_zero_z), fl, st)
     _lib.call("fgb_split_bf16", _lib.ptr(zf), _lib.ptr(sh[:nz]), _lib.ptr(sl[:nz]), nz * K, st)
     for split in (False, True):
@@ -304,7 +304,7 @@ def test_phase_a_bf16_output_matches_fp32(terrain_op):
     xl = torch.empty_like(xh)
     _lib.call("fgb_split_bf16", _lib.ptr(X), _lib.ptr(xh), _lib.ptr(xl), N * K, st)
     z32 = torch.empty((nz, K), device="cuda")
-    _lib.call("fgb_tc_phase_a", C.byref(FF._desc), _lib.ptr(tc["vt_hi"]), _lib.ptr(tc["vt_lo"]),
+    _lib.call("fgb_tc_phase_a", C.byref(FF._desc_tc_items), _lib.ptr(tc["vt_hi"]), _lib.ptr(tc["vt_lo"]),
               _lib.ptr(xh), _lib.ptr(xl), _lib.ptr(z32), K, int(FF._needs_zero_z), fl, st)
     zh = torch.full((nz, K), float("nan"), dtype=torch.bfloat16, device="cuda")
     zl = torch.full_like(zh, float("nan"))

@@ -126,11 +126,6 @@ __device__ __forceinline__ void block_argmax(float v, int idx, float* shv, int* 
   __syncthreads();
 }
 
-__device__ __forceinline__ unsigned lcg(unsigned& s) {
-  s = s * 1664525u + 1013904223u;
-  return s >> 8;
-}
-
 template <class R>
 __global__ void __launch_bounds__(kAcaThreads)
 aca_kernel(AcaArgs a, EntryCtx<R> e) {

@@ -47,16 +47,8 @@
 namespace fgb {
 namespace {
 
-constexpr int kTcRows = 64;        // output rows per CTA (MMA N)
-constexpr int kTcNC = 256;         // right-hand-side columns per CTA (2 x MMA M)
-constexpr int kTcStages = 5;
+constexpr int kTcRows = 64;        // rows of a phase-B tile
 constexpr int kTcThreads = 256;
-constexpr int kTcStageBytes = 40 * 1024;
-constexpr int kTcSmemBytes = kTcStages * kTcStageBytes + 1024;  // + alignment slack
-// TMEM columns: 2 accumulators (one per 128-column half) x 64 rows, and in
-// split mode two such sets used by alternate accumulation windows
-constexpr int kTcTmemCols = 128;
-constexpr int kTcTmemColsSplit = 256;
 // split mode: the tensor core's FP32 accumulation loses up to ~2^-23 of the
 // running sum per MMA, which over thousands of reduction steps exceeds the
 // split operands' 2^-16 accuracy; every kTcWin chunks (12 MMAs) the window's
@@ -117,7 +109,8 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr, uint32_t lbo, uin
 }
 // Instruction descriptor, kind::f16: D FP32 (bits 4-5 = 1), A and B BF16
 // (bits 7-9, 10-12 = 1), A and B MN-major (bits 15, 16), N >> 3 in bits
-// 17-22, M >> 4 in bits 24-28.
+// 17-22, M >> 4 in bits 24-28 (here N = 64, M = 128; the per-mode shapes of
+// tc_gather_gemm build their own).
 constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (1u << 15) | (1u << 16) |
                             ((uint32_t)(kTcRows >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
 

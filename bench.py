@@ -351,7 +351,14 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
                   _lib.ptr(xl) if split else None, _lib.ptr(zh), _lib.ptr(zl) if split else None,
                   K, _lib.ptr(flags), st())
 
-    def tc_b(split):
+    def tc_b(split, rows128=True):
+        # plain products run on the 128-row tiles, split ones on the 64-row
+        # panel (as the solver does)
+        if not split and rows128:
+            _lib.call("fgb_tc_phase_b", C.byref(FF._desc128), _lib.ptr(tc["w128"]), None,
+                      _lib.ptr(xh), None, _lib.ptr(zh), None, _lib.ptr(Y), K, _lib.ptr(Ek), 1.0,
+                      _lib.ptr(flags), st())
+            return
         _lib.call("fgb_tc_phase_b", desc, _lib.ptr(tc["w_hi"]),
                   _lib.ptr(tc["w_lo"]) if split else None, _lib.ptr(xh),
                   _lib.ptr(xl) if split else None, _lib.ptr(zh), _lib.ptr(zl) if split else None,
@@ -370,6 +377,7 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
           "phaseB_tc_split": t_events(lambda: tc_b(True)),
           "phaseA_f32": t_events(lambda: f32(1), 3), "phaseB_f32": t_events(lambda: f32(2), 3)}
     ms_tma = t_events(tc_b_tma, 3)
+    ms_b64 = t_events(lambda: tc_b(False, rows128=False), 3)
     FF.check_device_flags()
     # algorithmic work per launch: every stored weight read once, every
     # distinct source row read once, outputs written once; flops 2 per
@@ -418,6 +426,7 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
                            "peak_source": src, "algorithmic_bytes": byts,
                            "algorithmic_flops": fl, "ms_per_launch": t_ms, "fp32_tflops": tfl}
     out["kernel_ms"] = {"columns": K, **ms, "phaseB_tc_tma_gather_variant": ms_tma,
+                        "phaseB_tc_64row_tiles": ms_b64,
                         "per_step_ms": per_step,
                         "tflops": {k: work[k][1] / (ms[k] * 1e-3) / 1e12 for k in ms}}
     del X32, xh, xl, Z32, zh, zl, sh, sl, Y, Ek

@@ -162,6 +162,7 @@ class fgb_op_desc(C.Structure):
         ("num_tiles", C.c_longlong), ("N", C.c_longlong), ("num_zrows", C.c_longlong),
         ("max_group_tiles", C.c_int), ("g_kzp", C.c_void_p), ("g_vtoff", C.c_void_p),
         ("a_woff", C.c_void_p), ("num_work", C.c_longlong), ("panel_rows", C.c_longlong),
+        ("tile_rows", C.c_int),
     ]
 
 
@@ -658,6 +659,7 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         else:
             L_nf = np.zeros(ntiles, np.int64)
         L = L_lr + L_nf
+        self._tile_L = L
         Lpad = (L + PANEL_ALIGN - 1) // PANEL_ALIGN * PANEL_ALIGN
         t_p0 = np.zeros(ntiles + 1, np.int64)
         np.cumsum(Lpad, out=t_p0[1:])
@@ -754,6 +756,7 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         desc.max_group_tiles = max_gt
         desc.num_work = num_work
         desc.panel_rows = int(self._panel_rows)
+        desc.tile_rows = TILE_ROWS
         return desc
 
     def _make_desc_tc_items(self):
@@ -925,17 +928,89 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
             buf = torch.empty((zr + self.num_faces, K), dtype=torch.bfloat16, device=device)
         return buf, buf[:zr], buf[zr:]
 
+    def _build_tc128(self, panel32):
+        """The 128-row phase-B layout for the BF16 tensor-core product: the
+        64-row panel's rows of tiles 2t and 2t + 1 that gather the same
+        source become one 128-weight row of tile t (each source appears at
+        most once per 64-row tile, so the halves never collide)."""
+        dev = panel32.device
+        t_p0 = self._dev["t_p0"]
+        ntiles = int(t_p0.numel() - 1)
+        P = int(self._panel_rows)
+        counts = t_p0[1:] - t_p0[:-1]
+        tile = torch.repeat_interleave(torch.arange(ntiles, device=dev), counts)
+        pos = torch.arange(P, device=dev) - t_p0[:-1][tile]
+        Lt = torch.as_tensor(self._tile_L, device=dev)
+        vidx = torch.nonzero(pos < Lt[tile]).squeeze(1)     # rows that are not padding
+        del pos
+        vtile = tile[vidx]
+        half = (tile & 1).to(torch.uint8)
+        del tile
+        vkey = (vtile >> 1) * (1 << 31) + self._dev["src"].to(torch.int64)[vidx]
+        del vtile
+        skey, order = torch.sort(vkey)
+        del vkey
+        newflag = torch.ones(skey.numel(), dtype=torch.bool, device=dev)
+        newflag[1:] = skey[1:] != skey[:-1]
+        uid_sorted = torch.cumsum(newflag.to(torch.int64), 0) - 1
+        ukeys = skey[newflag]
+        del skey, newflag
+        u_tile = ukeys >> 31
+        u_src = (ukeys & ((1 << 31) - 1)).to(torch.int32)
+        del ukeys
+        nt2 = (self.num_faces + 127) // 128
+        L2 = torch.bincount(u_tile, minlength=nt2)
+        t2 = torch.zeros(nt2 + 1, dtype=torch.int64, device=dev)
+        t2[1:] = torch.cumsum((L2 + PANEL_ALIGN - 1) // PANEL_ALIGN * PANEL_ALIGN, 0)
+        ufirst = torch.zeros(nt2 + 1, dtype=torch.int64, device=dev)
+        ufirst[1:] = torch.cumsum(L2, 0)
+        u_row = t2[u_tile] + torch.arange(u_tile.numel(), device=dev) - ufirst[u_tile]
+        del ufirst, u_tile
+        new_row = torch.full((P,), -1, dtype=torch.int64, device=dev)
+        new_row[vidx[order]] = u_row[uid_sorted]
+        del vidx, order, uid_sorted
+        total2 = int(t2[-1].item())
+        src2 = torch.zeros(max(total2, 1), dtype=torch.int32, device=dev)
+        src2[u_row] = u_src
+        del u_row, u_src
+        w128 = torch.zeros(max(total2, 1) * 128, dtype=torch.bfloat16, device=dev)
+        _lib.call("fgb_retile_panel_bf16", _lib.ptr(panel32), P, _lib.ptr(new_row),
+                  _lib.ptr(half), _lib.ptr(w128), _lib.stream_handle())
+        del new_row, half
+        desc = fgb_op_desc.from_buffer_copy(self._desc)
+        desc.t_p0 = t2.data_ptr()
+        desc.src = src2.data_ptr()
+        desc.num_tiles = nt2
+        desc.panel_rows = total2
+        desc.tile_rows = 128
+        self._dev128 = dict(t_p0=t2, src=src2)
+        self._desc128 = desc
+        self.stats["panel_rows_128"] = total2
+        return w128
+
     def tc_operands(self, split=False):
         """BF16 operands of the tensor-core products, built once from the
-        FP32 panels: 'w_hi' (phase-B panel), 'vt_hi' (transposed phase-A
-        panel) and, for split products, their low parts 'w_lo', 'vt_lo'
+        FP32 panels: 'w128' (phase-B panel with 128-row tiles, for the plain
+        product), 'vt_hi' (transposed phase-A panel) and, for split products,
+        the 64-row phase-B panel 'w_hi' / 'w_lo' and 'vt_lo'
         (hi = bf16(v), lo = bf16(v - hi))."""
         tc = self.__dict__.setdefault("_tc", {})
-        if "w_hi" in tc and (not split or "w_lo" in tc):
+        if "w128" in tc and (not split or "w_lo" in tc):
             return tc
         panel, vpanel = self.panels("fp32")
         dev = panel.device
         st = _lib.stream_handle()
+        if "w128" not in tc:
+            tc["w128"] = self._build_tc128(panel)
+        if not split:
+            if "vt_hi" not in tc:
+                vt_hi = torch.zeros(max(self._vtpanel_size, 8), dtype=torch.bfloat16, device=dev)
+                b = self._build_dev
+                _lib.call("fgb_vpanel_transpose_bf16", C.byref(self._desc), _lib.ptr(vpanel),
+                          _lib.ptr(b["vt_g"]), _lib.ptr(b["vt_s"]), _lib.ptr(b["vt_j"]),
+                          self._num_vt_tiles, _lib.ptr(vt_hi), None, st)
+                tc["vt_hi"] = vt_hi
+            return tc
         w_hi = tc.get("w_hi")
         if w_hi is None:
             w_hi = torch.empty(panel.numel(), dtype=torch.bfloat16, device=dev)
@@ -975,7 +1050,7 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
             # phase A writes Z directly in BF16 (Z, the FP32 scratch, is unused)
             _lib.call("fgb_tc_phase_a_bf16", C.byref(self._desc_tc), _lib.ptr(tc["vt_hi"]), None,
                       _lib.ptr(Xb), None, _lib.ptr(Zb), None, K, flags, st)
-        _lib.call("fgb_tc_phase_b", C.byref(self._desc), _lib.ptr(tc["w_hi"]), None,
+        _lib.call("fgb_tc_phase_b", C.byref(self._desc128), _lib.ptr(tc["w128"]), None,
                   _lib.ptr(Xb), None, _lib.ptr(Zb), None, _lib.ptr(Y), K, _lib.ptr(add),
                   float(alpha), flags, st)
         return Y
@@ -1170,6 +1245,8 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         st["_desc"] = None
         st["_desc_tc"] = None
         st["_desc_tc_items"] = None
+        st["_desc128"] = None
+        st["_dev128"] = None
         st["_panels"] = {}
         st["_tc"] = {}
         st["_flags_d"] = None

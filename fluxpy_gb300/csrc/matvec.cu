@@ -53,6 +53,7 @@ struct PanelView {
   const long long* t_p0;  // num_tiles + 1 panel row offsets
   const int* src;         // per panel row
   long long num_tiles;
+  int tile_rows;
   long long N;
   long long num_zrows;
 };
@@ -723,6 +724,10 @@ int check_op(const PanelView& op) {
     set_error("bad operator sizes");
     return FGB_BAD_ARG;
   }
+  if (op.tile_rows != 0 && op.tile_rows != kTileRows) {
+    set_error("these kernels take the 64-row panel (tile_rows 64)");
+    return FGB_BAD_ARG;
+  }
   return FGB_OK;
 }
 
@@ -734,6 +739,7 @@ PanelView to_view(const fgb_op_desc* d) {
   v.num_items = d->num_items;
   v.a_woff = d->a_woff; v.num_work = d->num_work;
   v.t_p0 = d->t_p0; v.src = d->src; v.num_tiles = d->num_tiles;
+  v.tile_rows = d->tile_rows;
   v.N = d->N;
   v.num_zrows = d->num_zrows;
   return v;

@@ -202,9 +202,9 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
 // row feeds twice the flops; phase B keeps the 64-row tiles of the panel.
 // Split mode keeps 64 accumulator values per thread for the compensated
 // drains (phase A: NC = 128).
-template <int MODE, bool SPLIT>
+template <int MODE, bool SPLIT, int NR_ = (MODE == kModeA ? 128 : 64)>
 struct TcCfg {
-  static constexpr int NR = MODE == kModeA ? 128 : 64;
+  static constexpr int NR = NR_;
   static constexpr int NC = (MODE == kModeA && SPLIT) ? 128 : 256;
   static constexpr int CH = SPLIT ? 32 : 64;
   static constexpr int PARTS = SPLIT ? 2 : 1;
@@ -238,9 +238,9 @@ __device__ __forceinline__ void mma_bf16_tc_n(uint32_t dtmem, uint64_t adesc, ui
       ::"r"(dtmem), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate) : "memory");
 }
 
-template <int MODE, bool SPLIT>
+template <int MODE, bool SPLIT, int NRT>
 __global__ void __launch_bounds__(kTcThreads, 1) tc_gather_gemm(TcArgs a) {
-  using Cfg = TcCfg<MODE, SPLIT>;
+  using Cfg = TcCfg<MODE, SPLIT, NRT>;
   constexpr int NR = Cfg::NR, NC = Cfg::NC, CH = Cfg::CH, WB = Cfg::WB, SB = Cfg::SB;
   constexpr int BLK = Cfg::BLK, S = Cfg::STAGES, STAGE = Cfg::STAGE;
   extern __shared__ uint8_t smem_raw[];
@@ -531,6 +531,27 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gather_gemm(TcArgs a) {
   }
 }
 
+// 128-row panel from the 64-row FP32 one: old panel row r (tile t) with
+// new_row[r] >= 0 lands in half (t & 1) of new row new_row[r], as BF16; the
+// new panel is zeroed by the caller (a new row gets at most one old row per
+// half: a source appears once per 64-row tile).  One warp per old row.
+__global__ void retile_panel_kernel(const float* __restrict__ panel64, long long num_rows,
+                                    const long long* __restrict__ new_row,
+                                    const unsigned char* __restrict__ half,
+                                    __nv_bfloat16* __restrict__ panel128) {
+  const int lane = threadIdx.x & 31;
+  const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+  for (long long r = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; r < num_rows;
+       r += warps) {
+    const long long nr = new_row[r];
+    if (nr < 0) continue;
+    const float2 w = reinterpret_cast<const float2*>(panel64 + r * 64)[lane];
+    __nv_bfloat16* out = panel128 + nr * 128 + half[r] * 64 + 2 * lane;
+    out[0] = __float2bfloat16(w.x);
+    out[1] = __float2bfloat16(w.y);
+  }
+}
+
 __global__ void split_bf16_kernel(const float* __restrict__ in, __nv_bfloat16* __restrict__ hi,
                                   __nv_bfloat16* __restrict__ lo, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
@@ -581,12 +602,12 @@ __global__ void vpanel_transpose_kernel(const int* __restrict__ g_n, const int* 
   }
 }
 
-template <int MODE, bool SPLIT>
+template <int MODE, bool SPLIT, int NRT = (MODE == kModeA ? 128 : 64)>
 int launch_tc(const TcArgs& a, long long units, cudaStream_t st) {
-  using Cfg = TcCfg<MODE, SPLIT>;
+  using Cfg = TcCfg<MODE, SPLIT, NRT>;
   static bool attr_set = false;
   if (!attr_set) {
-    FGB_CUDA_TRY(cudaFuncSetAttribute(tc_gather_gemm<MODE, SPLIT>,
+    FGB_CUDA_TRY(cudaFuncSetAttribute(tc_gather_gemm<MODE, SPLIT, NRT>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM));
     attr_set = true;
   }
@@ -594,7 +615,7 @@ int launch_tc(const TcArgs& a, long long units, cudaStream_t st) {
   const long long grid = units * nks;
   if (grid <= 0) return FGB_OK;
   if (grid > 0x7fffffffLL) { set_error("grid too large"); return FGB_BAD_ARG; }
-  tc_gather_gemm<MODE, SPLIT><<<(unsigned)grid, kTcThreads, Cfg::SMEM, st>>>(a);
+  tc_gather_gemm<MODE, SPLIT, NRT><<<(unsigned)grid, kTcThreads, Cfg::SMEM, st>>>(a);
   FGB_LAUNCH_CHECK("tc_gather_gemm");
   return FGB_OK;
 }
@@ -1032,8 +1053,14 @@ int fgb_tc_phase_b(const struct fgb_op_desc* d, const void* w_hi, const void* w_
   a.z_lo = static_cast<const __nv_bfloat16*>(Z_lo);
   a.lds = K; a.K = K; a.out = Y; a.add = add; a.alpha = alpha; a.flags = flags;
   cudaStream_t st = fgb::as_stream(stream);
-  return split ? fgb::launch_tc<fgb::kModeB, true>(a, d->num_tiles, st)
-               : fgb::launch_tc<fgb::kModeB, false>(a, d->num_tiles, st);
+  const int tr = d->tile_rows ? d->tile_rows : 64;
+  if (tr == 128) {
+    if (split) { fgb::set_error("split products take the 64-row panel"); return FGB_BAD_ARG; }
+    return fgb::launch_tc<fgb::kModeB, false, 128>(a, d->num_tiles, st);
+  }
+  if (tr != 64) { fgb::set_error("tile_rows must be 64 or 128"); return FGB_BAD_ARG; }
+  return split ? fgb::launch_tc<fgb::kModeB, true, 64>(a, d->num_tiles, st)
+               : fgb::launch_tc<fgb::kModeB, false, 64>(a, d->num_tiles, st);
 }
 
 int fgb_tc_phase_b_tma(const struct fgb_op_desc* d, const void* w_hi, const void* w_lo,
@@ -1050,12 +1077,24 @@ int fgb_tc_phase_b_tma(const struct fgb_op_desc* d, const void* w_hi, const void
   }
   if (d->num_tiles <= 0) return FGB_OK;
   if (d->panel_rows <= 0) { fgb::set_error("panel_rows not set"); return FGB_BAD_ARG; }
+  if (d->tile_rows != 0 && d->tile_rows != 64) { fgb::set_error("the TMA variant takes 64-row tiles"); return FGB_BAD_ARG; }
   fgb::TcArgs a{};
   a.t_p0 = d->t_p0; a.src = d->src; a.N = d->N; a.num_zrows = d->num_zrows;
   a.K = K; a.lds = K; a.out = Y; a.add = add; a.alpha = alpha; a.flags = flags;
   cudaStream_t st = fgb::as_stream(stream);
   return split ? fgb::launch_tma_b<true>(d, w_hi, w_lo, S_hi, S_lo, a, st)
                : fgb::launch_tma_b<false>(d, w_hi, nullptr, S_hi, nullptr, a, st);
+}
+
+int fgb_retile_panel_bf16(const float* panel64, long long num_rows, const long long* new_row,
+                          const unsigned char* half, void* panel128, void* stream) {
+  if (num_rows < 0 || !panel64 || !panel128) { fgb::set_error("bad arguments"); return FGB_BAD_ARG; }
+  if (num_rows == 0) return FGB_OK;
+  fgb::retile_panel_kernel<<<fgb::grid_for(num_rows * 32, 256, 152LL * 64), 256, 0,
+                             fgb::as_stream(stream)>>>(
+      panel64, num_rows, new_row, half, static_cast<__nv_bfloat16*>(panel128));
+  FGB_LAUNCH_CHECK("retile_panel_kernel");
+  return FGB_OK;
 }
 
 int fgb_split_bf16(const float* in, void* hi, void* lo, long long n, void* stream) {

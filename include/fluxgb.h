@@ -322,6 +322,8 @@ struct fgb_op_desc {
   const long long* a_woff;
   long long num_work;   /* a_woff[num_items] */
   long long panel_rows; /* t_p0[num_tiles] */
+  int tile_rows;        /* rows per phase-B tile: 64 (every kernel), or 128
+                           (tensor-core BF16 phase B only); 0 means 64 */
 };
 /*
  * y = F x (or y = add + alpha F x), vectors in cluster order.  Replaces
@@ -386,6 +388,13 @@ int fgb_tc_phase_b(const struct fgb_op_desc* d, const void* w_hi, const void* w_
 int fgb_tc_phase_b_tma(const struct fgb_op_desc* d, const void* w_hi, const void* w_lo,
                        const void* S_hi, const void* S_lo, float* Y, int K, const float* add,
                        float alpha, unsigned* flags, void* stream);
+/* 128-row phase-B panel (BF16) from the 64-row FP32 one: old row r goes to
+ * half half[r] (0/1) of new row new_row[r] (skipped when < 0); panel128 must
+ * be zeroed.  With a descriptor of tile_rows = 128, fgb_tc_phase_b computes
+ * 128 output rows per CTA, so each gathered source row feeds twice the
+ * flops. */
+int fgb_retile_panel_bf16(const float* panel64, long long num_rows, const long long* new_row,
+                          const unsigned char* half, void* panel128, void* stream);
 /* hi = bf16(in), lo = bf16(in - hi) elementwise (lo may be NULL). */
 int fgb_split_bf16(const float* in, void* hi, void* lo, long long n, void* stream);
 /* Transposed BF16 phase-A panel from the FP32 one (layouts in fgb_op_desc);

@@ -327,3 +327,34 @@ def test_fp32_multi_rhs_product_any_width(terrain_op, K):
     Y32 = FF.matmat_permuted(X.float().contiguous(), "fp32")
     Y64 = FF.matmat_permuted(X, "fp64")
     assert (Y32.double() - Y64).abs().max().item() <= 5e-6 * Y64.abs().max().item()
+
+
+@pytest.mark.parametrize("K", [256, 520])
+def test_phase_b_128_row_tiles_match_64(terrain_op, K):
+    """The plain BF16 phase B on the re-tiled 128-row panel (rows of tiles
+    2t and 2t + 1 that gather the same source merged) against the 64-row
+    panel: same products, summed in another order."""
+    import ctypes as C
+    from fluxpy_gb300 import _lib
+    sm, FF = terrain_op
+    N = sm.num_faces
+    nz = FF._num_zrows
+    tc = FF.tc_operands(split=True)
+    g = torch.Generator(device="cuda").manual_seed(K + 5)
+    S = torch.rand((nz + N, K), device="cuda", generator=g).to(torch.bfloat16)
+    add = torch.rand((N, K), device="cuda", generator=g)
+    fl = _lib.ptr(FF.device_flags())
+    st = _lib.stream_handle()
+    Y64 = torch.full((N, K), float("nan"), device="cuda")
+    Y128 = torch.full((N, K), float("nan"), device="cuda")
+    _lib.call("fgb_tc_phase_b", C.byref(FF._desc), _lib.ptr(tc["w_hi"]), None,
+              _lib.ptr(S[nz:]), None, _lib.ptr(S[:nz]), None, _lib.ptr(Y64), K, _lib.ptr(add),
+              0.5, fl, st)
+    _lib.call("fgb_tc_phase_b", C.byref(FF._desc128), _lib.ptr(tc["w128"]), None,
+              _lib.ptr(S[nz:]), None, _lib.ptr(S[:nz]), None, _lib.ptr(Y128), K, _lib.ptr(add),
+              0.5, fl, st)
+    FF.check_device_flags()
+    assert torch.isfinite(Y128).all()
+    ref = (Y64 - add).abs().max().item()
+    assert (Y128 - Y64).abs().max().item() <= 1e-5 * ref
+    assert FF.stats["panel_rows_128"] > 0

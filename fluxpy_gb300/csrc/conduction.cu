@@ -10,6 +10,9 @@
 //     without FMA contraction (this file is compiled with -fmad=false);
 //   * the temperature rows (num_faces x (nz+1), the reference's row-major
 //     layout) are staged through shared memory with coalesced loads/stores;
+//     the sweep reads the pre-step profile from there and keeps its own
+//     arrays (u, gam) in shared memory too, so no per-thread local arrays
+//     spill past L1; the facets per CTA (32..128) follow from nz;
 //   * the linearised radiative boundary (predictor-corrector, at most 10
 //     redos, conductionQ.c:103-172) and the Thomas solve are fused: the
 //     right-hand side is formed on the fly during the forward sweep from the
@@ -26,82 +29,183 @@ template <class R> struct Consts;
 template <> struct Consts<double> { static constexpr double sigSB = 5.6704e-8; };
 template <> struct Consts<float> { static constexpr float sigSB = 5.6704e-8f; };
 
-// Grid coefficients shared by all facets (conductionQ.c:69-97).
+// Grid coefficients shared by all facets (conductionQ.c:69-97), computed by
+// the CTA's threads in parallel, one layer each, with the reference's
+// operations for every element (bit-identical to the serial loops).
 template <class R>
 __device__ void grid_coeffs_q(int nz, const R* z, R dt, const R* ti, const R* rhoc,
                               R* k, R* alpha, R* gamma, R* a, R* b, R* c, R* k1_out) {
-  for (int i = 1; i <= nz; i++) k[i] = ti[i] * ti[i] / rhoc[i];
-  R dz = R(2) * z[1];
-  R beta = dt / rhoc[1] / (R(2) * dz * dz);
-  alpha[1] = beta * k[2];
-  gamma[1] = beta * k[1];
-  for (int i = 2; i < nz; i++) {
-    R buf = dt / (z[i + 1] - z[i - 1]);
-    alpha[i] = R(2) * k[i + 1] * buf / (rhoc[i] + rhoc[i + 1]) / (z[i + 1] - z[i]);
-    gamma[i] = R(2) * k[i] * buf / (rhoc[i] + rhoc[i + 1]) / (z[i] - z[i - 1]);
+  for (int i = threadIdx.x + 1; i <= nz; i += blockDim.x) k[i] = ti[i] * ti[i] / rhoc[i];
+  __syncthreads();
+  const R dz = R(2) * z[1];
+  for (int i = threadIdx.x + 1; i <= nz; i += blockDim.x) {
+    R al, ga;
+    if (i == 1) {
+      const R beta = dt / rhoc[1] / (R(2) * dz * dz);
+      al = beta * k[2];
+      ga = beta * k[1];
+    } else if (i < nz) {
+      const R buf = dt / (z[i + 1] - z[i - 1]);
+      al = R(2) * k[i + 1] * buf / (rhoc[i] + rhoc[i + 1]) / (z[i + 1] - z[i]);
+      ga = R(2) * k[i] * buf / (rhoc[i] + rhoc[i + 1]) / (z[i] - z[i - 1]);
+    } else {
+      const R buf = dt / (z[nz] - z[nz - 1]) / (z[nz] - z[nz - 1]);
+      ga = k[nz] * buf / (R(2) * rhoc[nz]);
+      al = R(0);  // never read by the solve (c[nz] unused, b[nz] reset)
+    }
+    alpha[i] = al;
+    gamma[i] = ga;
+    a[i] = -ga;
+    b[i] = (i == nz) ? R(1) + ga : R(1) + al + ga;
+    c[i] = -al;
   }
-  R buf = dt / (z[nz] - z[nz - 1]) / (z[nz] - z[nz - 1]);
-  gamma[nz] = k[nz] * buf / (R(2) * rhoc[nz]);
-  alpha[nz] = R(0);  // never read by the solve (c[nz] unused, b[nz] reset)
-  *k1_out = k[1] / dz;
-  for (int i = 1; i <= nz; i++) {
-    a[i] = -gamma[i];
-    b[i] = R(1) + alpha[i] + gamma[i];
-    c[i] = -alpha[i];
-  }
-  b[nz] = R(1) + gamma[nz];
+  if (threadIdx.x == 0) *k1_out = k[1] / dz;
 }
 
 // Grid coefficients for the prescribed-temperature boundary (conductionT.c:45-64).
 template <class R>
 __device__ void grid_coeffs_t(int nz, const R* z, R dt, const R* ti, const R* rhoc,
                               R* k, R* alpha, R* gamma, R* a, R* b, R* c) {
-  for (int i = 1; i <= nz; i++) k[i] = ti[i] * ti[i] / rhoc[i];
-  alpha[1] = k[2] * dt / rhoc[1] / (z[2] - z[1]) / z[2];
-  gamma[1] = k[1] * dt / rhoc[1] / z[1] / z[2];
-  for (int i = 2; i < nz; i++) {
-    R buf = dt / (z[i + 1] - z[i - 1]);
-    alpha[i] = R(2) * k[i + 1] * buf / (rhoc[i] + rhoc[i + 1]) / (z[i + 1] - z[i]);
-    gamma[i] = R(2) * k[i] * buf / (rhoc[i] + rhoc[i + 1]) / (z[i] - z[i - 1]);
+  for (int i = threadIdx.x + 1; i <= nz; i += blockDim.x) k[i] = ti[i] * ti[i] / rhoc[i];
+  __syncthreads();
+  for (int i = threadIdx.x + 1; i <= nz; i += blockDim.x) {
+    R al, ga;
+    if (i == 1) {
+      al = k[2] * dt / rhoc[1] / (z[2] - z[1]) / z[2];
+      ga = k[1] * dt / rhoc[1] / z[1] / z[2];
+    } else if (i < nz) {
+      const R buf = dt / (z[i + 1] - z[i - 1]);
+      al = R(2) * k[i + 1] * buf / (rhoc[i] + rhoc[i + 1]) / (z[i + 1] - z[i]);
+      ga = R(2) * k[i] * buf / (rhoc[i] + rhoc[i + 1]) / (z[i] - z[i - 1]);
+    } else {
+      const R buf = dt / (z[nz] - z[nz - 1]) / (z[nz] - z[nz - 1]);
+      ga = k[nz] * buf / (rhoc[nz] + rhoc[nz]);
+      al = R(0);
+    }
+    alpha[i] = al;
+    gamma[i] = ga;
+    a[i] = -ga;
+    b[i] = (i == nz) ? R(1) + ga : R(1) + al + ga;
+    c[i] = -al;
   }
-  R buf = dt / (z[nz] - z[nz - 1]) / (z[nz] - z[nz - 1]);
-  gamma[nz] = k[nz] * buf / (rhoc[nz] + rhoc[nz]);
-  alpha[nz] = R(0);
-  for (int i = 1; i <= nz; i++) {
-    a[i] = -gamma[i];
-    b[i] = R(1) + alpha[i] + gamma[i];
-    c[i] = -alpha[i];
-  }
-  b[nz] = R(1) + gamma[nz];
 }
 
-constexpr int kThreads = 128;
+constexpr int kMaxThreads = 128;
+constexpr size_t kSmemBudget = 227 * 1024;  // the per-CTA opt-in maximum
 
-// Shared layout: per-layer coefficient arrays (7 x (nz+1)) then the staged
-// temperature tile (kThreads x (nz+1)).
+// Shared layout, all of element type R:
+//   7 coefficient arrays of nz+1 (k, alpha, gamma, a, b, c, misc);
+//   the staged temperature tile, nt rows of stride ws = (nz+1)|1 (odd, so
+//   that the threads of a warp reading element i of their own rows hit
+//   distinct banks);
+//   u and gam of the Thomas solve, layer-major ((nz+1) x nt: layer j of
+//   thread t at j*nt + t, consecutive threads on consecutive words).
+__host__ __device__ inline int tile_stride(int nz) { return (nz + 1) | 1; }
+
+template <class R>
+size_t cond_smem(int nz, int nt) {
+  return sizeof(R) * ((size_t)7 * (nz + 1) + (size_t)nt * tile_stride(nz) + (size_t)2 * (nz + 1) * nt);
+}
+
+// Facets per CTA: the largest multiple of 32 (at most 128) whose shared
+// layout fits the budget; 0 if even one warp does not fit.
+template <class R>
+int cond_threads(int nz) {
+  for (int nt = kMaxThreads; nt >= 32; nt -= 32)
+    if (cond_smem<R>(nz, nt) <= kSmemBudget) return nt;
+  return 0;
+}
+
 template <class R>
 __device__ inline R* coeff(R* sh, int which, int nz) { return sh + which * (nz + 1); }
 
+// Row-major global rows [f0, f0+rows) x w  <->  tile rows of stride ws.
 template <class R>
-__device__ void stage_in(R* tile, const R* T, long long f0, int rows, int w) {
+__device__ void stage_in(R* tile, const R* T, long long f0, int rows, int w, int ws) {
   const R* src = T + f0 * w;
-  long long n = (long long)rows * w;
-  for (long long q = threadIdx.x; q < n; q += blockDim.x) tile[q] = src[q];
+  const int n = rows * w;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    const int r = q / w;
+    tile[r * ws + (q - r * w)] = src[q];
+  }
 }
 
 template <class R>
-__device__ void stage_out(R* T, const R* tile, long long f0, int rows, int w) {
+__device__ void stage_out(R* T, const R* tile, long long f0, int rows, int w, int ws) {
   R* dst = T + f0 * w;
-  long long n = (long long)rows * w;
-  for (long long q = threadIdx.x; q < n; q += blockDim.x) dst[q] = tile[q];
+  const int n = rows * w;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    const int r = q / w;
+    dst[q] = tile[r * ws + (q - r * w)];
+  }
 }
 
 template <class R>
 __device__ inline bool finite_val(R x) { return isfinite(x); }
 
+// x / d. FP64 keeps the IEEE quotient of the reference's C code (results
+// bit-identical to it); FP32 multiplies by one correctly rounded reciprocal
+// of the pivot per layer (the FP32 kernel is a faster, less exact variant).
+template <class R> struct Pivot;
+template <> struct Pivot<double> {
+  double d;
+  __device__ explicit Pivot(double v) : d(v) {}
+  __device__ double div(double x) const { return x / d; }
+};
+template <> struct Pivot<float> {
+  float r;
+  __device__ explicit Pivot(float v) { r = __frcp_rn(v); }
+  __device__ float div(float x) const { return x * r; }
+};
+
+// Forward sweep and back substitution of the tridiagonal system with
+// sub/main/super diagonals (a, b, c) from shared memory, except the first
+// main-diagonal entry b1 (facet dependent under the radiative boundary).
+// The right-hand side is formed on the fly from the pre-step profile Trow
+// (crank-nicolson explicit half, conductionQ.c:123-137 / conductionT.c:66-77).
+// u and gam are layer-major with stride nt. Returns false on a zero pivot.
+template <class R>
+__device__ bool thomas_cn(int nz, const R* Trow, R r1, R b1, R rhs_bottom,
+                          const R* s_alpha, const R* s_gamma, const R* s_a, const R* s_b,
+                          const R* s_c, R* u, R* gam, int nt) {
+  R bet = b1;
+  if (bet == R(0)) return false;
+  Pivot<R> pv(bet);
+  R uprev = pv.div(r1);
+  u[nt] = uprev;
+  R tm1 = Trow[1], t0 = Trow[2];
+  for (int j = 2; j <= nz; j++) {
+    R rj;
+    if (j < nz) {
+      const R tp1 = Trow[j + 1];
+      const R ga = s_gamma[j], al = s_alpha[j];
+      rj = ga * tm1 + (R(1) - al - ga) * t0 + al * tp1;
+      tm1 = t0;
+      t0 = tp1;
+    } else {
+      const R ga = s_gamma[nz];
+      rj = ga * tm1 + (R(1) - ga) * t0 + rhs_bottom;
+    }
+    const R aj = s_a[j];
+    const R g = pv.div(s_c[j - 1]);
+    gam[j * nt] = g;
+    bet = s_b[j] - aj * g;
+    if (bet == R(0)) return false;
+    pv = Pivot<R>(bet);
+    uprev = pv.div(rj - aj * uprev);
+    u[j * nt] = uprev;
+  }
+  R unext = uprev;
+  for (int j = nz - 1; j >= 1; j--) {
+    unext = u[j * nt] - gam[(j + 1) * nt] * unext;
+    u[j * nt] = unext;
+  }
+  return true;
+}
+
 // One step of the radiative-flux boundary problem for every facet.
-template <class R, int NZMAX>
-__global__ void __launch_bounds__(kThreads)
+template <class R>
+__global__ void __launch_bounds__(kMaxThreads)
 conduction_q_kernel(int num_faces, int nz, const R* __restrict__ z, R dt,
                     const R* __restrict__ Qn, const R* __restrict__ Qnp1,
                     const R* T_in, R* T_out,
@@ -110,7 +214,7 @@ conduction_q_kernel(int num_faces, int nz, const R* __restrict__ z, R dt,
                     R* __restrict__ Fsurf, unsigned* __restrict__ flags) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   R* sh = reinterpret_cast<R*>(smem_raw);
-  const int w = nz + 1;
+  const int w = nz + 1, ws = tile_stride(nz), nt = blockDim.x;
   R* s_k = coeff(sh, 0, nz);
   R* s_alpha = coeff(sh, 1, nz);
   R* s_gamma = coeff(sh, 2, nz);
@@ -119,26 +223,22 @@ conduction_q_kernel(int num_faces, int nz, const R* __restrict__ z, R dt,
   R* s_c = coeff(sh, 5, nz);
   R* s_misc = coeff(sh, 6, nz);  // [0] = k1
   R* tile = sh + 7 * w;
+  R* s_u = tile + nt * ws;
+  R* s_gam = s_u + w * nt;
 
-  if (threadIdx.x == 0) {
-    R k1;
-    grid_coeffs_q<R>(nz, z, dt, ti, rhoc, s_k, s_alpha, s_gamma, s_a, s_b, s_c, &k1);
-    s_misc[0] = k1;
-  }
-  const long long f0 = (long long)blockIdx.x * kThreads;
-  const int rows = (int)min((long long)kThreads, (long long)num_faces - f0);
-  stage_in(tile, T_in, f0, rows, w);
+  grid_coeffs_q<R>(nz, z, dt, ti, rhoc, s_k, s_alpha, s_gamma, s_a, s_b, s_c, &s_misc[0]);
+  const long long f0 = (long long)blockIdx.x * nt;
+  const int rows = (int)min((long long)nt, (long long)num_faces - f0);
+  stage_in(tile, T_in, f0, rows, w, ws);
   __syncthreads();
 
   const int t = threadIdx.x;
   unsigned my_flags = 0;
   if (t < rows) {
     const long long f = f0 + t;
-    R* Trow = tile + (long long)t * w;
-    R Told[NZMAX + 1];
-    R u[NZMAX + 1];
-    R gam[NZMAX + 1];
-    for (int i = 1; i <= nz; i++) Told[i] = Trow[i];
+    R* Trow = tile + t * ws;
+    R* u = s_u + t;
+    R* gam = s_gam + t;
     const R qn = Qn[f], qnp1 = Qnp1[f], em = emiss[f], fg = Fgeotherm[f];
     if (!finite_val(qnp1)) my_flags |= kFlagNonfiniteIn;
     if (qnp1 < R(0)) my_flags |= kFlagNegativeIn;
@@ -156,30 +256,14 @@ conduction_q_kernel(int num_faces, int nz, const R* __restrict__ z, R dt,
       R annp1 = (qnp1 - arad) / (k1 + brad);
       R bn = (k1 - brad) / (k1 + brad);
       R b1 = R(1) + alpha1 + gamma1 - gamma1 * bn;
-      // Thomas forward sweep, right-hand side formed from Told on the fly.
-      R r1 = gamma1 * (annp1 + ann) + (R(1) - alpha1 - gamma1 + gamma1 * bn) * Told[1] +
-             alpha1 * Told[2];
-      R bet = b1;
-      if (bet == R(0)) { my_flags |= kFlagZeroPivot; break; }
-      u[1] = r1 / bet;
-      for (int j = 2; j <= nz; j++) {
-        R rj;
-        if (j < nz) {
-          const R ga = s_gamma[j], al = s_alpha[j];
-          rj = ga * Told[j - 1] + (R(1) - al - ga) * Told[j] + al * Told[j + 1];
-        } else {
-          const R ga = s_gamma[nz];
-          rj = ga * Told[nz - 1] + (R(1) - ga) * Told[nz] + rhs_bottom;
-        }
-        const R aj = s_a[j];
-        gam[j] = s_c[j - 1] / bet;
-        bet = s_b[j] - aj * gam[j];
-        if (bet == R(0)) { my_flags |= kFlagZeroPivot; break; }
-        u[j] = (rj - aj * u[j - 1]) / bet;
+      R r1 = gamma1 * (annp1 + ann) + (R(1) - alpha1 - gamma1 + gamma1 * bn) * Trow[1] +
+             alpha1 * Trow[2];
+      if (!thomas_cn<R>(nz, Trow, r1, b1, rhs_bottom, s_alpha, s_gamma, s_a, s_b, s_c, u,
+                        gam, nt)) {
+        my_flags |= kFlagZeroPivot;
+        break;
       }
-      if (my_flags & kFlagZeroPivot) break;
-      for (int j = nz - 1; j >= 1; j--) u[j] -= gam[j + 1] * u[j + 1];
-      T0 = R(0.5) * (annp1 + bn * u[1] + u[1]);
+      T0 = R(0.5) * (annp1 + bn * u[nt] + u[nt]);
       if ((T0 > R(1.2) * Tr || T0 < R(0.8) * Tr) && iter < 10) {
         iter++;
         Tr = sqrt(Tr * T0);
@@ -189,21 +273,21 @@ conduction_q_kernel(int num_faces, int nz, const R* __restrict__ z, R dt,
     }
     if (iter >= 9) my_flags |= kFlagPredCorrMax;
     Trow[0] = T0;
-    for (int i = 1; i <= nz; i++) Trow[i] = u[i];
-    Fsurf[f] = -s_k[1] * (u[1] - T0) / z[1];
+    for (int i = 1; i <= nz; i++) Trow[i] = u[i * nt];
+    Fsurf[f] = -s_k[1] * (u[nt] - T0) / z[1];
     for (int i = 0; i <= nz; i++) {
       if (!finite_val(Trow[i])) my_flags |= kFlagNonfiniteOut;
       if (Trow[i] < R(0)) my_flags |= kFlagNegativeOut;
     }
   }
   __syncthreads();
-  stage_out(T_out, tile, f0, rows, w);
+  stage_out(T_out, tile, f0, rows, w, ws);
   if (my_flags) atomicOr(flags, my_flags);
 }
 
 // One step of the prescribed-surface-temperature problem (conductionT.c).
-template <class R, int NZMAX>
-__global__ void __launch_bounds__(kThreads)
+template <class R>
+__global__ void __launch_bounds__(kMaxThreads)
 conduction_t_kernel(int num_faces, int nz, const R* __restrict__ z, R dt,
                     const R* __restrict__ Tsurf, const R* __restrict__ Tsurfp1,
                     const R* T_in, R* T_out,
@@ -212,7 +296,7 @@ conduction_t_kernel(int num_faces, int nz, const R* __restrict__ z, R dt,
                     unsigned* __restrict__ flags) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   R* sh = reinterpret_cast<R*>(smem_raw);
-  const int w = nz + 1;
+  const int w = nz + 1, ws = tile_stride(nz), nt = blockDim.x;
   R* s_k = coeff(sh, 0, nz);
   R* s_alpha = coeff(sh, 1, nz);
   R* s_gamma = coeff(sh, 2, nz);
@@ -220,51 +304,32 @@ conduction_t_kernel(int num_faces, int nz, const R* __restrict__ z, R dt,
   R* s_b = coeff(sh, 4, nz);
   R* s_c = coeff(sh, 5, nz);
   R* tile = sh + 7 * w;
-  if (threadIdx.x == 0)
-    grid_coeffs_t<R>(nz, z, dt, ti, rhoc, s_k, s_alpha, s_gamma, s_a, s_b, s_c);
-  const long long f0 = (long long)blockIdx.x * kThreads;
-  const int rows = (int)min((long long)kThreads, (long long)num_faces - f0);
-  stage_in(tile, T_in, f0, rows, w);
+  R* s_u = tile + nt * ws;
+  R* s_gam = s_u + w * nt;
+  grid_coeffs_t<R>(nz, z, dt, ti, rhoc, s_k, s_alpha, s_gamma, s_a, s_b, s_c);
+  const long long f0 = (long long)blockIdx.x * nt;
+  const int rows = (int)min((long long)nt, (long long)num_faces - f0);
+  stage_in(tile, T_in, f0, rows, w, ws);
   __syncthreads();
   const int t = threadIdx.x;
   unsigned my_flags = 0;
   if (t < rows) {
     const long long f = f0 + t;
-    R* Trow = tile + (long long)t * w;
-    R Told[NZMAX + 1];
-    R u[NZMAX + 1];
-    R gam[NZMAX + 1];
-    for (int i = 1; i <= nz; i++) Told[i] = Trow[i];
+    R* Trow = tile + t * ws;
+    R* u = s_u + t;
+    R* gam = s_gam + t;
     const R ts = Tsurf[f], tsp1 = Tsurfp1[f], fg = Fgeotherm[f];
     if (!finite_val(tsp1)) my_flags |= kFlagNonfiniteIn;
     if (tsp1 < R(0)) my_flags |= kFlagNegativeIn;
     const R alpha1 = s_alpha[1], gamma1 = s_gamma[1];
-    R r1 = alpha1 * Told[2] + (R(1) - alpha1 - gamma1) * Told[1] + gamma1 * (ts + tsp1);
-    R bet = s_b[1];
-    if (bet == R(0)) my_flags |= kFlagZeroPivot;
-    else {
-      u[1] = r1 / bet;
-      const R rhs_bottom = dt / rhoc[nz] * fg / (z[nz] - z[nz - 1]);
-      for (int j = 2; j <= nz; j++) {
-        R rj;
-        if (j < nz) {
-          const R ga = s_gamma[j], al = s_alpha[j];
-          rj = ga * Told[j - 1] + (R(1) - al - ga) * Told[j] + al * Told[j + 1];
-        } else {
-          const R ga = s_gamma[nz];
-          rj = ga * Told[nz - 1] + (R(1) - ga) * Told[nz] + rhs_bottom;
-        }
-        const R aj = s_a[j];
-        gam[j] = s_c[j - 1] / bet;
-        bet = s_b[j] - aj * gam[j];
-        if (bet == R(0)) { my_flags |= kFlagZeroPivot; break; }
-        u[j] = (rj - aj * u[j - 1]) / bet;
-      }
-      if (!(my_flags & kFlagZeroPivot)) {
-        for (int j = nz - 1; j >= 1; j--) u[j] -= gam[j + 1] * u[j + 1];
-        for (int i = 1; i <= nz; i++) Trow[i] = u[i];
-        Fsurf[f] = -s_k[1] * (u[1] - tsp1) / z[1];
-      }
+    R r1 = alpha1 * Trow[2] + (R(1) - alpha1 - gamma1) * Trow[1] + gamma1 * (ts + tsp1);
+    const R rhs_bottom = dt / rhoc[nz] * fg / (z[nz] - z[nz - 1]);
+    if (!thomas_cn<R>(nz, Trow, r1, s_b[1], rhs_bottom, s_alpha, s_gamma, s_a, s_b, s_c, u,
+                      gam, nt)) {
+      my_flags |= kFlagZeroPivot;
+    } else {
+      for (int i = 1; i <= nz; i++) Trow[i] = u[i * nt];
+      Fsurf[f] = -s_k[1] * (u[nt] - tsp1) / z[1];
     }
     for (int i = 1; i <= nz; i++) {
       if (!finite_val(Trow[i])) my_flags |= kFlagNonfiniteOut;
@@ -272,46 +337,15 @@ conduction_t_kernel(int num_faces, int nz, const R* __restrict__ z, R dt,
     }
   }
   __syncthreads();
-  stage_out(T_out, tile, f0, rows, w);
+  stage_out(T_out, tile, f0, rows, w, ws);
   if (my_flags) atomicOr(flags, my_flags);
-}
-
-template <class R>
-size_t smem_bytes(int nz) { return sizeof(R) * (size_t)(nz + 1) * (7 + kThreads); }
-
-template <class R, int NZMAX>
-int launch_q(int num_faces, int nz, const R* z, R dt, const R* Qn, const R* Qnp1,
-             const R* T_in, R* T_out, const R* ti, const R* rhoc, const R* emiss,
-             const R* Fgeotherm, R* Fsurf, unsigned* flags, cudaStream_t s) {
-  size_t sm = smem_bytes<R>(nz);
-  auto k = conduction_q_kernel<R, NZMAX>;
-  FGB_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-  unsigned grid = (unsigned)((num_faces + kThreads - 1) / kThreads);
-  k<<<grid, kThreads, sm, s>>>(num_faces, nz, z, dt, Qn, Qnp1, T_in, T_out, ti, rhoc, emiss,
-                               Fgeotherm, Fsurf, flags);
-  FGB_LAUNCH_CHECK("conduction_q_kernel");
-  return FGB_OK;
-}
-
-template <class R, int NZMAX>
-int launch_t(int num_faces, int nz, const R* z, R dt, const R* Ts, const R* Tsp1,
-             const R* T_in, R* T_out, const R* ti, const R* rhoc, const R* Fgeotherm,
-             R* Fsurf, unsigned* flags, cudaStream_t s) {
-  size_t sm = smem_bytes<R>(nz);
-  auto k = conduction_t_kernel<R, NZMAX>;
-  FGB_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-  unsigned grid = (unsigned)((num_faces + kThreads - 1) / kThreads);
-  k<<<grid, kThreads, sm, s>>>(num_faces, nz, z, dt, Ts, Tsp1, T_in, T_out, ti, rhoc, Fgeotherm,
-                               Fsurf, flags);
-  FGB_LAUNCH_CHECK("conduction_t_kernel");
-  return FGB_OK;
 }
 
 template <class R>
 int check_args(int num_faces, int nz) {
   if (num_faces < 0) { set_error("num_faces must be >= 0"); return FGB_BAD_ARG; }
   if (nz < 2 || nz > 255) { set_error("nz (interior layers) must be in [2, 255], got %d", nz); return FGB_BAD_ARG; }
-  if (smem_bytes<R>(nz) > 227 * 1024) { set_error("nz too large for the staged tile"); return FGB_BAD_ARG; }
+  if (cond_threads<R>(nz) == 0) { set_error("nz too large for the staged tile"); return FGB_BAD_ARG; }
   return FGB_OK;
 }
 
@@ -323,10 +357,15 @@ int dispatch_q(int num_faces, int nz, const R* z, R dt, const R* Qn, const R* Qn
   if (st) return st;
   if (num_faces == 0) return FGB_OK;
   cudaStream_t s = as_stream(stream);
-  if (nz <= 47) return launch_q<R, 47>(num_faces, nz, z, dt, Qn, Qnp1, T_in, T_out, ti, rhoc, emiss, Fgeotherm, Fsurf, flags, s);
-  if (nz <= 63) return launch_q<R, 63>(num_faces, nz, z, dt, Qn, Qnp1, T_in, T_out, ti, rhoc, emiss, Fgeotherm, Fsurf, flags, s);
-  if (nz <= 127) return launch_q<R, 127>(num_faces, nz, z, dt, Qn, Qnp1, T_in, T_out, ti, rhoc, emiss, Fgeotherm, Fsurf, flags, s);
-  return launch_q<R, 255>(num_faces, nz, z, dt, Qn, Qnp1, T_in, T_out, ti, rhoc, emiss, Fgeotherm, Fsurf, flags, s);
+  const int nt = cond_threads<R>(nz);
+  const size_t sm = cond_smem<R>(nz, nt);
+  auto k = conduction_q_kernel<R>;
+  FGB_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  const unsigned grid = (unsigned)((num_faces + nt - 1) / nt);
+  k<<<grid, nt, sm, s>>>(num_faces, nz, z, dt, Qn, Qnp1, T_in, T_out, ti, rhoc, emiss,
+                         Fgeotherm, Fsurf, flags);
+  FGB_LAUNCH_CHECK("conduction_q_kernel");
+  return FGB_OK;
 }
 
 template <class R>
@@ -337,10 +376,15 @@ int dispatch_t(int num_faces, int nz, const R* z, R dt, const R* Ts, const R* Ts
   if (st) return st;
   if (num_faces == 0) return FGB_OK;
   cudaStream_t s = as_stream(stream);
-  if (nz <= 47) return launch_t<R, 47>(num_faces, nz, z, dt, Ts, Tsp1, T_in, T_out, ti, rhoc, Fgeotherm, Fsurf, flags, s);
-  if (nz <= 63) return launch_t<R, 63>(num_faces, nz, z, dt, Ts, Tsp1, T_in, T_out, ti, rhoc, Fgeotherm, Fsurf, flags, s);
-  if (nz <= 127) return launch_t<R, 127>(num_faces, nz, z, dt, Ts, Tsp1, T_in, T_out, ti, rhoc, Fgeotherm, Fsurf, flags, s);
-  return launch_t<R, 255>(num_faces, nz, z, dt, Ts, Tsp1, T_in, T_out, ti, rhoc, Fgeotherm, Fsurf, flags, s);
+  const int nt = cond_threads<R>(nz);
+  const size_t sm = cond_smem<R>(nz, nt);
+  auto k = conduction_t_kernel<R>;
+  FGB_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  const unsigned grid = (unsigned)((num_faces + nt - 1) / nt);
+  k<<<grid, nt, sm, s>>>(num_faces, nz, z, dt, Ts, Tsp1, T_in, T_out, ti, rhoc, Fgeotherm,
+                         Fsurf, flags);
+  FGB_LAUNCH_CHECK("conduction_t_kernel");
+  return FGB_OK;
 }
 
 }  // namespace

@@ -2,19 +2,20 @@
 // 5th-generation tensor cores (tcgen05.mma, FP32 accumulators in tensor
 // memory), for both phases of the panel layout of matvec.cu:
 //
-//   phase B (row tiles): tile t owns 64 operator rows and the panel rows
-//     [p0, p1) (a multiple of 64); panel row l holds 64 BF16 weights W[l, i]
-//     for the tile's rows i and a source index src[l] into S = [Z; X]:
-//       Y[t*64 + i, c] = add[., c] + alpha * sum_l W[l, i] S[src[l], c];
+//   phase B (row tiles): tile t owns R operator rows (R = 64, or 128 for the
+//     re-tiled BF16 panel) and the panel rows [p0, p1) (a multiple of 64);
+//     panel row l holds R BF16 weights W[l, i] for the tile's rows i and a
+//     source index src[l] into S = [Z; X]:
+//       Y[t*R + i, c] = add[., c] + alpha * sum_l W[l, i] S[src[l], c];
 //   phase A (low-rank groups): group g (kz stacked V^T rows, columns
 //     [c0, c0 + n)) is stored transposed, Vt[j, r], and work slice s of an
 //     item (columns [j0, j1) of the group) computes
-//       Z[z0 + 64 s + r, c] (+)= sum_j Vt[j, 64 s + r] X[c0 + j, c].
+//       Z[z0 + 128 s + r, c] (+)= sum_j Vt[j, 128 s + r] X[c0 + j, c].
 //
 // Both are one "gather GEMM" with the reduction over rows l (panel rows, or
 // group columns j): the product is taken transposed so that the long
 // right-hand-side dimension is the MMA's M,
-//   D (M = 128 columns of S, N = 64 output rows) += A (S^T chunk) . B (W chunk),
+//   D (M = 128 columns of S, N = NR output rows) += A (S^T chunk) . B (W chunk),
 // 16 reduction rows per MMA.  Both operands are stored "MN-major" (their
 // contiguous dimension is M resp. N) in the canonical 128-byte-swizzled
 // layout: per 64-element block along M (or N) the reduction rows are
@@ -26,14 +27,15 @@
 // k-step into the same accumulator, hi.hi + lo.hi + hi.lo (the lo.lo term is
 // below 2^-16 relative and dropped).
 //
-// CTA = (tile or work slice, slice of NC = 256 right-hand-side columns), 8
-// warps.  All warps gather the next chunks with cp.async into a 5-stage ring
-// (40 KiB a stage: 64 rows, or 32 rows in split mode); thread 0 issues the
-// MMAs of the current chunk and commits them to the stage's mbarrier, which
-// the producers wait on before they refill that stage.  The accumulators (2
-// x 64 TMEM columns, 128 lanes) are read back with tcgen05.ld (warp w reads
-// lanes 32 (w mod 4) ..) for an epilogue whose stores are coalesced along the
-// right-hand-side columns.
+// CTA = (tile or work slice, slice of NC right-hand-side columns), 8 warps,
+// shapes per mode in TcCfg.  All warps gather the next chunks (CH reduction
+// rows) with cp.async into a ring of stages (up to 200 KiB); thread 0 issues
+// the MMAs of the current chunk and commits them to the stage's mbarrier,
+// which the producers wait on before they refill that stage.  The
+// accumulators (NC / 128 halves of NR TMEM columns, 128 lanes; two sets in
+// split mode) are read back with tcgen05.ld (warp w reads lanes 32 (w mod 4)
+// ..) for an epilogue whose stores are coalesced along the right-hand-side
+// columns.
 //
 // Every mbarrier wait is bounded (about 2 s of global time); a wait that
 // runs out sets FGB_FLAG_DEVICE_TIMEOUT in the caller's flag word and the
@@ -199,7 +201,8 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
 // Per-mode shapes.  NR = output rows per CTA (MMA N), NC = right-hand-side
 // columns per CTA (a multiple of the MMA M = 128), CH = reduction rows per
 // stage.  Phase A computes 128 rows of Z per CTA, so that each gathered X
-// row feeds twice the flops; phase B keeps the 64-row tiles of the panel.
+// row feeds twice the flops; phase B runs 128-row tiles for the plain BF16
+// product (the re-tiled panel) and the 64-row tiles for the split one.
 // Split mode keeps 64 accumulator values per thread for the compensated
 // drains (phase A: NC = 128).
 template <int MODE, bool SPLIT, int NR_ = (MODE == kModeA ? 128 : 64)>
@@ -219,8 +222,8 @@ struct TcCfg {
   static constexpr int TMEM_COLS = SETS * HALVES * NR;
   static constexpr int SEGS = HALVES * NR / 64;      // 64-column TMEM segments per set
   static constexpr int PPR = NC / 8;                 // 16-byte pieces per S row
-  static constexpr int RPI = 32 / PPR;               // S rows per warp instruction
-  static constexpr int SROWS = CH / (8 * RPI);       // S rows per thread and chunk
+  static constexpr int RPP = kTcThreads / PPR;      // S rows per pass of the CTA
+  static constexpr int SROWS = CH / RPP;             // S rows per thread and chunk
   // instruction descriptor, kind::f16: D FP32, A and B BF16, both MN-major,
   // N = NR, M = 128
   static constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | (1u << 15) |
@@ -314,9 +317,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gather_gemm(TcArgs a) {
   auto s_at = [&](int st, int part) {
     return sbase + st * STAGE + Cfg::PARTS * WB + part * SB;
   };
-  // S rows handled by this thread: k = (warp * RPI + lane / PPR) + 8 RPI j
-  const int srow0 = warp * Cfg::RPI + lane / Cfg::PPR;
-  const int spiece = lane % Cfg::PPR;
+  // S rows handled by this thread: k = tid / PPR + RPP j, 16-byte piece
+  // tid % PPR of each (consecutive threads on consecutive pieces of a row)
+  const int srow0 = tid / Cfg::PPR;
+  const int spiece = tid % Cfg::PPR;
   // phase B: source rows of this thread's S rows of chunk c (through src[]),
   // fetched one chunk ahead so that the dependent index load does not stall
   // the copies
@@ -325,7 +329,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gather_gemm(TcArgs a) {
   auto fetch_src = [&](int c, int (&dst)[RPW]) {
 #pragma unroll
     for (int j = 0; j < RPW; j++) {
-      const long long l = r_first + (long long)c * CH + srow0 + 8 * Cfg::RPI * j;
+      const long long l = r_first + (long long)c * CH + srow0 + Cfg::RPP * j;
       dst[j] = (MODE == kModeB && c < nch && l < r_end) ? __ldg(a.src + l) : 0;
     }
   };
@@ -349,7 +353,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gather_gemm(TcArgs a) {
     const int b = spiece >> 3, q = spiece & 7;
 #pragma unroll
     for (int j = 0; j < RPW; j++) {
-      const int k = srow0 + 8 * Cfg::RPI * j;
+      const int k = srow0 + Cfg::RPP * j;
       const long long l = l0 + k;
       const bool okr = l < r_end;
       const __nv_bfloat16* rh;

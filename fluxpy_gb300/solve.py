@@ -235,9 +235,15 @@ def _auto_chunk(FF, N, K, fp32_z=True):
     free += torch.cuda.memory_reserved() - torch.cuda.memory_allocated()
     # per column: E, B, R, D, Y, X (FP32), X hi/lo (BF16); Z hi/lo (BF16),
     # and Z in FP32 for the CUDA-core and mma.sync products
-    per_col = N * (6 * 4 + 2 * 2) + max(FF._num_zrows, 1) * (8 if fp32_z else 4)
-    c = int(0.5 * free / per_col) // 8 * 8
-    return max(8, min(K, c))
+    # (+ the unpermuted result); a fixed reserve for the allocator's slack
+    per_col = N * (7 * 4 + 2 * 2) + max(FF._num_zrows, 1) * (8 if fp32_z else 4)
+    c = int(0.85 * max(free - (6 << 30), 0) / per_col) // 8 * 8
+    c = max(8, min(K, c))
+    if c < K:
+        # equal chunks (a narrow last chunk runs the products at low width)
+        n = -(-K // c)
+        c = (-(-K // n) + 7) // 8 * 8
+    return c
 
 
 def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_iter=200,

@@ -28,7 +28,7 @@ def test_oracle_reproduces_golden_files():
     sc.check_against_golden(prof, surf, golden)
 
 
-ZFAC = {40: 1.0817, 60: 1.05, 100: 1.03}
+ZFAC = {40: 1.0817, 60: 1.05, 100: 1.03, 255: 1.01}
 
 
 def _random_case(rng, n, nz):

@@ -10,9 +10,9 @@
 //     without FMA contraction (this file is compiled with -fmad=false);
 //   * the temperature rows (num_faces x (nz+1), the reference's row-major
 //     layout) are staged through shared memory with coalesced loads/stores;
-//     the sweep reads the pre-step profile from there and keeps its own
-//     arrays (u, gam) in shared memory too, so no per-thread local arrays
-//     spill past L1; the facets per CTA (32..128) follow from nz;
+//     the sweep reads the pre-step profile from there (its own arrays u,
+//     gam stay per-thread, so the shared layout is small and many warps
+//     share an SM); the facets per CTA (32..128) follow from nz;
 //   * the linearised radiative boundary (predictor-corrector, at most 10
 //     redos, conductionQ.c:103-172) and the Thomas solve are fused: the
 //     right-hand side is formed on the fly during the forward sweep from the
@@ -93,18 +93,17 @@ __device__ void grid_coeffs_t(int nz, const R* z, R dt, const R* ti, const R* rh
 constexpr int kMaxThreads = 128;
 constexpr size_t kSmemBudget = 227 * 1024;  // the per-CTA opt-in maximum
 
-// Shared layout, all of element type R:
-//   7 coefficient arrays of nz+1 (k, alpha, gamma, a, b, c, misc);
-//   the staged temperature tile, nt rows of stride ws = (nz+1)|1 (odd, so
-//   that the threads of a warp reading element i of their own rows hit
-//   distinct banks);
-//   u and gam of the Thomas solve, layer-major ((nz+1) x nt: layer j of
-//   thread t at j*nt + t, consecutive threads on consecutive words).
+// Shared layout, all of element type R: 7 coefficient arrays of nz+1 (k,
+// alpha, gamma, a, b, c, misc), then the staged temperature tile, nt rows
+// of stride ws = (nz+1)|1 (odd, so that the threads of a warp reading
+// element i of their own rows hit distinct banks).  The sweep's own arrays
+// (u, gam) are per-thread local arrays: the shared layout stays small, so
+// that many CTAs (warps) share an SM and hide the sweep's dependent chain.
 __host__ __device__ inline int tile_stride(int nz) { return (nz + 1) | 1; }
 
 template <class R>
 size_t cond_smem(int nz, int nt) {
-  return sizeof(R) * ((size_t)7 * (nz + 1) + (size_t)nt * tile_stride(nz) + (size_t)2 * (nz + 1) * nt);
+  return sizeof(R) * ((size_t)7 * (nz + 1) + (size_t)nt * tile_stride(nz));
 }
 
 // Facets per CTA: the largest multiple of 32 (at most 128) whose shared
@@ -120,23 +119,23 @@ template <class R>
 __device__ inline R* coeff(R* sh, int which, int nz) { return sh + which * (nz + 1); }
 
 // Row-major global rows [f0, f0+rows) x w  <->  tile rows of stride ws.
-template <class R>
-__device__ void stage_in(R* tile, const R* T, long long f0, int rows, int w, int ws) {
-  const R* src = T + f0 * w;
+// Thread q of the CTA visits elements q, q + nt, ... of the rows (coalesced
+// in global memory); its (row, column) advances by (nt / w, nt % w) per
+// step, one division per thread.
+template <class R, bool IN>
+__device__ void stage(R* tile, R* T, long long f0, int rows, int w, int ws) {
+  const int nt = blockDim.x;
   const int n = rows * w;
-  for (int q = threadIdx.x; q < n; q += blockDim.x) {
-    const int r = q / w;
-    tile[r * ws + (q - r * w)] = src[q];
-  }
-}
-
-template <class R>
-__device__ void stage_out(R* T, const R* tile, long long f0, int rows, int w, int ws) {
-  R* dst = T + f0 * w;
-  const int n = rows * w;
-  for (int q = threadIdx.x; q < n; q += blockDim.x) {
-    const int r = q / w;
-    dst[q] = tile[r * ws + (q - r * w)];
+  const int dr = nt / w, dc = nt - dr * w;
+  int q = threadIdx.x;
+  int r = q / w, c = q - r * w;
+  R* g = T + f0 * w;
+  for (; q < n; q += nt) {
+    if (IN) tile[r * ws + c] = g[q];
+    else g[q] = tile[r * ws + c];
+    r += dr;
+    c += dc;
+    if (c >= w) { c -= w; r++; }
   }
 }
 
@@ -163,16 +162,16 @@ template <> struct Pivot<float> {
 // main-diagonal entry b1 (facet dependent under the radiative boundary).
 // The right-hand side is formed on the fly from the pre-step profile Trow
 // (crank-nicolson explicit half, conductionQ.c:123-137 / conductionT.c:66-77).
-// u and gam are layer-major with stride nt. Returns false on a zero pivot.
+// Returns false on a zero pivot.
 template <class R>
 __device__ bool thomas_cn(int nz, const R* Trow, R r1, R b1, R rhs_bottom,
                           const R* s_alpha, const R* s_gamma, const R* s_a, const R* s_b,
-                          const R* s_c, R* u, R* gam, int nt) {
+                          const R* s_c, R* u, R* gam) {
   R bet = b1;
   if (bet == R(0)) return false;
   Pivot<R> pv(bet);
   R uprev = pv.div(r1);
-  u[nt] = uprev;
+  u[1] = uprev;
   R tm1 = Trow[1], t0 = Trow[2];
   for (int j = 2; j <= nz; j++) {
     R rj;
@@ -188,23 +187,23 @@ __device__ bool thomas_cn(int nz, const R* Trow, R r1, R b1, R rhs_bottom,
     }
     const R aj = s_a[j];
     const R g = pv.div(s_c[j - 1]);
-    gam[j * nt] = g;
+    gam[j] = g;
     bet = s_b[j] - aj * g;
     if (bet == R(0)) return false;
     pv = Pivot<R>(bet);
     uprev = pv.div(rj - aj * uprev);
-    u[j * nt] = uprev;
+    u[j] = uprev;
   }
   R unext = uprev;
   for (int j = nz - 1; j >= 1; j--) {
-    unext = u[j * nt] - gam[(j + 1) * nt] * unext;
-    u[j * nt] = unext;
+    unext = u[j] - gam[j + 1] * unext;
+    u[j] = unext;
   }
   return true;
 }
 
 // One step of the radiative-flux boundary problem for every facet.
-template <class R>
+template <class R, int NZMAX>
 __global__ void __launch_bounds__(kMaxThreads)
 conduction_q_kernel(int num_faces, int nz, const R* __restrict__ z, R dt,
                     const R* __restrict__ Qn, const R* __restrict__ Qnp1,
@@ -223,13 +222,11 @@ conduction_q_kernel(int num_faces, int nz, const R* __restrict__ z, R dt,
   R* s_c = coeff(sh, 5, nz);
   R* s_misc = coeff(sh, 6, nz);  // [0] = k1
   R* tile = sh + 7 * w;
-  R* s_u = tile + nt * ws;
-  R* s_gam = s_u + w * nt;
 
   grid_coeffs_q<R>(nz, z, dt, ti, rhoc, s_k, s_alpha, s_gamma, s_a, s_b, s_c, &s_misc[0]);
   const long long f0 = (long long)blockIdx.x * nt;
   const int rows = (int)min((long long)nt, (long long)num_faces - f0);
-  stage_in(tile, T_in, f0, rows, w, ws);
+  stage<R, true>(tile, const_cast<R*>(T_in), f0, rows, w, ws);
   __syncthreads();
 
   const int t = threadIdx.x;
@@ -237,8 +234,8 @@ conduction_q_kernel(int num_faces, int nz, const R* __restrict__ z, R dt,
   if (t < rows) {
     const long long f = f0 + t;
     R* Trow = tile + t * ws;
-    R* u = s_u + t;
-    R* gam = s_gam + t;
+    R u[NZMAX + 1];
+    R gam[NZMAX + 1];
     const R qn = Qn[f], qnp1 = Qnp1[f], em = emiss[f], fg = Fgeotherm[f];
     if (!finite_val(qnp1)) my_flags |= kFlagNonfiniteIn;
     if (qnp1 < R(0)) my_flags |= kFlagNegativeIn;
@@ -259,11 +256,11 @@ conduction_q_kernel(int num_faces, int nz, const R* __restrict__ z, R dt,
       R r1 = gamma1 * (annp1 + ann) + (R(1) - alpha1 - gamma1 + gamma1 * bn) * Trow[1] +
              alpha1 * Trow[2];
       if (!thomas_cn<R>(nz, Trow, r1, b1, rhs_bottom, s_alpha, s_gamma, s_a, s_b, s_c, u,
-                        gam, nt)) {
+                        gam)) {
         my_flags |= kFlagZeroPivot;
         break;
       }
-      T0 = R(0.5) * (annp1 + bn * u[nt] + u[nt]);
+      T0 = R(0.5) * (annp1 + bn * u[1] + u[1]);
       if ((T0 > R(1.2) * Tr || T0 < R(0.8) * Tr) && iter < 10) {
         iter++;
         Tr = sqrt(Tr * T0);
@@ -273,20 +270,20 @@ conduction_q_kernel(int num_faces, int nz, const R* __restrict__ z, R dt,
     }
     if (iter >= 9) my_flags |= kFlagPredCorrMax;
     Trow[0] = T0;
-    for (int i = 1; i <= nz; i++) Trow[i] = u[i * nt];
-    Fsurf[f] = -s_k[1] * (u[nt] - T0) / z[1];
+    for (int i = 1; i <= nz; i++) Trow[i] = u[i];
+    Fsurf[f] = -s_k[1] * (u[1] - T0) / z[1];
     for (int i = 0; i <= nz; i++) {
       if (!finite_val(Trow[i])) my_flags |= kFlagNonfiniteOut;
       if (Trow[i] < R(0)) my_flags |= kFlagNegativeOut;
     }
   }
   __syncthreads();
-  stage_out(T_out, tile, f0, rows, w, ws);
+  stage<R, false>(tile, T_out, f0, rows, w, ws);
   if (my_flags) atomicOr(flags, my_flags);
 }
 
 // One step of the prescribed-surface-temperature problem (conductionT.c).
-template <class R>
+template <class R, int NZMAX>
 __global__ void __launch_bounds__(kMaxThreads)
 conduction_t_kernel(int num_faces, int nz, const R* __restrict__ z, R dt,
                     const R* __restrict__ Tsurf, const R* __restrict__ Tsurfp1,
@@ -304,20 +301,18 @@ conduction_t_kernel(int num_faces, int nz, const R* __restrict__ z, R dt,
   R* s_b = coeff(sh, 4, nz);
   R* s_c = coeff(sh, 5, nz);
   R* tile = sh + 7 * w;
-  R* s_u = tile + nt * ws;
-  R* s_gam = s_u + w * nt;
   grid_coeffs_t<R>(nz, z, dt, ti, rhoc, s_k, s_alpha, s_gamma, s_a, s_b, s_c);
   const long long f0 = (long long)blockIdx.x * nt;
   const int rows = (int)min((long long)nt, (long long)num_faces - f0);
-  stage_in(tile, T_in, f0, rows, w, ws);
+  stage<R, true>(tile, const_cast<R*>(T_in), f0, rows, w, ws);
   __syncthreads();
   const int t = threadIdx.x;
   unsigned my_flags = 0;
   if (t < rows) {
     const long long f = f0 + t;
     R* Trow = tile + t * ws;
-    R* u = s_u + t;
-    R* gam = s_gam + t;
+    R u[NZMAX + 1];
+    R gam[NZMAX + 1];
     const R ts = Tsurf[f], tsp1 = Tsurfp1[f], fg = Fgeotherm[f];
     if (!finite_val(tsp1)) my_flags |= kFlagNonfiniteIn;
     if (tsp1 < R(0)) my_flags |= kFlagNegativeIn;
@@ -325,11 +320,11 @@ conduction_t_kernel(int num_faces, int nz, const R* __restrict__ z, R dt,
     R r1 = alpha1 * Trow[2] + (R(1) - alpha1 - gamma1) * Trow[1] + gamma1 * (ts + tsp1);
     const R rhs_bottom = dt / rhoc[nz] * fg / (z[nz] - z[nz - 1]);
     if (!thomas_cn<R>(nz, Trow, r1, s_b[1], rhs_bottom, s_alpha, s_gamma, s_a, s_b, s_c, u,
-                      gam, nt)) {
+                      gam)) {
       my_flags |= kFlagZeroPivot;
     } else {
-      for (int i = 1; i <= nz; i++) Trow[i] = u[i * nt];
-      Fsurf[f] = -s_k[1] * (u[nt] - tsp1) / z[1];
+      for (int i = 1; i <= nz; i++) Trow[i] = u[i];
+      Fsurf[f] = -s_k[1] * (u[1] - tsp1) / z[1];
     }
     for (int i = 1; i <= nz; i++) {
       if (!finite_val(Trow[i])) my_flags |= kFlagNonfiniteOut;
@@ -337,8 +332,38 @@ conduction_t_kernel(int num_faces, int nz, const R* __restrict__ z, R dt,
     }
   }
   __syncthreads();
-  stage_out(T_out, tile, f0, rows, w, ws);
+  stage<R, false>(tile, T_out, f0, rows, w, ws);
   if (my_flags) atomicOr(flags, my_flags);
+}
+
+template <class R, int NZMAX>
+int launch_q(int num_faces, int nz, const R* z, R dt, const R* Qn, const R* Qnp1,
+             const R* T_in, R* T_out, const R* ti, const R* rhoc, const R* emiss,
+             const R* Fgeotherm, R* Fsurf, unsigned* flags, cudaStream_t s) {
+  const int nt = cond_threads<R>(nz);
+  const size_t sm = cond_smem<R>(nz, nt);
+  auto k = conduction_q_kernel<R, NZMAX>;
+  FGB_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  const unsigned grid = (unsigned)((num_faces + nt - 1) / nt);
+  k<<<grid, nt, sm, s>>>(num_faces, nz, z, dt, Qn, Qnp1, T_in, T_out, ti, rhoc, emiss,
+                         Fgeotherm, Fsurf, flags);
+  FGB_LAUNCH_CHECK("conduction_q_kernel");
+  return FGB_OK;
+}
+
+template <class R, int NZMAX>
+int launch_t(int num_faces, int nz, const R* z, R dt, const R* Ts, const R* Tsp1,
+             const R* T_in, R* T_out, const R* ti, const R* rhoc, const R* Fgeotherm,
+             R* Fsurf, unsigned* flags, cudaStream_t s) {
+  const int nt = cond_threads<R>(nz);
+  const size_t sm = cond_smem<R>(nz, nt);
+  auto k = conduction_t_kernel<R, NZMAX>;
+  FGB_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  const unsigned grid = (unsigned)((num_faces + nt - 1) / nt);
+  k<<<grid, nt, sm, s>>>(num_faces, nz, z, dt, Ts, Tsp1, T_in, T_out, ti, rhoc, Fgeotherm,
+                         Fsurf, flags);
+  FGB_LAUNCH_CHECK("conduction_t_kernel");
+  return FGB_OK;
 }
 
 template <class R>
@@ -357,15 +382,10 @@ int dispatch_q(int num_faces, int nz, const R* z, R dt, const R* Qn, const R* Qn
   if (st) return st;
   if (num_faces == 0) return FGB_OK;
   cudaStream_t s = as_stream(stream);
-  const int nt = cond_threads<R>(nz);
-  const size_t sm = cond_smem<R>(nz, nt);
-  auto k = conduction_q_kernel<R>;
-  FGB_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-  const unsigned grid = (unsigned)((num_faces + nt - 1) / nt);
-  k<<<grid, nt, sm, s>>>(num_faces, nz, z, dt, Qn, Qnp1, T_in, T_out, ti, rhoc, emiss,
-                         Fgeotherm, Fsurf, flags);
-  FGB_LAUNCH_CHECK("conduction_q_kernel");
-  return FGB_OK;
+  if (nz <= 47) return launch_q<R, 47>(num_faces, nz, z, dt, Qn, Qnp1, T_in, T_out, ti, rhoc, emiss, Fgeotherm, Fsurf, flags, s);
+  if (nz <= 63) return launch_q<R, 63>(num_faces, nz, z, dt, Qn, Qnp1, T_in, T_out, ti, rhoc, emiss, Fgeotherm, Fsurf, flags, s);
+  if (nz <= 127) return launch_q<R, 127>(num_faces, nz, z, dt, Qn, Qnp1, T_in, T_out, ti, rhoc, emiss, Fgeotherm, Fsurf, flags, s);
+  return launch_q<R, 255>(num_faces, nz, z, dt, Qn, Qnp1, T_in, T_out, ti, rhoc, emiss, Fgeotherm, Fsurf, flags, s);
 }
 
 template <class R>
@@ -376,15 +396,10 @@ int dispatch_t(int num_faces, int nz, const R* z, R dt, const R* Ts, const R* Ts
   if (st) return st;
   if (num_faces == 0) return FGB_OK;
   cudaStream_t s = as_stream(stream);
-  const int nt = cond_threads<R>(nz);
-  const size_t sm = cond_smem<R>(nz, nt);
-  auto k = conduction_t_kernel<R>;
-  FGB_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-  const unsigned grid = (unsigned)((num_faces + nt - 1) / nt);
-  k<<<grid, nt, sm, s>>>(num_faces, nz, z, dt, Ts, Tsp1, T_in, T_out, ti, rhoc, Fgeotherm,
-                         Fsurf, flags);
-  FGB_LAUNCH_CHECK("conduction_t_kernel");
-  return FGB_OK;
+  if (nz <= 47) return launch_t<R, 47>(num_faces, nz, z, dt, Ts, Tsp1, T_in, T_out, ti, rhoc, Fgeotherm, Fsurf, flags, s);
+  if (nz <= 63) return launch_t<R, 63>(num_faces, nz, z, dt, Ts, Tsp1, T_in, T_out, ti, rhoc, Fgeotherm, Fsurf, flags, s);
+  if (nz <= 127) return launch_t<R, 127>(num_faces, nz, z, dt, Ts, Tsp1, T_in, T_out, ti, rhoc, Fgeotherm, Fsurf, flags, s);
+  return launch_t<R, 255>(num_faces, nz, z, dt, Ts, Tsp1, T_in, T_out, ti, rhoc, Fgeotherm, Fsurf, flags, s);
 }
 
 }  // namespace

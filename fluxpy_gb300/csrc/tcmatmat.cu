@@ -205,18 +205,35 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
 // product (the re-tiled panel) and the 64-row tiles for the split one.
 // Split mode keeps 64 accumulator values per thread for the compensated
 // drains (phase A: NC = 128).
+// CTAS = CTAs per SM the shape is built for.  The plain products run four
+// (NC = 128, CH = 32, a 3-stage ring of 16 KiB stages): each CTA's loop
+// waits, per chunk, for its copies and for the previous chunk's MMAs, and
+// per work item for its TMEM allocation and epilogue; the other CTAs fill
+// those waits.  At 522k facets and 1,024 columns this measured 44 ms for
+// phase B and 31 ms for phase A, against 53 and 51 ms for one CTA per SM
+// with NC = 256, CH = 64 and a 4-stage ring (the median phase-A group has
+// 62 columns: one or two chunks per work item).  The split products keep one
+// CTA per SM: their compensated sums take ~225 registers per thread.
 template <int MODE, bool SPLIT, int NR_ = (MODE == kModeA ? 128 : 64)>
 struct TcCfg {
   static constexpr int NR = NR_;
-  static constexpr int NC = (MODE == kModeA && SPLIT) ? 128 : 256;
-  static constexpr int CH = SPLIT ? 32 : 64;
+  static constexpr int NC = SPLIT ? (MODE == kModeA ? 128 : 256) : 128;
+  static constexpr int CH = 32;
+  static constexpr int CTAS = SPLIT ? 1 : 4;
   static constexpr int PARTS = SPLIT ? 2 : 1;
   static constexpr int WB = CH * NR * 2;             // W bytes per stage and part
   static constexpr int SB = CH * NC * 2;             // S bytes per stage and part
   static constexpr int BLK = CH * 128;               // one 64-element block (W or S)
   static constexpr int STAGE = PARTS * (WB + SB);
-  static constexpr int STAGES = (200 * 1024) / STAGE < 6 ? (200 * 1024) / STAGE : 6;
-  static constexpr int SMEM = STAGES * STAGE + 1024;
+  static constexpr int RING = (200 * 1024) / CTAS;   // ring bytes per CTA
+  static constexpr int STAGES = RING / STAGE < 6 ? RING / STAGE : 6;
+  // dynamic shared memory: the ring, 1 KiB for alignment, and at least a
+  // third of the SM's 228 KiB when TMEM allows only two CTAs per SM (more
+  // would wait in tcgen05.alloc)
+  static constexpr int SMEM_RING = STAGES * STAGE + 1024;
+  static constexpr int MAX_RES = 512 / ((SPLIT ? 2 : 1) * (NC / 128) * NR);
+  static constexpr int SMEM_MIN = 233472 / (MAX_RES + 1) + 16;
+  static constexpr int SMEM = SMEM_RING > SMEM_MIN ? SMEM_RING : SMEM_MIN;
   static constexpr int HALVES = NC / 128;            // accumulators per set
   static constexpr int SETS = SPLIT ? 2 : 1;
   static constexpr int TMEM_COLS = SETS * HALVES * NR;
@@ -229,7 +246,9 @@ struct TcCfg {
   static constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | (1u << 15) |
                                     (1u << 16) | ((uint32_t)(NR >> 3) << 17) |
                                     ((uint32_t)(128 >> 4) << 24);
-  static_assert(TMEM_COLS == 128 || TMEM_COLS == 256, "TMEM allocation");
+  static_assert(TMEM_COLS == 64 || TMEM_COLS == 128 || TMEM_COLS == 256, "TMEM allocation");
+  static_assert(STAGES >= 2, "ring of at least two stages");
+  static_assert(CTAS * TMEM_COLS <= 512, "TMEM of the CTAs of one SM");
   static_assert(SPLIT ? SEGS == 2 : true, "split drains: one 64-row segment per warp");
 };
 
@@ -242,7 +261,8 @@ __device__ __forceinline__ void mma_bf16_tc_n(uint32_t dtmem, uint64_t adesc, ui
 }
 
 template <int MODE, bool SPLIT, int NRT>
-__global__ void __launch_bounds__(kTcThreads, 1) tc_gather_gemm(TcArgs a) {
+__global__ void __launch_bounds__(kTcThreads, (TcCfg<MODE, SPLIT, NRT>::CTAS))
+tc_gather_gemm(TcArgs a) {
   using Cfg = TcCfg<MODE, SPLIT, NRT>;
   constexpr int NR = Cfg::NR, NC = Cfg::NC, CH = Cfg::CH, WB = Cfg::WB, SB = Cfg::SB;
   constexpr int BLK = Cfg::BLK, S = Cfg::STAGES, STAGE = Cfg::STAGE;

@@ -342,10 +342,12 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
         torch.cuda.synchronize()
         return a.elapsed_time(b) / reps
 
-    def tc_a(split):
+    def tc_a(split, rows64=True):
         # phase A as the solver runs it: whole-group work items, Z written
-        # directly as BF16 (hi, and lo for the split product)
-        _lib.call("fgb_tc_phase_a_bf16", C.byref(FF._desc_tc), _lib.ptr(tc["vt_hi"]),
+        # directly as BF16 (hi, and lo for the split product, on 64-row work
+        # slices)
+        dsc = FF._desc_tc64 if split and rows64 else FF._desc_tc
+        _lib.call("fgb_tc_phase_a_bf16", C.byref(dsc), _lib.ptr(tc["vt_hi"]),
                   _lib.ptr(tc["vt_lo"]) if split else None, _lib.ptr(xh),
                   _lib.ptr(xl) if split else None, _lib.ptr(zh), _lib.ptr(zl) if split else None,
                   K, _lib.ptr(flags), st())
@@ -375,6 +377,7 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
           "phaseA_tc_split": t_events(lambda: tc_a(True)),
           "phaseB_tc_split": t_events(lambda: tc_b(True))}
     ms_tma = t_events(tc_b_tma, 3)
+    ms_a128 = t_events(lambda: tc_a(True, rows64=False), 3)
     ms_b64 = t_events(lambda: tc_b(False, rows128=False), 3)
     # the FP32 kernels write Z in FP32 (the BF16 sources are not needed)
     del xh, xl, zh, zl, sh, sl
@@ -430,6 +433,7 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
                            "algorithmic_flops": fl, "ms_per_launch": t_ms, "fp32_tflops": tfl}
     out["kernel_ms"] = {"columns": K, **ms, "phaseB_tc_tma_gather_variant": ms_tma,
                         "phaseB_tc_64row_tiles": ms_b64,
+                        "phaseA_tc_split_128row_slices": ms_a128,
                         "per_step_ms": per_step,
                         "tflops": {k: work[k][1] / (ms[k] * 1e-3) / 1e12 for k in ms}}
     del X32, Z32, Y, Ek

@@ -162,7 +162,7 @@ class fgb_op_desc(C.Structure):
         ("num_tiles", C.c_longlong), ("N", C.c_longlong), ("num_zrows", C.c_longlong),
         ("max_group_tiles", C.c_int), ("g_kzp", C.c_void_p), ("g_vtoff", C.c_void_p),
         ("a_woff", C.c_void_p), ("num_work", C.c_longlong), ("panel_rows", C.c_longlong),
-        ("tile_rows", C.c_int),
+        ("tile_rows", C.c_int), ("slice_rows", C.c_int),
     ]
 
 
@@ -565,6 +565,10 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         # whole group (every CTA owns its output rows: no atomics, no FP32 Z)
         tg_woff = np.zeros(ng + 1, np.int64)
         np.cumsum(g_kzp // TC_A_ROWS, out=tg_woff[1:])
+        # ... and, for the split products, 64-row slices (two CTAs per SM);
+        # only slices that hold rows of the group
+        tg_woff64 = np.zeros(ng + 1, np.int64)
+        np.cumsum((g_kz + 63) // 64, out=tg_woff64[1:])
         tsl = g_kzp // 64
         tjb = (g_n + 63) // 64
         tcnt = tsl * tjb
@@ -719,7 +723,8 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
             a_woff=d(a_woff, np.int64), a_woff_tc=d(a_woff_tc, np.int64))
         self._dev_tc = dict(
             a_grp=d(np.arange(ng), np.int32), a_j0=d(np.zeros(ng), np.int32),
-            a_j1=d(g_n, np.int32), a_excl=d(np.ones(ng), np.uint8), a_woff=d(tg_woff, np.int64))
+            a_j1=d(g_n, np.int32), a_excl=d(np.ones(ng), np.uint8), a_woff=d(tg_woff, np.int64),
+            a_woff64=d(tg_woff64, np.int64))
         self._build_dev = dict(
             vt_g=d(vt_g, np.int32), vt_s=d(vt_s, np.int32), vt_j=d(vt_j, np.int32),
             vr_src=d(vr_src, np.int64), vr_dst=d(vr_dst, np.int64), vr_n=d(vr_n, np.int32),
@@ -733,6 +738,7 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         self._num_pairs = int(all_p0.size)
         self._desc = self._make_desc(int(a_grp.size), ntiles, max_gt, int(a_woff[-1]))
         self._desc_tc = self._make_desc_tc()
+        self._desc_tc64 = self._make_desc_tc(64)
         self._desc_tc_items = self._make_desc_tc_items()
         self._lr_blocks = lr
         self._lr_u, self._lr_v = lr_u, lr_v
@@ -767,13 +773,17 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         desc.num_work = int(self._dev["a_woff_tc"][-1].item())
         return desc
 
-    def _make_desc_tc(self):
-        """The descriptor with one phase-A work item per whole group."""
+    def _make_desc_tc(self, slice_rows=TC_A_ROWS):
+        """The descriptor with one phase-A work item per whole group, in work
+        slices of TC_A_ROWS rows, or of 64 rows (split products)."""
         desc = fgb_op_desc.from_buffer_copy(self._desc)
-        for key in ("a_grp", "a_j0", "a_j1", "a_excl", "a_woff"):
+        woff = "a_woff" if slice_rows == TC_A_ROWS else "a_woff64"
+        for key in ("a_grp", "a_j0", "a_j1", "a_excl"):
             setattr(desc, key, self._dev_tc[key].data_ptr())
+        desc.a_woff = self._dev_tc[woff].data_ptr()
         desc.num_items = int(self._dev_tc["a_grp"].numel()) if self._num_zrows > 0 else 0
-        desc.num_work = int(self._dev_tc["a_woff"][-1].item())
+        desc.num_work = int(self._dev_tc[woff][-1].item())
+        desc.slice_rows = slice_rows
         return desc
 
     # -- device products --------------------------------------------------
@@ -1084,8 +1094,9 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         flags = _lib.ptr(self.device_flags())
         _lib.call("fgb_split_bf16", _lib.ptr(X), _lib.ptr(xh), _lib.ptr(xl), N * K, st)
         if self._num_zrows > 0:
-            # phase A writes the hi / lo BF16 parts of Z directly
-            _lib.call("fgb_tc_phase_a_bf16", C.byref(self._desc_tc), _lib.ptr(tc["vt_hi"]),
+            # phase A writes the hi / lo BF16 parts of Z directly (64-row
+            # work slices: two CTAs per SM)
+            _lib.call("fgb_tc_phase_a_bf16", C.byref(self._desc_tc64), _lib.ptr(tc["vt_hi"]),
                       _lib.ptr(tc["vt_lo"]), _lib.ptr(xh), _lib.ptr(xl), _lib.ptr(zh),
                       _lib.ptr(zl), K, flags, st)
         _lib.call("fgb_tc_phase_b", C.byref(self._desc), _lib.ptr(tc["w_hi"]),
@@ -1244,6 +1255,7 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         st["_root_cache"] = None
         st["_desc"] = None
         st["_desc_tc"] = None
+        st["_desc_tc64"] = None
         st["_desc_tc_items"] = None
         st["_desc128"] = None
         st["_dev128"] = None
@@ -1280,6 +1292,7 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
                                      int(self.stats["max_group_tiles"]),
                                      int(self._dev["a_woff"][-1].item()))
         self._desc_tc = self._make_desc_tc()
+        self._desc_tc64 = self._make_desc_tc(64)
         self._desc_tc_items = self._make_desc_tc_items()
 
     # -- leaf data for the Python block objects --------------------------

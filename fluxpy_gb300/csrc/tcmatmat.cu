@@ -203,8 +203,8 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
 // stage.  Phase A computes 128 rows of Z per CTA, so that each gathered X
 // row feeds twice the flops; phase B runs 128-row tiles for the plain BF16
 // product (the re-tiled panel) and the 64-row tiles for the split one.
-// Split mode keeps 64 accumulator values per thread for the compensated
-// drains (phase A: NC = 128).
+// Split mode keeps SEGS x 32 compensated sums per thread (32 for 64-row
+// tiles or slices, 64 for 128-row ones).
 // CTAS = CTAs per SM the shape is built for.  The plain products run four
 // (NC = 128, CH = 32, a 3-stage ring of 16 KiB stages): each CTA's loop
 // waits, per chunk, for its copies and for the previous chunk's MMAs, and
@@ -212,14 +212,15 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
 // those waits.  At 522k facets and 1,024 columns this measured 44 ms for
 // phase B and 31 ms for phase A, against 53 and 51 ms for one CTA per SM
 // with NC = 256, CH = 64 and a 4-stage ring (the median phase-A group has
-// 62 columns: one or two chunks per work item).  The split products keep one
-// CTA per SM: their compensated sums take ~225 registers per thread.
+// 62 columns: one or two chunks per work item).  The split products run two
+// CTAs per SM on 64-row tiles / slices (~120 registers per thread) and one
+// on 128-row slices (~225: 64 compensated sums per thread).
 template <int MODE, bool SPLIT, int NR_ = (MODE == kModeA ? 128 : 64)>
 struct TcCfg {
   static constexpr int NR = NR_;
-  static constexpr int NC = SPLIT ? (MODE == kModeA ? 128 : 256) : 128;
+  static constexpr int NC = 128;
   static constexpr int CH = 32;
-  static constexpr int CTAS = SPLIT ? 1 : 4;
+  static constexpr int CTAS = SPLIT ? (NR == 64 ? 2 : 1) : 4;
   static constexpr int PARTS = SPLIT ? 2 : 1;
   static constexpr int WB = CH * NR * 2;             // W bytes per stage and part
   static constexpr int SB = CH * NC * 2;             // S bytes per stage and part
@@ -249,7 +250,7 @@ struct TcCfg {
   static_assert(TMEM_COLS == 64 || TMEM_COLS == 128 || TMEM_COLS == 256, "TMEM allocation");
   static_assert(STAGES >= 2, "ring of at least two stages");
   static_assert(CTAS * TMEM_COLS <= 512, "TMEM of the CTAs of one SM");
-  static_assert(SPLIT ? SEGS == 2 : true, "split drains: one 64-row segment per warp");
+  static_assert(SEGS >= 1, "at least one 64-column TMEM segment per set");
 };
 
 __device__ __forceinline__ void mma_bf16_tc_n(uint32_t dtmem, uint64_t adesc, uint64_t bdesc,
@@ -406,25 +407,26 @@ tc_gather_gemm(TcArgs a) {
   }
   fetch_src(S - 1, src_cur);
   // epilogue / drain mapping: warp w reads TMEM lanes 32 (w % 4) .. + 31
-  // (right-hand-side columns) of the 64-column segments seg = w / 4,
-  // w / 4 + 2, ..., segment = (accumulator half h, 64-row block rb)
-  const int quarter = warp & 3, sg0 = warp >> 2;
-  float racc[SPLIT ? 64 : 1], rcmp[SPLIT ? 64 : 1];
+  // (right-hand-side columns) of the 32-column pieces pc = w / 4 + 2 k,
+  // k < SEGS; piece pc = (accumulator half pc / (NR / 32), output rows
+  // 32 (pc % (NR / 32)) .. + 31)
+  const int quarter = warp & 3, pc0 = warp >> 2;
+  constexpr int NV = SPLIT ? Cfg::SEGS * 32 : 1;      // compensated sums per thread
+  float racc[NV], rcmp[NV];
 #pragma unroll
-  for (int i = 0; i < (SPLIT ? 64 : 1); i++) { racc[i] = 0.f; rcmp[i] = 0.f; }
-  auto seg_col = [&](int seg) {          // TMEM column of segment seg (in a set)
-    const int h = seg / (NR / 64), rb = seg % (NR / 64);
-    return h * NR + rb * 64;
+  for (int i = 0; i < NV; i++) { racc[i] = 0.f; rcmp[i] = 0.f; }
+  auto piece_col = [&](int pc) {         // TMEM column of piece pc (in a set)
+    return (pc / (NR / 32)) * NR + (pc % (NR / 32)) * 32;
   };
   auto drain = [&](int set) {
     if (SPLIT) {
 #pragma unroll
-      for (int half = 0; half < 2; half++) {
+      for (int k = 0; k < Cfg::SEGS; k++) {
         float v[32];
         tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + set * (Cfg::HALVES * NR) +
-                      seg_col(sg0) + half * 32, v);
+                      piece_col(pc0 + 2 * k), v);
 #pragma unroll
-        for (int i = 0; i < 32; i++) kahan_add(racc[half * 32 + i], rcmp[half * 32 + i], v[i]);
+        for (int i = 0; i < 32; i++) kahan_add(racc[k * 32 + i], rcmp[k * 32 + i], v[i]);
       }
       tc_fence_before();
     }
@@ -503,17 +505,17 @@ tc_gather_gemm(TcArgs a) {
   // epilogue (mapping as for the drain)
   if (ok) {
 #pragma unroll
-    for (int seg = sg0; seg < Cfg::SEGS; seg += 2) {
-      const int h = seg / (NR / 64), rb = seg % (NR / 64);
+    for (int k = 0; k < Cfg::SEGS; k++) {
+      const int pc = pc0 + 2 * k;
+      const int h = pc / (NR / 32), rr = pc % (NR / 32);
       const int col = c_base + h * 128 + quarter * 32 + lane;
-#pragma unroll
-      for (int half = 0; half < 2; half++) {
+      {
         float v[32];
         if (SPLIT) {
 #pragma unroll
-          for (int i = 0; i < 32; i++) v[i] = racc[half * 32 + i];
+          for (int i = 0; i < 32; i++) v[i] = racc[k * 32 + i];
         } else if (nch > 0) {
-          tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + seg_col(seg) + half * 32, v);
+          tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + piece_col(pc), v);
         } else {
 #pragma unroll
           for (int i = 0; i < 32; i++) v[i] = 0.f;
@@ -521,7 +523,7 @@ tc_gather_gemm(TcArgs a) {
         if (col < a.K) {
 #pragma unroll
           for (int i = 0; i < 32; i++) {
-            const int r = rb * 64 + half * 32 + i;
+            const int r = rr * 32 + i;
             if (r < out_rows) {
               const long long row = out_row0 + r;
               const long long o = row * (long long)a.K + col;
@@ -999,6 +1001,10 @@ int fgb_tc_phase_a(const struct fgb_op_desc* d, const void* vt_hi, const void* v
     fgb::set_error("tensor-core operands must be 16-byte aligned");
     return FGB_BAD_ARG;
   }
+  if (d->slice_rows != 0 && d->slice_rows != 128) {
+    fgb::set_error("fgb_tc_phase_a takes 128-row work slices");
+    return FGB_BAD_ARG;
+  }
   if (d->num_items <= 0 || d->num_zrows <= 0) return FGB_OK;
   cudaStream_t st = fgb::as_stream(stream);
   if (zero_z) FGB_CUDA_TRY(cudaMemsetAsync(Z, 0, sizeof(float) * d->num_zrows * (size_t)K, st));
@@ -1045,6 +1051,12 @@ int fgb_tc_phase_a_bf16(const struct fgb_op_desc* d, const void* vt_hi, const vo
   a.lds = K; a.K = K; a.out = nullptr; a.add = nullptr; a.alpha = 1.f; a.flags = flags;
   a.N = d->N; a.num_zrows = d->num_zrows;
   cudaStream_t st = fgb::as_stream(stream);
+  const int sr = d->slice_rows ? d->slice_rows : 128;
+  if (sr == 64) {
+    if (!split) { fgb::set_error("plain phase A takes 128-row work slices"); return FGB_BAD_ARG; }
+    return fgb::launch_tc<fgb::kModeA, true, 64>(a, d->num_work, st);
+  }
+  if (sr != 128) { fgb::set_error("work slices of phase A must be 64 or 128 rows"); return FGB_BAD_ARG; }
   return split ? fgb::launch_tc<fgb::kModeA, true>(a, d->num_work, st)
                : fgb::launch_tc<fgb::kModeA, false>(a, d->num_work, st);
 }

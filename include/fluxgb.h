@@ -324,6 +324,9 @@ struct fgb_op_desc {
   long long panel_rows; /* t_p0[num_tiles] */
   int tile_rows;        /* rows per phase-B tile: 64 (every kernel), or 128
                            (tensor-core BF16 phase B only); 0 means 64 */
+  int slice_rows;       /* rows per tensor-core phase-A work slice (a_woff
+                           counts slices of this height): 128, or 64 for the
+                           split products of fgb_tc_phase_a_bf16; 0 means 128 */
 };
 /*
  * y = F x (or y = add + alpha F x), vectors in cluster order.  Replaces
@@ -372,7 +375,8 @@ int fgb_tc_phase_a(const struct fgb_op_desc* d, const void* vt_hi, const void* v
 /* Phase A writing Z directly as BF16 (Z_hi = bf16(z), and with the split
  * operands Z_lo = bf16(z - Z_hi)), num_zrows x K each: for a descriptor whose
  * work items all cover their whole group (a_excl == 1; an item that does not
- * is skipped and flagged FGB_FLAG_INDEX_RANGE). */
+ * is skipped and flagged FGB_FLAG_INDEX_RANGE).  Split products may take
+ * 64-row work slices (slice_rows = 64: two CTAs per SM). */
 int fgb_tc_phase_a_bf16(const struct fgb_op_desc* d, const void* vt_hi, const void* vt_lo,
                         const void* X_hi, const void* X_lo, void* Z_hi, void* Z_lo, int K,
                         unsigned* flags, void* stream);

@@ -287,9 +287,11 @@ def test_tma_gather_phase_b_matches_cp_async(terrain_op, K):
         assert torch.equal(Y_tma, Y_cp), split
 
 
-def test_phase_a_bf16_output_matches_fp32(terrain_op):
+@pytest.mark.parametrize("slice_rows", [128, 64])
+def test_phase_a_bf16_output_matches_fp32(terrain_op, slice_rows):
     """Phase A with whole-group work items writing Z as BF16 hi / lo parts
-    against phase A with column-split items accumulating FP32 Z."""
+    (work slices of 128 rows, or of 64 rows with two CTAs per SM) against
+    phase A with column-split items accumulating FP32 Z."""
     import ctypes as C
     from fluxpy_gb300 import _lib
     sm, FF = terrain_op
@@ -308,13 +310,20 @@ def test_phase_a_bf16_output_matches_fp32(terrain_op):
               _lib.ptr(xh), _lib.ptr(xl), _lib.ptr(z32), K, int(FF._needs_zero_z), fl, st)
     zh = torch.full((nz, K), float("nan"), dtype=torch.bfloat16, device="cuda")
     zl = torch.full_like(zh, float("nan"))
-    _lib.call("fgb_tc_phase_a_bf16", C.byref(FF._desc_tc), _lib.ptr(tc["vt_hi"]),
+    desc = FF._desc_tc if slice_rows == 128 else FF._desc_tc64
+    assert desc.slice_rows == slice_rows
+    _lib.call("fgb_tc_phase_a_bf16", C.byref(desc), _lib.ptr(tc["vt_hi"]),
               _lib.ptr(tc["vt_lo"]), _lib.ptr(xh), _lib.ptr(xl), _lib.ptr(zh), _lib.ptr(zl), K,
               fl, st)
     FF.check_device_flags()
     z = zh.float() + zl.float()
     assert torch.isfinite(z).all()
     assert (z - z32).abs().max().item() <= 1e-5 * z32.abs().max().item()
+    if slice_rows == 64:
+        # the plain product takes 128-row slices only
+        with pytest.raises(ValueError, match="128-row work slices"):
+            _lib.call("fgb_tc_phase_a_bf16", C.byref(desc), _lib.ptr(tc["vt_hi"]), None,
+                      _lib.ptr(xh), None, _lib.ptr(zh), None, K, fl, st)
 
 
 @pytest.mark.parametrize("K", [3, 5, 132])

@@ -247,8 +247,8 @@ def _auto_chunk(FF, N, K, fp32_z=True):
 
 
 def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_iter=200,
-                            inner=2, E_is_permuted=False, return_permuted=False, stats=None,
-                            chunk=None, inner0=3, engine="tc", residual="split-bf16",
+                            inner=1, E_is_permuted=False, return_permuted=False, stats=None,
+                            chunk=None, inner0=2, engine="tc", residual="split-bf16",
                             incremental=True):
     """Right-placement radiosity solve for K sun directions at once.
 

@@ -431,15 +431,28 @@ tc_gather_gemm(TcArgs a) {
       tc_fence_before();
     }
   };
+  // Per chunk c: every thread waits for its own copies of chunk c; thread 0
+  // alone waits for the MMAs of chunk c - 1 (the others sleep in the
+  // CTA barrier instead of polling, which would take issue slots from the
+  // copies); after the barrier chunk c is in shared memory and stage
+  // (c - 1) % S is free, so thread 0 issues chunk c's MMAs and everyone
+  // refills that stage with chunk c + S - 1.
   bool ok = true;
   for (int c = 0; c < nch; c++) {
     const int st = c % S;
     cp_wait<S - 2>();
     fence_proxy_async();
+    if (tid == 0 && c >= 1) {
+      const int sp = (c - 1) % S;
+      if (!mbar_wait(smem_addr(&bars[sp]), ((c - 1) / S) & 1)) {
+        atomicOr(a.flags, FGB_FLAG_DEVICE_TIMEOUT);
+        abort_flag = 1;
+      }
+    }
     __syncthreads();
     if (abort_flag) { ok = false; break; }
+    tc_fence_after();
     if (tid == 0) {
-      tc_fence_after();
       // split mode: window c / kTcWin accumulates into set (c / kTcWin) & 1
       const uint32_t dset = SPLIT ? (uint32_t)(((c / kTcWin) & 1) * (Cfg::HALVES * NR)) : 0u;
       const bool first = SPLIT ? (c % kTcWin) == 0 : c == 0;
@@ -466,38 +479,26 @@ tc_gather_gemm(TcArgs a) {
     }
     const int cn = c + S - 1;
     fetch_src(cn + 1, src_nxt);
-    // chunk c - 1 ends a window: its set is drained while chunk c's MMAs
-    // run on the other set
-    const bool drain_now = SPLIT && c >= 1 && (c % kTcWin) == 0;
-    if (c >= 1 && (cn < nch || drain_now)) {
-      const int sp = (c - 1) % S;
-      if (!mbar_wait(smem_addr(&bars[sp]), ((c - 1) / S) & 1)) {
-        atomicOr(a.flags, FGB_FLAG_DEVICE_TIMEOUT);
-        abort_flag = 1;
-      }
-    }
-    if (drain_now && !abort_flag) {
-      tc_fence_after();
-      drain(((c - 1) / kTcWin) & 1);
-    }
-    if (cn < nch && !abort_flag) load(cn, cn % S, src_cur);
+    // chunk c - 1 ended a window (its MMAs are complete): its set is drained
+    // while chunk c's MMAs run on the other set
+    if (SPLIT && c >= 1 && (c % kTcWin) == 0) drain(((c - 1) / kTcWin) & 1);
+    if (cn < nch) load(cn, cn % S, src_cur);
     cp_commit();
 #pragma unroll
     for (int j = 0; j < RPW; j++) src_cur[j] = src_nxt[j];
   }
   cp_wait_all();
-  // all MMAs of this CTA complete (they finish in order): last chunk's barrier
-  if (nch > 0 && ok) {
+  // all MMAs of this CTA complete (they finish in order): thread 0 waits for
+  // the last chunk's barrier
+  if (tid == 0 && nch > 0 && ok) {
     const int cl = nch - 1;
     if (!mbar_wait(smem_addr(&bars[cl % S]), (cl / S) & 1)) {
       atomicOr(a.flags, FGB_FLAG_DEVICE_TIMEOUT);
       ok = false;
     }
   }
-  tc_fence_after();
-  __syncthreads();
-  if (abort_flag) ok = false;
   ok = __syncthreads_and(ok) != 0;     // one decision for the whole CTA
+  tc_fence_after();
 
   // the last (possibly partial) window
   if (SPLIT && ok && nch > 0) drain(((nch - 1) / kTcWin) & 1);

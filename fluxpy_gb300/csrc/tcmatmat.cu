@@ -221,6 +221,10 @@ struct TcCfg {
   static constexpr int NC = 128;
   static constexpr int CH = 32;
   static constexpr int CTAS = SPLIT ? (NR == 64 ? 2 : 1) : 4;
+  // phase B: chunks ahead at which a thread loads the source indices of its
+  // gathered rows (the index load would otherwise stall the copies of the
+  // next chunk; measured 7 % on the plain product, nothing on the split one)
+  static constexpr int SRC_PF = SPLIT ? 1 : 4;
   static constexpr int PARTS = SPLIT ? 2 : 1;
   static constexpr int WB = CH * NR * 2;             // W bytes per stage and part
   static constexpr int SB = CH * NC * 2;             // S bytes per stage and part
@@ -343,10 +347,11 @@ tc_gather_gemm(TcArgs a) {
   const int srow0 = tid / Cfg::PPR;
   const int spiece = tid % Cfg::PPR;
   // phase B: source rows of this thread's S rows of chunk c (through src[]),
-  // fetched one chunk ahead so that the dependent index load does not stall
-  // the copies
-  constexpr int RPW = Cfg::SROWS;
-  int src_cur[RPW], src_nxt[RPW];
+  // fetched SRC_PF chunks ahead into a register ring (src_ring[p]: chunk
+  // cn + p of the loop below) so that the dependent index load does not
+  // stall the copies
+  constexpr int RPW = Cfg::SROWS, PF = Cfg::SRC_PF;
+  int src_ring[PF][RPW];
   auto fetch_src = [&](int c, int (&dst)[RPW]) {
 #pragma unroll
     for (int j = 0; j < RPW; j++) {
@@ -401,11 +406,13 @@ tc_gather_gemm(TcArgs a) {
   };
 
   for (int c = 0; c < S - 1; c++) {
-    fetch_src(c, src_cur);
-    if (c < nch) load(c, c, src_cur);
+    int src_pro[RPW];
+    fetch_src(c, src_pro);
+    if (c < nch) load(c, c, src_pro);
     cp_commit();
   }
-  fetch_src(S - 1, src_cur);
+#pragma unroll
+  for (int p = 0; p < PF; p++) fetch_src(S - 1 + p, src_ring[p]);
   // epilogue / drain mapping: warp w reads TMEM lanes 32 (w % 4) .. + 31
   // (right-hand-side columns) of the 32-column pieces pc = w / 4 + 2 k,
   // k < SEGS; piece pc = (accumulator half pc / (NR / 32), output rows
@@ -478,14 +485,19 @@ tc_gather_gemm(TcArgs a) {
       mma_commit(smem_addr(&bars[st]));
     }
     const int cn = c + S - 1;
-    fetch_src(cn + 1, src_nxt);
+    int src_new[RPW];
+    fetch_src(cn + PF, src_new);
     // chunk c - 1 ended a window (its MMAs are complete): its set is drained
     // while chunk c's MMAs run on the other set
     if (SPLIT && c >= 1 && (c % kTcWin) == 0) drain(((c - 1) / kTcWin) & 1);
-    if (cn < nch) load(cn, cn % S, src_cur);
+    if (cn < nch) load(cn, cn % S, src_ring[0]);
     cp_commit();
 #pragma unroll
-    for (int j = 0; j < RPW; j++) src_cur[j] = src_nxt[j];
+    for (int p = 0; p < PF - 1; p++)
+#pragma unroll
+      for (int j = 0; j < RPW; j++) src_ring[p][j] = src_ring[p + 1][j];
+#pragma unroll
+    for (int j = 0; j < RPW; j++) src_ring[PF - 1][j] = src_new[j];
   }
   cp_wait_all();
   // all MMAs of this CTA complete (they finish in order): thread 0 waits for

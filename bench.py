@@ -417,18 +417,29 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
     dom = max(per_step, key=per_step.get)
     t_ms = ms[dom]
     byts, fl = work[dom]
+    # DRAM traffic per launch of the dominant kernel, from the committed ncu
+    # capture of this workload (dram__bytes_read.sum + dram__bytes_write.sum)
+    traffic = None
+    rec = ROOT / "profiles" / "dram_traffic.json"
+    if rec.exists():
+        try:
+            tr = json.loads(rec.read_text())
+            if tr.get("facets") == N and tr.get("columns") == K:
+                traffic = tr.get("kernels", {}).get(dom, {}).get("dram_bytes_per_launch")
+        except Exception:
+            traffic = None
     gbs = byts / (t_ms * 1e-3) / 1e9
     tfl = fl / (t_ms * 1e-3) / 1e12
     if "tc" in dom:
         # BF16 tensor-core gather-GEMM over the panels: bounded by the tensor pipe
         out["roofline"] = {"kernel": dom, "bound": "tensor", "achieved": tfl, "peak": tf,
-                           "unit": "TFLOP/s", "frac": tfl / tf, "traffic": None,
+                           "unit": "TFLOP/s", "frac": tfl / tf, "traffic": traffic,
                            "peak_source": src, "algorithmic_flops": fl,
                            "algorithmic_bytes": byts, "ms_per_launch": t_ms,
                            "hbm_gbs_algorithmic": gbs, "hbm_peak": hbm}
     else:
         out["roofline"] = {"kernel": dom, "bound": "hbm", "achieved": gbs, "peak": hbm,
-                           "unit": "GB/s", "frac": gbs / hbm, "traffic": None,
+                           "unit": "GB/s", "frac": gbs / hbm, "traffic": traffic,
                            "peak_source": src, "algorithmic_bytes": byts,
                            "algorithmic_flops": fl, "ms_per_launch": t_ms, "fp32_tflops": tfl}
     out["kernel_ms"] = {"columns": K, **ms, "phaseB_tc_tma_gather_variant": ms_tma,

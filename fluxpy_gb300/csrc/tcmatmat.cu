@@ -189,6 +189,11 @@ struct TcArgs {
   const float* add;
   float alpha;
   unsigned* flags;
+  // phase B: the sources as one row-major tensor S = [Z; X] (hi, and lo),
+  // when X follows Z in memory (one base pointer for every gathered row);
+  // null otherwise
+  const __nv_bfloat16* s_hi;
+  const __nv_bfloat16* s_lo;
 };
 
 __device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
@@ -294,7 +299,12 @@ tc_gather_gemm(TcArgs a) {
     r_end = a.t_p0[unit + 1];
     out_row0 = unit * NR;
     out_rows = (int)min((long long)NR, a.N - out_row0);
-    if (tid == 0 && ((r_end - r_first) % 64) != 0) atomicOr(a.flags, FGB_FLAG_INDEX_RANGE);
+    if (((r_end - r_first) % 64) != 0) {
+      // not a whole number of chunks: flagged, and the tile is left empty
+      // (the copies below assume whole chunks)
+      if (tid == 0) atomicOr(a.flags, FGB_FLAG_INDEX_RANGE);
+      r_end = r_first;
+    }
   } else {
     long long lo = 0, hi = a.num_items - 1;
     while (lo < hi) {
@@ -352,56 +362,80 @@ tc_gather_gemm(TcArgs a) {
   // stall the copies
   constexpr int RPW = Cfg::SROWS, PF = Cfg::SRC_PF;
   int src_ring[PF][RPW];
+  // phase B tiles are whole chunks (their row counts are multiples of 64):
+  // a chunk below nch holds CH rows of the tile
+  const int* srcp = a.src + r_first + srow0;
   auto fetch_src = [&](int c, int (&dst)[RPW]) {
 #pragma unroll
-    for (int j = 0; j < RPW; j++) {
-      const long long l = r_first + (long long)c * CH + srow0 + Cfg::RPP * j;
-      dst[j] = (MODE == kModeB && c < nch && l < r_end) ? __ldg(a.src + l) : 0;
-    }
+    for (int j = 0; j < RPW; j++)
+      dst[j] = (MODE == kModeB && c < nch) ? __ldg(srcp + (long long)c * CH + Cfg::RPP * j) : 0;
   };
+  // this thread's copies, constant over the chunks: W pieces (row k, 16-byte
+  // piece (b, q)) and S rows (k = srow0 + RPP j, piece spiece), as shared
+  // offsets in a stage and global element offsets for chunk 0
+  constexpr int WPT = CH * NR / 8 / kTcThreads;
+  uint32_t w_so[WPT];
+  int w_k[WPT];
+  long long w_off[WPT];
+#pragma unroll
+  for (int j = 0; j < WPT; j++) {
+    const int p = tid + j * kTcThreads;
+    const int k = p / (NR / 8), rem = p % (NR / 8);
+    const int b = rem >> 3, q = rem & 7;
+    w_so[j] = b * BLK + k * 128 + ((q ^ (k & 7)) << 4);
+    w_k[j] = k;
+    w_off[j] = (r_first + k) * wstride + b * 64 + q * 8;
+  }
+  const long long w_step = (long long)CH * wstride;
+  uint32_t s_so[RPW];
+#pragma unroll
+  for (int j = 0; j < RPW; j++) {
+    const int k = srow0 + Cfg::RPP * j;
+    s_so[j] = (spiece >> 3) * BLK + k * 128 + (((spiece & 7) ^ (k & 7)) << 4);
+  }
+  const int col = c_base + spiece * 8;
+  const bool colok = col < a.K;
   auto load = [&](int c, int st, const int (&srcs)[RPW]) {
     const long long l0 = r_first + (long long)c * CH;
-    // W: CH rows x NR weights, 16-byte piece (b, q) of row k
-    constexpr int WP = CH * NR / 8;
+    const long long wc = (long long)c * w_step;
+    const uint32_t sw = w_at(st, 0), sw_lo = w_at(st, 1);
+    const uint32_t ss = s_at(st, 0), ss_lo = s_at(st, 1);
+    // W: CH rows x NR weights
 #pragma unroll
-    for (int j = 0; j < WP / kTcThreads; j++) {
-      const int p = tid + j * kTcThreads;
-      const int k = p / (NR / 8), rem = p % (NR / 8);
-      const int b = rem >> 3, q = rem & 7;
-      const bool ok = l0 + k < r_end;
-      const long long off = ok ? (l0 + k) * wstride + b * 64 + q * 8 : 0;
-      const uint32_t so = b * BLK + k * 128 + ((q ^ (k & 7)) << 4);
-      cp_async16_zfill(w_at(st, 0) + so, wbase_hi + off, ok);
-      if (SPLIT) cp_async16_zfill(w_at(st, 1) + so, wbase_lo + off, ok);
+    for (int j = 0; j < WPT; j++) {
+      const bool ok = MODE == kModeB || l0 + w_k[j] < r_end;
+      const long long off = ok ? w_off[j] + wc : 0;
+      cp_async16_zfill(sw + w_so[j], wbase_hi + off, ok);
+      if (SPLIT) cp_async16_zfill(sw_lo + w_so[j], wbase_lo + off, ok);
     }
     // S: CH gathered rows x NC columns
-    const int col = c_base + spiece * 8;
-    const int b = spiece >> 3, q = spiece & 7;
 #pragma unroll
     for (int j = 0; j < RPW; j++) {
-      const int k = srow0 + Cfg::RPP * j;
-      const long long l = l0 + k;
-      const bool okr = l < r_end;
       const __nv_bfloat16* rh;
       const __nv_bfloat16* rl = nullptr;
+      bool ok = colok;
       if (MODE == kModeB) {
-        const int sidx = okr ? srcs[j] : 0;
-        if (sidx < a.num_zrows) {
-          rh = a.z_hi + (long long)sidx * a.lds;
-          if (SPLIT) rl = a.z_lo + (long long)sidx * a.lds;
+        const long long sidx = srcs[j];
+        if (a.s_hi) {
+          rh = a.s_hi + sidx * a.lds;
+          if (SPLIT) rl = a.s_lo + sidx * a.lds;
+        } else if (sidx < a.num_zrows) {
+          rh = a.z_hi + sidx * a.lds;
+          if (SPLIT) rl = a.z_lo + sidx * a.lds;
         } else {
-          rh = a.x_hi + (long long)(sidx - a.num_zrows) * a.lds;
-          if (SPLIT) rl = a.x_lo + (long long)(sidx - a.num_zrows) * a.lds;
+          rh = a.x_hi + (sidx - a.num_zrows) * a.lds;
+          if (SPLIT) rl = a.x_lo + (sidx - a.num_zrows) * a.lds;
         }
       } else {
+        const long long l = l0 + srow0 + Cfg::RPP * j;
+        const bool okr = l < r_end;
+        ok = ok && okr;
         const long long xr = okr ? xrow0 + l : 0;
         rh = a.x_hi + xr * a.lds;
         if (SPLIT) rl = a.x_lo + xr * a.lds;
       }
-      const bool ok = okr && col < a.K;
-      const uint32_t so = b * BLK + k * 128 + ((q ^ (k & 7)) << 4);
-      cp_async16_zfill(s_at(st, 0) + so, ok ? rh + col : rh, ok);
-      if (SPLIT) cp_async16_zfill(s_at(st, 1) + so, ok ? rl + col : rl, ok);
+      cp_async16_zfill(ss + s_so[j], ok ? rh + col : rh, ok);
+      if (SPLIT) cp_async16_zfill(ss_lo + s_so[j], ok ? rl + col : rl, ok);
     }
   };
 
@@ -1101,6 +1135,14 @@ int fgb_tc_phase_b(const struct fgb_op_desc* d, const void* w_hi, const void* w_
   a.z_hi = static_cast<const __nv_bfloat16*>(Z_hi);
   a.z_lo = static_cast<const __nv_bfloat16*>(Z_lo);
   a.lds = K; a.K = K; a.out = Y; a.add = add; a.alpha = alpha; a.flags = flags;
+  // one base pointer for the gathered rows when X follows Z in memory
+  const long long zspan = d->num_zrows * (long long)K;
+  const bool stacked_hi = d->num_zrows == 0 || a.z_hi + zspan == a.x_hi;
+  const bool stacked_lo = !split || d->num_zrows == 0 || a.z_lo + zspan == a.x_lo;
+  if (stacked_hi && stacked_lo) {
+    a.s_hi = d->num_zrows ? a.z_hi : a.x_hi;
+    a.s_lo = split ? (d->num_zrows ? a.z_lo : a.x_lo) : nullptr;
+  }
   cudaStream_t st = fgb::as_stream(stream);
   const int tr = d->tile_rows ? d->tile_rows : 64;
   if (tr == 128) {

@@ -367,3 +367,40 @@ def test_phase_b_128_row_tiles_match_64(terrain_op, K):
     ref = (Y64 - add).abs().max().item()
     assert (Y128 - Y64).abs().max().item() <= 1e-5 * ref
     assert FF.stats["panel_rows_128"] > 0
+
+
+@pytest.mark.parametrize("split", [False, True])
+def test_phase_b_separate_sources_match_stacked(terrain_op, split):
+    """fgb_tc_phase_b with Z and X in separate buffers (a row select per
+    gathered row) against the same call on one stacked [Z; X] tensor (one
+    base pointer): identical results."""
+    import ctypes as C
+    from fluxpy_gb300 import _lib
+    sm, FF = terrain_op
+    N, K = sm.num_faces, 264
+    nz = FF._num_zrows
+    tc = FF.tc_operands(split=True)
+    g = torch.Generator(device="cuda").manual_seed(31 + split)
+    Sh = torch.rand((nz + N, K), device="cuda", generator=g).to(torch.bfloat16)
+    Sl = (torch.rand((nz + N, K), device="cuda", generator=g) * 1e-3).to(torch.bfloat16)
+    Zh, Xh = Sh[:nz].clone(), Sh[nz:].clone()
+    Zl, Xl = Sl[:nz].clone(), Sl[nz:].clone()
+    add = torch.rand((N, K), device="cuda", generator=g)
+    fl = _lib.ptr(FF.device_flags())
+    st = _lib.stream_handle()
+    desc = FF._desc if split else FF._desc128
+    w_hi = tc["w_hi"] if split else tc["w128"]
+    w_lo = _lib.ptr(tc["w_lo"]) if split else None
+    Y1 = torch.full((N, K), float("nan"), device="cuda")
+    Y2 = torch.full((N, K), float("nan"), device="cuda")
+    _lib.call("fgb_tc_phase_b", C.byref(desc), _lib.ptr(w_hi), w_lo,
+              _lib.ptr(Sh[nz:]), _lib.ptr(Sl[nz:]) if split else None,
+              _lib.ptr(Sh[:nz]), _lib.ptr(Sl[:nz]) if split else None,
+              _lib.ptr(Y1), K, _lib.ptr(add), 0.5, fl, st)
+    _lib.call("fgb_tc_phase_b", C.byref(desc), _lib.ptr(w_hi), w_lo,
+              _lib.ptr(Xh), _lib.ptr(Xl) if split else None,
+              _lib.ptr(Zh), _lib.ptr(Zl) if split else None,
+              _lib.ptr(Y2), K, _lib.ptr(add), 0.5, fl, st)
+    FF.check_device_flags()
+    assert torch.isfinite(Y1).all()
+    assert torch.equal(Y1, Y2)

@@ -162,7 +162,7 @@ class fgb_op_desc(C.Structure):
         ("num_tiles", C.c_longlong), ("N", C.c_longlong), ("num_zrows", C.c_longlong),
         ("max_group_tiles", C.c_int), ("g_kzp", C.c_void_p), ("g_vtoff", C.c_void_p),
         ("a_woff", C.c_void_p), ("num_work", C.c_longlong), ("panel_rows", C.c_longlong),
-        ("tile_rows", C.c_int), ("slice_rows", C.c_int),
+        ("tile_rows", C.c_int), ("slice_rows", C.c_int), ("a_witem", C.c_void_p),
     ]
 
 
@@ -569,6 +569,10 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         # only slices that hold rows of the group
         tg_woff64 = np.zeros(ng + 1, np.int64)
         np.cumsum((g_kz + 63) // 64, out=tg_woff64[1:])
+        # the item of every tensor-core work slice (no search per CTA)
+        a_witem_tc = np.repeat(np.arange(a_grp.size), g_kzp[a_grp] // TC_A_ROWS)
+        tg_witem = np.repeat(np.arange(ng), g_kzp // TC_A_ROWS)
+        tg_witem64 = np.repeat(np.arange(ng), (g_kz + 63) // 64)
         tsl = g_kzp // 64
         tjb = (g_n + 63) // 64
         tcnt = tsl * tjb
@@ -720,11 +724,13 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
             a_grp=d(a_grp, np.int32), a_j0=d(a_j0, np.int32), a_j1=d(a_j1, np.int32),
             a_excl=d(a_ex, np.uint8), t_p0=d(t_p0, np.int64), src=src_d,
             g_kzp=d(g_kzp, np.int32), g_vtoff=d(g_vtoff[:-1], np.int64),
-            a_woff=d(a_woff, np.int64), a_woff_tc=d(a_woff_tc, np.int64))
+            a_woff=d(a_woff, np.int64), a_woff_tc=d(a_woff_tc, np.int64),
+            a_witem_tc=d(a_witem_tc, np.int32))
         self._dev_tc = dict(
             a_grp=d(np.arange(ng), np.int32), a_j0=d(np.zeros(ng), np.int32),
             a_j1=d(g_n, np.int32), a_excl=d(np.ones(ng), np.uint8), a_woff=d(tg_woff, np.int64),
-            a_woff64=d(tg_woff64, np.int64))
+            a_woff64=d(tg_woff64, np.int64), a_witem=d(tg_witem, np.int32),
+            a_witem64=d(tg_witem64, np.int32))
         self._build_dev = dict(
             vt_g=d(vt_g, np.int32), vt_s=d(vt_s, np.int32), vt_j=d(vt_j, np.int32),
             vr_src=d(vr_src, np.int64), vr_dst=d(vr_dst, np.int64), vr_n=d(vr_n, np.int32),
@@ -770,6 +776,7 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         TC_A_ROWS rows (tensor-core phase A with FP32 output)."""
         desc = fgb_op_desc.from_buffer_copy(self._desc)
         desc.a_woff = self._dev["a_woff_tc"].data_ptr()
+        desc.a_witem = self._dev["a_witem_tc"].data_ptr()
         desc.num_work = int(self._dev["a_woff_tc"][-1].item())
         return desc
 
@@ -778,9 +785,11 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         slices of TC_A_ROWS rows, or of 64 rows (split products)."""
         desc = fgb_op_desc.from_buffer_copy(self._desc)
         woff = "a_woff" if slice_rows == TC_A_ROWS else "a_woff64"
+        witem = "a_witem" if slice_rows == TC_A_ROWS else "a_witem64"
         for key in ("a_grp", "a_j0", "a_j1", "a_excl"):
             setattr(desc, key, self._dev_tc[key].data_ptr())
         desc.a_woff = self._dev_tc[woff].data_ptr()
+        desc.a_witem = self._dev_tc[witem].data_ptr()
         desc.num_items = int(self._dev_tc["a_grp"].numel()) if self._num_zrows > 0 else 0
         desc.num_work = int(self._dev_tc[woff][-1].item())
         desc.slice_rows = slice_rows

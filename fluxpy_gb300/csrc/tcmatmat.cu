@@ -166,6 +166,7 @@ struct TcArgs {
   const int* a_j1;
   const unsigned char* a_excl;
   const long long* a_woff;
+  const int* a_witem;      // work slice -> item (optional)
   long long num_items;
   const int* g_c0;
   const int* g_kz;
@@ -307,9 +308,13 @@ tc_gather_gemm(TcArgs a) {
     }
   } else {
     long long lo = 0, hi = a.num_items - 1;
-    while (lo < hi) {
-      const long long mid = (lo + hi + 1) >> 1;
-      if (a.a_woff[mid] <= unit) lo = mid; else hi = mid - 1;
+    if (a.a_witem) {
+      lo = a.a_witem[unit];
+    } else {
+      while (lo < hi) {
+        const long long mid = (lo + hi + 1) >> 1;
+        if (a.a_woff[mid] <= unit) lo = mid; else hi = mid - 1;
+      }
     }
     const long long it = lo;
     const int sl = (int)(unit - a.a_woff[it]);
@@ -550,7 +555,53 @@ tc_gather_gemm(TcArgs a) {
   if (SPLIT && ok && nch > 0) drain(((nch - 1) / kTcWin) & 1);
 
   // epilogue (mapping as for the drain)
-  if (ok) {
+  const bool bf16_out = MODE == kModeA && a.zout_hi != nullptr;
+  if (ok && bf16_out) {
+    // phase A with BF16 Z: the NR x NC tile (hi, and lo) is staged in the
+    // idle ring, row-major, then written as whole 16-byte pieces of Z rows
+    // (a thread's accumulators are one column of 32-row pieces: stored
+    // directly, each would be a separate 2-byte store)
+    static_assert(MODE != kModeA || NR * NC * 2 * Cfg::PARTS <= S * STAGE,
+                  "BF16 tile staging in the ring");
+    __nv_bfloat16* t_hi = reinterpret_cast<__nv_bfloat16*>(smem);
+    __nv_bfloat16* t_lo = t_hi + NR * NC;
+    fence_proxy_async();
+#pragma unroll
+    for (int k = 0; k < Cfg::SEGS; k++) {
+      const int pc = pc0 + 2 * k;
+      const int h = pc / (NR / 32), rr = pc % (NR / 32);
+      const int cc = h * 128 + quarter * 32 + lane;
+      float v[32];
+      if (SPLIT) {
+#pragma unroll
+        for (int i = 0; i < 32; i++) v[i] = racc[k * 32 + i];
+      } else if (nch > 0) {
+        tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + piece_col(pc), v);
+      } else {
+#pragma unroll
+        for (int i = 0; i < 32; i++) v[i] = 0.f;
+      }
+#pragma unroll
+      for (int i = 0; i < 32; i++) {
+        const __nv_bfloat16 hv = __float2bfloat16(v[i]);
+        t_hi[(rr * 32 + i) * NC + cc] = hv;
+        if (SPLIT) t_lo[(rr * 32 + i) * NC + cc] = __float2bfloat16(v[i] - __bfloat162float(hv));
+      }
+    }
+    __syncthreads();
+    if (excl) {
+      for (int p = tid; p < NR * NC / 8; p += kTcThreads) {
+        const int r = p / (NC / 8), q = p % (NC / 8);
+        const int col = c_base + q * 8;
+        if (r < out_rows && col < a.K) {
+          const long long o = (out_row0 + r) * (long long)a.K + col;
+          *reinterpret_cast<uint4*>(a.zout_hi + o) = *reinterpret_cast<const uint4*>(t_hi + r * NC + q * 8);
+          if (SPLIT)
+            *reinterpret_cast<uint4*>(a.zout_lo + o) = *reinterpret_cast<const uint4*>(t_lo + r * NC + q * 8);
+        }
+      }
+    }
+  } else if (ok) {
 #pragma unroll
     for (int k = 0; k < Cfg::SEGS; k++) {
       const int pc = pc0 + 2 * k;
@@ -578,12 +629,6 @@ tc_gather_gemm(TcArgs a) {
                 float y = v[i];
                 if (a.add) y = a.add[o] + a.alpha * y;
                 a.out[o] = y;
-              } else if (a.zout_hi) {
-                if (excl) {
-                  const __nv_bfloat16 hv = __float2bfloat16(v[i]);
-                  a.zout_hi[o] = hv;
-                  if (a.zout_lo) a.zout_lo[o] = __float2bfloat16(v[i] - __bfloat162float(hv));
-                }
               } else if (excl) {
                 a.out[o] = v[i];
               } else {
@@ -1057,7 +1102,7 @@ int fgb_tc_phase_a(const struct fgb_op_desc* d, const void* vt_hi, const void* v
   if (zero_z) FGB_CUDA_TRY(cudaMemsetAsync(Z, 0, sizeof(float) * d->num_zrows * (size_t)K, st));
   fgb::TcArgs a{};
   a.a_grp = d->a_grp; a.a_j0 = d->a_j0; a.a_j1 = d->a_j1; a.a_excl = d->a_excl;
-  a.a_woff = d->a_woff; a.num_items = d->num_items;
+  a.a_woff = d->a_woff; a.a_witem = d->a_witem; a.num_items = d->num_items;
   a.g_c0 = d->g_c0; a.g_kz = d->g_kz; a.g_kzp = d->g_kzp; a.g_vtoff = d->g_vtoff; a.g_z0 = d->g_z0;
   a.w_hi = static_cast<const __nv_bfloat16*>(vt_hi);
   a.w_lo = static_cast<const __nv_bfloat16*>(vt_lo);
@@ -1080,14 +1125,14 @@ int fgb_tc_phase_a_bf16(const struct fgb_op_desc* d, const void* vt_hi, const vo
     return FGB_BAD_ARG;
   }
   if (fgb::misaligned(vt_hi) || fgb::misaligned(X_hi) || fgb::misaligned(vt_lo) ||
-      fgb::misaligned(X_lo)) {
-    fgb::set_error("tensor-core operands must be 16-byte aligned");
+      fgb::misaligned(X_lo) || fgb::misaligned(Z_hi) || fgb::misaligned(Z_lo)) {
+    fgb::set_error("tensor-core operands and Z must be 16-byte aligned");
     return FGB_BAD_ARG;
   }
   if (d->num_items <= 0 || d->num_zrows <= 0) return FGB_OK;
   fgb::TcArgs a{};
   a.a_grp = d->a_grp; a.a_j0 = d->a_j0; a.a_j1 = d->a_j1; a.a_excl = d->a_excl;
-  a.a_woff = d->a_woff; a.num_items = d->num_items;
+  a.a_woff = d->a_woff; a.a_witem = d->a_witem; a.num_items = d->num_items;
   a.g_c0 = d->g_c0; a.g_kz = d->g_kz; a.g_kzp = d->g_kzp; a.g_vtoff = d->g_vtoff; a.g_z0 = d->g_z0;
   a.w_hi = static_cast<const __nv_bfloat16*>(vt_hi);
   a.w_lo = static_cast<const __nv_bfloat16*>(vt_lo);

@@ -327,6 +327,10 @@ struct fgb_op_desc {
   int slice_rows;       /* rows per tensor-core phase-A work slice (a_woff
                            counts slices of this height): 128, or 64 for the
                            split products of fgb_tc_phase_a_bf16; 0 means 128 */
+  const int* a_witem;   /* optional, num_work entries: the item of each
+                           tensor-core phase-A work slice (the i with
+                           a_woff[i] <= slice < a_woff[i+1]); null: found by
+                           binary search over a_woff */
 };
 /*
  * y = F x (or y = add + alpha F x), vectors in cluster order.  Replaces

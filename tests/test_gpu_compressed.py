@@ -404,3 +404,31 @@ def test_phase_b_separate_sources_match_stacked(terrain_op, split):
     FF.check_device_flags()
     assert torch.isfinite(Y1).all()
     assert torch.equal(Y1, Y2)
+
+
+def test_phase_a_slice_item_table_matches_search(terrain_op):
+    """Tensor-core phase A with the per-slice item table (a_witem) against
+    the same descriptor without it (item found by binary search over
+    a_woff): identical BF16 Z."""
+    import ctypes as C
+    from fluxpy_gb300 import _lib
+    from fluxpy_gb300.compressed_form_factors import fgb_op_desc
+    sm, FF = terrain_op
+    N, K = sm.num_faces, 128
+    nz = FF._num_zrows
+    tc = FF.tc_operands(split=True)
+    g = torch.Generator(device="cuda").manual_seed(41)
+    X = torch.rand((N, K), device="cuda", generator=g).to(torch.bfloat16)
+    fl = _lib.ptr(FF.device_flags())
+    st = _lib.stream_handle()
+    bare = fgb_op_desc.from_buffer_copy(FF._desc_tc)
+    bare.a_witem = None
+    assert FF._desc_tc.a_witem
+    Z1 = torch.full((nz, K), float("nan"), dtype=torch.bfloat16, device="cuda")
+    Z2 = torch.full_like(Z1, float("nan"))
+    for desc, Z in ((FF._desc_tc, Z1), (bare, Z2)):
+        _lib.call("fgb_tc_phase_a_bf16", C.byref(desc), _lib.ptr(tc["vt_hi"]), None,
+                  _lib.ptr(X), None, _lib.ptr(Z), None, K, fl, st)
+    FF.check_device_flags()
+    assert torch.isfinite(Z1.float()).all()
+    assert torch.equal(Z1, Z2)

@@ -355,7 +355,7 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
     def tc_b(split, rows128=True):
         # plain products run on the 128-row tiles, split ones on the 64-row
         # panel (as the solver does)
-        if not split and rows128:
+        if rows128 and not split:
             _lib.call("fgb_tc_phase_b", C.byref(FF._desc128), _lib.ptr(tc["w128"]), None,
                       _lib.ptr(xh), None, _lib.ptr(zh), None, _lib.ptr(Y), K, _lib.ptr(Ek), 1.0,
                       _lib.ptr(flags), st())

@@ -111,6 +111,7 @@ SIGNATURES: dict[str, list] = {
     "fgb_tc_phase_b_tma": [P, P, P, P, P, P, I32, P, F32, P, P],
     "fgb_split_bf16": [P, P, P, I64, P],
     "fgb_retile_panel_bf16": [P, I64, P, P, P, P],
+    "fgb_retile_panel_split_bf16": [P, I64, P, P, P, P, P],
     "fgb_vpanel_transpose_bf16": [P, P, P, P, P, I64, P, P, P],
     # solve (a10-a12)
     "fgb_scale_rows_f32": [P, P, F32, P, I64, I32, P],

@@ -947,11 +947,12 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
             buf = torch.empty((zr + self.num_faces, K), dtype=torch.bfloat16, device=device)
         return buf, buf[:zr], buf[zr:]
 
-    def _build_tc128(self, panel32):
-        """The 128-row phase-B layout for the BF16 tensor-core product: the
+    def _build_tc128(self, panel32, split=False):
+        """The 128-row phase-B layout for the BF16 tensor-core products: the
         64-row panel's rows of tiles 2t and 2t + 1 that gather the same
         source become one 128-weight row of tile t (each source appears at
-        most once per 64-row tile, so the halves never collide)."""
+        most once per 64-row tile, so the halves never collide).  Returns
+        (hi, lo): BF16 weights, and with split their low parts (else None)."""
         dev = panel32.device
         t_p0 = self._dev["t_p0"]
         ntiles = int(t_p0.numel() - 1)
@@ -993,8 +994,14 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         src2[u_row] = u_src
         del u_row, u_src
         w128 = torch.zeros(max(total2, 1) * 128, dtype=torch.bfloat16, device=dev)
-        _lib.call("fgb_retile_panel_bf16", _lib.ptr(panel32), P, _lib.ptr(new_row),
-                  _lib.ptr(half), _lib.ptr(w128), _lib.stream_handle())
+        lo128 = None
+        if split:
+            lo128 = torch.zeros_like(w128)
+            _lib.call("fgb_retile_panel_split_bf16", _lib.ptr(panel32), P, _lib.ptr(new_row),
+                      _lib.ptr(half), _lib.ptr(w128), _lib.ptr(lo128), _lib.stream_handle())
+        else:
+            _lib.call("fgb_retile_panel_bf16", _lib.ptr(panel32), P, _lib.ptr(new_row),
+                      _lib.ptr(half), _lib.ptr(w128), _lib.stream_handle())
         del new_row, half
         desc = fgb_op_desc.from_buffer_copy(self._desc)
         desc.t_p0 = t2.data_ptr()
@@ -1005,50 +1012,68 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         self._dev128 = dict(t_p0=t2, src=src2)
         self._desc128 = desc
         self.stats["panel_rows_128"] = total2
-        return w128
+        return w128, lo128
 
     def tc_operands(self, split=False):
         """BF16 operands of the tensor-core products, built once from the
         FP32 panels: 'w128' (phase-B panel with 128-row tiles, for the plain
-        product), 'vt_hi' (transposed phase-A panel) and, for split products,
-        the 64-row phase-B panel 'w_hi' / 'w_lo' and 'vt_lo'
+        product) and 'vt_hi' (transposed phase-A panel) and, for split
+        products, the 64-row phase-B panel 'w_hi' / 'w_lo' and 'vt_lo'
         (hi = bf16(v), lo = bf16(v - hi))."""
         tc = self.__dict__.setdefault("_tc", {})
-        if "w128" in tc and (not split or "w_lo" in tc):
+        need = ("w128", "vt_hi") + (("w_hi", "w_lo", "vt_lo") if split else ())
+        if all(k in tc for k in need):
             return tc
         panel, vpanel = self.panels("fp32")
         dev = panel.device
         st = _lib.stream_handle()
         if "w128" not in tc:
-            tc["w128"] = self._build_tc128(panel)
-        if not split:
-            if "vt_hi" not in tc:
-                vt_hi = torch.zeros(max(self._vtpanel_size, 8), dtype=torch.bfloat16, device=dev)
-                b = self._build_dev
-                _lib.call("fgb_vpanel_transpose_bf16", C.byref(self._desc), _lib.ptr(vpanel),
-                          _lib.ptr(b["vt_g"]), _lib.ptr(b["vt_s"]), _lib.ptr(b["vt_j"]),
-                          self._num_vt_tiles, _lib.ptr(vt_hi), None, st)
-                tc["vt_hi"] = vt_hi
+            tc["w128"], _ = self._build_tc128(panel)
+        if "vt_hi" not in tc or (split and "vt_lo" not in tc):
+            nvt = max(self._vtpanel_size, 8)
+            vt_hi = tc.get("vt_hi")
+            if vt_hi is None:
+                vt_hi = torch.zeros(nvt, dtype=torch.bfloat16, device=dev)
+            vt_lo = torch.zeros(nvt, dtype=torch.bfloat16, device=dev) if split else None
+            b = self._build_dev
+            _lib.call("fgb_vpanel_transpose_bf16", C.byref(self._desc), _lib.ptr(vpanel),
+                      _lib.ptr(b["vt_g"]), _lib.ptr(b["vt_s"]), _lib.ptr(b["vt_j"]),
+                      self._num_vt_tiles, _lib.ptr(vt_hi), _lib.ptr(vt_lo), st)
+            tc["vt_hi"] = vt_hi
+            if split:
+                tc["vt_lo"] = vt_lo
+        if split:
+            self.tc_operands64(split=True)
+        return tc
+
+    def tc_operands64(self, split=False):
+        """The 64-row phase-B panel in BF16, 'w_hi' (and its low part 'w_lo'
+        with split), in the same dict as tc_operands: the operand of the
+        split products and of the 64-row kernels (the TMA gather variant,
+        comparisons)."""
+        tc = self.__dict__.setdefault("_tc", {})
+        if "w_hi" in tc and (not split or "w_lo" in tc):
             return tc
+        panel, _ = self.panels("fp32")
         w_hi = tc.get("w_hi")
         if w_hi is None:
-            w_hi = torch.empty(panel.numel(), dtype=torch.bfloat16, device=dev)
-        w_lo = torch.empty(panel.numel(), dtype=torch.bfloat16, device=dev) if split else None
+            w_hi = torch.empty(panel.numel(), dtype=torch.bfloat16, device=panel.device)
+        w_lo = torch.empty_like(w_hi) if split else None
         _lib.call("fgb_split_bf16", _lib.ptr(panel), _lib.ptr(w_hi), _lib.ptr(w_lo),
-                  panel.numel(), st)
-        nvt = max(self._vtpanel_size, 8)
-        vt_hi = tc.get("vt_hi")
-        if vt_hi is None:
-            vt_hi = torch.zeros(nvt, dtype=torch.bfloat16, device=dev)
-        vt_lo = torch.zeros(nvt, dtype=torch.bfloat16, device=dev) if split else None
-        b = self._build_dev
-        _lib.call("fgb_vpanel_transpose_bf16", C.byref(self._desc), _lib.ptr(vpanel),
-                  _lib.ptr(b["vt_g"]), _lib.ptr(b["vt_s"]), _lib.ptr(b["vt_j"]),
-                  self._num_vt_tiles, _lib.ptr(vt_hi), _lib.ptr(vt_lo), st)
-        tc.update(w_hi=w_hi, vt_hi=vt_hi)
+                  panel.numel(), _lib.stream_handle())
+        tc["w_hi"] = w_hi
         if split:
-            tc.update(w_lo=w_lo, vt_lo=vt_lo)
+            tc["w_lo"] = w_lo
         return tc
+
+    def tc_split128(self):
+        """hi and lo parts of the 128-row phase-B panel for split products
+        on 128-row tiles (16-warp CTAs, one per SM).  Measured slower than
+        the 64-row split product at two CTAs per SM (146 vs 119 ms at 522k
+        facets and 1,024 columns), so the solver does not use them; built on
+        request, not kept."""
+        panel, _ = self.panels("fp32")
+        return self._build_tc128(panel, split=True)
 
     def bf16_product(self, Xb, Z, Zb, Y, add=None, alpha=1.0, engine="tc"):
         """Y = add + alpha F X with BF16 operands (X: N x K bf16, K % 8 == 0)

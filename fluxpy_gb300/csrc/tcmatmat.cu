@@ -227,6 +227,11 @@ struct TcCfg {
   static constexpr int NC = 128;
   static constexpr int CH = 32;
   static constexpr int CTAS = SPLIT ? (NR == 64 ? 2 : 1) : 4;
+  // threads per CTA: the split products on 128-row tiles / slices run 16
+  // warps, so that each thread keeps 32 compensated sums (as on 64-row
+  // tiles with 8 warps), one CTA per SM
+  static constexpr int THREADS = (SPLIT && NR == 128) ? 512 : 256;
+  static constexpr int NQ = THREADS / 128;           // warps per TMEM lane quarter
   // phase B: chunks ahead at which a thread loads the source indices of its
   // gathered rows (the index load would otherwise stall the copies of the
   // next chunk; measured 7 % on the plain product, nothing on the split one)
@@ -250,7 +255,7 @@ struct TcCfg {
   static constexpr int TMEM_COLS = SETS * HALVES * NR;
   static constexpr int SEGS = HALVES * NR / 64;      // 64-column TMEM segments per set
   static constexpr int PPR = NC / 8;                 // 16-byte pieces per S row
-  static constexpr int RPP = kTcThreads / PPR;      // S rows per pass of the CTA
+  static constexpr int RPP = THREADS / PPR;         // S rows per pass of the CTA
   static constexpr int SROWS = CH / RPP;             // S rows per thread and chunk
   // instruction descriptor, kind::f16: D FP32, A and B BF16, both MN-major,
   // N = NR, M = 128
@@ -261,6 +266,11 @@ struct TcCfg {
   static_assert(STAGES >= 2, "ring of at least two stages");
   static_assert(CTAS * TMEM_COLS <= 512, "TMEM of the CTAs of one SM");
   static_assert(SEGS >= 1, "at least one 64-column TMEM segment per set");
+  // 32-column pieces of a set, shared out over the NQ warps of a lane quarter
+  static constexpr int PIECES = 2 * SEGS;
+  static constexpr int PPW = PIECES / NQ;            // pieces per warp
+  static_assert(PIECES % NQ == 0 && PPW >= 1, "pieces per warp");
+  static_assert((CH * NR / 8) % THREADS == 0 && CH % RPP == 0, "copy plan");
 };
 
 __device__ __forceinline__ void mma_bf16_tc_n(uint32_t dtmem, uint64_t adesc, uint64_t bdesc,
@@ -272,7 +282,7 @@ __device__ __forceinline__ void mma_bf16_tc_n(uint32_t dtmem, uint64_t adesc, ui
 }
 
 template <int MODE, bool SPLIT, int NRT>
-__global__ void __launch_bounds__(kTcThreads, (TcCfg<MODE, SPLIT, NRT>::CTAS))
+__global__ void __launch_bounds__((TcCfg<MODE, SPLIT, NRT>::THREADS), (TcCfg<MODE, SPLIT, NRT>::CTAS))
 tc_gather_gemm(TcArgs a) {
   using Cfg = TcCfg<MODE, SPLIT, NRT>;
   constexpr int NR = Cfg::NR, NC = Cfg::NC, CH = Cfg::CH, WB = Cfg::WB, SB = Cfg::SB;
@@ -378,13 +388,13 @@ tc_gather_gemm(TcArgs a) {
   // this thread's copies, constant over the chunks: W pieces (row k, 16-byte
   // piece (b, q)) and S rows (k = srow0 + RPP j, piece spiece), as shared
   // offsets in a stage and global element offsets for chunk 0
-  constexpr int WPT = CH * NR / 8 / kTcThreads;
+  constexpr int WPT = CH * NR / 8 / Cfg::THREADS;
   uint32_t w_so[WPT];
   int w_k[WPT];
   long long w_off[WPT];
 #pragma unroll
   for (int j = 0; j < WPT; j++) {
-    const int p = tid + j * kTcThreads;
+    const int p = tid + j * Cfg::THREADS;
     const int k = p / (NR / 8), rem = p % (NR / 8);
     const int b = rem >> 3, q = rem & 7;
     w_so[j] = b * BLK + k * 128 + ((q ^ (k & 7)) << 4);
@@ -453,11 +463,11 @@ tc_gather_gemm(TcArgs a) {
 #pragma unroll
   for (int p = 0; p < PF; p++) fetch_src(S - 1 + p, src_ring[p]);
   // epilogue / drain mapping: warp w reads TMEM lanes 32 (w % 4) .. + 31
-  // (right-hand-side columns) of the 32-column pieces pc = w / 4 + 2 k,
-  // k < SEGS; piece pc = (accumulator half pc / (NR / 32), output rows
+  // (right-hand-side columns) of the 32-column pieces pc = w / 4 + NQ k,
+  // k < PPW; piece pc = (accumulator half pc / (NR / 32), output rows
   // 32 (pc % (NR / 32)) .. + 31)
   const int quarter = warp & 3, pc0 = warp >> 2;
-  constexpr int NV = SPLIT ? Cfg::SEGS * 32 : 1;      // compensated sums per thread
+  constexpr int NV = SPLIT ? Cfg::PPW * 32 : 1;       // compensated sums per thread
   float racc[NV], rcmp[NV];
 #pragma unroll
   for (int i = 0; i < NV; i++) { racc[i] = 0.f; rcmp[i] = 0.f; }
@@ -467,10 +477,10 @@ tc_gather_gemm(TcArgs a) {
   auto drain = [&](int set) {
     if (SPLIT) {
 #pragma unroll
-      for (int k = 0; k < Cfg::SEGS; k++) {
+      for (int k = 0; k < Cfg::PPW; k++) {
         float v[32];
         tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + set * (Cfg::HALVES * NR) +
-                      piece_col(pc0 + 2 * k), v);
+                      piece_col(pc0 + Cfg::NQ * k), v);
 #pragma unroll
         for (int i = 0; i < 32; i++) kahan_add(racc[k * 32 + i], rcmp[k * 32 + i], v[i]);
       }
@@ -567,8 +577,8 @@ tc_gather_gemm(TcArgs a) {
     __nv_bfloat16* t_lo = t_hi + NR * NC;
     fence_proxy_async();
 #pragma unroll
-    for (int k = 0; k < Cfg::SEGS; k++) {
-      const int pc = pc0 + 2 * k;
+    for (int k = 0; k < Cfg::PPW; k++) {
+      const int pc = pc0 + Cfg::NQ * k;
       const int h = pc / (NR / 32), rr = pc % (NR / 32);
       const int cc = h * 128 + quarter * 32 + lane;
       float v[32];
@@ -590,7 +600,7 @@ tc_gather_gemm(TcArgs a) {
     }
     __syncthreads();
     if (excl) {
-      for (int p = tid; p < NR * NC / 8; p += kTcThreads) {
+      for (int p = tid; p < NR * NC / 8; p += Cfg::THREADS) {
         const int r = p / (NC / 8), q = p % (NC / 8);
         const int col = c_base + q * 8;
         if (r < out_rows && col < a.K) {
@@ -603,8 +613,8 @@ tc_gather_gemm(TcArgs a) {
     }
   } else if (ok) {
 #pragma unroll
-    for (int k = 0; k < Cfg::SEGS; k++) {
-      const int pc = pc0 + 2 * k;
+    for (int k = 0; k < Cfg::PPW; k++) {
+      const int pc = pc0 + Cfg::NQ * k;
       const int h = pc / (NR / 32), rr = pc % (NR / 32);
       const int col = c_base + h * 128 + quarter * 32 + lane;
       {
@@ -653,10 +663,12 @@ tc_gather_gemm(TcArgs a) {
 // new_row[r] >= 0 lands in half (t & 1) of new row new_row[r], as BF16; the
 // new panel is zeroed by the caller (a new row gets at most one old row per
 // half: a source appears once per 64-row tile).  One warp per old row.
+// lo (optional): the split operand's low part, bf16(w - bf16(w)).
 __global__ void retile_panel_kernel(const float* __restrict__ panel64, long long num_rows,
                                     const long long* __restrict__ new_row,
                                     const unsigned char* __restrict__ half,
-                                    __nv_bfloat16* __restrict__ panel128) {
+                                    __nv_bfloat16* __restrict__ panel128,
+                                    __nv_bfloat16* __restrict__ lo128) {
   const int lane = threadIdx.x & 31;
   const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
   for (long long r = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; r < num_rows;
@@ -664,9 +676,14 @@ __global__ void retile_panel_kernel(const float* __restrict__ panel64, long long
     const long long nr = new_row[r];
     if (nr < 0) continue;
     const float2 w = reinterpret_cast<const float2*>(panel64 + r * 64)[lane];
-    __nv_bfloat16* out = panel128 + nr * 128 + half[r] * 64 + 2 * lane;
-    out[0] = __float2bfloat16(w.x);
-    out[1] = __float2bfloat16(w.y);
+    const long long o = nr * 128 + half[r] * 64 + 2 * lane;
+    const __nv_bfloat16 hx = __float2bfloat16(w.x), hy = __float2bfloat16(w.y);
+    panel128[o] = hx;
+    panel128[o + 1] = hy;
+    if (lo128) {
+      lo128[o] = __float2bfloat16(w.x - __bfloat162float(hx));
+      lo128[o + 1] = __float2bfloat16(w.y - __bfloat162float(hy));
+    }
   }
 }
 
@@ -733,7 +750,7 @@ int launch_tc(const TcArgs& a, long long units, cudaStream_t st) {
   const long long grid = units * nks;
   if (grid <= 0) return FGB_OK;
   if (grid > 0x7fffffffLL) { set_error("grid too large"); return FGB_BAD_ARG; }
-  tc_gather_gemm<MODE, SPLIT, NRT><<<(unsigned)grid, kTcThreads, Cfg::SMEM, st>>>(a);
+  tc_gather_gemm<MODE, SPLIT, NRT><<<(unsigned)grid, Cfg::THREADS, Cfg::SMEM, st>>>(a);
   FGB_LAUNCH_CHECK("tc_gather_gemm");
   return FGB_OK;
 }
@@ -1190,10 +1207,9 @@ int fgb_tc_phase_b(const struct fgb_op_desc* d, const void* w_hi, const void* w_
   }
   cudaStream_t st = fgb::as_stream(stream);
   const int tr = d->tile_rows ? d->tile_rows : 64;
-  if (tr == 128) {
-    if (split) { fgb::set_error("split products take the 64-row panel"); return FGB_BAD_ARG; }
-    return fgb::launch_tc<fgb::kModeB, false, 128>(a, d->num_tiles, st);
-  }
+  if (tr == 128)
+    return split ? fgb::launch_tc<fgb::kModeB, true, 128>(a, d->num_tiles, st)
+                 : fgb::launch_tc<fgb::kModeB, false, 128>(a, d->num_tiles, st);
   if (tr != 64) { fgb::set_error("tile_rows must be 64 or 128"); return FGB_BAD_ARG; }
   return split ? fgb::launch_tc<fgb::kModeB, true, 64>(a, d->num_tiles, st)
                : fgb::launch_tc<fgb::kModeB, false, 64>(a, d->num_tiles, st);
@@ -1228,7 +1244,20 @@ int fgb_retile_panel_bf16(const float* panel64, long long num_rows, const long l
   if (num_rows == 0) return FGB_OK;
   fgb::retile_panel_kernel<<<fgb::grid_for(num_rows * 32, 256, 152LL * 64), 256, 0,
                              fgb::as_stream(stream)>>>(
-      panel64, num_rows, new_row, half, static_cast<__nv_bfloat16*>(panel128));
+      panel64, num_rows, new_row, half, static_cast<__nv_bfloat16*>(panel128), nullptr);
+  FGB_LAUNCH_CHECK("retile_panel_kernel");
+  return FGB_OK;
+}
+
+int fgb_retile_panel_split_bf16(const float* panel64, long long num_rows,
+                                const long long* new_row, const unsigned char* half,
+                                void* hi128, void* lo128, void* stream) {
+  if (num_rows < 0 || !panel64 || !hi128 || !lo128) { fgb::set_error("bad arguments"); return FGB_BAD_ARG; }
+  if (num_rows == 0) return FGB_OK;
+  fgb::retile_panel_kernel<<<fgb::grid_for(num_rows * 32, 256, 152LL * 64), 256, 0,
+                             fgb::as_stream(stream)>>>(
+      panel64, num_rows, new_row, half, static_cast<__nv_bfloat16*>(hi128),
+      static_cast<__nv_bfloat16*>(lo128));
   FGB_LAUNCH_CHECK("retile_panel_kernel");
   return FGB_OK;
 }

@@ -403,6 +403,11 @@ int fgb_tc_phase_b_tma(const struct fgb_op_desc* d, const void* w_hi, const void
  * flops. */
 int fgb_retile_panel_bf16(const float* panel64, long long num_rows, const long long* new_row,
                           const unsigned char* half, void* panel128, void* stream);
+/* The same for split products: hi128 = bf16(w), lo128 = bf16(w - hi), both
+ * zeroed by the caller (fgb_tc_phase_b takes them with tile_rows = 128). */
+int fgb_retile_panel_split_bf16(const float* panel64, long long num_rows,
+                                const long long* new_row, const unsigned char* half,
+                                void* hi128, void* lo128, void* stream);
 /* hi = bf16(in), lo = bf16(in - hi) elementwise (lo may be NULL). */
 int fgb_split_bf16(const float* in, void* hi, void* lo, long long n, void* stream);
 /* Transposed BF16 phase-A panel from the FP32 one (layouts in fgb_op_desc);

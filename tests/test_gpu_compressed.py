@@ -271,15 +271,16 @@ def test_tma_gather_phase_b_matches_cp_async(terrain_op, K):
     _lib.call("fgb_tc_phase_a", C.byref(FF._desc_tc_items), _lib.ptr(tc["vt_hi"]), _lib.ptr(tc["vt_lo"]),
               _lib.ptr(sh[nz:]), _lib.ptr(sl[nz:]), _lib.ptr(zf), K, int(FF._needs_zero_z), fl, st)
     _lib.call("fgb_split_bf16", _lib.ptr(zf), _lib.ptr(sh[:nz]), _lib.ptr(sl[:nz]), nz * K, st)
+    t64 = FF.tc_operands64(split=True)
     for split in (False, True):
-        wl = _lib.ptr(tc["w_lo"]) if split else None
+        wl = _lib.ptr(t64["w_lo"]) if split else None
         Y_cp = torch.full((N, K), float("nan"), device="cuda")
         Y_tma = torch.full((N, K), float("nan"), device="cuda")
-        _lib.call("fgb_tc_phase_b", C.byref(FF._desc), _lib.ptr(tc["w_hi"]), wl,
+        _lib.call("fgb_tc_phase_b", C.byref(FF._desc), _lib.ptr(t64["w_hi"]), wl,
                   _lib.ptr(sh[nz:]), _lib.ptr(sl[nz:]) if split else None, _lib.ptr(sh[:nz]),
                   _lib.ptr(sl[:nz]) if split else None, _lib.ptr(Y_cp), K, _lib.ptr(add), -0.25,
                   fl, st)
-        _lib.call("fgb_tc_phase_b_tma", C.byref(FF._desc), _lib.ptr(tc["w_hi"]), wl,
+        _lib.call("fgb_tc_phase_b_tma", C.byref(FF._desc), _lib.ptr(t64["w_hi"]), wl,
                   _lib.ptr(sh), _lib.ptr(sl) if split else None, _lib.ptr(Y_tma), K,
                   _lib.ptr(add), -0.25, fl, st)
         FF.check_device_flags()
@@ -356,7 +357,7 @@ def test_phase_b_128_row_tiles_match_64(terrain_op, K):
     st = _lib.stream_handle()
     Y64 = torch.full((N, K), float("nan"), device="cuda")
     Y128 = torch.full((N, K), float("nan"), device="cuda")
-    _lib.call("fgb_tc_phase_b", C.byref(FF._desc), _lib.ptr(tc["w_hi"]), None,
+    _lib.call("fgb_tc_phase_b", C.byref(FF._desc), _lib.ptr(FF.tc_operands64()["w_hi"]), None,
               _lib.ptr(S[nz:]), None, _lib.ptr(S[:nz]), None, _lib.ptr(Y64), K, _lib.ptr(add),
               0.5, fl, st)
     _lib.call("fgb_tc_phase_b", C.byref(FF._desc128), _lib.ptr(tc["w128"]), None,
@@ -432,3 +433,34 @@ def test_phase_a_slice_item_table_matches_search(terrain_op):
     FF.check_device_flags()
     assert torch.isfinite(Z1.float()).all()
     assert torch.equal(Z1, Z2)
+
+
+def test_split_phase_b_128_row_tiles_match_64(terrain_op):
+    """The split-BF16 phase B on the re-tiled 128-row panel (hi and lo
+    parts, 16 warps per CTA) against the 64-row panel: the same products
+    summed in another order, within the split product's rounding."""
+    import ctypes as C
+    from fluxpy_gb300 import _lib
+    sm, FF = terrain_op
+    N, K = sm.num_faces, 256
+    nz = FF._num_zrows
+    t64 = FF.tc_operands64(split=True)
+    w128, w128_lo = FF.tc_split128()
+    g = torch.Generator(device="cuda").manual_seed(53)
+    X = torch.rand((nz + N, K), device="cuda", generator=g)
+    Sh = torch.empty((nz + N, K), dtype=torch.bfloat16, device="cuda")
+    Sl = torch.empty_like(Sh)
+    st = _lib.stream_handle()
+    _lib.call("fgb_split_bf16", _lib.ptr(X), _lib.ptr(Sh), _lib.ptr(Sl), (nz + N) * K, st)
+    fl = _lib.ptr(FF.device_flags())
+    Y64 = torch.full((N, K), float("nan"), device="cuda")
+    Y128 = torch.full((N, K), float("nan"), device="cuda")
+    for desc, wh, wl, Y in ((FF._desc, t64["w_hi"], t64["w_lo"], Y64),
+                            (FF._desc128, w128, w128_lo, Y128)):
+        _lib.call("fgb_tc_phase_b", C.byref(desc), _lib.ptr(wh), _lib.ptr(wl),
+                  _lib.ptr(Sh[nz:]), _lib.ptr(Sl[nz:]), _lib.ptr(Sh[:nz]), _lib.ptr(Sl[:nz]),
+                  _lib.ptr(Y), K, None, 1.0, fl, st)
+    FF.check_device_flags()
+    assert torch.isfinite(Y128).all()
+    ref = Y64.abs().max().item()
+    assert (Y128 - Y64).abs().max().item() <= 2e-6 * ref

@@ -32,9 +32,9 @@ COMMON_FLAGS = [
     "--expt-relaxed-constexpr", "-Xptxas", "-v",
 ]
 # Translation units whose results must be bit-identical to plain IEEE C
-# arithmetic (no FMA contraction): the conduction step, the facet geometry
-# and the ray/triangle predicates.
-NO_FMAD = {"conduction.cu", "geometry.cu", "raycast.cu", "formfactor.cu"}
+# arithmetic (no FMA contraction): the conduction steps (plain and per-facet
+# thermal inertia), the facet geometry and the ray/triangle predicates.
+NO_FMAD = {"conduction.cu", "adjoint.cu", "geometry.cu", "raycast.cu", "formfactor.cu"}
 
 
 def _nvcc() -> str:

@@ -53,6 +53,9 @@ SIGNATURES: dict[str, list] = {
     "fgb_conduction_q_f64": [I32, I32, P, F64, P, P, P, P, P, P, P, P, P, U32P, P],
     "fgb_conduction_q_f32": [I32, I32, P, F32, P, P, P, P, P, P, P, P, P, U32P, P],
     "fgb_conduction_t_f64": [I32, I32, P, F64, P, P, P, P, P, P, P, P, U32P, P],
+    "fgb_conduction_q_ti_f64": [I32, I32, P, F64, P, P, P, P, P, I64, P, P, P, U32P, P],
+    "fgb_conduction_q_adjoint_f64": [I32, I32, P, F64, P, P, P, P, I64, P, P, P, P, P, P, P,
+                                     P, P, U32P, P],
     # facet geometry (a1)
     "fgb_facet_geometry_f64": [P, I64, P, I64, P, P, P, U32P, P],
     "fgb_facet_geometry_f32": [P, I64, P, I64, P, P, P, U32P, P],
@@ -103,6 +106,8 @@ SIGNATURES: dict[str, list] = {
     "fgb_matvec_f32": [P, P, P, P, P, P, P, F32, I32, P],
     "fgb_matvec_f64": [P, P, P, P, P, P, P, F64, I32, P],
     "fgb_matvec_f32_f64": [P, P, P, P, P, P, P, F64, I32, P],
+    "fgb_rmatvec_f64": [P, P, P, P, P, U32P, P],
+    "fgb_rmatvec_f32_f64": [P, P, P, P, P, U32P, P],
     "fgb_matmat_f32": [P, P, P, P, P, P, I32, P, F32, I32, I32, P],
     "fgb_matmat_bf16": [P, P, P, P, P, P, P, I32, P, F32, I32, I32, P],
     "fgb_tc_phase_a": [P, P, P, P, P, P, I32, I32, P, P],

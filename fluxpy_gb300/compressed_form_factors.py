@@ -899,6 +899,35 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
                   int(self._needs_zero_z), _lib.stream_handle())
         return out
 
+    def rmatvec_permuted(self, yp, precision=None):
+        """F^T y in cluster order, K = 1, FP64 vectors and arithmetic.
+
+        precision: 'fp64' (FP64 panels) or 'fp32-fp64' (the FP32-stored
+        operator); default: the pool's own precision.  The transposed
+        operator is the transposed panels, applied by libfluxgb
+        ``fgb_rmatvec_*`` (scatter of each panel row, then V_g Zbar_g per
+        low-rank group)."""
+        if precision is None:
+            precision = "fp64" if self._pool.dtype == torch.float64 else "fp32-fp64"
+        if precision == "fp64":
+            fn, pp = "fgb_rmatvec_f64", "fp64"
+        elif precision == "fp32-fp64":
+            fn, pp = "fgb_rmatvec_f32_f64", "fp32"
+        else:
+            raise ValueError(f"transpose products run in FP64 arithmetic, not {precision!r}")
+        yp = yp.to(torch.float64).contiguous()
+        work = torch.empty(self._num_zrows + self.num_faces, dtype=torch.float64,
+                           device=yp.device)
+        panel, vpanel = self.panels(pp)
+        _lib.call(fn, C.byref(self._desc), _lib.ptr(panel), _lib.ptr(vpanel), _lib.ptr(yp),
+                  _lib.ptr(work), _lib.ptr(self.device_flags()), _lib.stream_handle())
+        return work[self._num_zrows:]
+
+    def rmatmat_permuted(self, Yp, precision=None):
+        """F^T Y in cluster order for Y (N, K): one transpose product per column."""
+        return torch.stack([self.rmatvec_permuted(Yp[:, c], precision)
+                            for c in range(Yp.shape[1])], 1)
+
     def matmat_permuted(self, Xp, precision="fp32", out=None, add=None, alpha=1.0, Z=None):
         """Y = F X for K right-hand sides in cluster order (X: N x K)."""
         K = Xp.shape[1]
@@ -1182,8 +1211,25 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         return self._matmat(x)
 
     def _rmatvec(self, x):
-        raise NotImplementedError("the reference defines no transpose product here "
-                                  "(compressed_form_factors.py:701-873)")
+        """F^T x (host or device input, shape (N,) or (N, K)) in FP64
+        arithmetic: what ``x @ F`` gives for the reference's sparse and dense
+        form-factor matrices (CompressedKernelMatrix._rmatvec,
+        compressed_form_factors.py:904-913)."""
+        on_dev = isinstance(x, torch.Tensor)
+        xt = x if on_dev else torch.as_tensor(np.asarray(x), device=self.shape_model._device)
+        orig_dtype = xt.dtype
+        xp = self.permute(xt.to(torch.float64))
+        yp = self.rmatvec_permuted(xp) if xp.ndim == 1 else self.rmatmat_permuted(xp)
+        y = self.unpermute(yp)
+        if on_dev:
+            return y.to(orig_dtype if orig_dtype.is_floating_point else torch.float64)
+        return y.cpu().numpy().astype(self.dtype, copy=False)
+
+    def rmatvec(self, x):
+        return self._rmatvec(x)
+
+    def rmatmat(self, X):
+        return self._rmatvec(X)
 
     def __matmul__(self, x):
         if isinstance(x, torch.Tensor):
@@ -1785,6 +1831,15 @@ class CompressedKernelMatrix(scipy.sparse.linalg.LinearOperator):
     def __matmul__(self, x):
         return self._matvec(x)
 
+    # direct methods: scipy's LinearOperator dispatch needs state that this
+    # class (like the reference's, which never calls LinearOperator.__init__)
+    # does not set up
+    def matvec(self, x):
+        return self._matvec(x)
+
+    def rmatvec(self, x):
+        return self._rmatvec(x)
+
     def _rmatvec(self, x):
         y = x.copy() if not isinstance(x, torch.Tensor) else x.clone()
         FT = _transpose_product(self.form_factor_matrix)
@@ -1798,10 +1853,10 @@ class CompressedKernelMatrix(scipy.sparse.linalg.LinearOperator):
 
 
 def _transpose_product(F):
-    """x -> x @ F (i.e. F^T x) for scipy matrices and dense arrays."""
+    """x -> x @ F (i.e. F^T x) for scipy matrices, dense arrays and the
+    compressed operator (its transposed panel product on the device)."""
     def apply(x):
         if isinstance(F, CompressedFormFactorMatrix):
-            raise NotImplementedError("transpose products of the compressed operator "
-                                      "are not provided")
+            return F._rmatvec(x)
         return np.asarray(x @ F).ravel() if np.ndim(x) == 1 else np.asarray(x @ F)
     return apply

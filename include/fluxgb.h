@@ -97,6 +97,35 @@ int fgb_conduction_t_f64(int num_faces, int nz, const double* z, double dt,
                          const double* Fgeotherm, double* Fsurf, unsigned* flags,
                          void* stream);
 
+/*
+ * conductionQ (src/flux/pcc/conductionQ.c:10-186) for every facet with the
+ * thermal inertia given per facet and layer: ti is num_faces x (nz+1) with
+ * row stride ti_ld = nz + 1, or one shared profile with ti_ld = 0 (then the
+ * result is bit-identical to fgb_conduction_q_f64).  The reference takes one
+ * ti profile for all facets (thermal.pyx:89-156); per-facet thermal inertia
+ * is what the differentiable model fits.  nz <= 127.  No Fsurf output.
+ */
+int fgb_conduction_q_ti_f64(int num_faces, int nz, const double* z, double dt,
+                            const double* Qn, const double* Qnp1, const double* T_in,
+                            double* T_out, const double* ti, long long ti_ld,
+                            const double* rhoc, const double* emiss, const double* Fgeotherm,
+                            unsigned* flags, void* stream);
+/*
+ * Reverse-mode derivative of fgb_conduction_q_ti_f64 (no reference
+ * counterpart: the reference has no derivatives).  Given the cotangent
+ * gT_out of the new profiles (num_faces x (nz+1)), writes the cotangents of
+ * the pre-step profiles gT_in (may alias gT_out), of Qn and Qnp1, and ADDS
+ * those of emiss (num_faces) and of ti (num_faces x (nz+1), row stride
+ * nz+1, column 0 untouched) into gemiss and gti.  The step's
+ * predictor-corrector passes are replayed and differentiated exactly.
+ */
+int fgb_conduction_q_adjoint_f64(int num_faces, int nz, const double* z, double dt,
+                                 const double* Qn, const double* Qnp1, const double* T_in,
+                                 const double* ti, long long ti_ld, const double* rhoc,
+                                 const double* emiss, const double* Fgeotherm,
+                                 const double* gT_out, double* gT_in, double* gQn,
+                                 double* gQnp1, double* gemiss, double* gti, unsigned* flags,
+                                 void* stream);
 
 /* ---------------------------------------------- facet geometry (a1) */
 /*
@@ -351,6 +380,19 @@ int fgb_matvec_f64(const struct fgb_op_desc* d, const double* panel, const doubl
 int fgb_matvec_f32_f64(const struct fgb_op_desc* d, const float* panel, const float* vpanel,
                        const double* x, double* z, double* y, const double* add, double alpha,
                        int zero_z, void* stream);
+/*
+ * Transpose product y -> F^T y of the compressed operator in cluster order
+ * (the x @ F of CompressedKernelMatrix._rmatvec,
+ * src/flux/compressed_form_factors.py:904-913; the reference computes it for
+ * sparse / dense F only).  FP64 vectors and accumulation, panels in FP64 or
+ * FP32 (64-row phase-B panel).  work: num_zrows + N doubles, zeroed here;
+ * the result is work[num_zrows .. num_zrows + N).  Sums are formed with FP64
+ * atomics, so the last bits may differ between calls.
+ */
+int fgb_rmatvec_f64(const struct fgb_op_desc* d, const double* panel, const double* vpanel,
+                    const double* y, double* work, unsigned* flags, void* stream);
+int fgb_rmatvec_f32_f64(const struct fgb_op_desc* d, const float* panel, const float* vpanel,
+                        const double* y, double* work, unsigned* flags, void* stream);
 /* K right-hand sides (X, Y, add: N x K row-major; Z: num_zrows x K):
  * FP32 CUDA cores ...  phases: 1 = phase A only, 2 = phase B only, 3 = both. */
 int fgb_matmat_f32(const struct fgb_op_desc* d, const float* panel, const float* vpanel,

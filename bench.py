@@ -52,6 +52,14 @@ def parse():
     p.add_argument("--rhs", type=int, default=1024)
     p.add_argument("--tol", type=float, default=1e-5)
     p.add_argument("--no-extras", action="store_true", help="skip FP32/e2e/error/CPU legs")
+    p.add_argument("--workload", default="terrain", choices=["terrain", "craters64", "adjoint"],
+                   help="terrain: the headline solve (default); craters64: 64 uneven crater "
+                        "meshes, coupled time-dependent model; adjoint: misfit gradient of the "
+                        "coupled model on a 200k-facet terrain")
+    p.add_argument("--adjoint-steps", type=int, default=100,
+                   help="time steps of the adjoint workload")
+    p.add_argument("--adjoint-grid", type=int, default=317,
+                   help="terrain grid of the adjoint workload (317 -> 199,712 facets)")
     return p.parse_args()
 
 
@@ -179,11 +187,222 @@ def _config(args, nfacets):
             "parallelism": f"replicas x{args.gpus}"}
 
 
+# ------------------------------------------------ other workloads --
+def _events_ms(fn, reps=5):
+    import torch
+    s = torch.cuda.current_stream()
+    fn()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(s)
+    for _ in range(reps):
+        fn()
+    b.record(s)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / reps
+
+
+def run_craters64(args):
+    """64 independent crater meshes of 2k-60k facets (log-uniform sizes,
+    seed 3), each a spherical bowl (depth/diameter 0.2) triangulated from
+    random points, FP32 compressed operators (octree, ACA tol 1e-5, leaf 64);
+    the coupled time-dependent model of ThermalModel (lagged reflected and
+    infrared fluxes, 2 products per step) with PCC conduction on 40 layers
+    graded 2 mm -> 1 m, ti 55 -> 400, for 2 lunar days at 300 steps per day,
+    all meshes in one batch (one launch per kernel per step), the step pair
+    replayed from a CUDA graph.  Metric: facet-steps/s."""
+    import torch
+    from fluxpy_gb300 import _lib, shape, terrain
+    from fluxpy_gb300.batch import MultiMeshThermalModel
+    from fluxpy_gb300.compressed_form_factors import (CompressedFormFactorMatrix,
+                                                      FormFactorOctreeBlock)
+    from fluxpy_gb300.thermal import setgrid
+    rng = np.random.default_rng(3)
+    sizes = np.exp(rng.uniform(np.log(2000), np.log(60000), 64)).astype(np.int64)
+    t0 = time.perf_counter()
+    ops = []
+    for i, nf in enumerate(sizes):
+        g = max(10, int(np.sqrt(nf) / 3))
+        npts = int(max(50, (nf - 4 * (g - 1)) // 2))
+        V, F = terrain.spherical_crater(n_points=npts, seed=1000 + i, boundary_grid=g)
+        sm = shape.EmbreeTrimeshShapeModel(V, F)
+        ops.append(CompressedFormFactorMatrix(sm, tol=1e-5, min_size=4096, leaf_size=64,
+                                              RootBlock=FormFactorOctreeBlock,
+                                              dtype=np.float32))
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    period = 29.53 * 86400.0
+    per_day = 300
+    S = 2 * per_day
+    t = np.arange(S + 1) * (period / per_day)
+    h = 2 * np.pi * t / period
+    lat = np.deg2rad(45.0)
+    D = np.column_stack([-np.sin(h), -np.sin(lat) * np.cos(h), np.cos(lat) * np.cos(h)])
+    F0s = np.where(D[:, 2] > 0, F0, 0.0)
+    z = np.concatenate([[0.0], setgrid(40, 1.0817, 1.0)])
+    ti = np.linspace(55.0, 400.0, z.size)
+    kw = dict(rho=RHO, z=z, ti=ti, rhoc=np.full(z.size, 1.2e6), emiss=0.95, Fgeotherm=0.005,
+              T0=200.0)
+    warm = 4
+    res = {}
+    for graph in (True, False):
+        m = MultiMeshThermalModel(ops, t, D, F0s, use_graph=graph, **kw)
+        m.run(warm)
+        torch.cuda.synchronize()
+        clocks = ClockSampler(0)
+        clocks.start()
+        l0 = _lib.launch_count()
+        s = torch.cuda.current_stream()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(s)
+        m.run()
+        b.record(s)
+        torch.cuda.synchronize()
+        clk = clocks.stop()
+        m.check_errors()
+        ms = a.elapsed_time(b)
+        res[graph] = dict(ms=ms, steps=S - warm, clocks=clk,
+                          launches=_lib.launch_count() - l0, model=m)
+    m = res[True]["model"]
+    op = m.op
+    steps = res[True]["steps"]
+    nf_tot = op.num_faces
+    value = nf_tot * steps / (res[True]["ms"] / 1000.0)
+    u = torch.ones(op.num_rows, dtype=torch.float32, device="cuda")
+    prod_ms = _events_ms(lambda: op.matvec_cluster(u, out=m._y, z=m._zs))
+    cond_ms = _events_ms(lambda: _lib.call(
+        "fgb_conduction_q_f32", op.num_rows, m.nz, _lib.ptr(m.z), float(m.dts[0]),
+        _lib.ptr(m._Q[0]), _lib.ptr(m._Q[1]), _lib.ptr(m._T[0]), _lib.ptr(m._T[1]),
+        _lib.ptr(m.ti), _lib.ptr(m.rhoc), _lib.ptr(m.emiss), _lib.ptr(m.Fg), _lib.ptr(m._Fsurf),
+        _lib.ptr(m.flags), _lib.stream_handle()))
+    op_bytes = op.nbytes
+    hbm = _measured_hbm()
+    prod_gbs = (op_bytes + 8 * op.num_rows + 4 * op.num_zrows) / (prod_ms / 1e3) / 1e9
+    w = z.size
+    cond_gbs = op.num_rows * (2 * w * 4 + 5 * 4) / (cond_ms / 1e3) / 1e9
+    Ts = m.surface_temperature()
+    line = {
+        "metric": "facet-steps/s, 64 uneven crater meshes, coupled radiosity + conduction",
+        "value": value, "unit": "facet-steps/s", "n_gpus": 1, "steps": steps, "warmup": warm,
+        "ms_per_step": res[True]["ms"] / steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
+        "config": {"workload": "64 crater meshes 2k-60k facets (log-uniform, seed 3), "
+                               "2 lunar days x 300 steps, 40 layers 2 mm-1 m, ti 55-400",
+                   "facets": nf_tot, "meshes": 64, "rows_padded": op.num_rows,
+                   "l2": "operator and state larger than L2; no flush"},
+        # graph replays launch the captured kernels without passing the host
+        # counter: the eager run's count is the same set of launches
+        "clocks": res[True]["clocks"], "gpu_launches": int(res[False]["launches"]),
+        "graph_replays": steps // 2,
+        "eager": {"ms_per_step": res[False]["ms"] / steps,
+                  "facet_steps_per_s": nf_tot * steps / (res[False]["ms"] / 1000.0),
+                  "gpu_launches": int(res[False]["launches"])},
+        "kernel_ms": {"merged_product": prod_ms, "conduction_step": cond_ms},
+        "roofline": {"product": {"bound": "hbm", "achieved": prod_gbs, "peak": hbm,
+                                 "unit": "GB/s", "frac": prod_gbs / hbm},
+                     "conduction": {"bound": "hbm", "achieved": cond_gbs, "peak": hbm,
+                                    "unit": "GB/s", "frac": cond_gbs / hbm}},
+        "operator_bytes": int(op_bytes), "build_s": build_s,
+        "surface_T_range_K": [float(Ts.min().item()), float(Ts.max().item())],
+    }
+    print(json.dumps(line))
+
+
+def run_adjoint(args):
+    """Gradient of the coupled radiosity + conduction misfit with respect to
+    per-facet albedo, emissivity and thermal inertia (fluxpy_gb300.adjoint) on
+    an fBm terrain (seed 4; grid 317 -> 199,712 facets), compressed operator
+    (octree, ACA tol 1e-5, leaf 64) stored in FP32 and applied in FP64
+    arithmetic, as is everything else, 40 conduction layers, synthetic
+    observations from perturbed fields (albedo 0.07-0.2, emissivity
+    0.9-0.98, thermal inertia 40-120), checkpoints every 25 steps.  Times one
+    forward pass and one forward + reverse sweep."""
+    import torch
+    from fluxpy_gb300 import _lib, shape, terrain
+    from fluxpy_gb300.adjoint import ThermalMisfit
+    from fluxpy_gb300.compressed_form_factors import (CompressedFormFactorMatrix,
+                                                      FormFactorOctreeBlock)
+    from fluxpy_gb300.thermal import setgrid
+    t0 = time.perf_counter()
+    V, F = terrain.fbm_terrain(n=args.adjoint_grid, seed=4)
+    sm = shape.EmbreeTrimeshShapeModel(V, F)
+    FF = CompressedFormFactorMatrix(sm, tol=1e-5, min_size=4096, leaf_size=64,
+                                    RootBlock=FormFactorOctreeBlock, dtype=np.float32)
+    FF.offload_pool()
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    N = sm.num_faces
+    S = args.adjoint_steps
+    period = 29.53 * 86400.0
+    t = np.arange(S + 1) * (period / 300)
+    h = 2 * np.pi * t / period - np.pi / 3
+    lat = np.deg2rad(30.0)
+    D = np.column_stack([-np.sin(h), -np.sin(lat) * np.cos(h), np.cos(lat) * np.cos(h)])
+    F0s = np.where(D[:, 2] > 0, F0, 0.0)
+    E = sm.get_direct_irradiance_batch(F0s, D, out_dtype=torch.float64)
+    rng = np.random.default_rng(4)
+    true = dict(rho=rng.uniform(0.07, 0.2, N), emiss=rng.uniform(0.9, 0.98, N),
+                ti=rng.uniform(40, 120, N))
+    guess = dict(rho=np.full(N, 0.12), emiss=np.full(N, 0.94), ti=np.full(N, 80.0))
+    z = np.concatenate([[0.0], setgrid(40, 1.0817, 1.0)])
+    m = ThermalMisfit(FF, E, z, np.full(z.size, 1.2e6), period / 300, np.full((N, z.size), 220.0),
+                      np.full(N, 0.005), np.zeros((N, S)), checkpoint_every=25, tol=1e-12)
+    m.Tobs = m.surface_temperatures(**true)
+    torch.cuda.synchronize()
+    s = torch.cuda.current_stream()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    clocks = ClockSampler(0)
+    clocks.start()
+    l0 = _lib.launch_count()
+    ev[0].record(s)
+    L0 = m.value(**guess)
+    ev[1].record(s)
+    ev[2].record(s)
+    L, grho, gem, gti = m.value_and_grad(**guess)
+    ev[3].record(s)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    launches = _lib.launch_count() - l0
+    fwd_ms = ev[0].elapsed_time(ev[1])
+    grad_ms = ev[2].elapsed_time(ev[3])
+    line = {
+        "metric": "misfit gradient (albedo, emissivity, thermal inertia) of the coupled model",
+        "value": N * S / (grad_ms / 1000.0), "unit": "facet-steps/s (forward + reverse)",
+        "n_gpus": 1, "steps": S, "warmup": 0, "ms_per_step": grad_ms / S,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": f"fBm terrain {args.adjoint_grid}x{args.adjoint_grid} (seed 4), "
+                               f"{N} facets, {S} steps, 40 layers, checkpoint every 25",
+                   "facets": N},
+        "clocks": clk, "gpu_launches": int(launches),
+        "forward_ms": fwd_ms, "forward_and_gradient_ms": grad_ms,
+        "gradient_over_forward": grad_ms / fwd_ms,
+        "misfit": float(L.item()), "misfit_forward_only": float(L0.item()),
+        "grad_norms": {"rho": float(grho.norm().item()), "emiss": float(gem.norm().item()),
+                       "ti": float(gti.norm().item())},
+        "build_s": build_s, "operator_device_bytes": int(FF.device_nbytes),
+    }
+    print(json.dumps(line))
+
+
+def _measured_hbm():
+    try:
+        return float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"])
+    except Exception:
+        return 6800.0
+
+
 # ------------------------------------------------------------- GPU arm --
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.workload == "craters64":
+        run_craters64(args)
+        return
+    if args.workload == "adjoint":
+        run_adjoint(args)
         return
     # the operator and the solver's buffers take most of the device: let the
     # caching allocator grow segments instead of fragmenting

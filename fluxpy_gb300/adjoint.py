@@ -337,6 +337,20 @@ class ThermalMisfit:
         tif, ld = _ti_full(ti, N, w)
         return rho, em, ti, tif, ld
 
+    def surface_temperatures(self, rho, emiss, ti):
+        """Forward model only: Ts_n for n = 1..S as an (N, S) device tensor
+        (e.g. synthetic observations from known fields)."""
+        rho, em, ti, tif, ld = self._params(rho, emiss, ti)
+        flags = torch.zeros(1, dtype=torch.int32, device=self.dev)
+        B = solve_right(self.ops, self.E, rho, self.tol, self.max_iter)
+        st = self._initial(B, rho, em)
+        out = torch.empty((self.N, self.S), dtype=F64, device=self.dev)
+        for n in range(1, self.S + 1):
+            st = self._advance(n, st, B, rho, em, tif, ld, flags)
+            out[:, n - 1] = st[2]
+        _raise_flags(flags)
+        return out
+
     def value(self, rho, emiss, ti):
         rho, em, ti, tif, ld = self._params(rho, emiss, ti)
         flags = torch.zeros(1, dtype=torch.int32, device=self.dev)

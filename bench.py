@@ -432,6 +432,8 @@ def main():
     # block pool and the exact-leaf CSR (not used by the products) to host
     FF.offload_pool()
     FF.tc_operands(split=True)
+    # kernel layouts of the BF16 / split products: timed on this operator
+    tune = FF.autotune_products(args.rhs)
     nf = sm.num_faces
     dirs = terrain.random_sun_directions(args.rhs, seed=2 + rank)
     E = sm.get_direct_irradiance_batch(F0, dirs, out_dtype=torch.float32)
@@ -504,7 +506,8 @@ def main():
                    "fp32_matmats": stats[-1]["fp32_matmats"], "chunks": stats[-1].get("chunks", 1),
                    "residual_checked": stats[-1].get("residual")},
         "setup_s": setup_s, "build": {k: (round(v, 3) if isinstance(v, float) else v)
-                                      for k, v in FF.stats.items()},
+                                      for k, v in FF.stats.items() if k != "autotune"},
+        "autotune_ms": tune,
     }
     line.update(extras)
     fp = extras.get("fp32_plain")

@@ -1123,7 +1123,11 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
             # phase A writes Z directly in BF16 (Z, the FP32 scratch, is unused)
             _lib.call("fgb_tc_phase_a_bf16", C.byref(self._desc_tc), _lib.ptr(tc["vt_hi"]), None,
                       _lib.ptr(Xb), None, _lib.ptr(Zb), None, K, flags, st)
-        _lib.call("fgb_tc_phase_b", C.byref(self._desc128), _lib.ptr(tc["w128"]), None,
+        if self.product_plan()["plain"] == "b64":
+            desc, w = self._desc, self.tc_operands64()["w_hi"]
+        else:
+            desc, w = self._desc128, tc["w128"]
+        _lib.call("fgb_tc_phase_b", C.byref(desc), _lib.ptr(w), None,
                   _lib.ptr(Xb), None, _lib.ptr(Zb), None, _lib.ptr(Y), K, _lib.ptr(add),
                   float(alpha), flags, st)
         return Y
@@ -1155,17 +1159,102 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         zl, xl = sl[:nz], sl[nz:]
         tc = self.tc_operands(split=True)
         flags = _lib.ptr(self.device_flags())
+        plan = self.product_plan()["split"]
         _lib.call("fgb_split_bf16", _lib.ptr(X), _lib.ptr(xh), _lib.ptr(xl), N * K, st)
         if self._num_zrows > 0:
-            # phase A writes the hi / lo BF16 parts of Z directly (64-row
-            # work slices: two CTAs per SM)
-            _lib.call("fgb_tc_phase_a_bf16", C.byref(self._desc_tc64), _lib.ptr(tc["vt_hi"]),
+            # phase A writes the hi / lo BF16 parts of Z directly: 64-row work
+            # slices (two CTAs per SM) or 128-row ones (16-warp CTAs)
+            dA = self._desc_tc if plan.startswith("a128") else self._desc_tc64
+            _lib.call("fgb_tc_phase_a_bf16", C.byref(dA), _lib.ptr(tc["vt_hi"]),
                       _lib.ptr(tc["vt_lo"]), _lib.ptr(xh), _lib.ptr(xl), _lib.ptr(zh),
                       _lib.ptr(zl), K, flags, st)
-        _lib.call("fgb_tc_phase_b", C.byref(self._desc), _lib.ptr(tc["w_hi"]),
-                  _lib.ptr(tc["w_lo"]), _lib.ptr(xh), _lib.ptr(xl), _lib.ptr(zh), _lib.ptr(zl),
-                  _lib.ptr(Y), K, _lib.ptr(add), float(alpha), flags, st)
+        if plan.endswith("b128"):
+            # 128-row tiles: the hi part is the plain product's panel
+            dB, wh, wl = self._desc128, tc["w128"], self._split128_lo()
+        else:
+            dB, wh, wl = self._desc, tc["w_hi"], tc["w_lo"]
+        _lib.call("fgb_tc_phase_b", C.byref(dB), _lib.ptr(wh), _lib.ptr(wl), _lib.ptr(xh),
+                  _lib.ptr(xl), _lib.ptr(zh), _lib.ptr(zl), _lib.ptr(Y), K, _lib.ptr(add),
+                  float(alpha), flags, st)
         return Y
+
+    # -- product plans (autotuned) ------------------------------------------
+    # plain BF16 product: phase-B tiles of 128 rows (merged tile pairs) or 64
+    PLAIN_PLANS = ("b128", "b64")
+    # split product: phase-A work slices of 64 / 128 rows, phase-B tiles of 64 / 128
+    SPLIT_PLANS = ("a64-b64", "a128-b64", "a64-b128", "a128-b128")
+
+    def product_plan(self):
+        """Kernel layouts used by bf16_product and split_product: the
+        defaults, or what autotune_products measured fastest."""
+        return self.__dict__.setdefault("_plan", {"plain": "b128", "split": "a64-b64"})
+
+    def _split128_lo(self):
+        tc = self.tc_operands()
+        if "w128_lo" not in tc:
+            panel, _ = self.panels("fp32")
+            _, tc["w128_lo"] = self._build_tc128(panel, split=True)
+        return tc["w128_lo"]
+
+    def autotune_products(self, K, reps=3, plans=None):
+        """Time every kernel layout of the BF16 and split-BF16 products on this
+        operator at K right-hand-side columns (CUDA events, after one warm-up
+        product each) and keep the fastest in product_plan().  A layout whose
+        extra operand does not fit in free device memory is skipped.  Returns
+        {'plain': {plan: ms}, 'split': {plan: ms}, 'chosen': plan dict}; also
+        kept in stats['autotune'].  The candidates compute the same product
+        (up to the order of FP32 sums)."""
+        if K < 8 or K % 8:
+            raise ValueError("K must be a positive multiple of 8")
+        dev = self._perm_d.device
+        N = self.num_faces
+        plans = plans or {"plain": self.PLAIN_PLANS, "split": self.SPLIT_PLANS}
+        tc = self.tc_operands(split=True)
+        g = torch.Generator(device=dev).manual_seed(0)
+        X = torch.rand((N, K), generator=g, device=dev, dtype=torch.float32)
+        Y = torch.empty_like(X)
+        Sb, Zb, Xb = self.stacked_sources(K, dev)
+        Xb.copy_(X)
+        work = {"s_hi": Sb}     # as the solver does: the split sources reuse Sb
+        plan = self.product_plan()
+        old = dict(plan)
+        stream = torch.cuda.current_stream()
+
+        def timed(fn):
+            fn()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for _ in range(reps):
+                fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            return a.elapsed_time(b) / reps
+
+        table = {"plain": {}, "split": {}}
+        for p_ in plans["plain"]:
+            plan["plain"] = p_
+            table["plain"][p_] = timed(lambda: self.bf16_product(Xb, None, Zb, Y))
+        for p_ in plans["split"]:
+            if p_.endswith("b128") and "w128_lo" not in tc:
+                # the 128-row split layout is built as hi and lo parts
+                need = 2 * tc["w128"].numel() * 2 + (1 << 33)
+                if torch.cuda.mem_get_info(dev)[0] < need:
+                    table["split"][p_] = None   # does not fit beside the other operands
+                    continue
+            plan["split"] = p_
+            table["split"][p_] = timed(lambda: self.split_product(X, Y, work=work))
+        self.check_device_flags()
+        best = {k: min((t, p_) for p_, t in v.items() if t is not None)[1]
+                for k, v in table.items() if any(t is not None for t in v.values())}
+        plan.update(old)
+        plan.update(best)
+        if not plan["split"].endswith("b128"):
+            tc.pop("w128_lo", None)      # not used: give the memory back
+        del X, Y, Sb, Zb, Xb, work
+        torch.cuda.empty_cache()
+        table["chosen"] = dict(plan)
+        self.stats["autotune"] = table
+        return table
 
     def device_flags(self):
         """Device status word (FGB_FLAG_*) of the operator's kernels."""
@@ -1342,6 +1431,7 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         st["_panels"] = {}
         st["_tc"] = {}
         st["_flags_d"] = None
+        st.pop("_fgb_adjoint_ops", None)
         for key in ("_pool", "_perm_d", "_iperm_d"):
             st[key] = st[key].cpu()
         for key in self._DEV_DICTS:

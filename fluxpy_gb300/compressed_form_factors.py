@@ -57,7 +57,7 @@ class ClusterTree:
     possibly empty), ordered as itertools.product([le, gt], repeat=d).
     """
 
-    def __init__(self, P, ndim, leaf_size=64, max_levels=64):
+    def __init__(self, P, ndim, leaf_size=64, max_levels=64, parts=None):
         X = np.ascontiguousarray(P[:, :ndim], dtype=np.float64)
         N = X.shape[0]
         nch = 1 << ndim
@@ -72,6 +72,32 @@ class ClusterTree:
         hi_list = [X.max(0) if N else np.zeros(ndim)]
         frontier = np.array([0], dtype=np.int64) if N > leaf_size else np.zeros(0, np.int64)
         lev = 0
+        if parts is not None:
+            # the root's children are the given parts (a partition of the
+            # facets, each in ascending order), split further as usual
+            perm = np.concatenate([np.sort(np.asarray(I, np.int64)) for I in parts])
+            ch, cs, nxt = [], 0, []
+            for I in parts:
+                n_c = int(np.size(I))
+                cid = len(start)
+                start.append(cs)
+                size.append(n_c)
+                level.append(1)
+                children.append(None)
+                if n_c:
+                    seg_pts = X[perm[cs:cs + n_c]]
+                    lo_list.append(seg_pts.min(0))
+                    hi_list.append(seg_pts.max(0))
+                    if n_c > leaf_size and not np.all(seg_pts.min(0) == seg_pts.max(0)):
+                        nxt.append(cid)
+                else:
+                    lo_list.append(np.full(ndim, np.nan))
+                    hi_list.append(np.full(ndim, np.nan))
+                ch.append(cid)
+                cs += n_c
+            children[0] = ch
+            frontier = np.array(nxt, dtype=np.int64)
+            lev = 1
         while frontier.size and lev < max_levels:
             starts = np.array([start[f] for f in frontier], dtype=np.int64)
             sizes = np.array([size[f] for f in frontier], dtype=np.int64)
@@ -199,6 +225,24 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
             raise ValueError("rmax must be in [1, 64]")
         if RootBlock is None:
             RootBlock = FormFactorQuadtreeBlock
+        self._parts = None
+        self._ChildBlock = None
+        if issubclass(RootBlock, FormFactorPartitionBlock):
+            # compressed_form_factors.py:660-690: the rows and the columns
+            # are split into the given parts first, then every (part, part)
+            # block into the child block type
+            parts = kwargs.get("parts")
+            if parts is None:
+                parts = [np.arange(shape_model.num_faces)]
+            parts = [np.asarray(I, dtype=np.int64).ravel() for I in parts]
+            union = np.unique(np.concatenate(parts)) if parts else np.zeros(0, np.int64)
+            if union.size != sum(I.size for I in parts):
+                raise Exception('parts must be disjoint')
+            if union.size != shape_model.num_faces or (union.size and (
+                    union[0] != 0 or union[-1] != shape_model.num_faces - 1)):
+                raise ValueError("parts must cover every facet exactly once")
+            self._parts = parts
+            self._ChildBlock = kwargs.get("ChildBlock", FormFactorQuadtreeBlock)
         self.shape_model = shape_model
         self._tol = tol
         self._min_size = min_size
@@ -251,8 +295,9 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         sm = self.shape_model
         dev = sm._device
         P = np.asarray(sm.P, dtype=np.float64)
-        ndim = 3 if issubclass(self._RootBlock, FormFactorOctreeBlock) else 2
-        tree = ClusterTree(P, ndim, leaf_size=self._leaf_size)
+        split_cls = self._ChildBlock if self._parts is not None else self._RootBlock
+        ndim = 3 if issubclass(split_cls, FormFactorOctreeBlock) else 2
+        tree = ClusterTree(P, ndim, leaf_size=self._leaf_size, parts=self._parts)
         self._tree = tree
         lo3, hi3 = _bbox3(P, tree)
         N = P.shape[0]
@@ -1823,6 +1868,19 @@ class FormFactorOctreeBlock(FormFactor2dTreeBlock):
     """Octree interior block (compressed_form_factors.py:643-658)."""
 
 
+class FormFactorPartitionBlock(FormFactorBlockMatrix):
+    """Root block split into user-given parts of the facets
+    (compressed_form_factors.py:660-698).  Build it with
+    ``CompressedFormFactorMatrix(shape_model, RootBlock=FormFactorPartitionBlock,
+    parts=[I_0, I_1, ...], ChildBlock=FormFactorQuadtreeBlock)``: the parts
+    must be disjoint (the reference's check and message) and, here, cover
+    every facet; each part is used in ascending index order."""
+
+    @property
+    def is_empty_leaf(self):
+        return True
+
+
 def _make_tree_block(op: CompressedFormFactorMatrix, b, parent_nodes):
     """Materialise block b of the plan as a reference-style block object,
     applying the reference's collapse of all-dense / all-sparse children
@@ -1845,6 +1903,8 @@ def _make_tree_block(op: CompressedFormFactorMatrix, b, parent_nodes):
     # interior
     cls = op._RootBlock if b == 0 else (
         FormFactorOctreeBlock if tree.ndim == 3 else FormFactorQuadtreeBlock)
+    if b == 0 and getattr(op, "_parts", None) is not None:
+        cls = FormFactorPartitionBlock
     blk = cls.__new__(cls)
     CompressedFormFactorBlock.__init__(blk, op, (m, n))
     first = op._child0[b]

@@ -178,6 +178,31 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+# ------------------------------------------------------------ replicas --
+# N > 1 runs N independent replicas, one per GPU: each rank solves its own
+# sun directions on its own copy of the operator (the solve has no
+# cross-rank exchange); the job's time is the slowest rank's.
+def replica_directions(terrain, rhs, rank):
+    """The sun directions of one rank: seed 2 for rank 0 (the workload's
+    own), 2 + rank for the others, so the replicas solve different columns."""
+    return terrain.random_sun_directions(rhs, seed=2 + rank)
+
+
+def job_time_ms(ms_local, dist, device):
+    """Max over ranks of the timed region (identity without a process group)."""
+    if dist is None:
+        return float(ms_local)
+    import torch
+    t = torch.tensor([float(ms_local)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(units_per_rank, world, steps, ms_total):
+    """Whole-job throughput: the units all ranks processed over the job's time."""
+    return world * units_per_rank * steps / (ms_total / 1000.0)
+
+
 def _config(args, nfacets):
     return {"workload": (f"fBm terrain {args.grid}x{args.grid} + 30 craters ({nfacets} facets), "
                          f"{args.rhs} sun directions (elev 1-30 deg, seed 2), rho {RHO}, "
@@ -435,7 +460,7 @@ def main():
     # kernel layouts of the BF16 / split products: timed on this operator
     tune = FF.autotune_products(args.rhs)
     nf = sm.num_faces
-    dirs = terrain.random_sun_directions(args.rhs, seed=2 + rank)
+    dirs = replica_directions(terrain, args.rhs, rank)
     E = sm.get_direct_irradiance_batch(F0, dirs, out_dtype=torch.float32)
     Ep = FF.permute(E).contiguous()
     torch.cuda.synchronize()
@@ -471,14 +496,11 @@ def main():
     torch.cuda.nvtx.range_pop()
     launches = _lib.launch_count() - launches0
     clk = clocks.stop()
-    ms_total = ev0.elapsed_time(ev1)
+    ms_total = job_time_ms(ev0.elapsed_time(ev1), dist, dev)
     if dist:
-        t = torch.tensor([ms_total], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_total = float(t.item())
         dist.barrier()
     ms_step = ms_total / args.steps
-    value = world * args.rhs * args.steps / (ms_total / 1000.0)
+    value = job_rate(args.rhs, world, args.steps, ms_total)
 
     extras = {}
     if rank == 0 and not args.no_extras:

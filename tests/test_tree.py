@@ -32,3 +32,25 @@ def test_tree_matches_reference_rule(ndim):
         assert checked > 1
         # every node is a contiguous range of the cluster order
         assert np.array_equal(np.sort(t.perm), np.arange(P.shape[0]))
+
+
+@pytest.mark.parametrize("ndim", [2, 3])
+def test_partition_root_children_are_the_parts(ndim):
+    """FormFactorPartitionBlock roots (compressed_form_factors.py:660-698):
+    the root's children are the given parts, each split below by the
+    orthant rule."""
+    rng = np.random.default_rng(7)
+    P = rng.random((2500, 3))
+    parts = [np.flatnonzero(P[:, 0] < 0.3), np.flatnonzero((P[:, 0] >= 0.3) & (P[:, 1] < 0.5)),
+             np.flatnonzero((P[:, 0] >= 0.3) & (P[:, 1] >= 0.5))]
+    t = ClusterTree(P, ndim, leaf_size=64, parts=parts)
+    ch = t.children[0]
+    assert len(ch) == len(parts)
+    for c, I in zip(ch, parts):
+        assert np.array_equal(t.ref_indices(c), np.sort(I))
+        sub = t.children[c]
+        assert sub is not None and len(sub) == 2**ndim
+        ref = [I[x] for x in orthant_order(P[I, :ndim])]
+        for s, r in zip(sub, ref):
+            assert np.array_equal(t.ref_indices(s), np.sort(r))
+    assert np.array_equal(np.sort(t.perm), np.arange(P.shape[0]))

@@ -59,3 +59,9 @@ def test_reference_arm_runs_on_rank_zero_only(capsys, monkeypatch):
     ns = argparse.Namespace(gpus=2, steps=1, warmup=0, grid=512, rhs=1024, tol=1e-5)
     bench.run_reference(ns)
     assert capsys.readouterr().out == ""
+
+
+def test_cpu_baseline_uses_every_requested_process():
+    r = bench.cpu_baseline(None, seconds=1.0, workers=2)
+    assert r["cores"] == 2 and r["kind"] == "port"
+    assert r["value"] > 0 and r["value"] == r["measured_solves_per_s_at_sample"]

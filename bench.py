@@ -288,6 +288,87 @@ def _events_ms(fn, reps=5):
     return a.elapsed_time(b) / reps
 
 
+def craters_cpu_baseline(sizes, seconds=8.0):
+    """The reference's ThermalModel step (model.py:44-69, 218-224: two sparse
+    form-factor products and conductionQ for every facet, restated by the
+    oracle: scipy CSR and oracle/pcc_oracle.c) on one host core, timed on the
+    4.2k-facet spherical crater with its exact form factors and a 41-node
+    grid.  Extrapolated to the batch of meshes with ``sizes`` facets by the
+    cost model  step = sum_i (N_i c_cond + 2 nnz_i c_mv),  nnz_i = d N_i^2
+    (d: the sample's fraction of visible pairs; the bowls are the same
+    shape, so d does not depend on the facet count)."""
+    from oracle import pcc as opcc
+    from oracle import vis
+    from fluxpy_gb300 import terrain
+    from fluxpy_gb300.thermal import setgrid
+    V, F = terrain.spherical_crater(n_points=2000, seed=0)
+    P, N, A = vis.geometry(V, F)
+    FFc = vis.Scene(V, F).ff_csr(P, N, A)
+    n = F.shape[0]
+    z = np.concatenate([[0.0], setgrid(40, 1.0817, 1.0)])
+    T = np.full((n, z.size), 200.0)
+    ti, rhoc = np.linspace(55.0, 400.0, z.size), np.full(z.size, 1.2e6)
+    em, Fg = np.full(n, 0.95), np.full(n, 0.005)
+    rng = np.random.default_rng(0)
+    Q = rng.uniform(0, 600, n)
+    x = rng.uniform(0, 600, n)
+    # conduction: c_cond per facet-step
+    reps, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < seconds / 2:
+        opcc.step_q(z, 8504.0, Q, Q, T, ti, rhoc, em, Fg)
+        reps += 1
+    c_cond = (time.perf_counter() - t0) / (reps * n)
+    # products: c_mv per stored entry
+    reps, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < seconds / 2:
+        FFc @ x
+        reps += 1
+    c_mv = (time.perf_counter() - t0) / (reps * FFc.nnz)
+    d = FFc.nnz / float(n) ** 2
+    sizes = np.asarray(sizes, np.float64)
+    step_s = float(np.sum(sizes * c_cond + 2 * d * sizes**2 * c_mv))
+    return {"value": float(sizes.sum()) / step_s, "unit": "facet-steps/s", "cores": 1,
+            "kind": "port",
+            "sample": (f"oracle conductionQ (C) and scipy CSR products on the {n}-facet "
+                       f"spherical crater ({FFc.nnz} nonzeros): {c_cond * 1e6:.2f} us per "
+                       f"facet-step, {c_mv * 1e9:.2f} ns per nonzero; extrapolated to the "
+                       f"batch with nnz = {d:.4f} N^2 per mesh (cost model)"),
+            "sample_facet_steps_per_s": 1.0 / (c_cond + 2 * FFc.nnz * c_mv / n)}
+
+
+def adjoint_cpu_baseline(seconds=8.0):
+    """The oracle's forward model and hand-written gradient of the coupled
+    misfit (oracle/adjoint.py, FP64, dense form factors) on one host core, on
+    a 24 x 24 fBm terrain sample (1,058 facets) for 8 steps; facet-steps/s
+    of the gradient at the sample's size (no extrapolation)."""
+    from oracle import adjoint as oadj
+    from oracle import vis
+    from fluxpy_gb300 import terrain
+    from fluxpy_gb300.thermal import setgrid
+    V, F = terrain.fbm_terrain(n=24, seed=4, n_craters=2)
+    P, Nn, Ar = vis.geometry(V, F)
+    FF = vis.Scene(V, F).ff_csr(P, Nn, Ar)
+    n = F.shape[0]
+    S = 8
+    rng = np.random.default_rng(4)
+    dirs = terrain.random_sun_directions(S + 1, seed=2, elev=(5, 40))
+    E = np.stack([F0 * np.maximum(0, Nn @ dd) for dd in dirs], 1)
+    z = np.concatenate([[0.0], setgrid(40, 1.0817, 1.0)])
+    args = (rng.uniform(0.07, 0.2, n), rng.uniform(0.9, 0.98, n), rng.uniform(40, 120, n), z,
+            np.full(z.size, 1.2e6), 3600.0, np.full((n, z.size), 220.0), np.full(n, 0.005),
+            rng.uniform(150, 300, (n, S)))
+    reps, t0 = 0, time.perf_counter()
+    while reps == 0 or time.perf_counter() - t0 < seconds:
+        oadj.coupled_gradient(FF, E, *args)
+        reps += 1
+    dt = (time.perf_counter() - t0) / reps
+    return {"value": n * S / dt, "unit": "facet-steps/s (forward + reverse)", "cores": 1,
+            "kind": "port",
+            "sample": (f"oracle coupled_gradient (numpy, FP64, sparse exact F) on a "
+                       f"{n}-facet fBm terrain, {S} steps, 40 layers: {dt:.2f} s per "
+                       f"gradient; at the sample's size, not extrapolated")}
+
+
 def run_craters64(args):
     """64 independent crater meshes of 2k-60k facets (log-uniform sizes,
     seed 3), each a spherical bowl (depth/diameter 0.2) triangulated from
@@ -390,6 +471,7 @@ def run_craters64(args):
                                     "unit": "GB/s", "frac": cond_gbs / hbm}},
         "operator_bytes": int(op_bytes), "build_s": build_s,
         "surface_T_range_K": [float(Ts.min().item()), float(Ts.max().item())],
+        "cpu_baseline": craters_cpu_baseline(sizes),
     }
     print(json.dumps(line))
 
@@ -467,6 +549,7 @@ def run_adjoint(args):
         "grad_norms": {"rho": float(grho.norm().item()), "emiss": float(gem.norm().item()),
                        "ti": float(gti.norm().item())},
         "build_s": build_s, "operator_device_bytes": int(FF.device_nbytes),
+        "cpu_baseline": adjoint_cpu_baseline(),
     }
     print(json.dumps(line))
 

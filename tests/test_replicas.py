@@ -65,3 +65,11 @@ def test_cpu_baseline_uses_every_requested_process():
     r = bench.cpu_baseline(None, seconds=1.0, workers=2)
     assert r["cores"] == 2 and r["kind"] == "port"
     assert r["value"] > 0 and r["value"] == r["measured_solves_per_s_at_sample"]
+
+
+def test_workload_cpu_baselines_run():
+    sizes = np.array([2000, 5000, 60000])
+    r = bench.craters_cpu_baseline(sizes, seconds=0.5)
+    assert r["cores"] == 1 and 0 < r["value"] < r["sample_facet_steps_per_s"]
+    r = bench.adjoint_cpu_baseline(seconds=0.1)
+    assert r["cores"] == 1 and r["value"] > 0

@@ -396,9 +396,13 @@ int fgb_aca_scratch_floats(int rmax, long long mmax, long long nmax, long long* 
 
 namespace fgb {
 namespace {
-// Scratch of fgb_aca_f64_static: one file-scope device array per device
-// (the module's static data), sized for small batches.  Its address is
-// looked up once per device; the entry point allocates nothing.
+// Scratch of fgb_aca_f64_static, the entry point for callers that cannot
+// allocate device memory (their allocator owns the device, or they call
+// from a region where cudaMalloc is not allowed): one file-scope device
+// array per device (the module's static data), sized for small batches.
+// In host code the array's name is not a device address: the address is
+// looked up with cudaGetSymbolAddress by the first call on each device
+// (before any stream capture), with that device current.
 constexpr long long kAcaStaticFloats = 8LL << 20;   // 32 MiB
 static __device__ __align__(256) float g_aca_static_scratch[kAcaStaticFloats];
 static __device__ __align__(256) int g_aca_static_queue[64];

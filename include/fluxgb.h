@@ -290,16 +290,21 @@ int fgb_aca_f64(const void* bvh, const double* P, const double* N, const double*
                 float* pool, long long pool_capacity, unsigned long long* pool_used,
                 int* rank_out, long long* off_out, int* queue, unsigned* flags, void* stream);
 /*
- * fgb_aca_f64 without caller-provided scratch (no reference counterpart):
- * the factor scratch, the dense-block scratch and the work queue live in
- * the library's static device memory (32 MiB of floats per device, found
- * once per device with cudaGetSymbolAddress); the call allocates nothing.
+ * fgb_aca_f64 without caller-provided scratch (no reference counterpart),
+ * for callers that cannot allocate device memory: a host whose memory is
+ * managed by its own pool or fixed budget, or code that issues the call
+ * inside a region where cudaMalloc is not allowed or too slow.  The factor
+ * scratch, the dense-block scratch and the work queue live in the
+ * library's static device memory (32 MiB of floats per device).  The first
+ * call on a device looks up its address with cudaGetSymbolAddress; make
+ * that first call before any stream capture.  The call allocates nothing.
  * A call whose num_ctas * (fgb_aca_scratch_floats(...) + exact_max) floats
  * exceed that returns FGB_BAD_ARG with the sizes in fgb_last_error().  The
  * queue is zeroed by the call (cudaMemsetAsync on `stream`); *pool_used
  * must be zero on entry, as for fgb_aca_f64.  The static scratch is shared
- * by every call on a device: calls must not overlap (issue them on one
- * stream, or synchronise between streams / host threads).
+ * by every call on a device and keeps the last call's contents: calls that
+ * overlap on the GPU race, so issue them on one stream or synchronise
+ * between streams / host threads.
  */
 int fgb_aca_f64_static(const void* bvh, const double* P, const double* N, const double* A,
                        const long long* perm, long long nblocks, const int* r0, const int* m,

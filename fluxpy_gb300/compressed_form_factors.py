@@ -1390,13 +1390,14 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
 
     @property
     def device_nbytes(self):
-        """Bytes held on the device by the operator (pool, panels, tables)."""
-        tot = self._pool.numel() * self._pool.element_size()
-        for v in list(self._dev.values()) + list(self._build_dev.values()):
-            tot += v.numel() * v.element_size()
+        """Bytes held on the device by the operator (pool unless offloaded,
+        panels, tensor-core operands, tables)."""
+        ts = [self._pool, *self._dev.values(), *self._build_dev.values(),
+              *self.__dict__.get("_tc", {}).values()]
         for pnl, vp in self._panels.values():
-            tot += pnl.numel() * pnl.element_size() + vp.numel() * vp.element_size()
-        return tot
+            ts += [pnl, vp]
+        return sum(t.numel() * t.element_size() for t in ts
+                   if isinstance(t, torch.Tensor) and t.is_cuda)
 
     @property
     def depth(self):

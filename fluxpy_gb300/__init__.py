@@ -7,6 +7,10 @@ Modules mirror the reference package ``flux``:
   solve                    radiosity solves (reference Jacobi / CG; batched BF16)
   model                    steady-state temperature, time-dependent model
   thermal                  per-facet 1-D conduction (Crank-Nicolson)
+  adjoint                  hand-written adjoints of the solve and the conduction
+                           step (torch.autograd.Function), coupled misfit gradient
+  batch                    uneven batches of independent meshes in shared
+                           launches; batched thermal model with CUDA graphs
   terrain                  synthetic meshes used by the benchmarks
 All compute runs in libfluxgb.so (hand-written sm_103a CUDA, C ABI in
 include/fluxgb.h); there is no CPU fallback.

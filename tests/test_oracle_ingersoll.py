@@ -11,7 +11,6 @@ horizon, albedo 0.12, emissivity 0.95).  This pins visibility by other
 geometry (the crater's own rim casts the shadow and blocks the exchange),
 for which the reference's tests hold no fixture."""
 import numpy as np
-import pytest
 from scipy.constants import sigma
 
 from oracle import solve as osolve

@@ -109,3 +109,32 @@ def test_coupled_gradient_matches_finite_differences():
                                    T0=T0, Fgeotherm=Fg, Tobs=Tobs)
             fd = (Lp - Lm) / (2 * h)
             assert abs(fd - grads[key][i]) <= 1e-6 * abs(fd), (key, i, fd, grads[key][i])
+
+
+@pytest.mark.parametrize("nz", [2, 40])
+def test_many_redos_and_the_smallest_grid(nz):
+    """Up to 8 predictor-corrector redos per step (tiny surface temperature
+    with a large flux, a day-long step) and nz = 2: forward bit-identical to
+    the C restatement, adjoint equal to central differences."""
+    z = np.concatenate([[0.0], setgrid(nz, 1.0817 if nz > 2 else 1.0, 1.0 if nz > 2 else 0.1)])
+    w = z.size
+    N = 6
+    T = np.full((N, w), 200.0)
+    T[:, 0] = [1.0, 5.0, 20.0, 200.0, 400.0, 50.0]
+    ti, rhoc = np.full(w, 100.0), np.full(w, 1.2e6)
+    em, Fg = np.full(N, 0.95), np.full(N, 0.02)
+    Qn = np.array([5000.0, 3000.0, 2000.0, 0.0, 0.0, 1000.0])
+    Qnp1 = 1.1 * Qn
+    dt = 86400.0
+    out, _, npass = A.pcc_q_forward(z, dt, Qn, Qnp1, T, ti, rhoc, em, Fg, record=True)
+    ref = T.copy()
+    opcc.step_q(z, dt, Qn, Qnp1, ref, ti, rhoc, em, Fg)
+    assert np.array_equal(out, ref)
+    assert npass.max() >= 6
+    gT = np.random.default_rng(0).standard_normal((N, w))
+    g = A.pcc_q_adjoint(z, dt, Qn, Qnp1, T, np.tile(ti, (N, 1)), rhoc, em, Fg, gT)
+
+    def loss(q):
+        return np.sum(gT * A.pcc_q_forward(z, dt, q, Qnp1, T, ti, rhoc, em, Fg), axis=1)
+    fd = (loss(Qn + 1e-4) - loss(Qn - 1e-4)) / 2e-4
+    assert np.all(np.abs(fd - g[1]) <= 1e-5 * np.abs(fd))

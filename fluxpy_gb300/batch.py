@@ -206,7 +206,10 @@ class MultiMeshThermalModel:
         f32 = torch.float32
 
         def facetvec(v, name):
-            a = np.broadcast_to(np.asarray(v, np.float64), (n,))
+            a = np.asarray(v, np.float64)
+            if a.ndim and a.shape != (n,):
+                raise ValueError(f'"{name}" should be a scalar or have one value per facet')
+            a = np.broadcast_to(a, (n,))
             return op.to_cluster(torch.as_tensor(np.ascontiguousarray(a), dtype=f32,
                                                  device=dev))
 

@@ -37,3 +37,23 @@ def test_version_and_error_strings():
     lib = _lib.lib()
     assert lib.fgb_version().decode().startswith("fluxgb")
     assert isinstance(lib.fgb_last_error().decode(), str)
+
+
+def test_status_codes_map_to_the_reference_exception_types():
+    import pytest
+    _lib.check(_lib.FGB_OK)
+    with pytest.raises(ValueError):
+        _lib.check(_lib.FGB_BAD_ARG, "fgb_x")
+    for st in (_lib.FGB_NONFINITE, _lib.FGB_ZERO_PIVOT, _lib.FGB_CUDA_ERR,
+               _lib.FGB_DEVICE_TIMEOUT, _lib.FGB_NO_MEMORY):
+        with pytest.raises(RuntimeError) as e:
+            _lib.check(st, "fgb_x")
+        assert isinstance(e.value, _lib.FluxGBError) and e.value.status == st
+
+
+def test_no_cpu_fallback_without_a_device(monkeypatch):
+    import pytest
+    import torch
+    monkeypatch.setattr(torch.cuda, "is_available", lambda: False)
+    with pytest.raises(RuntimeError, match="no CPU fallback"):
+        _lib.require_cuda()

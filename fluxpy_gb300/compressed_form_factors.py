@@ -178,6 +178,154 @@ def _bbox3(P, tree):
 LEAF_ZERO, LEAF_DENSE, LEAF_SPARSE, LEAF_LOWRANK, NODE = 0, 1, 2, 3, 4
 
 
+def _nbytes_csr(nnz, m, itemsize):
+    # data + int32 indices + int32 indptr (scipy's index dtype for these sizes)
+    return nnz * (itemsize + 4) + (m + 1) * 4
+
+
+def _classify_exact(nnz, m, n, min_size, itemsize):
+    """Kinds of exact leaves with nnz nonzeros in m x n: zero, dense when
+    below min_size entries and smaller than CSR, else sparse (the
+    reference's choice by bytes, compressed_form_factors.py:313-341)."""
+    nnz = np.asarray(nnz, np.int64)
+    mn = np.asarray(m, np.int64) * np.asarray(n, np.int64)
+    dense = (mn < min_size) & (mn * itemsize < _nbytes_csr(nnz, np.asarray(m, np.int64), itemsize))
+    return np.where(nnz == 0, LEAF_ZERO, np.where(dense, LEAF_DENSE, LEAF_SPARSE)).astype(np.int64)
+
+
+def _admissible_blocks(lo3, hi3, r, c, eta):
+    """min(diam_r, diam_c) <= eta dist(r, c) and dist > 0, per block (bounding
+    boxes of the clusters)."""
+    dr = np.linalg.norm(hi3[r] - lo3[r], axis=1)
+    dc = np.linalg.norm(hi3[c] - lo3[c], axis=1)
+    gap = np.maximum(0.0, np.maximum(lo3[r] - hi3[c], lo3[c] - hi3[r]))
+    dist = np.linalg.norm(gap, axis=1)
+    return (np.minimum(dr, dc) <= eta * dist) & (dist > 0)
+
+
+def _plan_blocks(tree, lo3, hi3, *, tol, min_size, max_depth, force_max_depth, eta, run_aca):
+    """The block tree of the compressed operator, level by level (the
+    decisions of FormFactorBlockMatrix.make_block,
+    compressed_form_factors.py:285-386, with ACA in place of the SVD):
+    a block of an empty cluster is zero; at max_depth or between leaf
+    clusters it is exact; below min_size entries exact; admissible blocks
+    (tol > 0) go to ACA, and those ACA cannot compress are split (or exact
+    where they cannot be); the rest is split into all child-cluster pairs.
+    run_aca(r, c, pool_base) -> (ranks, offsets, pool part or None) for node
+    id arrays r, c.  Block ids follow creation order: the root, its children,
+    then per level the children of the blocks split in level order,
+    followed by the children of the blocks ACA gave back.  Returns the block
+    arrays, the exact leaves and the ACA pool parts."""
+    nch = tree.nch
+    nn = tree.num_nodes
+    has_ch = np.array([ch is not None for ch in tree.children], bool)
+    child_arr = np.full((nn, nch), -1, np.int64)
+    for i in range(1, nn):
+        ch = tree.children[i]
+        if ch is not None:
+            child_arr[i] = ch
+    size = tree.size.astype(np.int64)
+    parts = {k: [] for k in ("rows", "cols", "parent", "depth")}
+    sets = {k: [] for k in ("kind", "child0", "rank", "pool_off")}
+    count = [0]
+
+    def add(r, c, p, d):
+        k = r.size
+        ids = np.arange(count[0], count[0] + k, dtype=np.int64)
+        count[0] += k
+        for key, v in (("rows", r), ("cols", c), ("parent", p), ("depth", d)):
+            parts[key].append(np.asarray(v, np.int64))
+        return ids
+
+    def split(ids, r, c, d):
+        """Children of blocks ids (in order): all pairs of child clusters."""
+        k = ids.size
+        cr, cc = child_arr[r], child_arr[c]
+        R = np.broadcast_to(cr[:, :, None], (k, nch, nch)).reshape(-1)
+        Cc = np.broadcast_to(cc[:, None, :], (k, nch, nch)).reshape(-1)
+        new = add(R, Cc, np.repeat(ids, nch * nch), np.repeat(d + 1, nch * nch))
+        sets["kind"].append((ids, np.full(k, NODE)))
+        sets["child0"].append((ids, new[::nch * nch]))
+        return new, R, Cc, np.repeat(d + 1, nch * nch)
+
+    root = add(np.zeros(1), np.zeros(1), np.full(1, -1), np.zeros(1))
+    sets["kind"].append((root, np.full(1, NODE)))
+    ch_root = tree.children[0]
+    if ch_root is None:
+        lv = (add(np.zeros(1), np.zeros(1), np.zeros(1), np.ones(1)),
+              np.zeros(1, np.int64), np.zeros(1, np.int64), np.ones(1, np.int64))
+        root_bshape = (1, 1)
+    else:
+        cr = np.asarray(ch_root, np.int64)
+        R, Cc = np.repeat(cr, cr.size), np.tile(cr, cr.size)
+        one = np.ones(R.size, np.int64)
+        lv = (add(R, Cc, np.zeros(R.size), one), R, Cc, one)
+        root_bshape = (cr.size, cr.size)
+    sets["child0"].append((root, lv[0][:1]))
+    exact = []
+    pool_parts = []
+    aca_total = 0
+    n_aca = n_failed = 0
+    while lv[0].size:
+        ids, r, c, d = lv
+        m, n = size[r], size[c]
+        zero = (m == 0) | (n == 0)
+        at_max = (d >= max_depth) if max_depth is not None else np.zeros(ids.size, bool)
+        can_split = has_ch[r] & has_ch[c] & ~at_max
+        live = ~zero
+        if force_max_depth and max_depth is not None:
+            fsplit = live & can_split
+        else:
+            fsplit = np.zeros(ids.size, bool)
+        live &= ~fsplit
+        small = live & (m * n < min_size) & (not force_max_depth)
+        live &= ~small
+        cand = np.zeros(ids.size, bool)
+        if tol > 0 and live.any():
+            li = np.flatnonzero(live)
+            cand[li] = _admissible_blocks(lo3, hi3, r[li], c[li], eta)
+        live &= ~cand
+        do_split = fsplit | (live & can_split)
+        sets["kind"].append((ids[zero], np.full(int(zero.sum()), LEAF_ZERO)))
+        exact.append(ids[small | (live & ~can_split)])
+        nxt = []
+        if do_split.any():
+            nxt.append(split(ids[do_split], r[do_split], c[do_split], d[do_split]))
+        if cand.any():
+            ci = np.flatnonzero(cand)
+            ranks, offs, pool = run_aca(r[ci], c[ci], aca_total)
+            n_aca += ci.size
+            if pool is not None:
+                pool_parts.append(pool)
+                aca_total += pool.numel()
+            ok = ranks >= 0
+            sets["kind"].append((ids[ci[ok]], np.full(int(ok.sum()), LEAF_LOWRANK)))
+            sets["rank"].append((ids[ci[ok]], ranks[ok].astype(np.int64)))
+            sets["pool_off"].append((ids[ci[ok]], offs[ok].astype(np.int64)))
+            bad = ci[~ok]
+            n_failed += bad.size
+            sp = bad[can_split[bad]]
+            exact.append(ids[bad[~can_split[bad]]])
+            if sp.size:
+                nxt.append(split(ids[sp], r[sp], c[sp], d[sp]))
+        if nxt:
+            lv = tuple(np.concatenate([x[i] for x in nxt]) for i in range(4))
+        else:
+            lv = (np.zeros(0, np.int64),) * 4
+    nb = count[0]
+    out = {k: np.concatenate(v) for k, v in parts.items()}
+    defaults = {"kind": -1, "child0": -1, "rank": 0, "pool_off": -1}
+    for key, dflt in defaults.items():
+        a = np.full(nb, dflt, np.int64)
+        for ids, vals in sets[key]:
+            a[ids] = vals
+        out[key] = a
+    out.update(exact=np.concatenate(exact) if exact else np.zeros(0, np.int64),
+               aca_pool_parts=pool_parts, root_bshape=root_bshape, aca_blocks=n_aca,
+               aca_failed=n_failed)
+    return out
+
+
 class fgb_op_desc(C.Structure):
     """ctypes mirror of struct fgb_op_desc (include/fluxgb.h)."""
     _fields_ = [
@@ -199,11 +347,6 @@ ITEM_COLS = 2048
 PANEL_ALIGN = 64
 # Z rows computed per CTA by the tensor-core phase A
 TC_A_ROWS = 128
-
-
-def _nbytes_csr(nnz, m, itemsize):
-    # data + int32 indices + int32 indptr (scipy's index dtype for these sizes)
-    return nnz * (itemsize + 4) + (m + 1) * 4
 
 
 class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
@@ -307,145 +450,55 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         iperm[tree.perm] = np.arange(N)
         self._iperm_d = torch.as_tensor(iperm, device=dev)
 
-        # block records
-        rows, cols, parent, kind, child0, depth = [], [], [], [], [], []
-        rank, pool_off = [], []
-
-        def add(r, c, p, d):
-            rows.append(r); cols.append(c); parent.append(p); kind.append(-1)
-            child0.append(-1); depth.append(d); rank.append(0); pool_off.append(-1)
-            return len(rows) - 1
-
-        root = add(0, 0, -1, 0)
-        kind[root] = NODE
-        ch_root = tree.children[0]
-        if ch_root is None:
-            # a single cluster: one exact leaf below a 1 x 1 root
-            level = [add(0, 0, root, 1)]
-            child0[root] = level[0]
-            self._root_bshape = (1, 1)
-        else:
-            level = []
-            for r in ch_root:
-                for c in ch_root:
-                    level.append(add(r, c, root, 1))
-            child0[root] = level[0]
-            self._root_bshape = (len(ch_root), len(ch_root))
-
         tol = float(self._tol)
-        maxd = self._max_depth
-        exact = []
-        aca_pool_parts = []
-        aca_total = 0
-        t_aca = 0.0
-        n_aca_blocks = 0
-        n_aca_failed = 0
-        while level:
-            cand_aca = []
-            next_level = []
-            for b in level:
-                r, c, d = rows[b], cols[b], depth[b]
-                m, n = tree.size[r], tree.size[c]
-                if m == 0 or n == 0:
-                    kind[b] = LEAF_ZERO
-                    continue
-                at_max = maxd is not None and d >= maxd
-                can_split = (tree.children[r] is not None and tree.children[c] is not None
-                             and not at_max)
-                if self._force_max_depth and maxd is not None and not at_max and can_split:
-                    self._split(b, tree, rows, cols, parent, kind, child0, depth, rank,
-                                pool_off, next_level, add)
-                    continue
-                if m * n < self._min_size and not self._force_max_depth:
-                    exact.append(b)
-                    continue
-                if tol > 0 and self._admissible(lo3, hi3, r, c):
-                    cand_aca.append(b)
-                    continue
-                if can_split:
-                    self._split(b, tree, rows, cols, parent, kind, child0, depth, rank,
-                                pool_off, next_level, add)
-                else:
-                    exact.append(b)
-            if cand_aca:
-                t0 = time.perf_counter()
-                ranks, offs, pool = self._run_aca(cand_aca, rows, cols, tree, perm_d, aca_total)
-                t_aca += time.perf_counter() - t0
-                n_aca_blocks += len(cand_aca)
-                if pool is not None:
-                    aca_pool_parts.append(pool)
-                    aca_total += pool.numel()
-                for b, k, off in zip(cand_aca, ranks, offs):
-                    if k >= 0:
-                        kind[b] = LEAF_LOWRANK
-                        rank[b] = int(k)
-                        pool_off[b] = int(off)
-                    else:
-                        n_aca_failed += 1
-                        r, c, d = rows[b], cols[b], depth[b]
-                        at_max = maxd is not None and d >= maxd
-                        if (tree.children[r] is not None and tree.children[c] is not None
-                                and not at_max):
-                            self._split(b, tree, rows, cols, parent, kind, child0, depth, rank,
-                                        pool_off, next_level, add)
-                        else:
-                            exact.append(b)
-            level = next_level
+        t_aca = [0.0]
 
-        self._rows = np.array(rows, np.int64)
-        self._cols = np.array(cols, np.int64)
-        self._parent = np.array(parent, np.int64)
-        self._kind = np.array(kind, np.int64)
-        self._child0 = np.array(child0, np.int64)
-        self._depth = np.array(depth, np.int64)
-        self._rank = np.array(rank, np.int64)
+        def run_aca(r, c, base):
+            t0 = time.perf_counter()
+            out = self._run_aca(r, c, tree, perm_d, base)
+            t_aca[0] += time.perf_counter() - t0
+            return out
+
+        plan = _plan_blocks(tree, lo3, hi3, tol=tol, min_size=self._min_size,
+                            max_depth=self._max_depth, force_max_depth=self._force_max_depth,
+                            eta=self._eta, run_aca=run_aca)
+        self._rows, self._cols = plan["rows"], plan["cols"]
+        self._parent, self._kind = plan["parent"], plan["kind"]
+        self._child0, self._depth = plan["child0"], plan["depth"]
+        self._rank = plan["rank"]
+        self._root_bshape = plan["root_bshape"]
+        exact = plan["exact"]
         t0 = time.perf_counter()
-        self._assemble(exact, aca_pool_parts, pool_off)
+        self._assemble(exact, plan["aca_pool_parts"], plan["pool_off"])
         t_exact = time.perf_counter() - t0
         torch.cuda.synchronize()
-        self.stats.update(build_s=time.perf_counter() - t_start, aca_s=t_aca, exact_s=t_exact,
-                          aca_blocks=n_aca_blocks, aca_failed=n_aca_failed,
-                          lowrank_blocks=int((self._kind == LEAF_LOWRANK).sum()),
-                          exact_blocks=len(exact), num_blocks=len(rows),
-                          lowrank_entries=int(sum(self._rank[b] * (tree.size[self._rows[b]] +
-                                                                   tree.size[self._cols[b]])
-                                                  for b in np.where(self._kind == LEAF_LOWRANK)[0])))
+        lrm = self._kind == LEAF_LOWRANK
+        self.stats.update(build_s=time.perf_counter() - t_start, aca_s=t_aca[0], exact_s=t_exact,
+                          aca_blocks=plan["aca_blocks"], aca_failed=plan["aca_failed"],
+                          lowrank_blocks=int(lrm.sum()),
+                          exact_blocks=int(exact.size), num_blocks=int(self._rows.size),
+                          lowrank_entries=int(np.sum(self._rank[lrm] *
+                                                     (tree.size[self._rows[lrm]] +
+                                                      tree.size[self._cols[lrm]]))))
 
-    def _split(self, b, tree, rows, cols, parent, kind, child0, depth, rank, pool_off,
-               next_level, add):
-        r, c, d = rows[b], cols[b], depth[b]
-        kind[b] = NODE
-        first = None
-        for rc in tree.children[r]:
-            for cc in tree.children[c]:
-                nb = add(rc, cc, b, d + 1)
-                if first is None:
-                    first = nb
-                next_level.append(nb)
-        child0[b] = first
-
-    def _admissible(self, lo3, hi3, r, c):
-        dr = np.linalg.norm(hi3[r] - lo3[r])
-        dc = np.linalg.norm(hi3[c] - lo3[c])
-        gap = np.maximum(0.0, np.maximum(lo3[r] - hi3[c], lo3[c] - hi3[r]))
-        dist = np.linalg.norm(gap)
-        return min(dr, dc) <= self._eta * dist and dist > 0
-
-    def _run_aca(self, blocks, rows, cols, tree, perm_d, pool_base):
+    def _run_aca(self, r, c, tree, perm_d, pool_base):
+        """ACA of the blocks with row clusters r and column clusters c (node
+        id arrays); returns per block the rank (-1: not compressible under
+        the cap), the pool offset and the new pool part."""
         sm = self.shape_model
         dev = sm._device
         if np.dtype(sm.dtype) != np.float64:
             raise NotImplementedError("low-rank compression needs a float64 shape model")
         P, Nn, A = sm.device_geometry()
         # largest blocks first
-        sizes = np.array([tree.size[rows[b]] * tree.size[cols[b]] for b in blocks])
+        sizes = tree.size[r] * tree.size[c]
         order = np.argsort(-sizes, kind="stable")
-        blocks_sorted = [blocks[i] for i in order]
-        r0 = np.array([tree.start[rows[b]] for b in blocks_sorted], np.int32)
-        m = np.array([tree.size[rows[b]] for b in blocks_sorted], np.int32)
-        c0 = np.array([tree.start[cols[b]] for b in blocks_sorted], np.int32)
-        n = np.array([tree.size[cols[b]] for b in blocks_sorted], np.int32)
-        nb = len(blocks_sorted)
+        rs, cs = r[order], c[order]
+        r0 = tree.start[rs].astype(np.int32)
+        m = tree.size[rs].astype(np.int32)
+        c0 = tree.start[cs].astype(np.int32)
+        n = tree.size[cs].astype(np.int32)
+        nb = int(rs.size)
         mmax, nmax = int(m.max()), int(n.max())
         rmax = self._rmax
         per_cta = C.c_longlong()
@@ -495,7 +548,7 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         perm_d = self._perm_d
         sdt = self._store_dtype
         tdt = torch.float64 if sdt == np.float64 else torch.float32
-        exact = np.array(sorted(exact), dtype=np.int64)
+        exact = np.sort(np.asarray(exact, dtype=np.int64))
         if exact.size:
             er = tree.start[self._rows[exact]]
             em = tree.size[self._rows[exact]]
@@ -507,7 +560,9 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         ex_n = tree.size[self._cols[exact]].astype(np.int64) if exact.size else np.zeros(0, np.int64)
         self._leaf_nnz = np.zeros(len(self._rows), np.int64)
         self._exact = exact
-        self._exact_index = {int(b): q for q, b in enumerate(exact)}
+        # position of each exact leaf in the pair kernel's output (-1: none)
+        self._exact_pos = np.full(len(self._rows), -1, np.int64)
+        self._exact_pos[exact] = np.arange(exact.size)
         if exact.size:
             tcsr = ff_tiles(sm, perm_d, perm_d, ex_r0, ex_m, ex_c0, ex_n, self._eps,
                             keep_bits=True, out_dtype=tdt)
@@ -522,15 +577,8 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
             self._exact_csr = None
         # classify exact leaves as the reference would (zero / dense / CSR by bytes)
         isz = np.dtype(self.shape_model.dtype).itemsize
-        for q, b in enumerate(exact):
-            nnz = self._leaf_nnz[b]
-            m, n = ex_m[q], ex_n[q]
-            if nnz == 0:
-                self._kind[b] = LEAF_ZERO
-            elif m * n < self._min_size and m * n * isz < _nbytes_csr(nnz, m, isz):
-                self._kind[b] = LEAF_DENSE
-            else:
-                self._kind[b] = LEAF_SPARSE
+        self._kind[exact] = _classify_exact(self._leaf_nnz[exact], ex_m, ex_n,
+                                            self._min_size, isz)
         aca = (torch.cat(aca_pool_parts) if aca_pool_parts else
                torch.zeros(1, dtype=torch.float32, device=dev))
         self._pool = aca.to(tdt)
@@ -1493,6 +1541,10 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
     def __setstate__(self, st):
         from .form_factors import TileCSR
         self.__dict__.update(st)
+        if "_exact_pos" not in st and "_exact_index" in st:
+            self._exact_pos = np.full(len(self._rows), -1, np.int64)
+            for b, q in st["_exact_index"].items():
+                self._exact_pos[b] = q
         dev = self.shape_model._device
         for key in ("_pool", "_perm_d", "_iperm_d"):
             setattr(self, key, getattr(self, key).to(dev))
@@ -1517,10 +1569,10 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         columns in the reference's ascending-id order."""
         tree = self._tree
         m, n = int(tree.size[self._rows[b]]), int(tree.size[self._cols[b]])
-        q = self._exact_index.get(int(b))
+        q = int(self._exact_pos[b])
         mat = np.zeros((m, n), dtype=self.dtype)
         tc = self._exact_csr
-        if q is None or tc is None:
+        if q < 0 or tc is None:
             return mat
         r0, r1 = int(tc.row_off[q]), int(tc.row_off[q + 1])
         ip = tc.indptr[r0:r1 + 1].cpu().numpy()

@@ -39,7 +39,7 @@ def _rank(rank, world, port, out):
 def test_two_gloo_ranks_replicas():
     world = 2
     port = _free_port()
-    with mp.Manager() as man:
+    with mp.get_context("spawn").Manager() as man:
         out = man.dict()
         mp.spawn(_rank, args=(world, port, out), nprocs=world, join=True)
         res = dict(out)

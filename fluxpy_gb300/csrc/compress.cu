@@ -13,7 +13,19 @@
 // it fails, the row of the worst sample becomes the next pivot row.
 // A block whose rank would reach its cap (storage no smaller than half the
 // dense block, or rmax) is reported as failed (rank -1) and is subdivided by
-// the host.
+// the host.  Two more outcomes guard against visibility-made sparsity:
+//  * a sampled block accepted with k > 0 terms whose nonzeros, estimated
+//    from the random samples, would take no more bytes stored exactly than
+//    its factors (2 nnz <= k (m + n): the reference's choice between a CSR
+//    and an SVD block by bytes) is reported as failed too: such blocks are
+//    scattered visible pairs that partial pivoting misses, and their
+//    children are approximated again (small ones with every entry known);
+//  * a block whose every entry is known is reported as "store exactly"
+//    (rank -3) when the near-field panel rows its nonzeros need (one
+//    64-weight row per 64-row tile and column that holds a nonzero) take no
+//    more weights than the factors.
+// A sampled block is accepted as zero only after kZeroRounds rounds of
+// samples without a nonzero entry.
 //
 // One CTA per block (persistent CTAs take blocks from a queue, largest
 // first).  The residual row/column, U and V live in a per-CTA FP32 scratch
@@ -24,7 +36,10 @@
 #include "common.cuh"
 #include "ffentry.cuh"
 
+#include <climits>
 #include <mutex>
+
+#include <cuda.h>  // CUcontext and the driver types, resolved at run time
 
 namespace fgb {
 BvhView view_of(const void* handle);
@@ -32,6 +47,8 @@ BvhView view_of(const void* handle);
 namespace {
 
 constexpr int kAcaThreads = 256;
+// sampling rounds that must all find nothing before a block is zero
+constexpr int kZeroRounds = 4;
 
 struct AcaArgs {
   BvhView bvh;
@@ -161,8 +178,10 @@ aca_kernel(AcaArgs a, EntryCtx<R> e) {
     const unsigned bseed = 0x9e3779b9u ^ (unsigned)(b * 2654435761ull);
     int istar = m / 2;
     bool failed = false;
+    bool store_exact = false;
     int rounds = 0;
     bool verify = false;
+    double hits = 0.0, samples = 0.0;   // random samples and their nonzero entries
     const int max_rounds = 4 * a.rmax + 8;
     __syncthreads();
     if ((long long)m * n <= a.exact_max) {
@@ -181,6 +200,22 @@ aca_kernel(AcaArgs a, EntryCtx<R> e) {
         if (pq < 0 || fabsf(val) > fabsf(pv)) { pv = val; pq = (int)q; }
       }
       a2 = block_sum(a2, sh_d);
+      // near-field panel rows the exact block would need: (64-row tile,
+      // column) pairs that hold a nonzero
+      double prows = 0.0;
+      {
+        const long long t_first = r0 >> 6;
+        const int ntile = (int)(((r0 + m - 1) >> 6) - t_first + 1);
+        for (long long q = tid; q < (long long)ntile * n; q += kAcaThreads) {
+          const int t = (int)(q / n), j = (int)(q % n);
+          const long long i0 = max(0LL, ((t_first + t) << 6) - r0);
+          const long long i1 = min((long long)m, ((t_first + t + 1) << 6) - r0);
+          bool any = false;
+          for (long long i = i0; i < i1 && !any; i++) any = Rm[i * n + j] != 0.f;
+          prows += any ? 1.0 : 0.0;
+        }
+      }
+      prows = block_sum(prows, sh_d);
       double res2 = a2;
       while (res2 > (double)a.tol * a.tol * a2) {
         float piv;
@@ -206,6 +241,7 @@ aca_kernel(AcaArgs a, EntryCtx<R> e) {
         res2 = block_sum(r2, sh_d);
         k++;
       }
+      if (!failed && k > 0 && 64.0 * prows <= (double)k * (double)(m + n)) store_exact = true;
     } else
     while (true) {
       if (!verify) {
@@ -294,7 +330,7 @@ aca_kernel(AcaArgs a, EntryCtx<R> e) {
       }
       // ---- verification: Monte Carlo estimate of |R|_F^2 from nsample random entries
       if (++rounds > max_rounds) { failed = true; break; }
-      double rs = 0.0;
+      double rs = 0.0, nzr = 0.0;
       float wmax_v = 0.f;
       int wmax_i = -1;
       bool any_nz = false;
@@ -305,20 +341,32 @@ aca_kernel(AcaArgs a, EntryCtx<R> e) {
         unsigned h2 = h * 0x9e3779b1u + 0x7f4a7c15u;
         h2 ^= h2 >> 13; h2 *= 0x5bd1e995u; h2 ^= h2 >> 15;
         const int j = (int)(h2 % (unsigned)n);
-        float val = entry<R>(a, e, prow[i], pcol[j], &overflow);
+        const float raw = entry<R>(a, e, prow[i], pcol[j], &overflow);
+        float val = raw;
         for (int l = 0; l < k; l++) val -= U[(long long)l * a.mmax + i] * V[(long long)l * a.nmax + j];
         rs += (double)val * val;
+        nzr += raw != 0.f ? 1.0 : 0.0;
         if (val != 0.f) any_nz = true;
         if (used_r[i] == 0.f && (wmax_i < 0 || fabsf(val) > fabsf(wmax_v))) { wmax_v = val; wmax_i = i; }
       }
       rs = block_sum(rs, sh_d);
+      hits += block_sum(nzr, sh_d);
+      samples += (double)a.nsample;
       const int nz = __syncthreads_or(any_nz);
       float wv;
       int wi;
       block_argmax(wmax_v, wmax_i, sh_v, sh_i, &wv, &wi);
       const double est = rs * ((double)m * (double)n / (double)a.nsample);
       const bool ok = (normS2 > 0.0) ? (est <= (double)a.tol * a.tol * normS2) : (nz == 0);
-      if (ok) break;
+      // a zero block needs kZeroRounds empty rounds (fresh samples each)
+      if (ok && normS2 == 0.0 && rounds < kZeroRounds) continue;
+      if (ok) {
+        // scattered visible pairs: cheaper stored exactly than as factors,
+        // and what partial pivoting misses; approximate the children again
+        if (k > 0 && 2.0 * (hits / samples) * (double)m * (double)n <= (double)k * (double)(m + n))
+          failed = true;
+        break;
+      }
       if (wi < 0 || wv == 0.0f) {
         // the worst sample sits on an already used row: fall back to any unused row
         int cand = -1;
@@ -344,8 +392,8 @@ aca_kernel(AcaArgs a, EntryCtx<R> e) {
       }
       if (__syncthreads_or(bad)) failed = true;
     }
-    if (failed) {
-      if (tid == 0) { a.rank_out[b] = -1; a.off_out[b] = -1; }
+    if (failed || store_exact) {
+      if (tid == 0) { a.rank_out[b] = failed ? -1 : -3; a.off_out[b] = -1; }
       continue;
     }
     // copy out U^T (k x m) then V^T (k x n)
@@ -384,8 +432,10 @@ aca_kernel(AcaArgs a, EntryCtx<R> e) {
 extern "C" {
 
 int fgb_aca_scratch_floats(int rmax, long long mmax, long long nmax, long long* per_cta) {
-  if (rmax < 1 || rmax > 128 || mmax < 1 || nmax < 1) {
-    fgb::set_error("bad ACA sizes (rmax in [1,128])");
+  // block sides are int in the kernel: bounding them also keeps the product
+  // below 2^40 (no overflow)
+  if (rmax < 1 || rmax > 128 || mmax < 1 || nmax < 1 || mmax > INT_MAX || nmax > INT_MAX) {
+    fgb::set_error("bad ACA sizes (rmax in [1,128], block sides in [1, 2^31))");
     return FGB_BAD_ARG;
   }
   *per_cta = (long long)rmax * (mmax + nmax) + 2 * (mmax + nmax);
@@ -408,25 +458,64 @@ static __device__ __align__(256) float g_aca_static_scratch[kAcaStaticFloats];
 static __device__ __align__(256) int g_aca_static_queue[64];
 
 struct StaticAcaSlot {
+  unsigned long long ctx_id = 0;   // context the addresses belong to
   float* scratch = nullptr;
   int* queue = nullptr;
 };
 std::mutex g_aca_static_mutex;
 StaticAcaSlot g_aca_static_slots[64];
 
+// The symbol addresses of the current device, looked up once per context:
+// a context created after cudaDeviceReset loads the module again, possibly
+// elsewhere, so the cached addresses are keyed by the context's unique id.
+// The two driver calls are resolved through the runtime
+// (cudaGetDriverEntryPoint), so the library does not link libcuda itself.
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+int current_context_id(unsigned long long* id) {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPoint("cuCtxGetCurrent", &f, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPoint("cuCtxGetId", &f, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<CtxGetIdFn>(f);
+  });
+  CUcontext ctx = nullptr;
+  if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx ||
+      get_id(ctx, id) != CUDA_SUCCESS) {
+    set_error("fgb_aca_f64_static: no current CUDA context");
+    return FGB_CUDA_ERR;
+  }
+  return FGB_OK;
+}
+
 int static_aca_slot(StaticAcaSlot* out) {
   int dev = 0;
   FGB_CUDA_TRY(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 64) { set_error("device index out of range"); return FGB_BAD_ARG; }
+  // make the runtime's context current (a no-op when it already is)
+  FGB_CUDA_TRY(cudaFree(nullptr));
+  unsigned long long id = 0;
+  int st = current_context_id(&id);
+  if (st) return st;
   std::lock_guard<std::mutex> lock(g_aca_static_mutex);
   StaticAcaSlot& s = g_aca_static_slots[dev];
-  if (!s.scratch) {
+  if (!s.scratch || s.ctx_id != id) {
     void* p = nullptr;
     void* q = nullptr;
     FGB_CUDA_TRY(cudaGetSymbolAddress(&p, g_aca_static_scratch));
     FGB_CUDA_TRY(cudaGetSymbolAddress(&q, g_aca_static_queue));
     s.scratch = static_cast<float*>(p);
     s.queue = static_cast<int*>(q);
+    s.ctx_id = id;
   }
   *out = s;
   return FGB_OK;
@@ -490,13 +579,14 @@ int fgb_aca_f64_static(const void* bvh, const double* P, const double* N, const 
   if (st) return st;
   if (exact_max < 0) exact_max = 0;
   // per CTA: the factor scratch slice, then (blocks with m n <= exact_max)
-  // the dense block
-  const long long need = (long long)num_ctas * (per_cta + exact_max);
-  if (need > fgb::kAcaStaticFloats) {
-    fgb::set_error("fgb_aca_f64_static: needs %lld floats of scratch for %d CTAs "
-                   "(rmax %d, mmax %lld, nmax %lld, exact_max %lld); the static scratch holds "
-                   "%lld: use fewer CTAs, smaller blocks or fgb_aca_f64",
-                   need, num_ctas, rmax, mmax, nmax, exact_max, fgb::kAcaStaticFloats);
+  // the dense block.  Each term is bounded before the sum and the division
+  // replaces the product, so no size wraps around.
+  const long long cap = fgb::kAcaStaticFloats;
+  if (per_cta > cap || exact_max > cap || per_cta + exact_max > cap / num_ctas) {
+    fgb::set_error("fgb_aca_f64_static: %d CTAs x (%lld + %lld) floats of scratch "
+                   "(rmax %d, mmax %lld, nmax %lld, exact_max %lld) exceed the static scratch "
+                   "of %lld floats: use fewer CTAs, smaller blocks or fgb_aca_f64",
+                   num_ctas, per_cta, exact_max, rmax, mmax, nmax, exact_max, cap);
     return FGB_BAD_ARG;
   }
   fgb::StaticAcaSlot slot;

@@ -52,6 +52,7 @@ enum fgb_status {
 #define FGB_FLAG_INDEX_RANGE    (1u << 7)
 #define FGB_FLAG_RANK_CAP       (1u << 8) /* ACA reached its rank cap       */
 #define FGB_FLAG_DEVICE_TIMEOUT (1u << 9) /* a bounded device-side wait ran out */
+#define FGB_FLAG_NO_CONVERGE    (1u << 10) /* a Jacobi eigen solve hit its sweep cap */
 
 /* Message of the last failed call on this host thread ("" if none). */
 const char* fgb_last_error(void);
@@ -297,7 +298,10 @@ int fgb_aca_f64(const void* bvh, const double* P, const double* N, const double*
  * scratch, the dense-block scratch and the work queue live in the
  * library's static device memory (32 MiB of floats per device).  The first
  * call on a device looks up its address with cudaGetSymbolAddress; make
- * that first call before any stream capture.  The call allocates nothing.
+ * that first call before any stream capture.  The address is kept for the
+ * life of the CUDA context it was looked up in: after cudaDeviceReset the
+ * next call (the first one in the new context) looks it up again.  The call
+ * allocates nothing.
  * A call whose num_ctas * (fgb_aca_scratch_floats(...) + exact_max) floats
  * exceed that returns FGB_BAD_ARG with the sizes in fgb_last_error().  The
  * queue is zeroed by the call (cudaMemsetAsync on `stream`); *pool_used
@@ -313,6 +317,26 @@ int fgb_aca_f64_static(const void* bvh, const double* P, const double* N, const 
                        int num_ctas, float* pool, long long pool_capacity,
                        unsigned long long* pool_used, int* rank_out, long long* off_out,
                        unsigned* flags, void* stream);
+/*
+ * Rank truncation of low-rank factors in FP64, replacing the reference's SVD
+ * truncation of a block (src/flux/linalg.py:20-51, estimate_rank, applied by
+ * FormFactor2dTreeBlock._get_svd_block, compressed_form_factors.py:388-405:
+ * keep the singular values with sigma_i / sigma_0 > tol).
+ * Block b holds U^T (k x m) then V^T (k x n) at pool_in + off_in[b], FP32,
+ * k = rank_in[b].  The singular values of U V^T come from the FP64 Gram
+ * matrices of U and V (Jacobi eigen-decompositions, no block formed); the
+ * truncated factors U'^T (r x m) then V'^T (r x n) (U' orthogonal columns
+ * scaled by sigma, V' orthonormal) are written to pool_out at off_out[b]
+ * (bump allocator *pool_used, zero on entry; pool_capacity floats), with
+ * r in rank_out[b].  Blocks of rank 0 or 1 are copied, blocks of rank above
+ * 64 copied with FGB_FLAG_INDEX_RANGE, negative ranks passed through.  A full
+ * pool gives rank -2 and FGB_FLAG_RANK_CAP; an eigen solve that hit its sweep
+ * cap sets FGB_FLAG_NO_CONVERGE.  queue: two zeroed ints.
+ */
+int fgb_recompress_f32(const float* pool_in, const long long* off_in, const int* rank_in,
+                       const int* m, const int* n, long long nblocks, float tol, float* pool_out,
+                       long long pool_capacity, unsigned long long* pool_used, int* rank_out,
+                       long long* off_out, int* queue, unsigned* flags, void* stream);
 
 /* ----------------------------------------------- block matvec (a9) */
 /*

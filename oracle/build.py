@@ -5,6 +5,9 @@
   (``src/flux/pcc/{conductionQ,conductionT,tridag}.c``) compiled directly
   with gcc from where they lie in the reference tree, when that tree is
   present (it is not on GPU machines, which then use ``liboracle.so``).
+  The tree is ``$FLUXPY_REFERENCE``; unset, this recipe looks at the
+  checkout's usual place in the build container, and without either it
+  builds only ``liboracle.so`` and says so.
 
 Both are compiled with ``-ffp-contract=off`` so that results do not depend on
 FMA contraction (gcc contracts by default on aarch64).
@@ -13,13 +16,22 @@ from __future__ import annotations
 
 import os
 import subprocess
+import sys
 from pathlib import Path
 
 ORACLE_DIR = Path(__file__).resolve().parent
 REF_DIR = ORACLE_DIR / "_ref"
 ORACLE_LIB = ORACLE_DIR / "liboracle.so"
 REF_PCC_LIB = REF_DIR / "libpcc_ref.so"
-REFERENCE_ROOT = Path(os.environ.get("FLUXPY_REFERENCE", "/root/reference"))
+# the build container's read-only checkout of the reference
+_CHECKOUT = Path("/root/reference")
+
+
+def reference_root() -> Path | None:
+    env = os.environ.get("FLUXPY_REFERENCE")
+    if env:
+        return Path(env)
+    return _CHECKOUT if _CHECKOUT.is_dir() else None
 REF_PCC_SOURCES = ["conductionQ.c", "conductionT.c", "tridag.c"]
 
 CFLAGS = ["-O2", "-fPIC", "-shared", "-std=gnu11", "-ffp-contract=off", "-fno-fast-math"]
@@ -47,9 +59,16 @@ def build_oracle() -> Path:
 
 
 def build_ref() -> Path | None:
-    pcc = REFERENCE_ROOT / "src" / "flux" / "pcc"
+    root = reference_root()
+    if root is None:
+        print("oracle/build.py: no reference tree (set FLUXPY_REFERENCE); "
+              "oracle/_ref not built", file=sys.stderr)
+        return None
+    pcc = root / "src" / "flux" / "pcc"
     srcs = [pcc / s for s in REF_PCC_SOURCES]
     if not all(s.exists() for s in srcs):
+        print(f"oracle/build.py: {pcc} lacks {REF_PCC_SOURCES}; oracle/_ref not built",
+              file=sys.stderr)
         return None
     REF_DIR.mkdir(exist_ok=True)
     if _newer(REF_PCC_LIB, srcs):

@@ -17,7 +17,7 @@
  *
  * Pinned against the reference's golden files
  * tests/data/thermal/pcc_thermal_model_1d/{Tsurface,Tprofile}_conductionQ
- * (tests/test_golden_pcc.py) and against the reference C sources compiled
+ * (tests/test_pcc_oracle.py) and against the reference C sources compiled
  * into oracle/_ref when they are available.
  */
 #include <math.h>

@@ -1,9 +1,9 @@
 """Generate the golden fixtures under tests/golden/ from the reference tree.
 
-Run in a container that has the fluxpy reference checked out (read-only) at
-$FLUXPY_REFERENCE (default /root/reference):
+Run where the fluxpy reference is checked out (read-only), with
+FLUXPY_REFERENCE naming that checkout:
 
-    python tests/golden/make_golden.py [section ...]
+    FLUXPY_REFERENCE=<checkout> python tests/golden/make_golden.py [section ...]
 
 Sections:
   pcc      the reference's PCC golden files
@@ -13,6 +13,11 @@ Sections:
   spheres  the reference's sphere meshes (tests/data/icosa_sphere*.npz,
            used by tests/test_shape.py / test_form_factors.py there) copied
            as V/F arrays into spheres.npz.
+  tree     the block-tree introspection of the reference's compressed
+           matrices at tol = 0 (compressed_form_factors.py:808-847:
+           get_blocks_at_depth, get_row_inds_at_depth, get_row_blocks,
+           get_col_inds_for_row, depth, nbytes) on the stretched octree
+           sphere and the quadtree crater at depths 1-3, into tree.npz.
   ffref    form-factor matrices and steady-state solves computed by the
            reference's Python code (src/flux/form_factors.py,
            compressed_form_factors.py, solve.py, model.py), imported from the
@@ -32,7 +37,19 @@ from pathlib import Path
 import numpy as np
 
 HERE = Path(__file__).resolve().parent
-REF = Path(os.environ.get("FLUXPY_REFERENCE", "/root/reference"))
+
+
+def _reference_root() -> Path:
+    root = os.environ.get("FLUXPY_REFERENCE")
+    if not root:
+        sys.exit("make_golden.py: set FLUXPY_REFERENCE to the fluxpy reference checkout")
+    path = Path(root)
+    if not (path / "src" / "flux").is_dir():
+        sys.exit(f"make_golden.py: FLUXPY_REFERENCE={root} holds no src/flux tree")
+    return path
+
+
+REF = _reference_root() if __name__ == "__main__" else None
 
 
 def make_pcc():
@@ -169,7 +186,64 @@ def make_ffref():
     print("ffref:", {k: getattr(v, "shape", v) for k, v in out.items()})
 
 
-SECTIONS = {"pcc": make_pcc, "spheres": make_spheres, "ffref": make_ffref}
+def _record_tree(out, p, C, rows):
+    """The reference operator C's introspection answers under prefix p."""
+    out[f"{p}_depth"] = C.depth
+    out[f"{p}_nbytes"] = C.nbytes
+    out[f"{p}_root_types"] = np.array([type(b).__name__ for b in C._root._blocks.ravel()])
+    out[f"{p}_root_nbytes"] = np.array([b.nbytes for b in C._root._blocks.ravel()], np.int64)
+    for d in range(C.depth + 1):
+        try:
+            blocks = list(C.get_blocks_at_depth(d))
+        except Exception as e:
+            # recorded as the exception's type (the reference's leaves lack
+            # _get_blocks_at_depth, so its traversal fails at any leaf below
+            # the root)
+            out[f"{p}_bad{d}_error"] = np.array(type(e).__name__)
+            blocks = None
+        if blocks is not None:
+            out[f"{p}_bad{d}_types"] = np.array([type(b).__name__ for b in blocks])
+            out[f"{p}_bad{d}_shapes"] = np.array([b.shape for b in blocks],
+                                                 np.int64).reshape(-1, 2)
+            out[f"{p}_bad{d}_nbytes"] = np.array([b.nbytes for b in blocks], np.int64)
+        sets = list(C.get_row_inds_at_depth(d))
+        out[f"{p}_rid{d}"] = np.concatenate(sets).astype(np.int64)
+        out[f"{p}_rid{d}_len"] = np.array([len(x) for x in sets], np.int64)
+    out[f"{p}_rows"] = np.asarray(rows, np.int64)
+    for i, r in enumerate(rows):
+        blocks = list(C.get_row_blocks(int(r)))
+        out[f"{p}_rb{i}_types"] = np.array([type(b).__name__ for b in blocks])
+        out[f"{p}_rb{i}_shapes"] = np.array([b.shape for b in blocks], np.int64).reshape(-1, 2)
+        sets = list(C.get_col_inds_for_row(int(r)))
+        out[f"{p}_ci{i}"] = np.concatenate(sets).astype(np.int64)
+        out[f"{p}_ci{i}_len"] = np.array([len(x) for x in sets], np.int64)
+
+
+def make_tree():
+    """Block-tree introspection of the reference's compressed matrices."""
+    shape, ff, cff, solve, model = import_reference()
+    sys.path.insert(0, str(HERE.parent.parent))
+    from fluxpy_gb300 import terrain
+    Shape = oracle_shape_class(shape, 0)
+    out = {}
+    # the stretched sphere of tests/test_compressed_form_factors.py:25-76
+    ref = np.load(HERE / "ffref.npz")
+    sms = Shape(ref["octsphere_V"], ref["octsphere_F"])
+    sms.N[:] = ref["octsphere_N"]
+    C = cff.CompressedFormFactorMatrix(sms, tol=0, max_depth=1, force_max_depth=True,
+                                       RootBlock=cff.FormFactorOctreeBlock)
+    _record_tree(out, "octsphere", C, [0, 17, 160, sms.num_faces - 1])
+    V, F = terrain.spherical_crater()
+    sm = Shape(V, F)
+    for depth in (1, 2, 3):
+        Cq = cff.CompressedFormFactorMatrix(sm, tol=0, max_depth=depth, force_max_depth=False,
+                                            RootBlock=cff.FormFactorQuadtreeBlock, min_size=4096)
+        _record_tree(out, f"crater_quad{depth}", Cq, [0, 1234, 2500, sm.num_faces - 1])
+    np.savez_compressed(HERE / "tree.npz", **out)
+    print("tree:", len(out), "arrays")
+
+
+SECTIONS = {"pcc": make_pcc, "spheres": make_spheres, "ffref": make_ffref, "tree": make_tree}
 
 if __name__ == "__main__":
     todo = sys.argv[1:] or list(SECTIONS)

@@ -105,3 +105,14 @@ def test_static_scratch_aca_rejects_oversize():
         _lib.call("fgb_aca_f64_static", *common, 64, _lib.ptr(out["pool"]), capacity,
                   _lib.ptr(out["used"]), _lib.ptr(out["rank"]), _lib.ptr(out["off"]),
                   _lib.ptr(out["flags"]), _lib.stream_handle())
+    # sizes whose product would wrap around a signed 64-bit count are
+    # rejected too (each term is bounded before it is combined)
+    for exact_max, ctas in ((1 << 62, 64), ((1 << 63) - 1, 1), (1 << 40, 1 << 30)):
+        common[-1] = exact_max
+        with pytest.raises(ValueError, match="static scratch"):
+            _lib.call("fgb_aca_f64_static", *common, ctas, _lib.ptr(out["pool"]), capacity,
+                      _lib.ptr(out["used"]), _lib.ptr(out["rank"]), _lib.ptr(out["off"]),
+                      _lib.ptr(out["flags"]), _lib.stream_handle())
+    # nothing ran: the outputs are untouched
+    torch.cuda.synchronize()
+    assert (out["rank"].cpu().numpy() == -9).all()

@@ -36,6 +36,7 @@ FLAG_STACK_OVERFLOW = 1 << 6
 FLAG_INDEX_RANGE = 1 << 7
 FLAG_RANK_CAP = 1 << 8
 FLAG_DEVICE_TIMEOUT = 1 << 9
+FLAG_NO_CONVERGE = 1 << 10
 
 P = C.c_void_p
 I32 = C.c_int
@@ -92,6 +93,7 @@ SIGNATURES: dict[str, list] = {
                     P, I32, P, I64, P, P, P, P, U32P, P],
     "fgb_aca_f64_static": [P, P, P, P, P, I64, P, P, P, P, I64, I64, F64, I32, F32, I32, I32,
                            I64, I32, P, I64, P, P, P, U32P, P],
+    "fgb_recompress_f32": [P, P, P, P, P, I64, F32, P, I64, P, P, P, P, U32P, P],
     # block matvec (a9)
     "fgb_build_panel_f32_f32": [P, I64, P, P, P, P, P, I64, P, P],
     "fgb_build_panel_f32_bf16": [P, I64, P, P, P, P, P, I64, P, P],

@@ -13,8 +13,11 @@ What differs from the reference, by design:
     picks, per block, the smallest of {CSR, ARPACK SVD, children}; here a
     block is low-rank when its two clusters are well separated
     (min(diam) <= eta * dist) and its adaptive cross approximation
-    (libfluxgb ``fgb_aca_f64``, relative Frobenius tolerance ``tol``)
-    converges under its rank cap; blocks below ``min_size`` entries, at
+    (libfluxgb ``fgb_aca_f64``, relative Frobenius tolerance ``aca_tol``,
+    tol / 10 by default) converges under its rank cap; its factors are then
+    truncated in FP64 to the singular values above ``tol`` times the
+    largest (``fgb_recompress_f32``, the reference's SVD truncation rule,
+    linalg.py:20-51); blocks below ``min_size`` entries, at
     ``max_depth``, or between leaf clusters are evaluated exactly by the
     fused pair kernel (``fgb_ff_count/fill``).  Only O(N log N) entries and
     rays are evaluated, not N^2.
@@ -32,9 +35,7 @@ LinearOperator behaviour); with a CUDA tensor it stays on the device.
 """
 from __future__ import annotations
 
-import copy
 import ctypes as C
-import itertools as it
 import pickle
 
 import numpy as np
@@ -176,6 +177,9 @@ def _bbox3(P, tree):
 
 # ------------------------------------------------------------- builder --
 LEAF_ZERO, LEAF_DENSE, LEAF_SPARSE, LEAF_LOWRANK, NODE = 0, 1, 2, 3, 4
+# rank codes of fgb_aca_f64 besides k >= 0: not compressible (split the
+# block), pool full, and "every entry known, the exact leaf is smaller"
+ACA_FAILED, ACA_POOL_FULL, ACA_EXACT = -1, -2, -3
 
 
 def _nbytes_csr(nnz, m, itemsize):
@@ -265,7 +269,7 @@ def _plan_blocks(tree, lo3, hi3, *, tol, min_size, max_depth, force_max_depth, e
     exact = []
     pool_parts = []
     aca_total = 0
-    n_aca = n_failed = 0
+    n_aca = n_failed = n_exact_pref = 0
     while lv[0].size:
         ids, r, c, d = lv
         m, n = size[r], size[c]
@@ -302,7 +306,11 @@ def _plan_blocks(tree, lo3, hi3, *, tol, min_size, max_depth, force_max_depth, e
             sets["kind"].append((ids[ci[ok]], np.full(int(ok.sum()), LEAF_LOWRANK)))
             sets["rank"].append((ids[ci[ok]], ranks[ok].astype(np.int64)))
             sets["pool_off"].append((ids[ci[ok]], offs[ok].astype(np.int64)))
-            bad = ci[~ok]
+            # ACA_EXACT: every entry was known and the exact leaf is smaller
+            store = ci[ranks == ACA_EXACT]
+            exact.append(ids[store])
+            n_exact_pref += store.size
+            bad = ci[(ranks < 0) & (ranks != ACA_EXACT)]
             n_failed += bad.size
             sp = bad[can_split[bad]]
             exact.append(ids[bad[~can_split[bad]]])
@@ -322,7 +330,7 @@ def _plan_blocks(tree, lo3, hi3, *, tol, min_size, max_depth, force_max_depth, e
         out[key] = a
     out.update(exact=np.concatenate(exact) if exact else np.zeros(0, np.int64),
                aca_pool_parts=pool_parts, root_bshape=root_bshape, aca_blocks=n_aca,
-               aca_failed=n_failed)
+               aca_failed=n_failed, aca_stored_exactly=n_exact_pref)
     return out
 
 
@@ -355,7 +363,8 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
 
     def __init__(self, shape_model, tol=1e-5, min_size=16384, max_depth=None,
                  force_max_depth=False, RootBlock=None, *, leaf_size=64, eta=1.0, rmax=64,
-                 nsample=4096, exact_aca_max=262144, dtype=None, eps=None, **kwargs):
+                 nsample=16384, exact_aca_max=262144, dtype=None, eps=None, aca_tol=None,
+                 recompress=True, **kwargs):
         if tol < 0:
             raise RuntimeError('tol should be a nonnegative float')
         if max_depth is not None and not isinstance(max_depth, int):
@@ -397,6 +406,11 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         self._rmax = rmax
         self._nsample = nsample
         self._exact_aca_max = int(exact_aca_max)
+        # ACA runs below the block tolerance and the FP64 truncation brings
+        # every block to it (sigma_i / sigma_0 > tol kept, the reference's rule)
+        self._recompress = bool(recompress)
+        self._aca_tol = float(aca_tol if aca_tol is not None else
+                              (tol / 10 if recompress else tol))
         self._eps = config.DEFAULT_EPS if eps is None else eps
         self._store_dtype = np.dtype(shape_model.dtype if dtype is None else dtype)
         if self._store_dtype not in (np.float64, np.float32):
@@ -475,6 +489,7 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         lrm = self._kind == LEAF_LOWRANK
         self.stats.update(build_s=time.perf_counter() - t_start, aca_s=t_aca[0], exact_s=t_exact,
                           aca_blocks=plan["aca_blocks"], aca_failed=plan["aca_failed"],
+                          aca_stored_exactly=plan["aca_stored_exactly"],
                           lowrank_blocks=int(lrm.sum()),
                           exact_blocks=int(exact.size), num_blocks=int(self._rows.size),
                           lowrank_entries=int(np.sum(self._rank[lrm] *
@@ -522,22 +537,57 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         r0_d, m_d, c0_d, n_d = t(r0), t(m), t(c0), t(n)
         _lib.call("fgb_aca_f64", sm.bvh.handle, _lib.ptr(P), _lib.ptr(Nn), _lib.ptr(A),
                   _lib.ptr(perm_d), nb, _lib.ptr(r0_d), _lib.ptr(m_d), _lib.ptr(c0_d),
-                  _lib.ptr(n_d), mmax, nmax, float(self._eps), sm.semantics, float(self._tol),
+                  _lib.ptr(n_d), mmax, nmax, float(self._eps), sm.semantics, self._aca_tol,
                   rmax, self._nsample, ex_max, _lib.ptr(dscratch), _lib.ptr(scratch), num_ctas, _lib.ptr(pool), capacity,
                   _lib.ptr(used), _lib.ptr(rank_out), _lib.ptr(off_out), _lib.ptr(queue),
                   _lib.ptr(flags), _lib.stream_handle())
         fl = int(flags.item())
         if fl & _lib.FLAG_STACK_OVERFLOW:
             raise RuntimeError("BVH traversal stack overflow during compression")
+        del scratch, dscratch
+        nused = int(used.item())
+        if self._recompress and nused and self._tol > 0:
+            pool, nused = self._truncate(pool[:nused], rank_out, off_out, m_d, n_d)
         ranks_s = rank_out.cpu().numpy()
         offs_s = off_out.cpu().numpy()
-        nused = int(used.item())
-        del scratch, dscratch
         ranks = np.empty(nb, np.int64)
         offs = np.empty(nb, np.int64)
         ranks[order] = ranks_s
         offs[order] = np.where(offs_s >= 0, offs_s + pool_base, -1)
         return ranks, offs, (pool[:nused] if nused else None)
+
+    def _truncate(self, pool, rank, off, m_d, n_d):
+        """FP64 rank truncation of the ACA factors of one batch of blocks
+        (libfluxgb ``fgb_recompress_f32``): rank and off are updated in
+        place; returns the new pool part and its length."""
+        import time
+        t0 = time.perf_counter()
+        dev = pool.device
+        nb = rank.numel()
+        out = torch.empty(pool.numel(), dtype=torch.float32, device=dev)
+        used = torch.zeros(1, dtype=torch.int64, device=dev)
+        rank2 = torch.empty_like(rank)
+        off2 = torch.empty_like(off)
+        queue = torch.zeros(2, dtype=torch.int32, device=dev)
+        flags = torch.zeros(1, dtype=torch.int32, device=dev)
+        _lib.call("fgb_recompress_f32", _lib.ptr(pool), _lib.ptr(off), _lib.ptr(rank),
+                  _lib.ptr(m_d), _lib.ptr(n_d), nb, float(self._tol), _lib.ptr(out), out.numel(),
+                  _lib.ptr(used), _lib.ptr(rank2), _lib.ptr(off2), _lib.ptr(queue),
+                  _lib.ptr(flags), _lib.stream_handle())
+        fl = int(flags.item())
+        if fl & (_lib.FLAG_NO_CONVERGE | _lib.FLAG_RANK_CAP | _lib.FLAG_INDEX_RANGE):
+            raise RuntimeError(f"rank truncation of the ACA factors failed (flags {fl:#x})")
+        ok = rank > 0
+        st = self.stats
+        st["aca_rank_sum"] = st.get("aca_rank_sum", 0) + int(rank[ok].sum().item())
+        st["truncated_rank_sum"] = st.get("truncated_rank_sum", 0) + int(rank2[ok].sum().item())
+        st["aca_factor_floats"] = st.get("aca_factor_floats", 0) + int(pool.numel())
+        n = int(used.item())
+        rank.copy_(rank2)
+        off.copy_(off2)
+        torch.cuda.synchronize()
+        st["truncate_s"] = st.get("truncate_s", 0.0) + time.perf_counter() - t0
+        return out[:n], n
 
     def _assemble(self, exact, aca_pool_parts, pool_off):
         """Exact leaves (sparse, from the pair kernel) and low-rank factors ->
@@ -1432,9 +1482,13 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         return self @ x
 
     # -- reference API: size / structure ---------------------------------
+    # The block tree of the reference (compressed_form_factors.py:808-873)
+    # is answered from the plan arrays through _HostTree: which blocks the
+    # materialised tree holds, their kinds after the reference's
+    # post-processing, heights, bytes and depth-first order.
     @property
     def nbytes(self):
-        return self._root.nbytes
+        return int(self._host_tree.nbytes[0])
 
     @property
     def device_nbytes(self):
@@ -1449,49 +1503,87 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
 
     @property
     def depth(self):
-        return self._root.depth
+        return int(self._host_tree.height[0])
+
+    @property
+    def _host_tree(self):
+        ht = self.__dict__.get("_host_tree_cache")
+        if ht is None:
+            ht = _HostTree(self)
+            self._host_tree_cache = ht
+        return ht
 
     @property
     def _root(self):
         if self._root_cache is None:
-            self._root_cache = _make_tree_block(self, 0, None)
+            self._root_cache = self._block_view(0)
         return self._root_cache
 
-    def get_blocks_at_depth(self, depth):
+    def _check_depth(self, depth):
         if depth > self.depth:
             raise Exception('specified depth (%d) exceeds tree depth (%d)' % (depth, self.depth))
-        if depth == 0 or self._root.is_leaf:
+
+    def _check_row(self, row_ind):
+        if not (0 <= row_ind < self.num_faces):
+            raise Exception('row_ind (== %d) should be in range [0, %d)' % (row_ind, self.num_faces))
+
+    def get_blocks_at_depth(self, depth):
+        """The blocks of the tree at `depth`, depth-first (the root alone at
+        depth 0 or when it is a leaf)."""
+        self._check_depth(depth)
+        ht = self._host_tree
+        if depth == 0 or ht.kind[0] != NODE:
             yield self._root
-        else:
-            yield from self._root._get_blocks_at_depth(depth)
+            return
+        for b in ht.in_order(ht.alive & (self._depth == depth)):
+            yield self._block_view(b)
 
     def get_row_inds_at_depth(self, depth):
-        if depth > self.depth:
-            raise Exception('specified depth (%d) exceeds tree depth (%d)' % (depth, self.depth))
-        row_inds = np.arange(self.num_faces)
+        """Row index sets down the diagonal: every diagonal block at `depth`,
+        and every diagonal leaf above it, depth-first."""
+        self._check_depth(depth)
         if depth == 0:
-            yield row_inds
-        else:
-            yield from self._root._get_row_inds_at_depth(depth, row_inds)
+            yield np.arange(self.num_faces)
+            return
+        ht = self._host_tree
+        d = self._depth
+        sel = ht.alive & ht.diagonal & (d >= 1) & ((d == depth) | ((d < depth) & ht.is_leaf))
+        for b in ht.in_order(sel):
+            yield self._tree.ref_indices(self._rows[b])
 
     def get_row_blocks(self, row_ind):
-        if not (0 <= row_ind and row_ind < self.num_faces):
-            raise Exception('row_ind (== %d) should be in range [0, %d)' % (row_ind, self.num_faces))
-        block, row_inds = self._root, np.arange(self.num_faces)
-        if block.is_leaf:
-            yield block
-        else:
-            yield from block._get_row_blocks(row_ind, row_inds)
+        """The leaves of the tree whose rows hold facet `row_ind`, depth-first."""
+        self._check_row(row_ind)
+        ht = self._host_tree
+        if ht.kind[0] != NODE:
+            yield self._root
+            return
+        for b in ht.in_order(ht.alive & ht.is_leaf & ht.holds_row(row_ind)):
+            yield self._block_view(b)
 
     def get_col_inds_for_row(self, row_ind):
-        if not (0 <= row_ind and row_ind < self.num_faces):
-            raise Exception('row_ind (== %d) should be in range [0, %d)' % (row_ind, self.num_faces))
-        row_inds = np.arange(self.num_faces)
-        col_inds = np.arange(self.num_faces)
-        if self._root.is_leaf:
-            yield col_inds
-        else:
-            yield from self._root._get_col_inds_for_row(row_ind, row_inds, col_inds)
+        """Column index sets of the leaves get_row_blocks(row_ind) yields."""
+        self._check_row(row_ind)
+        ht = self._host_tree
+        if ht.kind[0] != NODE:
+            yield np.arange(self.num_faces)
+            return
+        for b in ht.in_order(ht.alive & ht.is_leaf & ht.holds_row(row_ind)):
+            yield self._tree.ref_indices(self._cols[b])
+
+    def _with_root(self, root):
+        return _HostOperator(self, root)
+
+    def get_individual_block(self, i, j):
+        """The operator with every top-level block but (i, j) set to zero
+        (as the reference's docstring states; a host-side operator)."""
+        return self._with_root(self._root.get_individual_block(i, j))
+
+    def get_diag_blocks(self):
+        return self._with_root(self._root.get_diag_blocks())
+
+    def get_off_diag_blocks(self):
+        return self._with_root(self._root.get_off_diag_blocks())
 
     def toarray(self):
         n = self.num_faces
@@ -1516,6 +1608,7 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
     def __getstate__(self):
         st = dict(self.__dict__)
         st["_root_cache"] = None
+        st.pop("_host_tree_cache", None)
         st["_desc"] = None
         st["_desc_tc"] = None
         st["_desc_tc64"] = None
@@ -1564,6 +1657,46 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         self._desc_tc_items = self._make_desc_tc_items()
 
     # -- leaf data for the Python block objects --------------------------
+    def _block_view(self, b):
+        """The block object of plan block b (its class from the kind the
+        materialised tree gives it)."""
+        ht = self._host_tree
+        tree = self._tree
+        shape = (int(tree.size[self._rows[b]]), int(tree.size[self._cols[b]]))
+        cls = _LEAF_CLASS.get(int(ht.kind[b]))
+        if cls is None:
+            if b == 0:
+                cls = FormFactorPartitionBlock if self._parts is not None else self._RootBlock
+            else:
+                cls = FormFactorOctreeBlock if tree.ndim == 3 else FormFactorQuadtreeBlock
+        return cls(self, shape, b)
+
+    def _ref_positions(self, b, sub, outer=None):
+        """Positions of the rows and columns of block `sub` within those of
+        block b, both in the reference's ascending-id order (`outer`: b's
+        own index sets, when the caller has them)."""
+        t = self._tree
+        Ib, Jb = outer if outer is not None else (t.ref_indices(self._rows[b]),
+                                                 t.ref_indices(self._cols[b]))
+        ri = np.searchsorted(Ib, t.ref_indices(self._rows[sub]))
+        ci = np.searchsorted(Jb, t.ref_indices(self._cols[sub]))
+        return ri, ci
+
+    def _block_matrix(self, b):
+        """Dense array of block b (an exact leaf or a block the tree holds
+        as one dense / sparse leaf), rows and columns in ascending-id order:
+        the exact leaves under b placed at their positions."""
+        ht = self._host_tree
+        m, n = (int(self._tree.size[self._rows[b]]), int(self._tree.size[self._cols[b]]))
+        mat = np.zeros((m, n), dtype=self.dtype)
+        outer = (self._tree.ref_indices(self._rows[b]), self._tree.ref_indices(self._cols[b]))
+        for leaf in ht.plan_leaves_under(b):
+            if self._exact_pos[leaf] < 0 or self._leaf_nnz[leaf] == 0:
+                continue
+            ri, ci = self._ref_positions(b, leaf, outer)
+            mat[np.ix_(ri, ci)] = self._leaf_dense(leaf)
+        return mat
+
     def _leaf_dense(self, b):
         """Dense (m x n) array of an exact leaf in the shape dtype, rows and
         columns in the reference's ascending-id order."""
@@ -1606,13 +1739,180 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         return Qu @ W, s, Xt @ Qv.T
 
 
+# ------------------------------------------------ host view of the tree --
+class _HostTree:
+    """The materialised block tree of an operator, derived from its plan
+    arrays level by level (no recursion over block objects).
+
+    The plan's leaves are the device's leaves.  On top of them the tree
+    follows the reference's post-processing of make_block
+    (compressed_form_factors.py:313-377), bottom-up: a block whose exact
+    leaves hold no nonzero is a zero block; a block made only of exact
+    leaves is one sparse leaf when its CSR takes no more bytes than its
+    children; else all-dense children become one dense leaf and all-sparse
+    (or zero) children one sparse leaf.  The root keeps its children.
+
+    Per block: ``kind`` (after that processing), ``alive`` (the block is in
+    the tree: every ancestor is an interior block), ``height`` (0 for
+    leaves), ``nbytes`` (the reference's byte count), ``pre`` (depth-first
+    preorder position) and ``span`` (blocks in its subtree)."""
+
+    def __init__(self, op):
+        tree = op._tree
+        rows, cols = op._rows, op._cols
+        nb = rows.size
+        self.op = op
+        m = tree.size[rows].astype(np.int64)
+        n = tree.size[cols].astype(np.int64)
+        isz = np.dtype(op.dtype).itemsize
+        kind = op._kind.astype(np.int64).copy()
+        rank = op._rank.astype(np.int64)
+        kind[(kind == LEAF_LOWRANK) & (rank == 0)] = LEAF_ZERO
+        nnz = op._leaf_nnz.astype(np.int64).copy()
+        has_lr = kind == LEAF_LOWRANK
+        nbytes = np.zeros(nb, np.int64)
+        for k_, per in ((LEAF_DENSE, m * n * isz), (LEAF_SPARSE, nnz * isz),
+                        (LEAF_LOWRANK, (m + n + 1) * rank * 8)):
+            sel = kind == k_
+            nbytes[sel] = per[sel]
+        self.nkids = np.zeros(nb, np.int64)
+        interior = np.flatnonzero(kind == NODE)
+        self.nkids[interior] = tree.nch ** 2
+        if kind[0] == NODE:
+            self.nkids[0] = int(np.prod(op._root_bshape))
+        height = np.zeros(nb, np.int64)
+        depth = op._depth
+        for d in np.unique(depth[interior])[::-1]:
+            at_d = interior[depth[interior] == d]
+            for k_ in np.unique(self.nkids[at_d]):
+                g = at_d[self.nkids[at_d] == k_]
+                kids = op._child0[g][:, None] + np.arange(k_)
+                kk = kind[kids]
+                any_lr = has_lr[kids].any(1)
+                tot = nnz[kids].sum(1)
+                child_bytes = nbytes[kids].sum(1) + 8 * (m[g] + n[g])
+                csr_bytes = tot * (isz + 4) + (m[g] + 1) * 4
+                may = (g != 0) & ~any_lr
+                zero = may & (tot == 0)
+                csr = may & ~zero & (csr_bytes <= child_bytes)
+                rest = (g != 0) & ~zero & ~csr
+                dense = rest & (kk == LEAF_DENSE).all(1)
+                sparse = rest & ~dense & np.isin(kk, (LEAF_SPARSE, LEAF_ZERO)).all(1)
+                new = np.full(g.size, NODE, np.int64)
+                new[zero] = LEAF_ZERO
+                new[csr | sparse] = LEAF_SPARSE
+                new[dense] = LEAF_DENSE
+                kind[g] = new
+                nnz[g] = tot
+                has_lr[g] = any_lr
+                nbytes[g] = np.select([new == NODE, new == LEAF_DENSE, new == LEAF_SPARSE],
+                                      [child_bytes, m[g] * n[g] * isz, tot * isz], 0)
+                height[g] = np.where(new == NODE, 1 + height[kids].max(1), 0)
+        self.kind, self.nbytes, self.height = kind, nbytes, height
+        self.is_leaf = kind != NODE
+        self.diagonal = rows == cols
+        # blocks in the tree, subtree sizes and preorder positions
+        parent = op._parent
+        alive = np.zeros(nb, bool)
+        alive[0] = True
+        levels = [np.flatnonzero(depth == d) for d in range(int(depth.max()) + 1)]
+        for ids in levels[1:]:
+            p = parent[ids]
+            alive[ids] = alive[p] & (kind[p] == NODE)
+        self.alive = alive
+        span = np.where(alive, 1, 0).astype(np.int64)
+        for ids in levels[:0:-1]:
+            ids = ids[alive[ids]]
+            np.add.at(span, parent[ids], span[ids])
+        pre = np.full(nb, -1, np.int64)
+        pre[0] = 0
+        for ids in levels[:-1]:
+            ids = ids[alive[ids] & (kind[ids] == NODE)]
+            for k_ in np.unique(self.nkids[ids]):
+                g = ids[self.nkids[ids] == k_]
+                kids = op._child0[g][:, None] + np.arange(k_)
+                before = np.cumsum(span[kids], 1) - span[kids]
+                pre[kids] = pre[g][:, None] + 1 + before
+        self.span, self.pre = span, pre
+
+    def in_order(self, mask):
+        """Block ids selected by `mask`, in depth-first order."""
+        ids = np.flatnonzero(mask)
+        return ids[np.argsort(self.pre[ids], kind="stable")]
+
+    def holds_row(self, row_ind):
+        """Blocks whose row cluster holds facet `row_ind`."""
+        tree = self.op._tree
+        if getattr(self, "_iperm", None) is None:
+            self._iperm = np.empty_like(tree.perm)
+            self._iperm[tree.perm] = np.arange(tree.perm.size)
+        p = int(self._iperm[row_ind])
+        r = self.op._rows
+        return (tree.start[r] <= p) & (p < tree.start[r] + tree.size[r])
+
+    def subtree(self, b):
+        """Blocks of the materialised tree under b (b first), depth-first."""
+        lo, hi = self.pre[b], self.pre[b] + self.span[b]
+        return self.in_order(self.alive & (self.pre >= lo) & (self.pre < hi))
+
+    def plan_leaves_under(self, b):
+        """The plan's own leaves under block b (whatever the tree made of
+        them): walk the plan's child ranges down from b."""
+        op = self.op
+        out, front = [], np.array([b], np.int64)
+        while front.size:
+            node = op._kind[front] == NODE
+            out.append(front[~node])
+            inner = front[node]
+            if not inner.size:
+                break
+            nk = np.where(inner == 0, int(np.prod(op._root_bshape)), op._tree.nch ** 2)
+            front = np.concatenate([op._child0[i] + np.arange(k) for i, k in zip(inner, nk)])
+        return np.concatenate(out) if out else np.zeros(0, np.int64)
+
+
+class _HostOperator(scipy.sparse.linalg.LinearOperator):
+    """A CompressedFormFactorMatrix with its top-level blocks replaced
+    (get_diag_blocks and friends): products on the host, through the
+    given root block."""
+
+    def __init__(self, op, root):
+        self._op = op
+        self._root = root
+        self.shape_model = op.shape_model
+
+    @property
+    def shape(self):
+        return self._op.shape
+
+    @property
+    def dtype(self):
+        return self._op.dtype
+
+    @property
+    def ndim(self):
+        return 2
+
+    def _matmat(self, x):
+        return self._root @ x
+
+    def _matvec(self, x):
+        return self._root @ x
+
+    def __matmul__(self, x):
+        return self._root @ x
+
+
 # ------------------------------------------------------- block classes --
 class CompressedFormFactorBlock:
-    """A block of a CompressedFormFactorMatrix (compressed_form_factors.py:35)."""
+    """A block of a CompressedFormFactorMatrix (compressed_form_factors.py:35):
+    a view of block b of the operator's plan, or (b < 0) a block made on
+    the host (the zero blocks of get_diag_blocks and friends)."""
 
-    def __init__(self, root, shape):
+    def __init__(self, root, shape, b=-1):
         self._root = root
-        self.shape = shape
+        self.shape = (int(shape[0]), int(shape[1]))
+        self._b = b
 
     @property
     def dtype(self):
@@ -1620,39 +1920,47 @@ class CompressedFormFactorBlock:
 
     @property
     def size(self):
-        return int(np.prod(self.shape))
+        return self.shape[0] * self.shape[1]
 
     @property
     def root(self):
         return self._root
 
+    @property
+    def nbytes(self):
+        return int(self._root._host_tree.nbytes[self._b]) if self._b >= 0 else 0
 
-class FormFactorLeafBlock(CompressedFormFactorBlock):
     @property
     def depth(self):
-        return 0
-
-    @property
-    def is_leaf(self):
-        return True
-
-    def get_blocks_at_depth(self, depth):
-        if depth == 0:
-            yield self
-
-    def _get_blocks_at_depth(self, depth):
-        if depth == 0:
-            yield self
+        return int(self._root._host_tree.height[self._b]) if self._b >= 0 else 0
 
     def __matmul__(self, x):
         return self._matmat(np.asarray(x))
 
 
+class FormFactorLeafBlock(CompressedFormFactorBlock):
+    is_leaf = True
+    is_empty_leaf = False
+
+    def get_blocks_at_depth(self, depth):
+        if depth == 0:
+            yield self
+
+    _get_blocks_at_depth = get_blocks_at_depth
+
+    def _matmat(self, x):
+        return self._mat @ x
+
+
 class FormFactorNullBlock(FormFactorLeafBlock):
-    def __init__(self, root, shape):
+    """A block with no rows or no columns (the plan gives such blocks to
+    FormFactorZeroBlock; kept for the reference's API)."""
+    is_empty_leaf = True
+
+    def __init__(self, root, shape, b=-1):
         if shape[0] != 0 and shape[1] != 0:
             raise RuntimeError('a null block must have a degenerate shape')
-        super().__init__(root, shape)
+        super().__init__(root, shape, b)
 
     def _matmat(self, x):
         if self.shape[1] != x.shape[0]:
@@ -1669,19 +1977,12 @@ class FormFactorNullBlock(FormFactorLeafBlock):
     def _mat(self):
         return np.empty(self.shape, dtype=self.dtype)
 
-    @property
-    def nbytes(self):
-        return 0
-
-    @property
-    def is_empty_leaf(self):
-        return True
-
 
 class FormFactorZeroBlock(FormFactorLeafBlock):
+    is_empty_leaf = True
+
     def _matmat(self, x):
-        m = self.shape[0]
-        return np.zeros((m,) if x.ndim == 1 else (m, x.shape[1]), dtype=self.dtype)
+        return np.zeros((self.shape[0],) + x.shape[1:], dtype=self.dtype)
 
     def is_dense(self):
         return False
@@ -1693,28 +1994,17 @@ class FormFactorZeroBlock(FormFactorLeafBlock):
     def _mat(self):
         return np.zeros(self.shape, self.dtype)
 
-    @property
-    def nbytes(self):
-        return 0
-
     def tocsr(self):
         return scipy.sparse.csr_matrix(self.shape, dtype=self.dtype)
 
-    @property
-    def is_empty_leaf(self):
-        return True
-
 
 class FormFactorDenseBlock(FormFactorLeafBlock):
-    def __init__(self, root, mat):
-        if isinstance(mat, scipy.sparse.spmatrix):
-            mat = mat.toarray()
-        super().__init__(root, mat.shape)
-        self._mat = mat
-
     @property
-    def nbytes(self):
-        return self._mat.nbytes
+    def _mat(self):
+        got = self.__dict__.get("_dense")
+        if got is None:
+            got = self._dense = self._root._block_matrix(self._b)
+        return got
 
     def toarray(self):
         return self._mat
@@ -1725,37 +2015,25 @@ class FormFactorDenseBlock(FormFactorLeafBlock):
     def is_sparse(self):
         return False
 
-    def _matmat(self, x):
-        return self._mat @ x
-
-    @property
-    def is_empty_leaf(self):
-        return False
-
 
 class FormFactorSparseBlock(FormFactorLeafBlock):
-    def _matmat(self, x):
-        return np.array(self._spmat @ x)
-
     def is_dense(self):
         return False
 
     def is_sparse(self):
         return True
 
-    @property
-    def is_empty_leaf(self):
-        return False
+    def _matmat(self, x):
+        return np.asarray(self._spmat @ x)
 
 
 class FormFactorCsrBlock(FormFactorSparseBlock):
-    def __init__(self, root, mat):
-        super().__init__(root, mat.shape)
-        self._spmat = mat if isinstance(mat, scipy.sparse.spmatrix) else scipy.sparse.csr_matrix(mat)
-
     @property
-    def nbytes(self):
-        return self._spmat.data.nbytes
+    def _spmat(self):
+        got = self.__dict__.get("_csr")
+        if got is None:
+            got = self._csr = scipy.sparse.csr_matrix(self._root._block_matrix(self._b))
+        return got
 
     def tocsr(self):
         return self._spmat
@@ -1766,17 +2044,35 @@ class FormFactorCsrBlock(FormFactorSparseBlock):
 
 
 class FormFactorSvdBlock(FormFactorLeafBlock):
-    """Low-rank leaf, exposed in the reference's (u, s, vt) form."""
+    """Low-rank leaf in the reference's (u, s, vt) form, orthogonalised
+    from the stored factors on first use."""
 
-    def __init__(self, root, u, s, vt):
-        super().__init__(root, (u.shape[0], vt.shape[1]))
-        self._k = s.size
-        self._u, self._s, self._vt = u, s, vt
+    def _factors(self):
+        got = self.__dict__.get("_usv")
+        if got is None:
+            got = self._usv = self._root._leaf_lowrank(self._b)
+        return got
+
+    @property
+    def _u(self):
+        return self._factors()[0]
+
+    @property
+    def _s(self):
+        return self._factors()[1]
+
+    @property
+    def _vt(self):
+        return self._factors()[2]
+
+    @property
+    def _k(self):
+        return self._s.size
 
     def _matmat(self, x):
-        y = self._vt @ x
-        y = (y.T * self._s).T
-        return self._u @ y
+        u, s, vt = self._factors()
+        t = vt @ x
+        return u @ (s.reshape((-1,) + (1,) * (t.ndim - 1)) * t)
 
     def is_dense(self):
         return False
@@ -1785,51 +2081,82 @@ class FormFactorSvdBlock(FormFactorLeafBlock):
         return False
 
     @property
-    def is_empty_leaf(self):
-        return False
-
-    @property
-    def nbytes(self):
-        return self._u.nbytes + self._s.nbytes + self._vt.nbytes
-
-    @property
     def _mat(self):
-        return (self._u * self._s) @ self._vt
+        u, s, vt = self._factors()
+        return (u * s) @ vt
+
+
+_LEAF_CLASS = {LEAF_ZERO: FormFactorZeroBlock, LEAF_DENSE: FormFactorDenseBlock,
+               LEAF_SPARSE: FormFactorCsrBlock, LEAF_LOWRANK: FormFactorSvdBlock}
 
 
 class FormFactorBlockMatrix(CompressedFormFactorBlock):
-    """Interior block (compressed_form_factors.py:279-510)."""
+    """Interior block (compressed_form_factors.py:279-510): its children
+    are the plan's child blocks, row-major over (row cluster, column
+    cluster); ``_zeroed`` lists children replaced by zero blocks."""
+    is_leaf = False
+    is_empty_leaf = False
+    _zeroed = frozenset()
 
-    def _matmat(self, x):
-        y = np.zeros((self.shape[0],) + x.shape[1:], dtype=self.dtype)
-        for i, row_inds in enumerate(self._row_block_inds):
-            for j, col_inds in enumerate(self._col_block_inds):
-                block = self._blocks[i, j]
-                if block.is_empty_leaf:
-                    continue
-                y[row_inds] += block._matmat(x[col_inds])
-        return y
+    def _child_ids(self):
+        op = self._root
+        return op._child0[self._b] + np.arange(int(op._host_tree.nkids[self._b]))
 
-    def __matmul__(self, x):
-        return self._matmat(np.asarray(x))
+    @property
+    def bshape(self):
+        op = self._root
+        if self._b == 0:
+            return tuple(op._root_bshape)
+        return (op._tree.nch, op._tree.nch)
+
+    def _index_sets(self, axis):
+        op = self._root
+        ids = self._child_ids()
+        nr, nc = self.bshape
+        first = ids[::nc] if axis == 0 else ids[:nc]
+        return [op._ref_positions(self._b, c)[axis] for c in first]
+
+    @property
+    def _row_block_inds(self):
+        got = self.__dict__.get("_rinds")
+        if got is None:
+            got = self._rinds = self._index_sets(0)
+        return got
+
+    @property
+    def _col_block_inds(self):
+        got = self.__dict__.get("_cinds")
+        if got is None:
+            got = self._cinds = self._index_sets(1)
+        return got
+
+    @property
+    def _blocks(self):
+        got = self.__dict__.get("_kids")
+        if got is None:
+            op = self._root
+            nr, nc = self.bshape
+            got = np.empty((nr, nc), dtype=object)
+            for q, c in enumerate(self._child_ids()):
+                i, j = divmod(q, nc)
+                got[i, j] = (FormFactorZeroBlock(op, got_shape(op, c)) if (i, j) in self._zeroed
+                             else op._block_view(c))
+            self._kids = got
+        return got
 
     @property
     def nbytes(self):
-        return sum(I.nbytes for I in self._row_block_inds) \
-            + sum(J.nbytes for J in self._col_block_inds) \
-            + sum(block.nbytes for block in self._blocks.flatten())
+        if not self._zeroed:
+            return super().nbytes
+        # the index arrays and the blocks left in place
+        return 8 * (self.shape[0] + self.shape[1]) + sum(
+            b.nbytes for b in self._blocks.ravel())
 
     @property
     def depth(self):
-        return 1 + max(block.depth for block in self._blocks.flatten())
-
-    @property
-    def is_leaf(self):
-        return False
-
-    @property
-    def is_empty_leaf(self):
-        return False
+        if not self._zeroed:
+            return super().depth
+        return 1 + max(b.depth for b in self._blocks.ravel())
 
     def is_dense(self):
         return all(isinstance(b, FormFactorDenseBlock) for b in self._blocks.ravel())
@@ -1838,75 +2165,67 @@ class FormFactorBlockMatrix(CompressedFormFactorBlock):
         return all(isinstance(b, (FormFactorSparseBlock, FormFactorZeroBlock))
                    for b in self._blocks.ravel())
 
-    @property
-    def bshape(self):
-        return (len(self._row_block_inds), len(self._col_block_inds))
-
     def _get_blocks_at_depth(self, depth):
+        """Blocks `depth` levels below this one, depth-first."""
         if depth == 0:
             yield self
-        else:
-            for block in self._blocks.ravel():
-                yield from block._get_blocks_at_depth(depth - 1)
-
-    def _get_row_inds_at_depth(self, depth, parent_inds):
+            return
         if depth == 1:
-            for row_block_inds in self._row_block_inds:
-                yield parent_inds[row_block_inds]
-        else:
-            for row_block_inds, block in zip(self._row_block_inds, np.diag(self._blocks)):
-                if block.is_leaf:
-                    yield parent_inds[row_block_inds]
-                else:
-                    yield from block._get_row_inds_at_depth(depth - 1, parent_inds[row_block_inds])
+            yield from self._blocks.ravel()
+            return
+        op = self._root
+        ht = op._host_tree
+        d0 = op._depth[self._b]
+        for c in ht.subtree(self._b):
+            if op._depth[c] - d0 == depth and not self._under_zeroed(c):
+                yield op._block_view(c)
 
-    def _get_row_blocks(self, row_ind, parent_inds):
-        for row_block_inds, row_blocks in zip(self._row_block_inds, self._blocks):
-            row_inds = parent_inds[row_block_inds]
-            if row_ind in row_inds:
-                for block in row_blocks:
-                    if block.is_leaf:
-                        yield block
-                    else:
-                        yield from block._get_row_blocks(row_ind, row_inds)
-                break
+    def _under_zeroed(self, c):
+        if not self._zeroed or c == self._b:
+            return False
+        ht = self._root._host_tree
+        nc = self.bshape[1]
+        for (i, j) in self._zeroed:
+            z = self._root._child0[self._b] + i * nc + j
+            if ht.pre[z] <= ht.pre[c] < ht.pre[z] + ht.span[z]:
+                return True
+        return False
 
-    def _get_col_inds_for_row(self, row_ind, parent_row_inds, parent_col_inds):
-        for row_block_inds, row_blocks in zip(self._row_block_inds, self._blocks):
-            row_inds = parent_row_inds[row_block_inds]
-            if row_ind in row_inds:
-                for block, col_block_inds in zip(row_blocks, self._col_block_inds):
-                    col_inds = parent_col_inds[col_block_inds]
-                    if block.is_leaf:
-                        yield col_inds
-                    else:
-                        yield from block._get_col_inds_for_row(row_ind, row_inds, col_inds)
-                break
+    def _matmat(self, x):
+        """y = block @ x: every leaf of the subtree applied once at its rows
+        and columns (leaves of zeroed children skipped)."""
+        op = self._root
+        ht = op._host_tree
+        y = np.zeros((self.shape[0],) + x.shape[1:], dtype=np.result_type(self.dtype, x.dtype))
+        outer = (op._tree.ref_indices(op._rows[self._b]), op._tree.ref_indices(op._cols[self._b]))
+        for c in ht.subtree(self._b):
+            if not ht.is_leaf[c] or ht.kind[c] == LEAF_ZERO or self._under_zeroed(c):
+                continue
+            ri, ci = op._ref_positions(self._b, c, outer)
+            y[ri] += op._block_view(c)._matmat(x[ci])
+        return y
+
+    def _masked(self, zeroed):
+        out = type(self)(self._root, self.shape, self._b)
+        out._zeroed = frozenset(zeroed)
+        return out
 
     def get_individual_block(self, i, j):
-        tmp = copy.copy(self)
-        tmp._blocks = copy.copy(tmp._blocks)
-        for i_, j_ in it.product(*(range(_) for _ in self.bshape)):
-            if i_ != i or j_ != j:
-                continue
-            tmp._blocks[i, j] = FormFactorZeroBlock(self.root, tmp._blocks[i, j].shape)
-        return tmp
+        """A copy in which every child but (i, j) is a zero block."""
+        nr, nc = self.bshape
+        return self._masked((a, b) for a in range(nr) for b in range(nc) if (a, b) != (i, j))
 
     def get_diag_blocks(self):
-        tmp = copy.copy(self)
-        tmp._blocks = copy.copy(tmp._blocks)
-        for i, j in it.product(*(range(_) for _ in self.bshape)):
-            if i != j:
-                tmp._blocks[i, j] = FormFactorZeroBlock(self.root, tmp._blocks[i, j].shape)
-        return tmp
+        nr, nc = self.bshape
+        return self._masked((a, b) for a in range(nr) for b in range(nc) if a != b)
 
     def get_off_diag_blocks(self):
-        tmp = copy.copy(self)
-        tmp._blocks = copy.copy(tmp._blocks)
-        for i, j in it.product(*(range(_) for _ in self.bshape)):
-            if i == j:
-                tmp._blocks[i, j] = FormFactorZeroBlock(self.root, tmp._blocks[i, j].shape)
-        return tmp
+        nr, nc = self.bshape
+        return self._masked((a, a) for a in range(min(nr, nc)))
+
+
+def got_shape(op, b):
+    return (int(op._tree.size[op._rows[b]]), int(op._tree.size[op._cols[b]]))
 
 
 class FormFactor2dTreeBlock(FormFactorBlockMatrix):
@@ -1927,71 +2246,9 @@ class FormFactorPartitionBlock(FormFactorBlockMatrix):
     ``CompressedFormFactorMatrix(shape_model, RootBlock=FormFactorPartitionBlock,
     parts=[I_0, I_1, ...], ChildBlock=FormFactorQuadtreeBlock)``: the parts
     must be disjoint (the reference's check and message) and, here, cover
-    every facet; each part is used in ascending index order."""
-
-    @property
-    def is_empty_leaf(self):
-        return True
-
-
-def _make_tree_block(op: CompressedFormFactorMatrix, b, parent_nodes):
-    """Materialise block b of the plan as a reference-style block object,
-    applying the reference's collapse of all-dense / all-sparse children
-    (compressed_form_factors.py:369-377)."""
-    tree = op._tree
-    r, c = op._rows[b], op._cols[b]
-    m, n = int(tree.size[r]), int(tree.size[c])
-    kind = op._kind[b]
-    if kind == LEAF_ZERO:
-        return FormFactorZeroBlock(op, (m, n))
-    if kind == LEAF_DENSE:
-        return FormFactorDenseBlock(op, op._leaf_dense(b))
-    if kind == LEAF_SPARSE:
-        return FormFactorCsrBlock(op, scipy.sparse.csr_matrix(op._leaf_dense(b)))
-    if kind == LEAF_LOWRANK:
-        u, s, vt = op._leaf_lowrank(b)
-        if s.size == 0:
-            return FormFactorZeroBlock(op, (m, n))
-        return FormFactorSvdBlock(op, u, s, vt)
-    # interior
-    cls = op._RootBlock if b == 0 else (
-        FormFactorOctreeBlock if tree.ndim == 3 else FormFactorQuadtreeBlock)
-    if b == 0 and getattr(op, "_parts", None) is not None:
-        cls = FormFactorPartitionBlock
-    blk = cls.__new__(cls)
-    CompressedFormFactorBlock.__init__(blk, op, (m, n))
-    first = op._child0[b]
-    if b == 0 and tree.children[0] is None:
-        rch, cch = [0], [0]
-    else:
-        rch, cch = tree.children[r], tree.children[c]
-    nr, nc = len(rch), len(cch)
-    Ip = tree.ref_indices(r)
-    Jp = tree.ref_indices(c)
-    blk._row_block_inds = [np.searchsorted(Ip, tree.ref_indices(x)) for x in rch]
-    blk._col_block_inds = [np.searchsorted(Jp, tree.ref_indices(x)) for x in cch]
-    children = np.empty((nr, nc), dtype=object)
-    for i in range(nr):
-        for j in range(nc):
-            children[i, j] = _make_tree_block(op, first + i * nc + j, None)
-    blk._blocks = children
-    if b != 0:
-        if blk.is_dense():
-            mat = np.zeros((m, n), dtype=op.dtype)
-            for i in range(nr):
-                for j in range(nc):
-                    mat[np.ix_(blk._row_block_inds[i], blk._col_block_inds[j])] = children[i, j]._mat
-            return FormFactorDenseBlock(op, mat)
-        if blk.is_sparse():
-            mat = np.zeros((m, n), dtype=op.dtype)
-            for i in range(nr):
-                for j in range(nc):
-                    if not isinstance(children[i, j], FormFactorZeroBlock):
-                        mat[np.ix_(blk._row_block_inds[i], blk._col_block_inds[j])] = children[i, j]._mat
-            if not mat.any():
-                return FormFactorZeroBlock(op, (m, n))
-            return FormFactorCsrBlock(op, scipy.sparse.csr_matrix(mat))
-    return blk
+    every facet; each part is used in ascending index order.  Like the
+    reference's, it reports itself as an empty leaf."""
+    is_empty_leaf = True
 
 
 class CompressedKernelMatrix(scipy.sparse.linalg.LinearOperator):

@@ -76,6 +76,7 @@ enum : unsigned {
   kFlagStackOverflow = 1u << 6,
   kFlagIndexRange = 1u << 7,
   kFlagRankCap = 1u << 8,
+  kFlagNoConverge = 1u << 10,
 };
 
 }  // namespace fgb

@@ -28,37 +28,68 @@ def _apply(FF, x):
     return FF @ x
 
 
+def _as_columns(E):
+    """(device tensor of shape (N, K), was-a-vector, was-on-the-host, numpy dtype)."""
+    on_dev = isinstance(E, torch.Tensor)
+    nd = E.ndim if on_dev else np.ndim(E)
+    if nd not in (1, 2):
+        raise Exception('E should be a vector or a 2D array')
+    if on_dev:
+        Ed = E
+        dt = np.float64 if E.dtype == torch.float64 else np.float32
+    else:
+        En = np.asarray(E)
+        dt = np.float64 if En.dtype != np.float32 else np.float32
+        Ed = torch.as_tensor(En.astype(dt, copy=False), device=_lib.require_cuda())
+    return Ed.reshape(Ed.shape[0], -1), nd == 1, not on_dev, dt
+
+
+def _per_facet(v, like):
+    """A scalar, or a per-facet array broadcast over the columns of `like`."""
+    if np.isscalar(v) or np.ndim(v) == 0:
+        return float(v)
+    t = v.to(like.device, like.dtype) if isinstance(v, torch.Tensor) else \
+        torch.as_tensor(np.asarray(v, dtype=np.float64), device=like.device).to(like.dtype)
+    return t.reshape(-1, 1)
+
+
 def compute_steady_state_temp(FF, E, rho, emiss, Fsurf=0., clamp=True,
                               tol=np.finfo(np.float64).eps, method='jacobi'):
-    """Steady-state surface temperature (model.py:8-42)."""
-    if E.ndim == 1:
-        B = solve_radiosity(FF, E, rho, 'right', method)[0]
-        if clamp:
-            B = np.maximum(0, B)
-        IR = FF @ ((1 - rho) * B + Fsurf)
-        Q = solve_radiosity(FF, IR, 1, 'right', method)[0]
-        if clamp:
-            Q = np.maximum(0, Q)
-        tot = (1 - rho) * B + emiss * Q + Fsurf
-        if clamp:
-            tot = np.maximum(0, tot)
-        return (tot / (emiss * sigSB))**0.25
-    elif E.ndim == 2:
-        B_arr = solve_radiosity(FF, E, rho, 'right', method)[0]
-        if len(B_arr.shape) == 1:
-            B_arr = B_arr[:, np.newaxis]
-        T = []
-        for B in B_arr.T:
-            if clamp:
-                B = np.maximum(0, B)
-            IR = FF @ ((1 - rho) * B)
-            Q = solve_radiosity(FF, IR, 1, 'right', method)[0]
-            if clamp:
-                Q = np.maximum(0, Q)
-            T.append((((1 - rho) * B + emiss * Q) / (emiss * sigSB))**0.25)
-        return np.array(T)
-    else:
-        raise Exception('E should be a vector or a 2D array')
+    """Steady-state surface temperature for one (E of shape (N,)) or K sun
+    directions (E of shape (N, K); result (K, N)), src/flux/model.py:8-42.
+
+    Every column goes through the same three device stages, all columns at
+    once: the visible solve B = E + F (rho B) (one solve for the block, with
+    the reference's single stopping test over all columns), one K-column
+    product IR = F((1 - rho) B [+ Fsurf]), and the infrared solve
+    Q = IR + F Q.  The infrared stage solves each column to its own
+    default tolerance (finfo.resolution * max|IR[:, k]|, as the reference's
+    per-column solve does): the block is solved with every column scaled
+    to unit maximum, and scaled back.  Then
+    T = ((1 - rho) B + emiss Q [+ Fsurf]) / (emiss sigma))^(1/4).
+    As in the reference, Fsurf enters (and the total is clamped) only for
+    a single direction.  Host arrays in, host arrays out."""
+    Ed, single, host, dt = _as_columns(E)
+    apply = _device_operator(FF, Ed.device, dt)
+    rho_c = _per_facet(rho, Ed)
+    em_c = _per_facet(emiss, Ed)
+    B = solve_radiosity(FF, Ed, rho, 'right', method)[0]
+    if clamp:
+        B = B.clamp_min(0)
+    absorbed = (1 - rho_c) * B
+    fs = _per_facet(Fsurf, Ed) if single else 0.0
+    IR = apply((absorbed + fs).contiguous())
+    scale = IR.abs().amax(0)
+    scale = torch.where(scale > 0, scale, torch.ones_like(scale))
+    Q = solve_radiosity(FF, (IR / scale).contiguous(), 1, 'right', method)[0] * scale
+    if clamp:
+        Q = Q.clamp_min(0)
+    total = absorbed + em_c * Q + fs
+    if single and clamp:
+        total = total.clamp_min(0)
+    T = (total / (em_c * sigSB)) ** 0.25
+    T = T[:, 0] if single else T.T.contiguous()
+    return T.cpu().numpy() if host else T
 
 
 def update_incoming_radiances(FF, E, rho, emiss, Qrefl, QIR, Tsurf, clamp=True):
@@ -81,6 +112,44 @@ def update_incoming_radiances(FF, E, rho, emiss, Qrefl, QIR, Tsurf, clamp=True):
     return Qrefl_np1, QIR_np1
 
 
+# Keyword inputs of ThermalModel, in the order they are checked: name, what
+# it is (for the error message, model.py:133-172), and its shape as a
+# function of (number of facets, number of grid nodes); None: not promoted.
+_THERMAL_KWARGS = (
+    ('z', 'skin depths', None),
+    ('T0', 'initial temperature', lambda nf, nz: (nf, nz)),
+    ('ti', 'thermal inertia', lambda nf, nz: (nz,)),
+    ('rhoc', 'thermal conductivity', lambda nf, nz: (nz,)),
+    ('emiss', 'emissivity', lambda nf, nz: (nf,)),
+    ('Fgeotherm', 'geothermal flux', lambda nf, nz: (nf,)),
+)
+
+
+def _thermal_fields(kwargs, num_faces):
+    """The conduction inputs of ThermalModel as arrays: a Python int or
+    float fills the array, an ndarray must already have the shape."""
+    out = {}
+    nz = None
+    for name, what, shape_of in _THERMAL_KWARGS:
+        if name not in kwargs:
+            raise ValueError(f'failed to pass {what} (keyword argument "{name}")')
+        v = kwargs[name]
+        if shape_of is None:
+            assert not isinstance(v, int)
+            out[name] = v
+            nz = v.size
+            continue
+        shape = shape_of(num_faces, nz)
+        if isinstance(v, (int, float)):
+            v = np.full(shape, v, np.float64)
+        elif not isinstance(v, np.ndarray):
+            raise TypeError(f'bad type: {type(v)}')
+        elif v.shape != shape:
+            raise ValueError('invalid shape')
+        out[name] = v
+    return out
+
+
 class ThermalModel:
     """Time-dependent thermal model (model.py:108-234): per step, direct
     insolation, lagged reflected/IR fluxes (two form-factor products) and a
@@ -94,92 +163,64 @@ class ThermalModel:
                              'number of time points ("t")')
         self._FF = FF
         self._shape_model = kwargs['shape_model'] if 'shape_model' in kwargs else FF.shape_model
-        self._t = t
-        self._D = D
-        self._F0 = F0
-        self._rho = rho
-        self._source_num_faces = int(self._D.shape[0] / self._t.shape[0])
+        self._t, self._D, self._F0, self._rho = t, D, F0, rho
+        self._source_num_faces = D.shape[0] // t.shape[0]
         self._return_flux = return_flux
-        num_faces = self._shape_model.num_faces
-        if 'z' not in kwargs:
-            raise ValueError('failed to pass skin depths (keyword argument "z")')
-        z = kwargs['z']
+        fields = _thermal_fields(kwargs, self._shape_model.num_faces)
+        z, T0, ti, rhoc = fields['z'], fields['T0'], fields['ti'], fields['rhoc']
+        emiss, Fgeotherm = fields['emiss'], fields['Fgeotherm']
 
-        def promote_to_array_if_necessary(value, shape, dtype=None):
-            if isinstance(value, (int, float)):
-                return np.full(shape, value, dtype)
-            elif isinstance(value, np.ndarray):
-                if value.shape != shape:
-                    raise ValueError('invalid shape')
-                return value
-            else:
-                raise TypeError(f'bad type: {type(value)}')
-
-        assert not isinstance(z, int)
-        if 'T0' not in kwargs:
-            raise ValueError('failed to pass initial temperature (keyword argument "T0")')
-        T0 = promote_to_array_if_necessary(kwargs['T0'], (num_faces, z.size), np.float64)
-        if 'ti' not in kwargs:
-            raise ValueError('failed to pass thermal inertia (keyword argument "ti")')
-        ti = promote_to_array_if_necessary(kwargs['ti'], (z.size,), np.float64)
-        if 'rhoc' not in kwargs:
-            raise ValueError('failed to pass thermal conductivity (keyword argument "rhoc")')
-        rhoc = promote_to_array_if_necessary(kwargs['rhoc'], (z.size,), np.float64)
-        if 'emiss' not in kwargs:
-            raise ValueError('failed to pass emissivity (keyword argument "emiss")')
-        emiss = promote_to_array_if_necessary(kwargs['emiss'], (num_faces,), np.float64)
-        if 'Fgeotherm' not in kwargs:
-            raise ValueError('failed to pass geothermal flux (keyword argument "Fgeotherm")')
-        Fgeotherm = promote_to_array_if_necessary(kwargs['Fgeotherm'], (num_faces,), np.float64)
-
-        if self._source_num_faces == 1:
-            E0 = self._shape_model.get_direct_irradiance(F0[0], D[0])
-        else:
-            E0 = self._shape_model.get_direct_irradiance(F0[:self._source_num_faces],
-                                                         D[:self._source_num_faces])
+        # initial state from direct illumination only (model.py:165-171)
+        E0 = self._insolation(0, device=False)
         Q0 = (1 - rho) * E0 + Fgeotherm
         Tsurf = (Q0 / (sigSB * emiss))**0.25
         self._pcc_thermal_model_1d = PccThermalModel1D(
             z, T0, ti, rhoc, emiss, Fgeotherm, Q0, Tsurf, bcond='Q')
-        dev = _lib.require_cuda()
-        self._dev = dev
-        self._Tsurf = torch.as_tensor(Tsurf, device=dev)
+        self._dev = _lib.require_cuda()
+        self._Tsurf = torch.as_tensor(Tsurf, device=self._dev)
         self._emiss_d = self._pcc_thermal_model_1d.emiss_device
         self._iter_count = 0
         self._Qrefl = None
         self._QIR = None
 
+    def _insolation(self, i, device=True):
+        """Direct insolation at time point i: one sun direction per time
+        point, or (source_num_faces > 1) that many source points averaged by
+        the shape model.  The single-direction case runs as a one-column
+        batch on the device."""
+        s = self._source_num_faces
+        if s == 1:
+            if device:
+                return self._shape_model.get_direct_irradiance_batch(
+                    self._F0[i], self._D[i], out_dtype=torch.float64)[:, 0]
+            return self._shape_model.get_direct_irradiance(self._F0[i], self._D[i])
+        part = slice(i * s, (i + 1) * s)
+        E = self._shape_model.get_direct_irradiance(self._F0[part], self._D[part])
+        return torch.as_tensor(E, device=self._dev) if device else E
+
     def __iter__(self):
         return self
 
     def __next__(self):
+        """One time step: E_i, the lagged fluxes from the previous step's
+        state, the absorbed flux Q, one conduction step; returns the
+        conduction profiles (and the fluxes with return_flux)."""
         self._iter_count += 1
         i = self._iter_count
-        if (self._source_num_faces == 1) & (i == self._D.shape[0]):
+        if i * self._source_num_faces >= self._D.shape[0]:
             raise StopIteration()
-        elif (self._source_num_faces > 1) & (self._source_num_faces * i == self._D.shape[0]):
-            raise StopIteration()
-        if self._source_num_faces == 1:
-            f, d, delta_t = self._F0[i], self._D[i], self._t[i] - self._t[i - 1]
-            E = self._shape_model.get_direct_irradiance_batch(
-                f, d, out_dtype=torch.float64)[:, 0]
-        else:
-            f = self._F0[i * self._source_num_faces:(i + 1) * self._source_num_faces]
-            d = self._D[i * self._source_num_faces:(i + 1) * self._source_num_faces, :]
-            delta_t = self._t[i] - self._t[i - 1]
-            E = torch.as_tensor(self._shape_model.get_direct_irradiance(f, d), device=self._dev)
-        zero = torch.zeros_like(E)
-        Qrefl_prev = zero if i == 1 else self._Qrefl
-        QIR_prev = zero if i == 1 else self._QIR
-        emiss = self._emiss_d
-        Qrefl, QIR = update_incoming_radiances(self._FF, E, self._rho, emiss, Qrefl=Qrefl_prev,
-                                               QIR=QIR_prev, Tsurf=self._Tsurf)
-        Q = (1 - self._rho) * (E + Qrefl) + emiss * QIR
-        self._pcc_thermal_model_1d.step(delta_t, Q)
-        self._Qrefl = Qrefl
-        self._QIR = QIR
-        self._Tsurf = self._pcc_thermal_model_1d.T_device[:, 0].contiguous()
+        E = self._insolation(i)
+        dt = self._t[i] - self._t[i - 1]
+        first = i == 1
+        Qrefl, QIR = update_incoming_radiances(
+            self._FF, E, self._rho, self._emiss_d,
+            Qrefl=torch.zeros_like(E) if first else self._Qrefl,
+            QIR=torch.zeros_like(E) if first else self._QIR, Tsurf=self._Tsurf)
+        Q = (1 - self._rho) * (E + Qrefl) + self._emiss_d * QIR
+        pcc = self._pcc_thermal_model_1d
+        pcc.step(dt, Q)
+        self._Qrefl, self._QIR = Qrefl, QIR
+        self._Tsurf = pcc.T_device[:, 0].contiguous()
         if self._return_flux:
-            return (self._pcc_thermal_model_1d.T, E.cpu().numpy(), Qrefl.cpu().numpy(),
-                    QIR.cpu().numpy())
-        return self._pcc_thermal_model_1d.T
+            return pcc.T, E.cpu().numpy(), Qrefl.cpu().numpy(), QIR.cpu().numpy()
+        return pcc.T

@@ -15,9 +15,10 @@ from fluxpy_gb300.compressed_form_factors import (LEAF_LOWRANK, LEAF_ZERO, NODE,
 
 
 def fake_aca(r, c, base):
-    """Rank from the cluster ids; negative = not compressible."""
+    """Rank from the cluster ids; -1 / -2 = not compressible (split), -3 =
+    store exactly (an exact leaf, never split)."""
     r, c = np.asarray(r), np.asarray(c)
-    ranks = ((r * 31 + c * 17) % 7) - 2
+    ranks = ((r * 31 + c * 17) % 8) - 3
     sz = np.where(ranks > 0, ranks * 3, 0)
     offs = base + np.cumsum(sz) - sz
     offs = np.where(ranks >= 0, offs, -1)
@@ -85,6 +86,8 @@ def loop_plan(tree, lo3, hi3, tol, min_size, maxd, force, eta):
             for b, k, off in zip(cand, ranks, offs):
                 if k >= 0:
                     kind[b], rank[b], pool_off[b] = LEAF_LOWRANK, int(k), int(off)
+                elif k == -3:
+                    exact.append(b)
                 else:
                     r, c, d = rows[b], cols[b], depth[b]
                     at_max = maxd is not None and d >= maxd

@@ -33,8 +33,11 @@ COMMON_FLAGS = [
 ]
 # Translation units whose results must be bit-identical to plain IEEE C
 # arithmetic (no FMA contraction): the conduction steps (plain and per-facet
-# thermal inertia), the facet geometry and the ray/triangle predicates.
-NO_FMAD = {"conduction.cu", "adjoint.cu", "geometry.cu", "raycast.cu", "formfactor.cu"}
+# thermal inertia), the facet geometry, the ray/triangle predicates and the
+# exact triangle view factor (whose parallel-edge terms cancel strongly, so
+# contraction choices would make its two kernels differ in the last bits).
+NO_FMAD = {"conduction.cu", "adjoint.cu", "geometry.cu", "raycast.cu", "formfactor.cu",
+           "viewfactor.cu"}
 
 
 def _nvcc() -> str:

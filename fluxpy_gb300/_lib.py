@@ -94,6 +94,9 @@ SIGNATURES: dict[str, list] = {
     "fgb_aca_f64_static": [P, P, P, P, P, I64, P, P, P, P, I64, I64, F64, I32, F32, I32, I32,
                            I64, I32, P, I64, P, P, P, U32P, P],
     "fgb_recompress_f32": [P, P, P, P, P, I64, F32, P, I64, P, P, P, P, U32P, P],
+    # exact triangle-triangle view factor (view_factor_narayanaswamy.c)
+    "fgb_ff_triangles_f64": [P, P, I64, P, U32P, P],
+    "fgb_ff_adjacent_fix_f64": [P, P, P, P, I64, P, P, P, P, U32P, P],
     # block matvec (a9)
     "fgb_build_panel_f32_f32": [P, I64, P, P, P, P, P, I64, P, P],
     "fgb_build_panel_f32_bf16": [P, I64, P, P, P, P, P, I64, P, P],
@@ -110,6 +113,7 @@ SIGNATURES: dict[str, list] = {
     "fgb_matvec_f32_f64": [P, P, P, P, P, P, P, F64, I32, P],
     "fgb_rmatvec_f64": [P, P, P, P, P, U32P, P],
     "fgb_rmatvec_f32_f64": [P, P, P, P, P, U32P, P],
+    "fgb_matmat_f32_f64": [P, P, P, P, P, P, I32, P, F64, I32, P],
     "fgb_matmat_f32": [P, P, P, P, P, P, I32, P, F32, I32, I32, P],
     "fgb_matmat_bf16": [P, P, P, P, P, P, P, I32, P, F32, I32, I32, P],
     "fgb_tc_phase_a": [P, P, P, P, P, P, I32, I32, P, P],

@@ -6,8 +6,11 @@ derivatives).
   B = E + F (rho B) (the 'right' albedo placement of src/flux/solve.py:36-45),
   FP64 Jacobi on the device.  Backward: the transposed solve
   lam = gB + rho (F^T lam), then dL/dE = lam and dL/drho = B (F^T lam)
-  (summed over columns); F^T is the compressed operator's transposed panel
-  product (libfluxgb ``fgb_rmatvec_*``) or a device CSR of F^T.
+  (summed over columns); F^T is the compressed operator's transposed copy
+  (``CompressedFormFactorMatrix.transposed``: the same kernels on the
+  transposed blocks, deterministic) or a device CSR of F^T.  Many columns of
+  a compressed FP32-stored operator are solved by iterative refinement:
+  FP32 sweeps of all columns, FP64 residuals of all columns.
 * ``ConductionStep`` / ``conduction_step(...)``: one conductionQ step
   (src/flux/pcc/conductionQ.c:10-186) with per-facet thermal inertia
   (``fgb_conduction_q_ti_f64``); backward: ``fgb_conduction_q_adjoint_f64``,
@@ -47,20 +50,39 @@ F64 = torch.float64
 
 # ------------------------------------------------------------ operators --
 class _Ops:
-    """y = F x and y = F^T x on FP64 device vectors in facet order."""
+    """y = F x and y = F^T x on FP64 device vectors in facet order (one
+    column or K columns).  A compressed operator with FP32 storage applies
+    K columns at once in FP64 arithmetic, its transpose through the
+    transposed operator (``CompressedFormFactorMatrix.transposed``, same
+    kernels, deterministic); ``batched`` tells the solves that they can
+    refine with FP32 sweeps (``_refine``)."""
 
     def __init__(self, FF, dev):
         from .compressed_form_factors import CompressedFormFactorMatrix
         self.FF = FF
+        self.batched = False
         if isinstance(FF, CompressedFormFactorMatrix):
             prec = "fp64" if FF._pool.dtype == torch.float64 else "fp32-fp64"
             self._prec = prec
+            self.batched = prec == "fp32-fp64"
 
             def fwd(x):
-                return FF.unpermute(FF.matvec_permuted(FF.permute(x), prec))
+                xp = FF.permute(x)
+                if x.ndim == 1:
+                    return FF.unpermute(FF.matvec_permuted(xp, prec))
+                if self.batched:
+                    return FF.unpermute(FF.matmat_permuted(xp.contiguous(), prec))
+                return FF.unpermute(torch.stack([FF.matvec_permuted(xp[:, c].contiguous(), prec)
+                                                 for c in range(xp.shape[1])], 1))
 
             def tr(y):
-                return FF.unpermute(FF.rmatvec_permuted(FF.permute(y), prec))
+                yp = FF.permute(y)
+                if y.ndim == 1:
+                    return FF.unpermute(FF.rmatvec_permuted(yp, prec))
+                if self.batched:
+                    return FF.unpermute(FF.rmatmat_permuted(yp.contiguous(), prec))
+                return FF.unpermute(torch.stack([FF.rmatvec_permuted(yp[:, c].contiguous(), prec)
+                                                 for c in range(yp.shape[1])], 1))
             self.N = FF.num_faces
         elif scipy.sparse.issparse(FF) or isinstance(FF, np.ndarray):
             A = scipy.sparse.csr_matrix(FF)
@@ -73,14 +95,10 @@ class _Ops:
         self._fwd, self._tr = fwd, tr
 
     def F(self, x):
-        if x.ndim == 1:
-            return self._fwd(x.contiguous())
-        return torch.stack([self._fwd(x[:, c].contiguous()) for c in range(x.shape[1])], 1)
+        return self._fwd(x.contiguous())
 
     def FT(self, y):
-        if y.ndim == 1:
-            return self._tr(y.contiguous())
-        return torch.stack([self._tr(y[:, c].contiguous()) for c in range(y.shape[1])], 1)
+        return self._tr(y.contiguous())
 
 
 def _ops(FF, dev):
@@ -115,14 +133,62 @@ def _jacobi(apply, E, rho, tol, max_iter):
     raise NoConvergence(f"Jacobi did not converge in {max_iter} iterations")
 
 
+def _refine(ops, E, rho, tol, transpose, max_outer=30, sweep_tol=1e-7, max_sweeps=200):
+    """Iterative refinement of the right-placement solve (transpose=False:
+    B = E + F (rho B)) or of its transpose (lam = E + rho (F^T lam)) for K
+    columns of a compressed FP32-stored operator: FP32 Jacobi sweeps of all
+    columns for each correction (the FP32 K-column kernels), FP64 residuals
+    of all columns (the FP32-stored operator in FP64 arithmetic) until
+    max|E - (B - apply(B))| <= tol max|E|.  Works in cluster order."""
+    FF = ops.FF
+    Op = FF.transposed() if transpose else FF
+    Ep = FF.permute(E).contiguous()
+    rp = FF.permute(rho.expand(ops.N)).reshape(-1, 1).contiguous()
+    rp32 = rp.to(torch.float32)
+    scale = float(Ep.abs().max().item()) if Ep.numel() else 0.0
+    if scale == 0.0:
+        return torch.zeros_like(E)
+
+    def ap64(X):
+        if transpose:
+            return rp * Op.matmat_permuted(X, "fp32-fp64")
+        return Op.matmat_permuted((rp * X).contiguous(), "fp32-fp64")
+
+    def ap32(X):
+        if transpose:
+            return rp32 * Op.matmat_permuted(X, "fp32")
+        return Op.matmat_permuted((rp32 * X).contiguous(), "fp32")
+    B = torch.zeros_like(Ep)
+    R = Ep
+    for _ in range(max_outer):
+        R32 = R.to(torch.float32)
+        thr = sweep_tol * float(R32.abs().max().item())
+        D = R32.clone()
+        for _ in range(max_sweeps):
+            D1 = R32 + ap32(D)
+            done = float((D1 - D).abs().max().item()) <= thr
+            D = D1
+            if done:
+                break
+        B = B + D.to(F64)
+        R = Ep - (B - ap64(B))
+        if float(R.abs().max().item()) <= tol * scale:
+            return FF.unpermute(B)
+    raise NoConvergence("refinement did not converge")
+
+
 def solve_right(ops, E, rho, tol=1e-13, max_iter=10000):
     """B = E + F (rho B) for E (N,) or (N, K), FP64."""
+    if ops.batched and E.ndim == 2:
+        return _refine(ops, E, rho, tol, transpose=False)
     r = _col(rho, E)
     return _jacobi(lambda X, E_: E_ + ops.F(r * X), E, rho, tol, max_iter)[0]
 
 
 def solve_right_T(ops, G, rho, tol=1e-13, max_iter=10000):
     """lam = G + rho (F^T lam): the transposed system of ``solve_right``."""
+    if ops.batched and G.ndim == 2:
+        return _refine(ops, G, rho, tol, transpose=True)
     r = _col(rho, G)
     return _jacobi(lambda X, G_: G_ + r * ops.FT(X), G, rho, tol, max_iter)[0]
 

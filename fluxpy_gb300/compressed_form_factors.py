@@ -357,6 +357,63 @@ PANEL_ALIGN = 64
 TC_A_ROWS = 128
 
 
+def _transpose_exact_csr(tcsr, ex_m, ex_n, chunk_nnz=200_000_000):
+    """The exact leaves' device CSR (one tile per leaf, rows local to the
+    leaf, columns local to it, visible-pair bitmask) of the transposed
+    leaves: leaf q becomes an ex_n[q] x ex_m[q] tile with the same values.
+    The entries of a leaf occupy the same range of the entry arrays before
+    and after, so leaves are transposed in chunks of about chunk_nnz entries."""
+    from .form_factors import TileCSR
+    dev = tcsr.indptr.device
+    nleaf = int(ex_m.size)
+    ex_m = np.asarray(ex_m, np.int64)
+    ex_n = np.asarray(ex_n, np.int64)
+    ro = np.asarray(tcsr.row_off, np.int64)
+    ro_t = np.zeros(nleaf + 1, np.int64)
+    np.cumsum(ex_n, out=ro_t[1:])
+    wpr_t = (ex_m + 31) // 32
+    wo_t = np.zeros(nleaf + 1, np.int64)
+    np.cumsum(ex_n * wpr_t, out=wo_t[1:])
+    indptr = tcsr.indptr
+    nnz = int(indptr[-1].item()) if indptr.numel() else 0
+    indices_t = torch.empty(max(nnz, 1), dtype=torch.int32, device=dev)
+    data_t = torch.empty(max(nnz, 1), dtype=tcsr.data.dtype, device=dev)
+    counts_t = torch.zeros(int(ro_t[-1]) + 1, dtype=torch.int64, device=dev)
+    bits64 = torch.zeros(max(int(wo_t[-1]), 1), dtype=torch.int64, device=dev)
+    leaf_e0 = indptr[torch.as_tensor(ro, device=dev)].cpu().numpy()   # first entry of each leaf
+    d = lambda a: torch.as_tensor(a, device=dev)
+    ro_d, ro_t_d, wo_t_d, wpr_t_d = d(ro), d(ro_t), d(wo_t), d(wpr_t)
+    q0 = 0
+    while q0 < nleaf:
+        q1 = int(np.searchsorted(leaf_e0, leaf_e0[q0] + chunk_nnz, side="right")) - 1
+        q1 = min(max(q1, q0 + 1), nleaf)
+        e0, e1 = int(leaf_e0[q0]), int(leaf_e0[q1])
+        r0, r1 = int(ro[q0]), int(ro[q1])
+        if e1 > e0:
+            cnt = indptr[r0 + 1:r1 + 1] - indptr[r0:r1]
+            row = torch.repeat_interleave(torch.arange(r0, r1, device=dev), cnt)
+            leaf = torch.searchsorted(ro_d, row, right=True) - 1
+            r = row - ro_d[leaf]
+            del row
+            c = tcsr.indices[e0:e1].to(torch.int64)
+            g = ro_t_d[leaf] + c                    # transposed row
+            key = g * int(ex_m[q0:q1].max() + 1) + r
+            order = torch.argsort(key)
+            del key
+            indices_t[e0:e1] = r[order].to(torch.int32)
+            data_t[e0:e1] = tcsr.data[e0:e1][order]
+            counts_t.index_add_(0, g, torch.ones_like(g))
+            word = wo_t_d[leaf] + c * wpr_t_d[leaf] + (r >> 5)
+            bits64.index_add_(0, word, torch.ones_like(r) << (r & 31))
+            del leaf, r, c, g, order, word
+        q0 = q1
+    indptr_t = torch.zeros(int(ro_t[-1]) + 1, dtype=torch.int64, device=dev)
+    torch.cumsum(counts_t[:-1], 0, out=indptr_t[1:])
+    bits = torch.where(bits64 >= 2**31, bits64 - 2**32, bits64).to(torch.int32)
+    return TileCSR(indptr_t, indices_t[:nnz], data_t[:nnz], ro_t, tcsr.kept_pairs,
+                   tcsr.near_edge_pairs, bits, wo_t)
+
+
 class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
     """A compressed form factor (view factor) matrix
     (src/flux/compressed_form_factors.py:701-873)."""
@@ -364,7 +421,7 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
     def __init__(self, shape_model, tol=1e-5, min_size=16384, max_depth=None,
                  force_max_depth=False, RootBlock=None, *, leaf_size=64, eta=1.0, rmax=64,
                  nsample=16384, exact_aca_max=262144, dtype=None, eps=None, aca_tol=None,
-                 recompress=True, **kwargs):
+                 recompress=True, exact_zero_blocks=True, **kwargs):
         if tol < 0:
             raise RuntimeError('tol should be a nonnegative float')
         if max_depth is not None and not isinstance(max_depth, int):
@@ -409,6 +466,7 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         # ACA runs below the block tolerance and the FP64 truncation brings
         # every block to it (sigma_i / sigma_0 > tol kept, the reference's rule)
         self._recompress = bool(recompress)
+        self._exact_zero_blocks = bool(exact_zero_blocks)
         self._aca_tol = float(aca_tol if aca_tol is not None else
                               (tol / 10 if recompress else tol))
         self._eps = config.DEFAULT_EPS if eps is None else eps
@@ -482,6 +540,8 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         self._rank = plan["rank"]
         self._root_bshape = plan["root_bshape"]
         exact = plan["exact"]
+        if self._exact_zero_blocks:
+            exact = np.concatenate([exact, self._visible_in_zero_blocks(perm_d)])
         t0 = time.perf_counter()
         self._assemble(exact, plan["aca_pool_parts"], plan["pool_off"])
         t_exact = time.perf_counter() - t0
@@ -555,6 +615,48 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         ranks[order] = ranks_s
         offs[order] = np.where(offs_s >= 0, offs_s + pool_base, -1)
         return ranks, offs, (pool[:nused] if nused else None)
+
+    def _visible_in_zero_blocks(self, perm_d, chunk_pairs=15_000_000_000):
+        """Blocks that ACA found to be zero from its random samples but that
+        hold visible pairs: every pair of those blocks is evaluated by the
+        pair kernel (in chunks of about chunk_pairs pairs); the blocks with
+        nonzeros become exact leaves (returned), the others stay zero.
+        Occluded far-field blocks can hide a few pairs that see each other
+        through a gap (thin slivers that no affordable random sample finds)."""
+        import time
+        t0 = time.perf_counter()
+        tree = self._tree
+        zb = np.flatnonzero((self._kind == LEAF_LOWRANK) & (self._rank == 0))
+        r0 = tree.start[self._rows[zb]]
+        m = tree.size[self._rows[zb]]
+        c0 = tree.start[self._cols[zb]]
+        n = tree.size[self._cols[zb]]
+        pairs = m.astype(np.int64) * n
+        found = []
+        kept = 0
+        lo = 0
+        cum = np.cumsum(pairs)
+        while lo < zb.size:
+            base = cum[lo - 1] if lo else 0
+            hi = int(np.searchsorted(cum, base + chunk_pairs, side="right"))
+            hi = max(hi, lo + 1)
+            sl = slice(lo, hi)
+            tc = ff_tiles(self.shape_model, perm_d, perm_d, r0[sl], m[sl], c0[sl], n[sl],
+                          self._eps)
+            kept += tc.kept_pairs
+            ro = torch.as_tensor(tc.row_off, device=perm_d.device)
+            nnz = (tc.indptr[ro[1:]] - tc.indptr[ro[:-1]]).cpu().numpy()
+            found.append(zb[sl][nnz > 0])
+            del tc
+            lo = hi
+        out = np.concatenate(found) if found else np.zeros(0, np.int64)
+        # these blocks are exact leaves now, no longer low-rank
+        self._kind[out] = -1
+        self._rank[out] = 0
+        self.stats.update(zero_blocks_checked=int(zb.size), zero_blocks_with_pairs=int(out.size),
+                          zero_block_pairs=int(pairs.sum()), zero_block_kept_pairs=int(kept),
+                          zero_block_check_s=time.perf_counter() - t0)
+        return out
 
     def _truncate(self, pool, rank, off, m_d, n_d):
         """FP64 rank truncation of the ACA factors of one batch of blocks
@@ -635,6 +737,12 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         lr = np.where((self._kind == LEAF_LOWRANK) & (self._rank > 0))[0]
         self._layout(lr, pool_off, ex_r0, ex_m, ex_c0, ex_n)
 
+    @staticmethod
+    def _factor_offsets(off, k, m, n):
+        """Pool offsets of U^T (k x m) and V^T (k x n) of low-rank blocks
+        stored at `off` (U^T first)."""
+        return off, off + k * m
+
     def _layout(self, lr, pool_off, ex_r0, ex_m, ex_c0, ex_n):
         """Panel layout consumed by libfluxgb's matvec kernels (matvec.cu)."""
         tree = self._tree
@@ -653,8 +761,7 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         lr_c0 = tree.start[self._cols[lr]].astype(np.int64)
         lr_n = tree.size[self._cols[lr]].astype(np.int64)
         lr_k = self._rank[lr].astype(np.int64)
-        lr_u = pool_off[lr]
-        lr_v = lr_u + lr_k * lr_m
+        lr_u, lr_v = self._factor_offsets(pool_off[lr], lr_k, lr_m, lr_n)
         order = np.lexsort((lr_n, lr_c0))
         lr, lr_r0, lr_m, lr_c0, lr_n, lr_k, lr_u, lr_v = (a[order] for a in
                                                          (lr, lr_r0, lr_m, lr_c0, lr_n, lr_k,
@@ -1006,6 +1113,52 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         self._panels[precision] = (panel, vpanel)
         return panel, vpanel
 
+    # keys of the device layout and caches that a transposed copy rebuilds
+    _LAYOUT_KEYS = ("_dev", "_dev_tc", "_build_dev", "_nf", "_desc", "_desc_tc", "_desc_tc64",
+                    "_desc_tc_items", "_desc128", "_dev128", "_panels", "_tc", "_flags_d",
+                    "_fgb_adjoint_ops", "_root_cache", "_host_tree_cache", "_transposed",
+                    "_exact_csr", "_lr_blocks", "_lr_u", "_lr_v", "_tile_L")
+
+    def transposed(self):
+        """F^T as an operator of the same kind (cached): the same blocks with
+        rows and columns exchanged, U and V exchanged in the low-rank blocks
+        and the exact leaves' CSR transposed on the device, laid out in
+        panels of its own.  Every product of F (K = 1 or K columns, FP32,
+        FP64 arithmetic, BF16 tensor cores) is then available for F^T, with
+        the same determinism (each output row tile written by one CTA)."""
+        T = self.__dict__.get("_transposed")
+        if T is not None:
+            return T
+        dev = self._perm_d.device
+        if self._pool.device != dev:
+            self._pool = self._pool.to(dev)
+        tc = self._exact_csr
+        if tc is not None and tc.indptr.device != dev:
+            tc.data, tc.indptr, tc.bits, tc.indices = (tc.data.to(dev), tc.indptr.to(dev),
+                                                       tc.bits.to(dev), tc.indices.to(dev))
+        tree = self._tree
+        exact = self._exact
+        ex_r0 = tree.start[self._rows[exact]].astype(np.int64)
+        ex_m = tree.size[self._rows[exact]].astype(np.int64)
+        ex_c0 = tree.start[self._cols[exact]].astype(np.int64)
+        ex_n = tree.size[self._cols[exact]].astype(np.int64)
+        T = CompressedFormFactorMatrix.__new__(CompressedFormFactorMatrix)
+        T.__dict__.update({k: v for k, v in self.__dict__.items() if k not in self._LAYOUT_KEYS})
+        T._rows, T._cols = self._cols, self._rows
+        T._root_cache = None
+        T.stats = {}
+        # a block's pool slot holds the original U^T (k x m) then V^T (k x n):
+        # the transposed block's U^T is the original V^T, its V^T the original U^T
+        T._factor_offsets = lambda off, k, m, n: (off + k * n, off)
+        T._exact_csr = (_transpose_exact_csr(tc, ex_m, ex_n) if tc is not None else None)
+        pool_off = np.full(len(self._rows), -1, np.int64)
+        pool_off[self._lr_blocks] = self._lr_u
+        lr = np.where((self._kind == LEAF_LOWRANK) & (self._rank > 0))[0]
+        T._layout(lr, pool_off, ex_c0, ex_n, ex_r0, ex_m)
+        T._is_transposed = True
+        self._transposed = T
+        return T
+
     def permute(self, x: torch.Tensor) -> torch.Tensor:
         """Facet order -> cluster order (rows)."""
         return x.index_select(0, self._perm_d)
@@ -1046,30 +1199,21 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         """F^T y in cluster order, K = 1, FP64 vectors and arithmetic.
 
         precision: 'fp64' (FP64 panels) or 'fp32-fp64' (the FP32-stored
-        operator); default: the pool's own precision.  The transposed
-        operator is the transposed panels, applied by libfluxgb
-        ``fgb_rmatvec_*`` (scatter of each panel row, then V_g Zbar_g per
-        low-rank group)."""
+        operator); default: the pool's own precision.  The product is the
+        transposed operator's (``transposed()``), deterministic."""
         if precision is None:
             precision = "fp64" if self._pool.dtype == torch.float64 else "fp32-fp64"
-        if precision == "fp64":
-            fn, pp = "fgb_rmatvec_f64", "fp64"
-        elif precision == "fp32-fp64":
-            fn, pp = "fgb_rmatvec_f32_f64", "fp32"
-        else:
+        if precision not in ("fp64", "fp32-fp64"):
             raise ValueError(f"transpose products run in FP64 arithmetic, not {precision!r}")
-        yp = yp.to(torch.float64).contiguous()
-        work = torch.empty(self._num_zrows + self.num_faces, dtype=torch.float64,
-                           device=yp.device)
-        panel, vpanel = self.panels(pp)
-        _lib.call(fn, C.byref(self._desc), _lib.ptr(panel), _lib.ptr(vpanel), _lib.ptr(yp),
-                  _lib.ptr(work), _lib.ptr(self.device_flags()), _lib.stream_handle())
-        return work[self._num_zrows:]
+        return self.transposed().matvec_permuted(yp.to(torch.float64).contiguous(), precision)
 
     def rmatmat_permuted(self, Yp, precision=None):
-        """F^T Y in cluster order for Y (N, K): one transpose product per column."""
-        return torch.stack([self.rmatvec_permuted(Yp[:, c], precision)
-                            for c in range(Yp.shape[1])], 1)
+        """F^T Y in cluster order for Y (N, K) (the transposed operator's
+        products: 'fp32', 'bf16', 'fp32-fp64' all columns at once, 'fp64'
+        column by column; default: FP64 arithmetic)."""
+        if precision is None:
+            precision = "fp64" if self._pool.dtype == torch.float64 else "fp32-fp64"
+        return self.transposed().matmat_permuted(Yp.contiguous(), precision)
 
     def matmat_permuted(self, Xp, precision="fp32", out=None, add=None, alpha=1.0, Z=None):
         """Y = F X for K right-hand sides in cluster order (X: N x K)."""
@@ -1094,6 +1238,20 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
             _lib.call("fgb_matmat_f32", C.byref(self._desc), _lib.ptr(panel), _lib.ptr(vpanel),
                       _lib.ptr(Xp), _lib.ptr(Z), _lib.ptr(out), K, _lib.ptr(add), float(alpha),
                       int(self._needs_zero_z), 3, _lib.stream_handle())
+            return out
+        if precision == "fp32-fp64":
+            # the FP32-stored operator in FP64 arithmetic, all K columns at once
+            Xp = Xp.to(torch.float64).contiguous()
+            if out is None:
+                out = torch.empty_like(Xp)
+            if Z is None:
+                Z = torch.empty((max(self._num_zrows, 1), K), dtype=torch.float64,
+                                device=Xp.device)
+            panel, vpanel = self.panels("fp32")
+            addc = None if add is None else add.to(torch.float64).contiguous()
+            _lib.call("fgb_matmat_f32_f64", C.byref(self._desc), _lib.ptr(panel), _lib.ptr(vpanel),
+                      _lib.ptr(Xp), _lib.ptr(Z), _lib.ptr(out), K, _lib.ptr(addc), float(alpha),
+                      int(self._needs_zero_z), _lib.stream_handle())
             return out
         if precision == "bf16":
             return self._matmat_bf16(Xp, out=out, add=add, alpha=alpha, Z=Z)
@@ -1609,6 +1767,7 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         st = dict(self.__dict__)
         st["_root_cache"] = None
         st.pop("_host_tree_cache", None)
+        st.pop("_transposed", None)
         st["_desc"] = None
         st["_desc_tc"] = None
         st["_desc_tc64"] = None

@@ -10,9 +10,13 @@
 //     without FMA contraction (this file is compiled with -fmad=false);
 //   * the temperature rows (num_faces x (nz+1), the reference's row-major
 //     layout) are staged through shared memory with coalesced loads/stores;
-//     the sweep reads the pre-step profile from there (its own arrays u,
-//     gam stay per-thread, so the shared layout is small and many warps
-//     share an SM); the facets per CTA (32..128) follow from nz;
+//     the sweep reads the pre-step profile from there;
+//   * the sweep's own arrays (u and gam, nz + 1 each) never touch local
+//     memory: for FP32 grids of up to 48 nodes (the thermal configurations
+//     use 41) they are registers (loops fully unrolled over the node count,
+//     guarded by the run-time nz); otherwise they are per-thread columns in
+//     shared memory (element j of thread t at j * nt + t, conflict-free);
+//     the facets per CTA (32..128) follow from nz and that layout;
 //   * the linearised radiative boundary (predictor-corrector, at most 10
 //     redos, conductionQ.c:103-172) and the Thomas solve are fused: the
 //     right-hand side is formed on the fly during the forward sweep from the
@@ -21,6 +25,8 @@
 //     bad input can be discarded by the host, as the reference raises before
 //     touching T (thermal.pyx:240-247).
 #include "common.cuh"
+
+#include <type_traits>
 
 namespace fgb {
 namespace {
@@ -101,19 +107,28 @@ constexpr size_t kSmemBudget = 227 * 1024;  // the per-CTA opt-in maximum
 // that many CTAs (warps) share an SM and hide the sweep's dependent chain.
 __host__ __device__ inline int tile_stride(int nz) { return (nz + 1) | 1; }
 
+// ncols: per-thread columns of the sweep after the tile (2 (nz + 1) for
+// SmemStore, 0 for RegStore).
 template <class R>
-size_t cond_smem(int nz, int nt) {
-  return sizeof(R) * ((size_t)7 * (nz + 1) + (size_t)nt * tile_stride(nz));
+size_t cond_smem(int nz, int nt, int ncols) {
+  return sizeof(R) * ((size_t)7 * (nz + 1) + (size_t)nt * (tile_stride(nz) + ncols));
 }
 
 // Facets per CTA: the largest multiple of 32 (at most 128) whose shared
 // layout fits the budget; 0 if even one warp does not fit.
 template <class R>
-int cond_threads(int nz) {
+int cond_threads(int nz, int ncols) {
   for (int nt = kMaxThreads; nt >= 32; nt -= 32)
-    if (cond_smem<R>(nz, nt) <= kSmemBudget) return nt;
+    if (cond_smem<R>(nz, nt, ncols) <= kSmemBudget) return nt;
   return 0;
 }
+
+// Register storage holds the sweep of FP32 grids with nz <= kRegNz.
+constexpr int kRegNz = 47;
+template <class R, int NZMAX>
+constexpr bool use_regs() { return sizeof(R) == 4 && NZMAX <= kRegNz; }
+template <class R, int NZMAX>
+int sweep_cols(int nz) { return use_regs<R, NZMAX>() ? 0 : 2 * (nz + 1); }
 
 template <class R>
 __device__ inline R* coeff(R* sh, int which, int nz) { return sh + which * (nz + 1); }
@@ -157,23 +172,48 @@ template <> struct Pivot<float> {
   __device__ float div(float x) const { return x * r; }
 };
 
+// Storage of the sweep's arrays u and gam.  RegStore: register arrays
+// indexed only by constants (the sweep loops are fully unrolled to NZMAX
+// and guarded by nz).  SmemStore: per-thread columns in shared memory.
+template <class R, int NZMAX>
+struct RegStore {
+  static constexpr bool kUnrolled = true;
+  R u_[NZMAX + 1];
+  R g_[NZMAX + 1];
+  __device__ R& u(int j) { return u_[j]; }
+  __device__ R& gam(int j) { return g_[j]; }
+};
+
+template <class R, int NZMAX>
+struct SmemStore {
+  static constexpr bool kUnrolled = false;
+  R* base;   // u column at base, gam column at base + goff
+  int nt;    // column stride (threads per CTA)
+  int goff;  // (nz + 1) * nt
+  __device__ R& u(int j) { return base[j * nt]; }
+  __device__ R& gam(int j) { return base[goff + j * nt]; }
+};
+
 // Forward sweep and back substitution of the tridiagonal system with
 // sub/main/super diagonals (a, b, c) from shared memory, except the first
 // main-diagonal entry b1 (facet dependent under the radiative boundary).
 // The right-hand side is formed on the fly from the pre-step profile Trow
 // (crank-nicolson explicit half, conductionQ.c:123-137 / conductionT.c:66-77).
+// The arithmetic is the reference's tridag (tridag.c:5-34) in its order.
 // Returns false on a zero pivot.
-template <class R>
+template <class R, int NZMAX, class Store>
 __device__ bool thomas_cn(int nz, const R* Trow, R r1, R b1, R rhs_bottom,
                           const R* s_alpha, const R* s_gamma, const R* s_a, const R* s_b,
-                          const R* s_c, R* u, R* gam) {
+                          const R* s_c, Store& st) {
   R bet = b1;
   if (bet == R(0)) return false;
   Pivot<R> pv(bet);
   R uprev = pv.div(r1);
-  u[1] = uprev;
+  st.u(1) = uprev;
   R tm1 = Trow[1], t0 = Trow[2];
-  for (int j = 2; j <= nz; j++) {
+  bool ok = true;
+  // forward sweep, row j (2 <= j <= nz)
+  auto forward = [&](int j) {
     R rj;
     if (j < nz) {
       const R tp1 = Trow[j + 1];
@@ -187,24 +227,40 @@ __device__ bool thomas_cn(int nz, const R* Trow, R r1, R b1, R rhs_bottom,
     }
     const R aj = s_a[j];
     const R g = pv.div(s_c[j - 1]);
-    gam[j] = g;
+    st.gam(j) = g;
     bet = s_b[j] - aj * g;
-    if (bet == R(0)) return false;
+    if (bet == R(0)) { ok = false; return; }
     pv = Pivot<R>(bet);
     uprev = pv.div(rj - aj * uprev);
-    u[j] = uprev;
-  }
+    st.u(j) = uprev;
+  };
   R unext = uprev;
-  for (int j = nz - 1; j >= 1; j--) {
-    unext = u[j] - gam[j + 1] * unext;
-    u[j] = unext;
+  // back substitution, row j (nz - 1 >= j >= 1)
+  auto backward = [&](int j) {
+    unext = st.u(j) - st.gam(j + 1) * unext;
+    st.u(j) = unext;
+  };
+  if constexpr (Store::kUnrolled) {
+#pragma unroll
+    for (int j = 2; j <= NZMAX; j++)
+      if (j <= nz && ok) forward(j);
+    if (!ok) return false;
+    unext = uprev;
+#pragma unroll
+    for (int j = NZMAX - 1; j >= 1; j--)
+      if (j <= nz - 1) backward(j);
+  } else {
+    for (int j = 2; j <= nz && ok; j++) forward(j);
+    if (!ok) return false;
+    unext = uprev;
+    for (int j = nz - 1; j >= 1; j--) backward(j);
   }
   return true;
 }
 
 // One step of the radiative-flux boundary problem for every facet.
-template <class R, int NZMAX>
-__global__ void __launch_bounds__(kMaxThreads)
+template <class R, int NZMAX, bool REG>
+__global__ void __launch_bounds__(kMaxThreads, 3)
 conduction_q_kernel(int num_faces, int nz, const R* __restrict__ z, R dt,
                     const R* __restrict__ Qn, const R* __restrict__ Qnp1,
                     const R* T_in, R* T_out,
@@ -231,11 +287,16 @@ conduction_q_kernel(int num_faces, int nz, const R* __restrict__ z, R dt,
 
   const int t = threadIdx.x;
   unsigned my_flags = 0;
+  using Store = typename std::conditional<REG, RegStore<R, NZMAX>, SmemStore<R, NZMAX>>::type;
+  Store st;
+  if constexpr (!REG) {
+    st.base = tile + nt * ws + t;
+    st.nt = nt;
+    st.goff = w * nt;
+  }
   if (t < rows) {
     const long long f = f0 + t;
     R* Trow = tile + t * ws;
-    R u[NZMAX + 1];
-    R gam[NZMAX + 1];
     const R qn = Qn[f], qnp1 = Qnp1[f], em = emiss[f], fg = Fgeotherm[f];
     if (!finite_val(qnp1)) my_flags |= kFlagNonfiniteIn;
     if (qnp1 < R(0)) my_flags |= kFlagNegativeIn;
@@ -255,12 +316,12 @@ conduction_q_kernel(int num_faces, int nz, const R* __restrict__ z, R dt,
       R b1 = R(1) + alpha1 + gamma1 - gamma1 * bn;
       R r1 = gamma1 * (annp1 + ann) + (R(1) - alpha1 - gamma1 + gamma1 * bn) * Trow[1] +
              alpha1 * Trow[2];
-      if (!thomas_cn<R>(nz, Trow, r1, b1, rhs_bottom, s_alpha, s_gamma, s_a, s_b, s_c, u,
-                        gam)) {
+      if (!thomas_cn<R, NZMAX>(nz, Trow, r1, b1, rhs_bottom, s_alpha, s_gamma, s_a, s_b, s_c,
+                               st)) {
         my_flags |= kFlagZeroPivot;
         break;
       }
-      T0 = R(0.5) * (annp1 + bn * u[1] + u[1]);
+      T0 = R(0.5) * (annp1 + bn * st.u(1) + st.u(1));
       if ((T0 > R(1.2) * Tr || T0 < R(0.8) * Tr) && iter < 10) {
         iter++;
         Tr = sqrt(Tr * T0);
@@ -270,8 +331,15 @@ conduction_q_kernel(int num_faces, int nz, const R* __restrict__ z, R dt,
     }
     if (iter >= 9) my_flags |= kFlagPredCorrMax;
     Trow[0] = T0;
-    for (int i = 1; i <= nz; i++) Trow[i] = u[i];
-    Fsurf[f] = -s_k[1] * (u[1] - T0) / z[1];
+    const R u1 = st.u(1);
+    if constexpr (REG) {
+#pragma unroll
+      for (int i = 1; i <= NZMAX; i++)
+        if (i <= nz) Trow[i] = st.u(i);
+    } else {
+      for (int i = 1; i <= nz; i++) Trow[i] = st.u(i);
+    }
+    Fsurf[f] = -s_k[1] * (u1 - T0) / z[1];
     for (int i = 0; i <= nz; i++) {
       if (!finite_val(Trow[i])) my_flags |= kFlagNonfiniteOut;
       if (Trow[i] < R(0)) my_flags |= kFlagNegativeOut;
@@ -283,8 +351,8 @@ conduction_q_kernel(int num_faces, int nz, const R* __restrict__ z, R dt,
 }
 
 // One step of the prescribed-surface-temperature problem (conductionT.c).
-template <class R, int NZMAX>
-__global__ void __launch_bounds__(kMaxThreads)
+template <class R, int NZMAX, bool REG>
+__global__ void __launch_bounds__(kMaxThreads, 3)
 conduction_t_kernel(int num_faces, int nz, const R* __restrict__ z, R dt,
                     const R* __restrict__ Tsurf, const R* __restrict__ Tsurfp1,
                     const R* T_in, R* T_out,
@@ -308,23 +376,35 @@ conduction_t_kernel(int num_faces, int nz, const R* __restrict__ z, R dt,
   __syncthreads();
   const int t = threadIdx.x;
   unsigned my_flags = 0;
+  using Store = typename std::conditional<REG, RegStore<R, NZMAX>, SmemStore<R, NZMAX>>::type;
+  Store st;
+  if constexpr (!REG) {
+    st.base = tile + nt * ws + t;
+    st.nt = nt;
+    st.goff = w * nt;
+  }
   if (t < rows) {
     const long long f = f0 + t;
     R* Trow = tile + t * ws;
-    R u[NZMAX + 1];
-    R gam[NZMAX + 1];
     const R ts = Tsurf[f], tsp1 = Tsurfp1[f], fg = Fgeotherm[f];
     if (!finite_val(tsp1)) my_flags |= kFlagNonfiniteIn;
     if (tsp1 < R(0)) my_flags |= kFlagNegativeIn;
     const R alpha1 = s_alpha[1], gamma1 = s_gamma[1];
     R r1 = alpha1 * Trow[2] + (R(1) - alpha1 - gamma1) * Trow[1] + gamma1 * (ts + tsp1);
     const R rhs_bottom = dt / rhoc[nz] * fg / (z[nz] - z[nz - 1]);
-    if (!thomas_cn<R>(nz, Trow, r1, s_b[1], rhs_bottom, s_alpha, s_gamma, s_a, s_b, s_c, u,
-                      gam)) {
+    if (!thomas_cn<R, NZMAX>(nz, Trow, r1, s_b[1], rhs_bottom, s_alpha, s_gamma, s_a, s_b, s_c,
+                             st)) {
       my_flags |= kFlagZeroPivot;
     } else {
-      for (int i = 1; i <= nz; i++) Trow[i] = u[i];
-      Fsurf[f] = -s_k[1] * (u[1] - tsp1) / z[1];
+      const R u1 = st.u(1);
+      if constexpr (REG) {
+#pragma unroll
+        for (int i = 1; i <= NZMAX; i++)
+          if (i <= nz) Trow[i] = st.u(i);
+      } else {
+        for (int i = 1; i <= nz; i++) Trow[i] = st.u(i);
+      }
+      Fsurf[f] = -s_k[1] * (u1 - tsp1) / z[1];
     }
     for (int i = 1; i <= nz; i++) {
       if (!finite_val(Trow[i])) my_flags |= kFlagNonfiniteOut;
@@ -340,9 +420,10 @@ template <class R, int NZMAX>
 int launch_q(int num_faces, int nz, const R* z, R dt, const R* Qn, const R* Qnp1,
              const R* T_in, R* T_out, const R* ti, const R* rhoc, const R* emiss,
              const R* Fgeotherm, R* Fsurf, unsigned* flags, cudaStream_t s) {
-  const int nt = cond_threads<R>(nz);
-  const size_t sm = cond_smem<R>(nz, nt);
-  auto k = conduction_q_kernel<R, NZMAX>;
+  const int cols = sweep_cols<R, NZMAX>(nz);
+  const int nt = cond_threads<R>(nz, cols);
+  const size_t sm = cond_smem<R>(nz, nt, cols);
+  auto k = conduction_q_kernel<R, NZMAX, use_regs<R, NZMAX>()>;
   FGB_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   const unsigned grid = (unsigned)((num_faces + nt - 1) / nt);
   k<<<grid, nt, sm, s>>>(num_faces, nz, z, dt, Qn, Qnp1, T_in, T_out, ti, rhoc, emiss,
@@ -355,9 +436,10 @@ template <class R, int NZMAX>
 int launch_t(int num_faces, int nz, const R* z, R dt, const R* Ts, const R* Tsp1,
              const R* T_in, R* T_out, const R* ti, const R* rhoc, const R* Fgeotherm,
              R* Fsurf, unsigned* flags, cudaStream_t s) {
-  const int nt = cond_threads<R>(nz);
-  const size_t sm = cond_smem<R>(nz, nt);
-  auto k = conduction_t_kernel<R, NZMAX>;
+  const int cols = sweep_cols<R, NZMAX>(nz);
+  const int nt = cond_threads<R>(nz, cols);
+  const size_t sm = cond_smem<R>(nz, nt, cols);
+  auto k = conduction_t_kernel<R, NZMAX, use_regs<R, NZMAX>()>;
   FGB_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   const unsigned grid = (unsigned)((num_faces + nt - 1) / nt);
   k<<<grid, nt, sm, s>>>(num_faces, nz, z, dt, Ts, Tsp1, T_in, T_out, ti, rhoc, Fgeotherm,
@@ -370,7 +452,10 @@ template <class R>
 int check_args(int num_faces, int nz) {
   if (num_faces < 0) { set_error("num_faces must be >= 0"); return FGB_BAD_ARG; }
   if (nz < 2 || nz > 255) { set_error("nz (interior layers) must be in [2, 255], got %d", nz); return FGB_BAD_ARG; }
-  if (cond_threads<R>(nz) == 0) { set_error("nz too large for the staged tile"); return FGB_BAD_ARG; }
+  if (cond_threads<R>(nz, (sizeof(R) == 4 && nz <= kRegNz) ? 0 : 2 * (nz + 1)) == 0) {
+    set_error("nz too large for the staged tile");
+    return FGB_BAD_ARG;
+  }
   return FGB_OK;
 }
 

@@ -454,6 +454,202 @@ phaseB_kn_f32(PanelView op, const float* __restrict__ panel, const float* __rest
   }
 }
 
+// ------------------------------- K RHS, FP32 panels, FP64 arithmetic ----
+// The FP32-stored operator applied to FP64 right-hand sides with FP64
+// products and sums (the FP32 weights are exact in FP64): FP64 residuals of
+// many columns at once.  Same work split as the FP32 kernels above, with 64
+// columns per CTA (thread (ty, tx) owns rows 8 ty .. + 7 and columns
+// 2 tx, 2 tx + 1) so that the staged FP64 rows fit the same shared memory.
+constexpr int kB64Cols = 64;
+
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem, bool pred) {
+  const unsigned s = smem_u32(smem);
+  const int n = pred ? 8 : 0;
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(s), "l"(gmem), "r"(n));
+}
+
+__global__ void __launch_bounds__(256, 2)
+phaseA_kn_w32d(PanelView op, const float* __restrict__ vpanel, const double* __restrict__ X,
+               long long ldx, double* __restrict__ Z, long long ldz, int K) {
+  __shared__ __align__(16) float s_v[kB32Chunk][68];
+  __shared__ __align__(16) double s_x[kB32Chunk][kB64Cols];
+  const int tid = threadIdx.x, ty = tid >> 5, tx = tid & 31;
+  const int nkt = (K + kB64Cols - 1) / kB64Cols;
+  const long long unit = blockIdx.x / nkt;
+  const int c_base = (int)(blockIdx.x % nkt) * kB64Cols;
+  long long lo = 0, hi = op.num_items - 1;
+  while (lo < hi) {
+    const long long mid = (lo + hi + 1) >> 1;
+    if (op.a_woff[mid] <= unit) lo = mid; else hi = mid - 1;
+  }
+  const long long it = lo;
+  const int sl = (int)(unit - op.a_woff[it]);
+  const int g = op.a_grp[it];
+  const int kz = op.g_kz[g];
+  const int r_base = sl * 64;
+  const int j0 = op.a_j0[it], j1 = op.a_j1[it];
+  const int ldv = op.g_ldv[g];
+  const long long c0 = op.g_c0[g];
+  const float* vg = vpanel + op.g_voff[g];
+  const bool vec = (K % 2) == 0 && (ldx % 2) == 0;
+  double acc[8][2];
+#pragma unroll
+  for (int r = 0; r < 8; r++) { acc[r][0] = 0.0; acc[r][1] = 0.0; }
+  for (int jc = j0; jc < j1; jc += kB32Chunk) {
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+      const int p = tid + q * 256;
+      const int r = p >> 3, j = (p & 7) * 4;
+      const int row = r_base + r;
+      float v[4] = {0.f, 0.f, 0.f, 0.f};
+      if (row < kz) {
+        const float* src = vg + (long long)row * ldv + jc + j;
+        if (jc + j + 3 < j1) {
+          const float4 f = *reinterpret_cast<const float4*>(src);
+          v[0] = f.x; v[1] = f.y; v[2] = f.z; v[3] = f.w;
+        } else {
+#pragma unroll
+          for (int e = 0; e < 4; e++)
+            if (jc + j + e < j1) v[e] = src[e];
+        }
+      }
+#pragma unroll
+      for (int e = 0; e < 4; e++) s_v[j + e][r] = v[e];
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int j = ty + 8 * q;
+      const bool okr = jc + j < j1;
+      const double* xrow = X + (c0 + (okr ? jc + j : 0)) * ldx;
+      const int c = c_base + tx * 2;
+      if (vec) {
+        const bool ok = okr && c < K;
+        cp_async16(&s_x[j][tx * 2], ok ? xrow + c : xrow, ok);
+      } else {
+#pragma unroll
+        for (int e = 0; e < 2; e++) {
+          const bool ok = okr && c + e < K;
+          cp_async8(&s_x[j][tx * 2 + e], ok ? xrow + c + e : xrow, ok);
+        }
+      }
+    }
+    cp_async_commit();
+    cp_async_wait<0>();
+    __syncthreads();
+#pragma unroll 4
+    for (int j = 0; j < kB32Chunk; j++) {
+      const float4 v0 = *reinterpret_cast<const float4*>(&s_v[j][ty * 8]);
+      const float4 v1 = *reinterpret_cast<const float4*>(&s_v[j][ty * 8 + 4]);
+      const double2 xv = *reinterpret_cast<const double2*>(&s_x[j][tx * 2]);
+      const float w[8] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
+#pragma unroll
+      for (int r = 0; r < 8; r++) {
+        acc[r][0] = fma((double)w[r], xv.x, acc[r][0]);
+        acc[r][1] = fma((double)w[r], xv.y, acc[r][1]);
+      }
+    }
+  }
+  const bool excl = op.a_excl[it];
+  double* zg = Z + op.g_z0[g] * ldz;
+  const int col = c_base + tx * 2;
+#pragma unroll
+  for (int r = 0; r < 8; r++) {
+    const int row = r_base + ty * 8 + r;
+    if (row >= kz) continue;
+#pragma unroll
+    for (int c = 0; c < 2; c++) {
+      if (col + c >= K) continue;
+      double* dst = zg + (long long)row * ldz + col + c;
+      if (excl) *dst = acc[r][c];
+      else atomicAdd(dst, acc[r][c]);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256, 2)
+phaseB_kn_w32d(PanelView op, const float* __restrict__ panel, const double* __restrict__ X,
+               long long ldx, const double* __restrict__ Z, long long ldz, double* __restrict__ Y,
+               long long ldy, int K, const double* __restrict__ add_mat, long long ld_add,
+               double alpha) {
+  __shared__ __align__(16) float s_w[2][kB32Chunk][kTileRows];
+  __shared__ __align__(16) double s_s[2][kB32Chunk][kB64Cols];
+  const int tid = threadIdx.x, ty = tid >> 5, tx = tid & 31;
+  const int nkt = (K + kB64Cols - 1) / kB64Cols;
+  const long long t = blockIdx.x / nkt;
+  const int c_base = (int)(blockIdx.x % nkt) * kB64Cols;
+  const long long p0 = op.t_p0[t], p1 = op.t_p0[t + 1];
+  const bool vec = (K % 2) == 0 && (ldx % 2) == 0 && (ldz % 2) == 0;
+  double acc[8][2];
+#pragma unroll
+  for (int r = 0; r < 8; r++) { acc[r][0] = 0.0; acc[r][1] = 0.0; }
+  auto load = [&](int buf, long long l0) {
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+      const int e = tid + q * 256;
+      const int l = e >> 4, i4 = (e & 15) * 4;
+      cp_async16(&s_w[buf][l][i4], panel + (l0 + l) * kTileRows + i4, true);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int l = ty + 8 * q;
+      const int sidx = op.src[l0 + l];
+      const double* srow = sidx < op.num_zrows ? Z + (long long)sidx * ldz
+                                               : X + (long long)(sidx - op.num_zrows) * ldx;
+      const int c = c_base + tx * 2;
+      if (vec) {
+        const bool ok = c < K;
+        cp_async16(&s_s[buf][l][tx * 2], ok ? srow + c : srow, ok);
+      } else {
+#pragma unroll
+        for (int e = 0; e < 2; e++) {
+          const bool ok = c + e < K;
+          cp_async8(&s_s[buf][l][tx * 2 + e], ok ? srow + c + e : srow, ok);
+        }
+      }
+    }
+    cp_async_commit();
+  };
+  int buf = 0;
+  if (p0 < p1) load(0, p0);
+  for (long long l0 = p0; l0 < p1; l0 += kB32Chunk) {
+    if (l0 + kB32Chunk < p1) {
+      load(buf ^ 1, l0 + kB32Chunk);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int l = 0; l < kB32Chunk; l++) {
+      const float4 w0 = *reinterpret_cast<const float4*>(&s_w[buf][l][ty * 8]);
+      const float4 w1 = *reinterpret_cast<const float4*>(&s_w[buf][l][ty * 8 + 4]);
+      const double2 sv = *reinterpret_cast<const double2*>(&s_s[buf][l][tx * 2]);
+      const float w[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+#pragma unroll
+      for (int r = 0; r < 8; r++) {
+        acc[r][0] = fma((double)w[r], sv.x, acc[r][0]);
+        acc[r][1] = fma((double)w[r], sv.y, acc[r][1]);
+      }
+    }
+    __syncthreads();
+    buf ^= 1;
+  }
+  const int col = c_base + tx * 2;
+#pragma unroll
+  for (int r = 0; r < 8; r++) {
+    const long long i = t * kTileRows + ty * 8 + r;
+    if (i >= op.N) continue;
+#pragma unroll
+    for (int c = 0; c < 2; c++) {
+      if (col + c >= K) continue;
+      double v = acc[r][c];
+      if (add_mat) v = add_mat[i * ld_add + col + c] + alpha * v;
+      Y[i * ldy + col + c] = v;
+    }
+  }
+}
+
 // ------------------------------------------ K RHS, BF16 tensor cores ----
 // mma.sync.m16n8k16 (bf16 x bf16 -> fp32).  Fragments come from shared
 // memory through ldmatrix (.trans where the operand is stored k-major).
@@ -827,6 +1023,33 @@ int fgb_matmat_f32(const fgb_op_desc* d, const float* panel, const float* vpanel
     fgb::phaseB_kn_f32<<<(unsigned)(op.num_tiles * kb), 256, 0, s>>>(op, panel, X, K, Z, K, Y, K, K,
                                                                       add, K, alpha);
     FGB_LAUNCH_CHECK("phaseB_kn_f32");
+  }
+  return FGB_OK;
+}
+
+int fgb_matmat_f32_f64(const fgb_op_desc* d, const float* panel, const float* vpanel,
+                       const double* X, double* Z, double* Y, int K, const double* add,
+                       double alpha, int zero_z, void* stream) {
+  fgb::PanelView op = fgb::to_view(d);
+  int st = fgb::check_op(op);
+  if (st) return st;
+  if (K < 1) { fgb::set_error("K must be >= 1"); return FGB_BAD_ARG; }
+  if (op.tile_rows != fgb::kTileRows) {
+    fgb::set_error("fgb_matmat_f32_f64 needs the 64-row panel");
+    return FGB_BAD_ARG;
+  }
+  cudaStream_t s = fgb::as_stream(stream);
+  const long long kb = (K + fgb::kB64Cols - 1) / fgb::kB64Cols;
+  if (op.num_items > 0) {
+    if (zero_z && d->num_zrows > 0)
+      FGB_CUDA_TRY(cudaMemsetAsync(Z, 0, sizeof(double) * d->num_zrows * (size_t)K, s));
+    fgb::phaseA_kn_w32d<<<(unsigned)(op.num_work * kb), 256, 0, s>>>(op, vpanel, X, K, Z, K, K);
+    FGB_LAUNCH_CHECK("phaseA_kn_w32d");
+  }
+  if (op.num_tiles > 0) {
+    fgb::phaseB_kn_w32d<<<(unsigned)(op.num_tiles * kb), 256, 0, s>>>(op, panel, X, K, Z, K, Y, K,
+                                                                       K, add, K, alpha);
+    FGB_LAUNCH_CHECK("phaseB_kn_w32d");
   }
   return FGB_OK;
 }

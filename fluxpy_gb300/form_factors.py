@@ -105,8 +105,33 @@ def _as_index(x, n):
     return np.asarray(x).astype(np.int64).reshape(-1)
 
 
-def get_form_factor_matrix(shape_model, I=None, J=None, eps=None):
-    """scipy CSR of F[I][:, J] (src/flux/form_factors.py:11-72)."""
+def exact_adjacent_fix(shape_model, I_d, J_d, t: TileCSR) -> int:
+    """Replace the entries of a one-tile device CSR (rows I_d, columns J_d)
+    whose two facets share a vertex by the exact triangle view factor
+    (libfluxgb ``fgb_ff_adjacent_fix_f64``); returns how many changed."""
+    dev = I_d.device
+    if t.data.dtype != torch.float64:
+        raise ValueError("the exact adjacent-facet correction needs an FP64 matrix")
+    V = torch.as_tensor(np.asarray(shape_model.V, np.float64), device=dev)
+    F = torch.as_tensor(np.asarray(shape_model.F, np.int64), device=dev)
+    fixed = torch.zeros(1, dtype=torch.int64, device=dev)
+    flags = torch.zeros(1, dtype=torch.int32, device=dev)
+    _lib.call("fgb_ff_adjacent_fix_f64", _lib.ptr(V), _lib.ptr(F), _lib.ptr(I_d), _lib.ptr(J_d),
+              int(I_d.numel()), _lib.ptr(t.indptr), _lib.ptr(t.indices), _lib.ptr(t.data),
+              _lib.ptr(fixed), _lib.ptr(flags), _lib.stream_handle())
+    if int(flags.item()) & _lib.FLAG_NONFINITE_OUT:
+        raise RuntimeError("non-finite exact view factor")
+    return int(fixed.item())
+
+
+def get_form_factor_matrix(shape_model, I=None, J=None, eps=None, exact_adjacent=False):
+    """scipy CSR of F[I][:, J] (src/flux/form_factors.py:11-72).
+
+    exact_adjacent (an addition): entries whose two facets share a vertex,
+    where the midpoint rule is least accurate, are replaced by the exact
+    view factor of the two triangles (the closed form that the reference
+    offers separately as flux.view_factor.ff_narayanaswamy); FP64 shape
+    models only."""
     n_faces = shape_model.P.shape[0]
     if shape_model.dtype not in _SFX:
         raise RuntimeError(f'unsupported dtype {shape_model.dtype}')
@@ -119,6 +144,8 @@ def get_form_factor_matrix(shape_model, I=None, J=None, eps=None):
     I_d = torch.as_tensor(I, device=dev)
     J_d = torch.as_tensor(J, device=dev)
     t = ff_tiles(shape_model, I_d, J_d, [0], [m], [0], [n], eps)
+    if exact_adjacent:
+        exact_adjacent_fix(shape_model, I_d, J_d, t)
     data = t.data.cpu().numpy()
     indices = t.indices.cpu().numpy()
     indptr = t.indptr.cpu().numpy()

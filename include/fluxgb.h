@@ -338,6 +338,31 @@ int fgb_recompress_f32(const float* pool_in, const long long* off_in, const int*
                        long long pool_capacity, unsigned long long* pool_used, int* rank_out,
                        long long* off_out, int* queue, unsigned* flags, void* stream);
 
+/* ------------------------------------- exact triangle view factor (f4) */
+/*
+ * View factor of triangle tri1[q] towards tri2[q] for q < n (each 3 x 3
+ * FP64, one vertex per row), the closed form of Narayanaswamy (2015) for two
+ * mutually visible planar triangles.  Replaces
+ *   double ff_narayanaswamy_impl(double const tri1[3][3], double const tri2[3][3])
+ * (src/flux/view_factor/view_factor.h:3, view_factor_narayanaswamy.c:338),
+ * bound as flux.view_factor.ff_narayanaswamy (view_factor.pyx:5-7).  A
+ * non-finite result sets FGB_FLAG_NONFINITE_OUT (the reference asserts).
+ */
+int fgb_ff_triangles_f64(const double* tri1, const double* tri2, long long n, double* out,
+                         unsigned* flags, void* stream);
+/*
+ * Near-field correction of a form-factor CSR (an addition; the reference
+ * keeps the midpoint rule of form_factors.py:62-64 for every pair): row r
+ * is facet rows[r], entry e of it is facet cols[indices[e]] (indptr int64,
+ * indices int32); entries whose two facets share a vertex (V: vertices x 3
+ * FP64, F: faces x 3 int64) are replaced by the exact view factor.  The
+ * number of replaced entries is added to *fixed.
+ */
+int fgb_ff_adjacent_fix_f64(const double* V, const long long* F, const long long* rows,
+                            const long long* cols, long long nrows, const long long* indptr,
+                            const int* indices, double* data, unsigned long long* fixed,
+                            unsigned* flags, void* stream);
+
 /* ----------------------------------------------- block matvec (a9) */
 /*
  * Flat description of a compressed operator in cluster order (device
@@ -427,6 +452,11 @@ int fgb_rmatvec_f32_f64(const struct fgb_op_desc* d, const float* panel, const f
 int fgb_matmat_f32(const struct fgb_op_desc* d, const float* panel, const float* vpanel,
                    const float* X, float* Z, float* Y, int K, const float* add, float alpha,
                    int zero_z, int phases, void* stream);
+/* ... the FP32-stored operator (64-row panel) in FP64 arithmetic: X, Z, Y,
+ * add FP64 (FP64 residuals of K columns; both phases). */
+int fgb_matmat_f32_f64(const struct fgb_op_desc* d, const float* panel, const float* vpanel,
+                       const double* X, double* Z, double* Y, int K, const double* add,
+                       double alpha, int zero_z, void* stream);
 /* ... and BF16 tensor cores with FP32 accumulation (X, panels bf16, K % 8 == 0;
  * Zb: num_zrows x K bf16 scratch). */
 int fgb_matmat_bf16(const struct fgb_op_desc* d, const void* panel, const void* vpanel,

@@ -26,3 +26,19 @@ def ref_pcc_lib() -> C.CDLL | None:
             return None
         _libs["ref_pcc"] = C.CDLL(str(path))
     return _libs["ref_pcc"]
+
+
+def ref_vf_lib() -> C.CDLL | None:
+    """The reference's exact triangle-triangle view factor compiled as-is
+    (ff_narayanaswamy_impl), or None when the reference tree is not
+    available."""
+    if "ref_vf" not in _libs:
+        if not _build.REF_VF_LIB.exists():
+            _build.build_ref()
+        if not _build.REF_VF_LIB.exists():
+            return None
+        lib = C.CDLL(str(_build.REF_VF_LIB))
+        lib.ff_narayanaswamy_impl.restype = C.c_double
+        lib.ff_narayanaswamy_impl.argtypes = [C.c_void_p, C.c_void_p]
+        _libs["ref_vf"] = lib
+    return _libs["ref_vf"]

@@ -2,7 +2,9 @@
 
 * ``oracle/liboracle.so``: the C restatements in ``oracle/*.c``.
 * ``oracle/_ref/libpcc_ref.so``: the reference's own conduction sources
-  (``src/flux/pcc/{conductionQ,conductionT,tridag}.c``) compiled directly
+  (``src/flux/pcc/{conductionQ,conductionT,tridag}.c``) and
+  ``oracle/_ref/libvf_ref.so``: its exact triangle-triangle view factor
+  (``src/flux/view_factor/view_factor_narayanaswamy.c``), compiled directly
   with gcc from where they lie in the reference tree, when that tree is
   present (it is not on GPU machines, which then use ``liboracle.so``).
   The tree is ``$FLUXPY_REFERENCE``; unset, this recipe looks at the
@@ -33,6 +35,8 @@ def reference_root() -> Path | None:
         return Path(env)
     return _CHECKOUT if _CHECKOUT.is_dir() else None
 REF_PCC_SOURCES = ["conductionQ.c", "conductionT.c", "tridag.c"]
+REF_VF_LIB = REF_DIR / "libvf_ref.so"
+REF_VF_SOURCES = ["view_factor_narayanaswamy.c"]
 
 CFLAGS = ["-O2", "-fPIC", "-shared", "-std=gnu11", "-ffp-contract=off", "-fno-fast-math"]
 
@@ -73,6 +77,10 @@ def build_ref() -> Path | None:
     REF_DIR.mkdir(exist_ok=True)
     if _newer(REF_PCC_LIB, srcs):
         _cc(srcs, REF_PCC_LIB, extra=["-I", str(pcc)])
+    vf = root / "src" / "flux" / "view_factor"
+    vsrcs = [vf / s for s in REF_VF_SOURCES]
+    if all(s.exists() for s in vsrcs) and _newer(REF_VF_LIB, vsrcs):
+        _cc(vsrcs, REF_VF_LIB, extra=["-I", str(vf)])
     return REF_PCC_LIB
 
 

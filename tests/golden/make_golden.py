@@ -18,6 +18,11 @@ Sections:
            get_blocks_at_depth, get_row_inds_at_depth, get_row_blocks,
            get_col_inds_for_row, depth, nbytes) on the stretched octree
            sphere and the quadtree crater at depths 1-3, into tree.npz.
+  vf       triangle pairs and the reference's exact view factor between
+           them (src/flux/view_factor/view_factor_narayanaswamy.c, compiled
+           under oracle/_ref by oracle/build.py): separated, edge- and
+           vertex-sharing (from a terrain mesh) and parallel-edge pairs,
+           into viewfactor.npz.
   ffref    form-factor matrices and steady-state solves computed by the
            reference's Python code (src/flux/form_factors.py,
            compressed_form_factors.py, solve.py, model.py), imported from the
@@ -243,7 +248,54 @@ def make_tree():
     print("tree:", len(out), "arrays")
 
 
-SECTIONS = {"pcc": make_pcc, "spheres": make_spheres, "ffref": make_ffref, "tree": make_tree}
+def make_vf():
+    """The reference's exact triangle-triangle view factors."""
+    sys.path.insert(0, str(HERE.parent.parent))
+    from oracle import viewfactor as ovf
+    from fluxpy_gb300 import terrain
+    if ovf.ff_ref(np.eye(3), np.eye(3) + 1) is None:
+        sys.exit("make_golden.py vf: build oracle/_ref first (python oracle/build.py)")
+    rng = np.random.default_rng(11)
+    T1, T2 = [], []
+    # separated pairs: a triangle near z = 0 facing up, one near z = 1 facing down
+    for _ in range(150):
+        a = rng.uniform(-0.5, 0.5, (3, 3)) * [1, 1, 0.1]
+        b = rng.uniform(-0.5, 0.5, (3, 3)) * [1, 1, 0.1] + [rng.uniform(-1, 1), 0, 1]
+        if np.cross(a[1] - a[0], a[2] - a[0])[2] < 0:
+            a = a[[0, 2, 1]]
+        if np.cross(b[1] - b[0], b[2] - b[0])[2] > 0:
+            b = b[[0, 2, 1]]
+        T1.append(a)
+        T2.append(b)
+    # facets of a terrain that share an edge or a vertex
+    V, F = terrain.fbm_terrain(n=12, seed=7, n_craters=1)
+    shared = []
+    for i in range(F.shape[0]):
+        for j in range(F.shape[0]):
+            k = np.intersect1d(F[i], F[j]).size
+            if i != j and k in (1, 2):
+                shared.append((i, j, k))
+    pick = rng.choice(len(shared), 200, replace=False)
+    for q in pick:
+        i, j, _ = shared[q]
+        T1.append(V[F[i]])
+        T2.append(V[F[j]])
+    # parallel edges: a triangle and a translated copy
+    for _ in range(50):
+        a = rng.uniform(-0.5, 0.5, (3, 3))
+        T1.append(a)
+        T2.append(a + rng.uniform(-1, 1, 3) + [0, 0, 2])
+    T1 = np.array(T1, np.float64)
+    T2 = np.array(T2, np.float64)
+    Fv = np.array([ovf.ff_ref(a, b) for a, b in zip(T1, T2)])
+    kind = np.array(["separated"] * 150 + ["shared_" + str(shared[q][2]) for q in pick] +
+                    ["parallel"] * 50)
+    np.savez_compressed(HERE / "viewfactor.npz", T1=T1, T2=T2, F=Fv, kind=kind)
+    print("vf:", T1.shape, float(Fv.min()), float(Fv.max()))
+
+
+SECTIONS = {"pcc": make_pcc, "spheres": make_spheres, "ffref": make_ffref, "tree": make_tree,
+            "vf": make_vf}
 
 if __name__ == "__main__":
     todo = sys.argv[1:] or list(SECTIONS)

@@ -15,6 +15,8 @@ from fluxpy_gb300.thermal import setgrid
 
 
 class _DenseOps:
+    batched = False   # plain Jacobi solves (no refinement)
+
     def __init__(self, Ad):
         self.M = torch.as_tensor(Ad)
         self.N = Ad.shape[0]

@@ -216,12 +216,104 @@ def test_thermal_misfit_gradient_matches_oracle_and_fd(op64):
     # the same gradient through torch.autograd, and with a sparse operator
     t = {k: _d(v).requires_grad_() for k, v in par.items()}
     G.thermal_misfit(m, t["rho"], t["emiss"], t["ti"]).backward()
-    # (F^T sums use FP64 atomics: equal to the last few bits)
-    assert torch.allclose(t["rho"].grad, grho, rtol=1e-12, atol=0)
-    assert torch.allclose(t["ti"].grad, gti, rtol=1e-12, atol=0)
+    # (the transposed operator's products are deterministic: bit-identical)
+    assert torch.equal(t["rho"].grad, grho)
+    assert torch.equal(t["ti"].grad, gti)
     ms = G.ThermalMisfit(scipy.sparse.csr_matrix(Ad), case["E"], case["z"], case["rhoc"],
                          case["dt"], case["T0"], case["Fgeotherm"], case["Tobs"],
                          checkpoint_every=25, tol=1e-14)
     Ls, grho_s, gem_s, gti_s = ms.value_and_grad(par["rho"], par["emiss"], par["ti"])
     assert abs(Ls.item() - Lo) / Lo < 1e-11
     assert np.abs(gem_s.cpu().numpy() - gem_o).max() / np.abs(gem_o).max() < 1e-9
+
+
+@pytest.fixture(scope="module")
+def op32():
+    V, F = terrain.fbm_terrain(n=32, seed=4, n_craters=2)
+    sm = gshape.EmbreeTrimeshShapeModel(V, F)
+    FF = CompressedFormFactorMatrix(sm, tol=1e-5, min_size=1024, dtype=np.float32,
+                                    RootBlock=FormFactorOctreeBlock)
+    N = sm.num_faces
+    # the stored operator in cluster order, FP64 arithmetic, column by column
+    eye = torch.eye(N, dtype=torch.float64, device="cuda")
+    D = torch.stack([FF.matvec_permuted(eye[:, c].contiguous(), "fp32-fp64") for c in range(N)], 1)
+    return sm, FF, D
+
+
+def test_transposed_operator_products(op32):
+    """F^T through the transposed copy of the operator, K columns at once,
+    in every precision, against the transpose of the stored operator."""
+    sm, FF, D = op32
+    N = sm.num_faces
+    T = FF.transposed()
+    assert T is FF.transposed()                       # cached
+    rng = np.random.default_rng(5)
+    Y = _d(rng.uniform(-1, 1, (N, 40)))
+    ref = D.T @ Y
+    scale = ref.abs().max().item()
+    got64 = T.matmat_permuted(Y, "fp32-fp64")
+    assert (got64 - ref).abs().max().item() <= 1e-13 * scale
+    # K = 1 products of the transpose are the same columns
+    assert torch.allclose(FF.rmatvec_permuted(Y[:, 3].contiguous()), got64[:, 3], rtol=0,
+                          atol=1e-14 * scale)
+    got32 = T.matmat_permuted(Y.float(), "fp32").double()
+    assert (got32 - ref).abs().max().item() <= 1e-5 * scale
+    got16 = T.matmat_permuted(Y.float(), "bf16").double()
+    assert (got16 - ref).abs().max().item() <= 3e-2 * scale
+    # the forward K-column FP64-arithmetic product agrees with the dense one too
+    fwd = FF.matmat_permuted(Y, "fp32-fp64")
+    assert (fwd - D @ Y).abs().max().item() <= 1e-13 * (D @ Y).abs().max().item()
+
+
+def test_refined_solves_match_dense(op32):
+    """Many columns solved by FP32 sweeps with FP64 residuals (the
+    adjoint's forward and transposed solves) against dense FP64 solves."""
+    sm, FF, D = op32
+    N = sm.num_faces
+    ops = G._ops(FF, torch.device("cuda"))
+    assert ops.batched
+    rng = np.random.default_rng(6)
+    E = _d(rng.uniform(0, 1000, (N, 24)))
+    rho = _d(rng.uniform(0.07, 0.2, N))
+    B = G.solve_right(ops, E, rho, tol=1e-13)
+    lam = G.solve_right_T(ops, E, rho, tol=1e-13)
+    perm = FF._perm_d
+    Ep = E[perm]
+    rp = rho[perm]
+    I = torch.eye(N, dtype=torch.float64, device="cuda")
+    Bd = torch.linalg.solve(I - D * rp[None, :], Ep)
+    Ld = torch.linalg.solve(I - rp[:, None] * D.T, Ep)
+    assert (B[perm] - Bd).abs().max().item() <= 1e-11 * Bd.abs().max().item()
+    assert (lam[perm] - Ld).abs().max().item() <= 1e-11 * Ld.abs().max().item()
+
+
+def test_gradient_at_10k_facets_matches_dense_fp64_oracle():
+    """The coupled misfit's gradient on a 9,800-facet fBm terrain against
+    the oracle's dense FP64 gradient: through the exact form factors (the
+    adjoint's own accuracy) and through the compressed FP32-stored operator
+    with refined many-column solves (the compression's share)."""
+    from fluxpy_gb300.form_factors import get_form_factor_matrix
+    V, F = terrain.fbm_terrain(n=71, seed=4)
+    sm = gshape.EmbreeTrimeshShapeModel(V, F)
+    assert 9000 < sm.num_faces < 11000
+    Fx = get_form_factor_matrix(sm)
+    case, par = _misfit_case(sm, S=6, seed=9)
+    Lo, grho_o, gem_o, gti_o = A.coupled_gradient(Fx.toarray(), case["E"], par["rho"],
+                                                  par["emiss"], par["ti"], case["z"], case["rhoc"],
+                                                  case["dt"], case["T0"], case["Fgeotherm"],
+                                                  case["Tobs"])
+    args = (case["E"], case["z"], case["rhoc"], case["dt"], case["T0"], case["Fgeotherm"],
+            case["Tobs"])
+    m = G.ThermalMisfit(Fx, *args, checkpoint_every=4, tol=1e-14)
+    L, grho, gem, gti = m.value_and_grad(par["rho"], par["emiss"], par["ti"])
+    assert abs(L.item() - Lo) / Lo < 1e-11
+    for g, r in ((grho, grho_o), (gem, gem_o), (gti, gti_o)):
+        assert np.abs(g.cpu().numpy() - r).max() / np.abs(r).max() < 1e-9
+    FF = CompressedFormFactorMatrix(sm, tol=1e-5, min_size=4096, dtype=np.float32,
+                                    RootBlock=FormFactorOctreeBlock)
+    mc = G.ThermalMisfit(FF, *args, checkpoint_every=4, tol=1e-13)
+    assert mc.ops.batched
+    Lc, grho_c, gem_c, gti_c = mc.value_and_grad(par["rho"], par["emiss"], par["ti"])
+    assert abs(Lc.item() - Lo) / Lo < 1e-5
+    for g, r in ((grho_c, grho_o), (gem_c, gem_o), (gti_c, gti_o)):
+        assert np.abs(g.cpu().numpy() - r).max() / np.abs(r).max() < 1e-3

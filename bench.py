@@ -58,10 +58,16 @@ def parse():
     p.add_argument("--rhs", type=int, default=1024)
     p.add_argument("--tol", type=float, default=1e-5)
     p.add_argument("--no-extras", action="store_true", help="skip FP32/e2e/error/CPU legs")
-    p.add_argument("--workload", default="terrain", choices=["terrain", "craters64", "adjoint"],
+    p.add_argument("--facets", type=int, default=522242,
+                   help="facets of the conduction workload")
+    p.add_argument("--conduction-spinup", type=int, default=300,
+                   help="spin-up steps of the conduction workload's diurnal regime")
+    p.add_argument("--workload", default="terrain",
+                   choices=["terrain", "craters64", "adjoint", "conduction"],
                    help="terrain: the headline solve (default); craters64: 64 uneven crater "
                         "meshes, coupled time-dependent model; adjoint: misfit gradient of the "
-                        "coupled model on a 200k-facet terrain")
+                        "coupled model on a 200k-facet terrain; conduction: the 1-D "
+                        "conduction step alone (FP32 and FP64, 41 nodes)")
     p.add_argument("--adjoint-steps", type=int, default=500,
                    help="time steps of the adjoint workload")
     p.add_argument("--adjoint-fd-steps", type=int, default=50,
@@ -614,6 +620,117 @@ def adjoint_fd_check(model, E, true, guess, N, steps, nfacets):
     return out
 
 
+def run_conduction(args):
+    """The PCC 1-D conduction step (PccThermalModel1D.step,
+    thermal.pyx:249-261 -> conductionQ.c:10-186) for --facets facets on the
+    41-node grid of the thermal configuration (setgrid(40, 1.0817, 1.0)),
+    FP32 and FP64, timed with CUDA events.  Two regimes:
+      diurnal    the time step of the thermal configuration (a lunar day in
+                 300 steps), absorbed flux A_f max(0, cos(2 pi n / 300 +
+                 phi_f)) per facet, after one day of spin-up: the state a
+                 time-dependent model steps through (few predictor-corrector
+                 redos);
+      cold_start every profile at 250 K and a random flux each step, one
+                 hour steps: most facets redo the linearisation several times.
+    Metric: facet-steps/s (diurnal, FP32); roofline: the algorithmic bytes
+    (profile read + write, Qprev, X, emiss, Fgeotherm, Fsurf) against the
+    measured HBM bandwidth."""
+    import torch
+    from fluxpy_gb300 import _lib
+    from fluxpy_gb300.thermal import PccThermalModel1D, setgrid
+    nf = args.facets
+    z = np.concatenate([[0.0], setgrid(40, 1.0817, 1.0)])
+    rng = np.random.default_rng(3)
+    ti = np.linspace(55.0, 400.0, z.size)
+    rhoc = np.full(z.size, 1.2e6)
+    hbm = _measured_hbm()
+    dev = torch.device("cuda")
+    steps = max(args.steps, 20)
+    day = 300
+    amp = rng.uniform(0, 1000, nf)
+    phase = rng.uniform(0, 2 * np.pi, nf)
+
+    def forcing(n, tdt):
+        x = amp * np.maximum(0.0, np.cos(2 * np.pi * n / day + phase))
+        return torch.as_tensor(x, device=dev, dtype=tdt)
+
+    def timed(dt, regime):
+        tdt = torch.float64 if dt == np.float64 else torch.float32
+        if regime == "diurnal":
+            m = PccThermalModel1D(z, np.full((nf, z.size), 250.0), ti, rhoc, np.full(nf, 0.95),
+                                  np.full(nf, 0.005), forcing(0, tdt).cpu().numpy().astype(np.float64),
+                                  np.full(nf, 250.0), dtype=dt)
+            step_dt = 29.53 * 86400.0 / day
+            spin = args.conduction_spinup
+            xs = [forcing(n, tdt) for n in range(1, spin + steps + 1)]
+            for n in range(spin):
+                m.step(step_dt, xs[n], check=False)
+            run = xs[spin:]
+        else:
+            m = PccThermalModel1D(z, np.full((nf, z.size), 250.0), ti, rhoc, np.full(nf, 0.95),
+                                  np.full(nf, 0.005), rng.uniform(0, 400, nf), np.full(nf, 250.0),
+                                  dtype=dt)
+            step_dt = 3600.0
+            run = [torch.as_tensor(rng.uniform(0, 400, nf), device=dev, dtype=tdt)
+                   for _ in range(steps + 3)]
+            for n in range(3):
+                m.step(step_dt, run[n], check=False)
+            run = run[3:]
+        torch.cuda.synchronize()
+        s = torch.cuda.current_stream()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0 = _lib.launch_count()
+        a.record(s)
+        for x in run:
+            m.step(step_dt, x, check=False)
+        b.record(s)
+        torch.cuda.synchronize()
+        m.check_errors()
+        ms = a.elapsed_time(b) / len(run)
+        isz = np.dtype(dt).itemsize
+        per = 2 * z.size * isz + 5 * isz
+        gbs = nf * per / (ms * 1e-3) / 1e9
+        del m
+        return {"facet_steps_per_s": nf / (ms * 1e-3), "ms_per_step": ms,
+                "bytes_per_facet_step": per, "achieved_gbs": gbs, "frac": gbs / hbm,
+                "launches": int(_lib.launch_count() - l0), "steps": len(run)}
+
+    clocks = ClockSampler(0)
+    clocks.start()
+    out = {f"{name}_{regime}": timed(dt, regime)
+           for regime in ("diurnal", "cold_start")
+           for name, dt in (("fp32", np.float32), ("fp64", np.float64))}
+    clk = clocks.stop()
+    from oracle import pcc as opcc
+    ns = 4096
+    Ts = np.full((ns, z.size), 250.0)
+    Q = rng.uniform(0, 400, ns)
+    t0 = time.perf_counter()
+    reps = 0
+    while time.perf_counter() - t0 < 3.0:
+        opcc.step_q(z, 3600.0, Q, Q, Ts, ti, rhoc, np.full(ns, 0.95), np.full(ns, 0.005))
+        reps += 1
+    cpu = ns * reps / (time.perf_counter() - t0)
+    f32 = out["fp32_diurnal"]
+    line = {"metric": "conduction facet-steps/s (41 nodes)", "value": f32["facet_steps_per_s"],
+            "unit": "facet-steps/s", "n_gpus": 1, "steps": f32["steps"],
+            "warmup": args.conduction_spinup,
+            "ms_per_step": f32["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
+            "config": {"workload": f"PCC conduction step, {nf} facets, 41-node grid "
+                                   "(2 mm - 1 m), ti 55-400, diurnal forcing, 300 steps per "
+                                   f"lunar day after {args.conduction_spinup} spin-up steps",
+                       "facets": nf,
+                       "l2": "profiles larger than L2 at the default size; no flush"},
+            "clocks": clk, "gpu_launches": f32["launches"],
+            "roofline": {"bound": "hbm", "achieved": f32["achieved_gbs"], "peak": hbm,
+                         "unit": "GB/s", "frac": f32["frac"], "traffic": None},
+            "regimes": out,
+            "cpu_baseline": {"value": cpu, "unit": "facet-steps/s", "cores": 1, "kind": "port",
+                             "sample": f"oracle conductionQ (C), {ns} facets x {reps} steps"}}
+    print(json.dumps(line))
+
+
 def _measured_hbm():
     try:
         return float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"])
@@ -632,6 +749,9 @@ def main():
         return
     if args.workload == "adjoint":
         run_adjoint(args)
+        return
+    if args.workload == "conduction":
+        run_conduction(args)
         return
     # the operator and the solver's buffers take most of the device: let the
     # caching allocator grow segments instead of fragmenting

@@ -11,12 +11,13 @@
 //   * the temperature rows (num_faces x (nz+1), the reference's row-major
 //     layout) are staged through shared memory with coalesced loads/stores;
 //     the sweep reads the pre-step profile from there;
-//   * the sweep's own arrays (u and gam, nz + 1 each) never touch local
-//     memory: for FP32 grids of up to 48 nodes (the thermal configurations
-//     use 41) they are registers (loops fully unrolled over the node count,
-//     guarded by the run-time nz); otherwise they are per-thread columns in
-//     shared memory (element j of thread t at j * nt + t, conflict-free);
-//     the facets per CTA (32..128) follow from nz and that layout;
+//   * the sweep's own arrays never touch local memory: the solution u is
+//     written in place into the staged row (the right-hand side has read
+//     each pre-step value before), and gam, the elimination factors, is a
+//     per-thread column of shared memory (element j of thread t at
+//     j * nt + t, conflict-free); a predictor-corrector redo reloads the
+//     pre-step row from T_in, which no CTA overwrites before its own
+//     rows are done; the facets per CTA (32..128) follow from nz;
 //   * the linearised radiative boundary (predictor-corrector, at most 10
 //     redos, conductionQ.c:103-172) and the Thomas solve are fused: the
 //     right-hand side is formed on the fly during the forward sweep from the
@@ -26,10 +27,17 @@
 //     touching T (thermal.pyx:240-247).
 #include "common.cuh"
 
-#include <type_traits>
-
 namespace fgb {
 namespace {
+
+// What the forward sweep reads for row j, packed so that a thread fetches it
+// with two or three 16-byte shared loads: gamma_j, alpha_j,
+// mid_j = 1 - alpha_j - gamma_j (the explicit half's diagonal, evaluated as
+// in conductionQ.c), a_j, b_j and c_{j-1}.
+template <class R>
+struct alignas(16) Layer {
+  R ga, al, mid, a, b, cm1;
+};
 
 template <class R> struct Consts;
 template <> struct Consts<double> { static constexpr double sigSB = 5.6704e-8; };
@@ -107,28 +115,42 @@ constexpr size_t kSmemBudget = 227 * 1024;  // the per-CTA opt-in maximum
 // that many CTAs (warps) share an SM and hide the sweep's dependent chain.
 __host__ __device__ inline int tile_stride(int nz) { return (nz + 1) | 1; }
 
-// ncols: per-thread columns of the sweep after the tile (2 (nz + 1) for
-// SmemStore, 0 for RegStore).
+// Shared layout: the coefficients, the tile (nt rows of stride ws), the
+// threads' gam columns (nz + 1 rows of nt), then the packed layer table
+// (nz + 1 entries, 16-byte aligned).
 template <class R>
-size_t cond_smem(int nz, int nt, int ncols) {
-  return sizeof(R) * ((size_t)7 * (nz + 1) + (size_t)nt * (tile_stride(nz) + ncols));
+__host__ __device__ inline size_t cond_smem_scalars(int nz, int nt) {
+  return (size_t)7 * (nz + 1) + (size_t)nt * (tile_stride(nz) + nz + 1);
 }
 
-// Facets per CTA: the largest multiple of 32 (at most 128) whose shared
-// layout fits the budget; 0 if even one warp does not fit.
 template <class R>
-int cond_threads(int nz, int ncols) {
-  for (int nt = kMaxThreads; nt >= 32; nt -= 32)
-    if (cond_smem<R>(nz, nt, ncols) <= kSmemBudget) return nt;
-  return 0;
+size_t cond_smem(int nz, int nt) {
+  const size_t bytes = sizeof(R) * cond_smem_scalars<R>(nz, nt);
+  return (bytes + 15) / 16 * 16 + sizeof(Layer<R>) * (size_t)(nz + 1);
 }
 
-// Register storage holds the sweep of FP32 grids with nz <= kRegNz.
-constexpr int kRegNz = 47;
-template <class R, int NZMAX>
-constexpr bool use_regs() { return sizeof(R) == 4 && NZMAX <= kRegNz; }
-template <class R, int NZMAX>
-int sweep_cols(int nz) { return use_regs<R, NZMAX>() ? 0 : 2 * (nz + 1); }
+template <class R>
+__device__ Layer<R>* layers_at(R* sh, int nz, int nt) {
+  const size_t bytes = sizeof(R) * cond_smem_scalars<R>(nz, nt);
+  return reinterpret_cast<Layer<R>*>(reinterpret_cast<unsigned char*>(sh) +
+                                     (bytes + 15) / 16 * 16);
+}
+
+// Facets per CTA: the multiple of 32 (at most 128) that keeps the most
+// facets resident per SM (228 KiB of shared memory, 1 KiB of it reserved
+// per CTA), the larger on ties; 0 if even one warp does not fit.
+template <class R>
+int cond_threads(int nz) {
+  int best = 0, best_res = 0;
+  for (int nt = 32; nt <= kMaxThreads; nt += 32) {
+    const size_t sm = cond_smem<R>(nz, nt);
+    if (sm > kSmemBudget) break;
+    const int ctas = (int)((228 * 1024) / (sm + 1024));
+    const int res = nt * (ctas < 2048 / nt ? ctas : 2048 / nt);
+    if (res >= best_res) { best_res = res; best = nt; }
+  }
+  return best;
+}
 
 template <class R>
 __device__ inline R* coeff(R* sh, int which, int nz) { return sh + which * (nz + 1); }
@@ -158,7 +180,7 @@ template <class R>
 __device__ inline bool finite_val(R x) { return isfinite(x); }
 
 // x / d. FP64 keeps the IEEE quotient of the reference's C code (results
-// bit-identical to it); FP32 multiplies by one correctly rounded reciprocal
+// bit-identical to it); FP32 multiplies by one fast approximate reciprocal
 // of the pivot per layer (the FP32 kernel is a faster, less exact variant).
 template <class R> struct Pivot;
 template <> struct Pivot<double> {
@@ -168,99 +190,68 @@ template <> struct Pivot<double> {
 };
 template <> struct Pivot<float> {
   float r;
-  __device__ explicit Pivot(float v) { r = __frcp_rn(v); }
+  __device__ explicit Pivot(float v) { r = __fdividef(1.0f, v); }
   __device__ float div(float x) const { return x * r; }
 };
 
-// Storage of the sweep's arrays u and gam.  RegStore: register arrays
-// indexed only by constants (the sweep loops are fully unrolled to NZMAX
-// and guarded by nz).  SmemStore: per-thread columns in shared memory.
-template <class R, int NZMAX>
-struct RegStore {
-  static constexpr bool kUnrolled = true;
-  R u_[NZMAX + 1];
-  R g_[NZMAX + 1];
-  __device__ R& u(int j) { return u_[j]; }
-  __device__ R& gam(int j) { return g_[j]; }
-};
-
-template <class R, int NZMAX>
-struct SmemStore {
-  static constexpr bool kUnrolled = false;
-  R* base;   // u column at base, gam column at base + goff
-  int nt;    // column stride (threads per CTA)
-  int goff;  // (nz + 1) * nt
-  __device__ R& u(int j) { return base[j * nt]; }
-  __device__ R& gam(int j) { return base[goff + j * nt]; }
-};
+template <class R>
+__device__ void pack_layers(int nz, const R* s_alpha, const R* s_gamma, const R* s_a,
+                            const R* s_b, const R* s_c, Layer<R>* L) {
+  for (int j = threadIdx.x + 2; j <= nz; j += blockDim.x) {
+    const R al = j < nz ? s_alpha[j] : R(0), ga = s_gamma[j];
+    L[j] = {ga, al, R(1) - al - ga, s_a[j], s_b[j], s_c[j - 1]};
+  }
+}
 
 // Forward sweep and back substitution of the tridiagonal system with
 // sub/main/super diagonals (a, b, c) from shared memory, except the first
 // main-diagonal entry b1 (facet dependent under the radiative boundary).
-// The right-hand side is formed on the fly from the pre-step profile Trow
-// (crank-nicolson explicit half, conductionQ.c:123-137 / conductionT.c:66-77).
+// The right-hand side is formed on the fly from the pre-step profile in
+// Trow (crank-nicolson explicit half, conductionQ.c:123-137 /
+// conductionT.c:66-77), r1 precomputed by the caller; the solution
+// overwrites Trow[1..nz] (each pre-step value is read before it is
+// overwritten).  gam: the thread's shared column (element j at gam[j * gs]).
 // The arithmetic is the reference's tridag (tridag.c:5-34) in its order.
 // Returns false on a zero pivot.
-template <class R, int NZMAX, class Store>
-__device__ bool thomas_cn(int nz, const R* Trow, R r1, R b1, R rhs_bottom,
-                          const R* s_alpha, const R* s_gamma, const R* s_a, const R* s_b,
-                          const R* s_c, Store& st) {
+template <class R>
+__device__ bool thomas_cn(int nz, R* Trow, R r1, R b1, R rhs_bottom, const Layer<R>* L, R* gam,
+                          int gs) {
   R bet = b1;
   if (bet == R(0)) return false;
   Pivot<R> pv(bet);
-  R uprev = pv.div(r1);
-  st.u(1) = uprev;
   R tm1 = Trow[1], t0 = Trow[2];
-  bool ok = true;
-  // forward sweep, row j (2 <= j <= nz)
-  auto forward = [&](int j) {
+  R uprev = pv.div(r1);
+  Trow[1] = uprev;
+  for (int j = 2; j <= nz; j++) {
+    const Layer<R> l = L[j];
     R rj;
     if (j < nz) {
       const R tp1 = Trow[j + 1];
-      const R ga = s_gamma[j], al = s_alpha[j];
-      rj = ga * tm1 + (R(1) - al - ga) * t0 + al * tp1;
+      rj = l.ga * tm1 + l.mid * t0 + l.al * tp1;
       tm1 = t0;
       t0 = tp1;
     } else {
-      const R ga = s_gamma[nz];
-      rj = ga * tm1 + (R(1) - ga) * t0 + rhs_bottom;
+      rj = l.ga * tm1 + l.mid * t0 + rhs_bottom;
     }
-    const R aj = s_a[j];
-    const R g = pv.div(s_c[j - 1]);
-    st.gam(j) = g;
-    bet = s_b[j] - aj * g;
-    if (bet == R(0)) { ok = false; return; }
+    const R g = pv.div(l.cm1);
+    gam[j * gs] = g;
+    bet = l.b - l.a * g;
+    if (bet == R(0)) return false;
     pv = Pivot<R>(bet);
-    uprev = pv.div(rj - aj * uprev);
-    st.u(j) = uprev;
-  };
+    uprev = pv.div(rj - l.a * uprev);
+    Trow[j] = uprev;
+  }
   R unext = uprev;
-  // back substitution, row j (nz - 1 >= j >= 1)
-  auto backward = [&](int j) {
-    unext = st.u(j) - st.gam(j + 1) * unext;
-    st.u(j) = unext;
-  };
-  if constexpr (Store::kUnrolled) {
-#pragma unroll
-    for (int j = 2; j <= NZMAX; j++)
-      if (j <= nz && ok) forward(j);
-    if (!ok) return false;
-    unext = uprev;
-#pragma unroll
-    for (int j = NZMAX - 1; j >= 1; j--)
-      if (j <= nz - 1) backward(j);
-  } else {
-    for (int j = 2; j <= nz && ok; j++) forward(j);
-    if (!ok) return false;
-    unext = uprev;
-    for (int j = nz - 1; j >= 1; j--) backward(j);
+  for (int j = nz - 1; j >= 1; j--) {
+    unext = Trow[j] - gam[(j + 1) * gs] * unext;
+    Trow[j] = unext;
   }
   return true;
 }
 
 // One step of the radiative-flux boundary problem for every facet.
-template <class R, int NZMAX, bool REG>
-__global__ void __launch_bounds__(kMaxThreads, 3)
+template <class R, int NZMAX>
+__global__ void __launch_bounds__(kMaxThreads, 1)
 conduction_q_kernel(int num_faces, int nz, const R* __restrict__ z, R dt,
                     const R* __restrict__ Qn, const R* __restrict__ Qnp1,
                     const R* T_in, R* T_out,
@@ -279,21 +270,18 @@ conduction_q_kernel(int num_faces, int nz, const R* __restrict__ z, R dt,
   R* s_misc = coeff(sh, 6, nz);  // [0] = k1
   R* tile = sh + 7 * w;
 
+  Layer<R>* s_L = layers_at(sh, nz, nt);
   grid_coeffs_q<R>(nz, z, dt, ti, rhoc, s_k, s_alpha, s_gamma, s_a, s_b, s_c, &s_misc[0]);
+  __syncthreads();
+  pack_layers<R>(nz, s_alpha, s_gamma, s_a, s_b, s_c, s_L);
   const long long f0 = (long long)blockIdx.x * nt;
   const int rows = (int)min((long long)nt, (long long)num_faces - f0);
   stage<R, true>(tile, const_cast<R*>(T_in), f0, rows, w, ws);
   __syncthreads();
 
   const int t = threadIdx.x;
+  R* gam = tile + nt * ws + t;   // this thread's column, stride nt
   unsigned my_flags = 0;
-  using Store = typename std::conditional<REG, RegStore<R, NZMAX>, SmemStore<R, NZMAX>>::type;
-  Store st;
-  if constexpr (!REG) {
-    st.base = tile + nt * ws + t;
-    st.nt = nt;
-    st.goff = w * nt;
-  }
   if (t < rows) {
     const long long f = f0 + t;
     R* Trow = tile + t * ws;
@@ -316,30 +304,24 @@ conduction_q_kernel(int num_faces, int nz, const R* __restrict__ z, R dt,
       R b1 = R(1) + alpha1 + gamma1 - gamma1 * bn;
       R r1 = gamma1 * (annp1 + ann) + (R(1) - alpha1 - gamma1 + gamma1 * bn) * Trow[1] +
              alpha1 * Trow[2];
-      if (!thomas_cn<R, NZMAX>(nz, Trow, r1, b1, rhs_bottom, s_alpha, s_gamma, s_a, s_b, s_c,
-                               st)) {
+      if (!thomas_cn<R>(nz, Trow, r1, b1, rhs_bottom, s_L, gam, nt)) {
         my_flags |= kFlagZeroPivot;
         break;
       }
-      T0 = R(0.5) * (annp1 + bn * st.u(1) + st.u(1));
+      T0 = R(0.5) * (annp1 + bn * Trow[1] + Trow[1]);
       if ((T0 > R(1.2) * Tr || T0 < R(0.8) * Tr) && iter < 10) {
         iter++;
         Tr = sqrt(Tr * T0);
+        // redo from the pre-step profile (conductionQ.c resets T)
+        const R* src = T_in + f * w;
+        for (int i = 1; i <= nz; i++) Trow[i] = src[i];
         continue;
       }
       break;
     }
     if (iter >= 9) my_flags |= kFlagPredCorrMax;
     Trow[0] = T0;
-    const R u1 = st.u(1);
-    if constexpr (REG) {
-#pragma unroll
-      for (int i = 1; i <= NZMAX; i++)
-        if (i <= nz) Trow[i] = st.u(i);
-    } else {
-      for (int i = 1; i <= nz; i++) Trow[i] = st.u(i);
-    }
-    Fsurf[f] = -s_k[1] * (u1 - T0) / z[1];
+    Fsurf[f] = -s_k[1] * (Trow[1] - T0) / z[1];
     for (int i = 0; i <= nz; i++) {
       if (!finite_val(Trow[i])) my_flags |= kFlagNonfiniteOut;
       if (Trow[i] < R(0)) my_flags |= kFlagNegativeOut;
@@ -351,8 +333,8 @@ conduction_q_kernel(int num_faces, int nz, const R* __restrict__ z, R dt,
 }
 
 // One step of the prescribed-surface-temperature problem (conductionT.c).
-template <class R, int NZMAX, bool REG>
-__global__ void __launch_bounds__(kMaxThreads, 3)
+template <class R, int NZMAX>
+__global__ void __launch_bounds__(kMaxThreads)
 conduction_t_kernel(int num_faces, int nz, const R* __restrict__ z, R dt,
                     const R* __restrict__ Tsurf, const R* __restrict__ Tsurfp1,
                     const R* T_in, R* T_out,
@@ -369,20 +351,17 @@ conduction_t_kernel(int num_faces, int nz, const R* __restrict__ z, R dt,
   R* s_b = coeff(sh, 4, nz);
   R* s_c = coeff(sh, 5, nz);
   R* tile = sh + 7 * w;
+  Layer<R>* s_L = layers_at(sh, nz, nt);
   grid_coeffs_t<R>(nz, z, dt, ti, rhoc, s_k, s_alpha, s_gamma, s_a, s_b, s_c);
+  __syncthreads();
+  pack_layers<R>(nz, s_alpha, s_gamma, s_a, s_b, s_c, s_L);
   const long long f0 = (long long)blockIdx.x * nt;
   const int rows = (int)min((long long)nt, (long long)num_faces - f0);
   stage<R, true>(tile, const_cast<R*>(T_in), f0, rows, w, ws);
   __syncthreads();
   const int t = threadIdx.x;
+  R* gam = tile + nt * ws + t;
   unsigned my_flags = 0;
-  using Store = typename std::conditional<REG, RegStore<R, NZMAX>, SmemStore<R, NZMAX>>::type;
-  Store st;
-  if constexpr (!REG) {
-    st.base = tile + nt * ws + t;
-    st.nt = nt;
-    st.goff = w * nt;
-  }
   if (t < rows) {
     const long long f = f0 + t;
     R* Trow = tile + t * ws;
@@ -392,19 +371,13 @@ conduction_t_kernel(int num_faces, int nz, const R* __restrict__ z, R dt,
     const R alpha1 = s_alpha[1], gamma1 = s_gamma[1];
     R r1 = alpha1 * Trow[2] + (R(1) - alpha1 - gamma1) * Trow[1] + gamma1 * (ts + tsp1);
     const R rhs_bottom = dt / rhoc[nz] * fg / (z[nz] - z[nz - 1]);
-    if (!thomas_cn<R, NZMAX>(nz, Trow, r1, s_b[1], rhs_bottom, s_alpha, s_gamma, s_a, s_b, s_c,
-                             st)) {
+    if (!thomas_cn<R>(nz, Trow, r1, s_b[1], rhs_bottom, s_L, gam, nt)) {
       my_flags |= kFlagZeroPivot;
+      // the reference leaves T as it was: put the pre-step row back
+      const R* src = T_in + f * w;
+      for (int i = 1; i <= nz; i++) Trow[i] = src[i];
     } else {
-      const R u1 = st.u(1);
-      if constexpr (REG) {
-#pragma unroll
-        for (int i = 1; i <= NZMAX; i++)
-          if (i <= nz) Trow[i] = st.u(i);
-      } else {
-        for (int i = 1; i <= nz; i++) Trow[i] = st.u(i);
-      }
-      Fsurf[f] = -s_k[1] * (u1 - tsp1) / z[1];
+      Fsurf[f] = -s_k[1] * (Trow[1] - tsp1) / z[1];
     }
     for (int i = 1; i <= nz; i++) {
       if (!finite_val(Trow[i])) my_flags |= kFlagNonfiniteOut;
@@ -420,10 +393,9 @@ template <class R, int NZMAX>
 int launch_q(int num_faces, int nz, const R* z, R dt, const R* Qn, const R* Qnp1,
              const R* T_in, R* T_out, const R* ti, const R* rhoc, const R* emiss,
              const R* Fgeotherm, R* Fsurf, unsigned* flags, cudaStream_t s) {
-  const int cols = sweep_cols<R, NZMAX>(nz);
-  const int nt = cond_threads<R>(nz, cols);
-  const size_t sm = cond_smem<R>(nz, nt, cols);
-  auto k = conduction_q_kernel<R, NZMAX, use_regs<R, NZMAX>()>;
+  const int nt = cond_threads<R>(nz);
+  const size_t sm = cond_smem<R>(nz, nt);
+  auto k = conduction_q_kernel<R, NZMAX>;
   FGB_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   const unsigned grid = (unsigned)((num_faces + nt - 1) / nt);
   k<<<grid, nt, sm, s>>>(num_faces, nz, z, dt, Qn, Qnp1, T_in, T_out, ti, rhoc, emiss,
@@ -436,10 +408,9 @@ template <class R, int NZMAX>
 int launch_t(int num_faces, int nz, const R* z, R dt, const R* Ts, const R* Tsp1,
              const R* T_in, R* T_out, const R* ti, const R* rhoc, const R* Fgeotherm,
              R* Fsurf, unsigned* flags, cudaStream_t s) {
-  const int cols = sweep_cols<R, NZMAX>(nz);
-  const int nt = cond_threads<R>(nz, cols);
-  const size_t sm = cond_smem<R>(nz, nt, cols);
-  auto k = conduction_t_kernel<R, NZMAX, use_regs<R, NZMAX>()>;
+  const int nt = cond_threads<R>(nz);
+  const size_t sm = cond_smem<R>(nz, nt);
+  auto k = conduction_t_kernel<R, NZMAX>;
   FGB_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   const unsigned grid = (unsigned)((num_faces + nt - 1) / nt);
   k<<<grid, nt, sm, s>>>(num_faces, nz, z, dt, Ts, Tsp1, T_in, T_out, ti, rhoc, Fgeotherm,
@@ -452,7 +423,7 @@ template <class R>
 int check_args(int num_faces, int nz) {
   if (num_faces < 0) { set_error("num_faces must be >= 0"); return FGB_BAD_ARG; }
   if (nz < 2 || nz > 255) { set_error("nz (interior layers) must be in [2, 255], got %d", nz); return FGB_BAD_ARG; }
-  if (cond_threads<R>(nz, (sizeof(R) == 4 && nz <= kRegNz) ? 0 : 2 * (nz + 1)) == 0) {
+  if (cond_threads<R>(nz) == 0) {
     set_error("nz too large for the staged tile");
     return FGB_BAD_ARG;
   }

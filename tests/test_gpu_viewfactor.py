@@ -25,12 +25,13 @@ def test_matches_reference_c(golden):
     F = ff_triangles(golden["T1"], golden["T2"])
     ref = golden["F"]
     rel = np.abs(F - ref) / np.abs(ref)
-    # parallel edges: the closed form's terms cancel to a few digits, so the
-    # last bits of two FP64 evaluations in different operation orders differ
-    bound = {"parallel": 1e-6}
+    # the nine edge-pair terms of the closed form are much larger than their
+    # sum (most for parallel edges), so two FP64 evaluations in different
+    # operation orders agree to ~1e-8 relative, not to the last bit
     for kind in np.unique(golden["kind"]):
         sel = golden["kind"] == kind
-        assert rel[sel].max() < bound.get(str(kind), 1e-9), (kind, rel[sel].max())
+        assert rel[sel].max() < 1e-7, (kind, rel[sel].max())
+    assert np.median(rel) < 1e-11
 
 
 def test_drop_in_single_pair(golden):

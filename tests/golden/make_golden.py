@@ -23,6 +23,13 @@ Sections:
            under oracle/_ref by oracle/build.py): separated, edge- and
            vertex-sharing (from a terrain mesh) and parallel-edge pairs,
            into viewfactor.npz.
+  cpuarm   the CPU baseline's 7,938-facet sample (64 x 64 fBm terrain, seed 1)
+           through the reference's own form factors, insolation and Jacobi
+           solves (tolerance 1e-5 max|E|): F's pattern (digest), F x and row
+           sums, E of 8 directions (sums and maxima; 2 in full), their
+           iteration counts and 2 solutions,
+           into cpuarm.npz, with the time per solve of the reference's solve
+           and of the oracle's on this machine.
   ffref    form-factor matrices and steady-state solves computed by the
            reference's Python code (src/flux/form_factors.py,
            compressed_form_factors.py, solve.py, model.py), imported from the
@@ -294,8 +301,62 @@ def make_vf():
     print("vf:", T1.shape, float(Fv.min()), float(Fv.max()))
 
 
+def _digest(*arrays):
+    import hashlib
+    h = hashlib.sha256()
+    for a in arrays:
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+def make_cpuarm():
+    """The CPU baseline's sample computed by the reference's own Python code:
+    its form factors (src/flux/form_factors.py:11-72, oracle visibility in
+    the backend seam), insolation (shape.py:181-244) and Jacobi solves
+    (solve.py:36-45, one direction per solve, stopping at an update of
+    1e-5 max|E|), with the time each solve took here beside the oracle's
+    restatement of the same solve on the same operator."""
+    import time
+    shape, ff, cff, solve, model = import_reference()
+    sys.path.insert(0, str(HERE.parent.parent))
+    from fluxpy_gb300 import terrain
+    from oracle import solve as osolve
+    Shape = oracle_shape_class(shape, 0)
+    V, F = terrain.fbm_terrain(n=64, seed=1, n_craters=4)
+    sm = Shape(V, F)
+    A = ff.get_form_factor_matrix(sm).tocsr()
+    dirs = terrain.random_sun_directions(64, seed=2)
+    cols = list(range(0, 64, 8))
+    E = np.column_stack([sm.get_direct_irradiance(1365.0, dirs[c]) for c in cols])
+    niter, Bs, t_ref, t_orc = [], [], 0.0, 0.0
+    for k in range(len(cols)):
+        e = np.ascontiguousarray(E[:, k])
+        tol = 1e-5 * float(np.abs(e).max())
+        t0 = time.perf_counter()
+        B, it = solve.solve_radiosity(A, e, 0.12, "right", "jacobi", tol=tol)
+        t_ref += time.perf_counter() - t0
+        t0 = time.perf_counter()
+        Bo, ito = osolve.solve_radiosity(A, e, 0.12, tol=tol)
+        t_orc += time.perf_counter() - t0
+        assert ito == it and np.array_equal(Bo, B)
+        niter.append(it)
+        Bs.append(B)
+    # the operator's pattern by digest, its values through a product with a
+    # fixed vector and the row sums; B of three of the directions in full
+    x = np.random.default_rng(0).uniform(0, 1, F.shape[0])
+    out = dict(num_faces=F.shape[0], nnz=A.nnz,
+               pattern_digest=_digest(A.indptr.astype(np.int64), A.indices.astype(np.int64)),
+               x=x, Ax=A @ x, rowsum=np.asarray(A.sum(1)).ravel(), cols=np.array(cols),
+               dirs=dirs, E_sum=E.sum(0), E_max=E.max(0), niter=np.array(niter),
+               full_cols=np.array([0, 7]), E=E[:, [0, 7]], B=np.column_stack([Bs[0], Bs[7]]),
+               seconds_reference=t_ref, seconds_oracle=t_orc)
+    np.savez_compressed(HERE / "cpuarm.npz", **out)
+    print("cpuarm:", F.shape[0], "facets", A.nnz, "nnz, niter", niter,
+          f"reference {t_ref / len(cols) * 1e3:.1f} ms/solve, oracle {t_orc / len(cols) * 1e3:.1f}")
+
+
 SECTIONS = {"pcc": make_pcc, "spheres": make_spheres, "ffref": make_ffref, "tree": make_tree,
-            "vf": make_vf}
+            "vf": make_vf, "cpuarm": make_cpuarm}
 
 if __name__ == "__main__":
     todo = sys.argv[1:] or list(SECTIONS)

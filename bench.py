@@ -58,6 +58,8 @@ def parse():
     p.add_argument("--rhs", type=int, default=1024)
     p.add_argument("--tol", type=float, default=1e-5)
     p.add_argument("--no-extras", action="store_true", help="skip FP32/e2e/error/CPU legs")
+    p.add_argument("--plain-tiles", default="auto", choices=["auto", "64", "128", "256"],
+                   help="phase-B tile rows of the plain BF16 product (auto: autotuned)")
     p.add_argument("--facets", type=int, default=522242,
                    help="facets of the conduction workload")
     p.add_argument("--conduction-spinup", type=int, default=300,
@@ -783,12 +785,16 @@ def main():
     FF.tc_operands(split=True)
     # kernel layouts of the BF16 / split products: timed on this operator
     tune = FF.autotune_products(args.rhs)
+    if args.plain_tiles != "auto":
+        FF.product_plan()["plain"] = "b" + args.plain_tiles
     nf = sm.num_faces
     dirs = replica_directions(terrain, args.rhs, rank)
     E = sm.get_direct_irradiance_batch(F0, dirs, out_dtype=torch.float32)
     Ep = FF.permute(E).contiguous()
     torch.cuda.synchronize()
     setup_s = time.perf_counter() - t_setup
+    # device memory held by the operator, its tensor-core operands and E
+    setup_bytes = int(torch.cuda.memory_allocated())
 
     def step():
         st = {}
@@ -843,13 +849,14 @@ def main():
                    "split_bf16_matmats": stats[-1].get("split_matmats", 0),
                    "fp32_matmats": stats[-1]["fp32_matmats"], "chunks": stats[-1].get("chunks", 1),
                    "residual_checked": stats[-1].get("residual")},
-        "setup_s": setup_s, "build": {k: (round(v, 3) if isinstance(v, float) else v)
+        "setup_s": setup_s, "device_bytes_after_setup": setup_bytes, "build": {k: (round(v, 3) if isinstance(v, float) else v)
                                       for k, v in FF.stats.items() if k != "autotune"},
         "near_edge_pairs": int(FF.stats.get("near_edge_pairs", 0)),
         "near_edge_note": ("visible pairs of the exact leaves whose ray passed within 1e-6 "
                            "(relative) of a triangle edge, decided in FP64 and counted"),
         "operator_entries": int(FF.stats["operator_entries"]),
         "autotune_ms": tune,
+        "product_plan": dict(FF.product_plan()),
     }
     line.update(extras)
     fp = extras.get("fp32_plain")
@@ -882,16 +889,23 @@ def operator_work(FF):
 # executed panel weights times the columns (units of work).  The small case
 # keeps more of its gathered source rows in L2 than the full size does, so
 # the scaled figure is a lower bound.
-TRAFFIC_CAPTURE = {"kernel": "phaseB_tc", "panel_rows_128": None, "columns": None,
-                   "dram_bytes": None, "source": "no capture recorded"}
+TRAFFIC_CAPTURE = {"kernel": "phaseB_tc", "tile_rows": 128, "panel_rows": 2006912,
+                   "columns": 1024, "dram_bytes": 1124346000 + 122825472,
+                   "source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum (1 pass) of one "
+                              "tc_gather_gemm<1, 0, 128> launch on the 128x128 terrain (32,258 "
+                              "facets, 2,006,912 panel rows, 1,024 columns), scaled by panel rows "
+                              "x columns; a lower bound at full size, where fewer gathered "
+                              "sources stay in L2")}
 
 
-def scaled_dram_traffic(kernel, FF, K):
+def scaled_dram_traffic(kernel, FF, K, tile_rows):
+    """The capture's DRAM bytes scaled to this launch (None when the timed
+    kernel or its tile layout is not the one captured)."""
     c = TRAFFIC_CAPTURE
-    if kernel != c["kernel"] or not c["dram_bytes"]:
+    if kernel != c["kernel"] or tile_rows != c["tile_rows"] or not c["dram_bytes"]:
         return None
-    rows = int(FF.stats.get("panel_rows_128", 0))
-    return c["dram_bytes"] * (rows * K) / (c["panel_rows_128"] * c["columns"])
+    rows = int(FF.stats.get(f"panel_rows_{tile_rows}", 0))
+    return c["dram_bytes"] * (rows * K) / (c["panel_rows"] * c["columns"])
 
 
 def fp64_solve_permuted(FF, Ep_cols, tol=1e-13, max_iter=200):
@@ -1082,11 +1096,17 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
                   _lib.ptr(xl) if split else None, _lib.ptr(zh), _lib.ptr(zl) if split else None,
                   K, _lib.ptr(flags), st())
 
-    def tc_b(split, rows128=True):
-        # plain products run on the 128-row tiles, split ones on the 64-row
-        # panel (as the solver does)
-        if rows128 and not split:
-            _lib.call("fgb_tc_phase_b", C.byref(FF._desc128), _lib.ptr(tc["w128"]), None,
+    plain_plan = FF.product_plan()["plain"]
+    plain_rows = {"b128": 128, "b256": 256}.get(plain_plan, 64)
+
+    def tc_b(split, rows=None):
+        # plain products run on the layout the autotuner chose (128- or
+        # 256-row tiles), split ones on the 64-row panel (as the solver does)
+        rows = plain_rows if rows is None else rows
+        if rows in (128, 256) and not split:
+            dsc, w = ((FF._desc128, tc["w128"]) if rows == 128 else
+                      (FF._desc256, FF.tc_operands256()["w256"]))
+            _lib.call("fgb_tc_phase_b", C.byref(dsc), _lib.ptr(w), None,
                       _lib.ptr(xh), None, _lib.ptr(zh), None, _lib.ptr(Y), K, _lib.ptr(Ek), 1.0,
                       _lib.ptr(flags), st())
             return
@@ -1108,7 +1128,9 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
           "phaseB_tc_split": t_events(lambda: tc_b(True))}
     ms_tma = t_events(tc_b_tma, 3)
     ms_a128 = t_events(lambda: tc_a(True, rows64=False), 3)
-    ms_b64 = t_events(lambda: tc_b(False, rows128=False), 3)
+    ms_b64 = t_events(lambda: tc_b(False, rows=64), 3)
+    ms_bwide = {r: t_events(lambda: tc_b(False, rows=r), 3) for r in (128, 256)
+                if r != plain_rows and (r == 128 or "w256" in FF.tc_operands())}
     # the FP32 kernels write Z in FP32 (the BF16 sources are not needed)
     del xh, xl, zh, zl, sh, sl
     Z32 = torch.zeros((zr, K), dtype=torch.float32, device=dev)
@@ -1124,12 +1146,12 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
     alg = operator_work(FF)
     U_, V_, nnz = alg["lowrank_u_entries"], alg["lowrank_v_entries"], alg["exact_nnz"]
     zrows = int(FF._num_zrows)
-    rows128 = int(FF.stats.get("panel_rows_128", 0))
+    rows_plain = int(FF.stats.get(f"panel_rows_{plain_rows}", FF._panel_rows))
     work = {   # (algorithmic bytes, algorithmic flops, executed flops)
         "phaseA_tc": (2 * V_ + 2 * K * N + 2 * K * zrows, 2.0 * V_ * K,
                       2.0 * int(FF._vpanel_size) * K),
         "phaseB_tc": (2 * U_ + 6 * nnz + 2 * K * (zrows + N) + 8 * K * N, 2.0 * (U_ + nnz) * K,
-                      2.0 * rows128 * 128 * K),
+                      2.0 * rows_plain * plain_rows * K),
         "phaseA_tc_split": (4 * V_ + 4 * K * N + 4 * K * zrows, 6.0 * V_ * K,
                             6.0 * int(FF._vpanel_size) * K),
         "phaseB_tc_split": (4 * U_ + 8 * nnz + 4 * K * (zrows + N) + 8 * K * N,
@@ -1161,7 +1183,7 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
     # the measured peaks
     ai = fl / byts
     ridge = tf * 1e12 / (hbm * 1e9)
-    traffic = scaled_dram_traffic(dom, FF, K)
+    traffic = scaled_dram_traffic(dom, FF, K, plain_rows)
     common = {"kernel": dom, "traffic": traffic, "traffic_source": TRAFFIC_CAPTURE["source"],
               "peak_source": src, "algorithmic_flops": fl, "algorithmic_bytes": byts,
               "executed_flops": fl_exec, "executed_tflops": fl_exec / (t_ms * 1e-3) / 1e12,
@@ -1176,7 +1198,9 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
         out["roofline"] = {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s",
                            "frac": gbs / hbm, **common}
     out["kernel_ms"] = {"columns": K, **ms, "phaseB_tc_tma_gather_variant": ms_tma,
+                        "phaseB_tc_tile_rows": plain_rows,
                         "phaseB_tc_64row_tiles": ms_b64,
+                        **{f"phaseB_tc_{r}row_tiles": v for r, v in ms_bwide.items()},
                         "phaseA_tc_split_128row_slices": ms_a128,
                         "per_step_ms": per_step,
                         "tflops_algorithmic": {k: work[k][1] / (ms[k] * 1e-3) / 1e12 for k in ms},

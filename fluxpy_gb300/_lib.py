@@ -122,6 +122,7 @@ SIGNATURES: dict[str, list] = {
     "fgb_tc_phase_b_tma": [P, P, P, P, P, P, I32, P, F32, P, P],
     "fgb_split_bf16": [P, P, P, I64, P],
     "fgb_retile_panel_bf16": [P, I64, P, P, P, P],
+    "fgb_retile_panel_bf16_n": [P, I64, P, P, I32, P, P],
     "fgb_retile_panel_split_bf16": [P, I64, P, P, P, P, P],
     "fgb_vpanel_transpose_bf16": [P, P, P, P, P, I64, P, P, P],
     # solve (a10-a12)

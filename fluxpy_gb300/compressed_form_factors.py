@@ -1115,7 +1115,8 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
 
     # keys of the device layout and caches that a transposed copy rebuilds
     _LAYOUT_KEYS = ("_dev", "_dev_tc", "_build_dev", "_nf", "_desc", "_desc_tc", "_desc_tc64",
-                    "_desc_tc_items", "_desc128", "_dev128", "_panels", "_tc", "_flags_d",
+                    "_desc_tc_items", "_desc128", "_dev128", "_desc256", "_dev256", "_panels",
+                    "_tc", "_flags_d",
                     "_fgb_adjoint_ops", "_root_cache", "_host_tree_cache", "_transposed",
                     "_exact_csr", "_lr_blocks", "_lr_u", "_lr_v", "_tile_L")
 
@@ -1283,6 +1284,18 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         source become one 128-weight row of tile t (each source appears at
         most once per 64-row tile, so the halves never collide).  Returns
         (hi, lo): BF16 weights, and with split their low parts (else None)."""
+        return self._build_tc_wide(panel32, 128, split)
+
+    def _build_tc_wide(self, panel32, width, split=False):
+        """Phase-B layout with tiles of `width` rows (128 or 256) for the
+        BF16 tensor-core products: the 64-row panel's rows of the width / 64
+        tiles that form one wide tile and gather the same source become one
+        row of `width` weights (64-row tile t fills part t mod (width / 64)).
+        Sets the layout's descriptor (_desc128 / _desc256) and returns (hi,
+        lo) as _build_tc128 does; lo only for width 128."""
+        assert width in (128, 256) and not (split and width != 128)
+        parts = width // 64
+        shift = parts.bit_length() - 1
         dev = panel32.device
         t_p0 = self._dev["t_p0"]
         ntiles = int(t_p0.numel() - 1)
@@ -1294,9 +1307,9 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         vidx = torch.nonzero(pos < Lt[tile]).squeeze(1)     # rows that are not padding
         del pos
         vtile = tile[vidx]
-        half = (tile & 1).to(torch.uint8)
+        half = (tile & (parts - 1)).to(torch.uint8)
         del tile
-        vkey = (vtile >> 1) * (1 << 31) + self._dev["src"].to(torch.int64)[vidx]
+        vkey = (vtile >> shift) * (1 << 31) + self._dev["src"].to(torch.int64)[vidx]
         del vtile
         skey, order = torch.sort(vkey)
         del vkey
@@ -1308,7 +1321,7 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         u_tile = ukeys >> 31
         u_src = (ukeys & ((1 << 31) - 1)).to(torch.int32)
         del ukeys
-        nt2 = (self.num_faces + 127) // 128
+        nt2 = (self.num_faces + width - 1) // width
         L2 = torch.bincount(u_tile, minlength=nt2)
         t2 = torch.zeros(nt2 + 1, dtype=torch.int64, device=dev)
         t2[1:] = torch.cumsum((L2 + PANEL_ALIGN - 1) // PANEL_ALIGN * PANEL_ALIGN, 0)
@@ -1323,9 +1336,12 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         src2 = torch.zeros(max(total2, 1), dtype=torch.int32, device=dev)
         src2[u_row] = u_src
         del u_row, u_src
-        w128 = torch.zeros(max(total2, 1) * 128, dtype=torch.bfloat16, device=dev)
+        w128 = torch.zeros(max(total2, 1) * width, dtype=torch.bfloat16, device=dev)
         lo128 = None
-        if split:
+        if width != 128:
+            _lib.call("fgb_retile_panel_bf16_n", _lib.ptr(panel32), P, _lib.ptr(new_row),
+                      _lib.ptr(half), width, _lib.ptr(w128), _lib.stream_handle())
+        elif split:
             lo128 = torch.zeros_like(w128)
             _lib.call("fgb_retile_panel_split_bf16", _lib.ptr(panel32), P, _lib.ptr(new_row),
                       _lib.ptr(half), _lib.ptr(w128), _lib.ptr(lo128), _lib.stream_handle())
@@ -1338,11 +1354,20 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         desc.src = src2.data_ptr()
         desc.num_tiles = nt2
         desc.panel_rows = total2
-        desc.tile_rows = 128
-        self._dev128 = dict(t_p0=t2, src=src2)
-        self._desc128 = desc
-        self.stats["panel_rows_128"] = total2
+        desc.tile_rows = width
+        setattr(self, f"_dev{width}", dict(t_p0=t2, src=src2))
+        setattr(self, f"_desc{width}", desc)
+        self.stats[f"panel_rows_{width}"] = total2
         return w128, lo128
+
+    def tc_operands256(self):
+        """The 256-row phase-B panel ('w256', BF16) of the plain product's
+        widest layout, in the same dict as tc_operands; built on request."""
+        tc = self.tc_operands()
+        if "w256" not in tc or self.__dict__.get("_desc256") is None:
+            panel, _ = self.panels("fp32")
+            tc["w256"], _ = self._build_tc_wide(panel, 256)
+        return tc
 
     def tc_operands(self, split=False):
         """BF16 operands of the tensor-core products, built once from the
@@ -1424,8 +1449,12 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
             # phase A writes Z directly in BF16 (Z, the FP32 scratch, is unused)
             _lib.call("fgb_tc_phase_a_bf16", C.byref(self._desc_tc), _lib.ptr(tc["vt_hi"]), None,
                       _lib.ptr(Xb), None, _lib.ptr(Zb), None, K, flags, st)
-        if self.product_plan()["plain"] == "b64":
+        plain = self.product_plan()["plain"]
+        if plain == "b64":
             desc, w = self._desc, self.tc_operands64()["w_hi"]
+        elif plain == "b256":
+            w = self.tc_operands256()["w256"]
+            desc = self._desc256
         else:
             desc, w = self._desc128, tc["w128"]
         _lib.call("fgb_tc_phase_b", C.byref(desc), _lib.ptr(w), None,
@@ -1480,8 +1509,9 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         return Y
 
     # -- product plans (autotuned) ------------------------------------------
-    # plain BF16 product: phase-B tiles of 128 rows (merged tile pairs) or 64
-    PLAIN_PLANS = ("b128", "b64")
+    # plain BF16 product: phase-B tiles of 128 rows (merged tile pairs), 64
+    # or 256 (merged tile quadruples)
+    PLAIN_PLANS = ("b128", "b64", "b256")
     # split product: phase-A work slices of 64 / 128 rows, phase-B tiles of 64 / 128
     SPLIT_PLANS = ("a64-b64", "a128-b64", "a64-b128", "a128-b128")
 
@@ -1533,6 +1563,12 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
 
         table = {"plain": {}, "split": {}}
         for p_ in plans["plain"]:
+            if p_ == "b256" and "w256" not in tc:
+                # at most as many rows as the 128-row panel, twice as wide
+                need = 2 * tc["w128"].numel() * 2 + (1 << 33)
+                if torch.cuda.mem_get_info(dev)[0] < need:
+                    table["plain"][p_] = None
+                    continue
             plan["plain"] = p_
             table["plain"][p_] = timed(lambda: self.bf16_product(Xb, None, Zb, Y))
         for p_ in plans["split"]:
@@ -1551,6 +1587,8 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         plan.update(best)
         if not plan["split"].endswith("b128"):
             tc.pop("w128_lo", None)      # not used: give the memory back
+        if plan["plain"] != "b256":
+            tc.pop("w256", None)
         del X, Y, Sb, Zb, Xb, work
         torch.cuda.empty_cache()
         table["chosen"] = dict(plan)
@@ -1774,6 +1812,8 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         st["_desc_tc_items"] = None
         st["_desc128"] = None
         st["_dev128"] = None
+        st["_desc256"] = None
+        st["_dev256"] = None
         st["_panels"] = {}
         st["_tc"] = {}
         st["_flags_d"] = None

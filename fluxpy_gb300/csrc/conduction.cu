@@ -332,6 +332,235 @@ conduction_q_kernel(int num_faces, int nz, const R* __restrict__ z, R dt,
   if (my_flags) atomicOr(flags, my_flags);
 }
 
+// FP32: the same step with the tridiagonal system eliminated from the bottom
+// up.  Rows 2..nz do not depend on the facet except through the right-hand
+// side, and only row 1 depends on the linearised radiative boundary, so
+//   * the pivots beta_j and factors e_j = c_j / beta_{j+1} of rows nz..2
+//     are computed once per CTA (UpRow / DownRow tables);
+//   * each facet sweeps up once, y_j = r_j - e_j y_{j+1}, forming r_j from
+//     the pre-step profile and overwriting it with y_j;
+//   * the predictor-corrector iterations (conductionQ.c:103-172) then solve
+//     row 1 alone, u_1 = (r_1 - e_1 y_2) / (b_1 - e_1 a_2), with r_1 and b_1
+//     from the current linearisation temperature: a redo costs O(1), not a
+//     new solve (the reference re-solves the whole system from the pre-step
+//     profile, which gives the same u in exact arithmetic);
+//   * one substitution down, u_j = (y_j - a_j u_{j-1}) / beta_j.
+// No per-facet pivots or elimination factors, no reloads; FMAs are explicit
+// (this file is compiled without contraction for the FP64 path).  The
+// system is strictly diagonally dominant, so elimination in either direction
+// is stable; the FP64 kernel keeps the reference's top-down order.
+struct alignas(16) UpRow {
+  float ga, mid, al, e;
+};
+struct alignas(8) DownRow {
+  float a, rb;
+};
+
+// Shared layout of the FP32 kernel: the 7 coefficient arrays (padded to a
+// multiple of 4 floats, so that the tile starts 16-byte aligned), the tile,
+// then the UpRow and DownRow tables.
+__host__ __device__ inline int cond_up_coeff_floats(int nz) { return (7 * (nz + 1) + 3) & ~3; }
+__host__ __device__ inline size_t cond_up_smem(int nz, int nt) {
+  const size_t base =
+      sizeof(float) * ((size_t)cond_up_coeff_floats(nz) + (size_t)nt * tile_stride(nz));
+  return (base + 15) / 16 * 16 + (sizeof(UpRow) + sizeof(DownRow)) * (size_t)(nz + 1);
+}
+
+// Row-major global rows [f0, f0 + rows) x w <-> the tile, when the tile's
+// stride is w (w odd) and both sides are 16-byte aligned: a contiguous copy
+// in 16-byte pieces (the last few floats one by one); otherwise stage().
+template <bool IN>
+__device__ void stage_up(float* tile, float* T, long long f0, int rows, int w, int ws) {
+  float* g = T + f0 * w;
+  if (ws != w || (reinterpret_cast<uintptr_t>(g) & 15) != 0) {
+    stage<float, IN>(tile, T, f0, rows, w, ws);
+    return;
+  }
+  const int n = rows * w, n4 = n >> 2, nt = blockDim.x;
+  float4* t4 = reinterpret_cast<float4*>(tile);
+  float4* g4 = reinterpret_cast<float4*>(g);
+  for (int i = threadIdx.x; i < n4; i += nt) {
+    if (IN) t4[i] = g4[i];
+    else g4[i] = t4[i];
+  }
+  for (int i = 4 * n4 + threadIdx.x; i < n; i += nt) {
+    if (IN) tile[i] = g[i];
+    else g[i] = tile[i];
+  }
+}
+
+constexpr int kUpThreads = 128;
+
+int cond_up_threads(int nz) {
+  int best = 0, best_res = 0;
+  for (int nt = 32; nt <= kUpThreads; nt += 32) {
+    const size_t sm = cond_up_smem(nz, nt);
+    if (sm > kSmemBudget) break;
+    const int ctas = (int)((228 * 1024) / (sm + 1024));
+    const int res = nt * (ctas < 2048 / nt ? ctas : 2048 / nt);
+    if (res >= best_res) { best_res = res; best = nt; }
+  }
+  return best;
+}
+
+__global__ void __launch_bounds__(kUpThreads, 9)
+conduction_q_up_kernel(int num_faces, int nz, const float* __restrict__ z, float dt,
+                       const float* __restrict__ Qn, const float* __restrict__ Qnp1,
+                       const float* T_in, float* T_out,
+                       const float* __restrict__ ti, const float* __restrict__ rhoc,
+                       const float* __restrict__ emiss, const float* __restrict__ Fgeotherm,
+                       float* __restrict__ Fsurf, unsigned* __restrict__ flags) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float* sh = reinterpret_cast<float*>(smem_raw);
+  const int w = nz + 1, ws = tile_stride(nz), nt = blockDim.x;
+  float* s_k = coeff(sh, 0, nz);
+  float* s_alpha = coeff(sh, 1, nz);
+  float* s_gamma = coeff(sh, 2, nz);
+  float* s_a = coeff(sh, 3, nz);
+  float* s_b = coeff(sh, 4, nz);
+  float* s_c = coeff(sh, 5, nz);
+  float* s_misc = coeff(sh, 6, nz);  // [0] k1, [1] e_1, [2] e_1 a_2, [3] zero pivot
+  float* tile = sh + cond_up_coeff_floats(nz);
+  const size_t base = sizeof(float) * ((size_t)cond_up_coeff_floats(nz) + (size_t)nt * ws);
+  UpRow* s_up = reinterpret_cast<UpRow*>(smem_raw + (base + 15) / 16 * 16);
+  DownRow* s_dn = reinterpret_cast<DownRow*>(s_up + w);
+
+  grid_coeffs_q<float>(nz, z, dt, ti, rhoc, s_k, s_alpha, s_gamma, s_a, s_b, s_c, &s_misc[0]);
+  __syncthreads();
+  const long long f0 = (long long)blockIdx.x * nt;
+  const int rows = (int)min((long long)nt, (long long)num_faces - f0);
+  // profiles first (their loads are in flight during the recurrence below)
+  stage_up<true>(tile, const_cast<float*>(T_in), f0, rows, w, ws);
+  // the rows' own coefficients, one row per thread (fields apart from the
+  // e and rb that thread 0 writes below)
+  for (int j = threadIdx.x + 2; j <= nz; j += nt) {
+    const float al = j < nz ? s_alpha[j] : 0.0f, ga = s_gamma[j];
+    s_up[j].ga = ga;
+    s_up[j].mid = 1.0f - al - ga;
+    s_up[j].al = al;
+    s_dn[j].a = s_a[j];
+  }
+  if (threadIdx.x == 0) {
+    // the facet-independent elimination of rows nz..2: a serial recurrence
+    // (one fast reciprocal per row)
+    float beta = s_b[nz], rb = __fdividef(1.0f, beta);
+    bool zero = beta == 0.0f;
+    s_up[nz].e = 0.0f;
+    s_dn[nz].rb = rb;
+#pragma unroll 4
+    for (int j = nz - 1; j >= 2; j--) {
+      const float e = s_c[j] * rb;
+      beta = __fmaf_rn(-e, s_a[j + 1], s_b[j]);
+      zero = zero || beta == 0.0f;
+      rb = __fdividef(1.0f, beta);
+      s_up[j].e = e;
+      s_dn[j].rb = rb;
+    }
+    const float e1 = s_c[1] * rb;
+    s_misc[1] = e1;
+    s_misc[2] = e1 * s_a[2];
+    s_misc[3] = zero ? 1.0f : 0.0f;
+  }
+  __syncthreads();
+
+  const int t = threadIdx.x;
+  unsigned my_flags = 0;
+  if (t < rows) {
+    const long long f = f0 + t;
+    float* Trow = tile + t * ws;
+    const float qn = Qn[f], qnp1 = Qnp1[f], em = emiss[f], fg = Fgeotherm[f];
+    if (!finite_val(qnp1)) my_flags |= kFlagNonfiniteIn;
+    if (qnp1 < 0.0f) my_flags |= kFlagNegativeIn;
+    if (s_misc[3] != 0.0f) my_flags |= kFlagZeroPivot;
+    const float rhs_bottom = dt / rhoc[nz] * fg / (z[nz] - z[nz - 1]);
+    // sweep up: y_j = r_j - e_j y_{j+1}, r_j from the pre-step profile
+    // (tj = T[j], tj1 = T[j+1] of the pre-step profile, in registers); row
+    // nz carries the bottom flux and e_nz = 0
+    float tj1 = Trow[nz], tj = Trow[nz - 1], y;
+    {
+      const UpRow u = s_up[nz];
+      y = __fmaf_rn(u.mid, tj1, __fmaf_rn(u.ga, tj, rhs_bottom));
+      Trow[nz] = y;
+    }
+#pragma unroll 4
+    for (int j = nz - 1; j >= 2; j--) {
+      const UpRow u = s_up[j];
+      const float tm1 = Trow[j - 1];
+      const float r = __fmaf_rn(u.al, tj1, __fmaf_rn(u.mid, tj, __fmul_rn(u.ga, tm1)));
+      y = __fmaf_rn(-u.e, y, r);
+      Trow[j] = y;
+      tj1 = tj;
+      tj = tm1;
+    }
+    const float t1 = tj, t2 = tj1, y2 = y;
+    // predictor-corrector on row 1 alone
+    const float k1 = s_misc[0], e1 = s_misc[1], e1a2 = s_misc[2];
+    const float sig = Consts<float>::sigSB;
+    const float alpha1 = s_alpha[1], gamma1 = s_gamma[1];
+    float Tr = Trow[0], T0 = Tr, u1 = t1;
+    int iter = 0;
+    while (true) {
+      const float arad = -3.0f * em * sig * Tr * Tr * Tr * Tr;
+      const float brad = 2.0f * em * sig * Tr * Tr * Tr;
+      const float inv = __fdividef(1.0f, k1 + brad);
+      const float ann = (qn - arad) * inv;
+      const float annp1 = (qnp1 - arad) * inv;
+      const float bn = (k1 - brad) * inv;
+      const float b1 = 1.0f + alpha1 + gamma1 - gamma1 * bn;
+      const float r1 = gamma1 * (annp1 + ann) + (1.0f - alpha1 - gamma1 + gamma1 * bn) * t1 +
+                       alpha1 * t2;
+      const float beta1 = b1 - e1a2;
+      if (beta1 == 0.0f) {
+        my_flags |= kFlagZeroPivot;
+        break;
+      }
+      u1 = __fdividef(r1 - e1 * y2, beta1);
+      T0 = 0.5f * (annp1 + bn * u1 + u1);
+      if ((T0 > 1.2f * Tr || T0 < 0.8f * Tr) && iter < 10) {
+        iter++;
+        Tr = sqrtf(Tr * T0);
+        continue;
+      }
+      break;
+    }
+    if (iter >= 9) my_flags |= kFlagPredCorrMax;
+    // substitute down: u_j = (y_j - a_j u_{j-1}) / beta_j; the output
+    // checks through a running sum (NaN and infinity propagate) and minimum
+    Trow[0] = T0;
+    Trow[1] = u1;
+    float up = u1, sum = T0 + u1, mn = fminf(T0, u1);
+#pragma unroll 4
+    for (int j = 2; j <= nz; j++) {
+      const DownRow d = s_dn[j];
+      up = __fmul_rn(__fmaf_rn(-d.a, up, Trow[j]), d.rb);
+      Trow[j] = up;
+      sum += up;
+      mn = fminf(mn, up);
+    }
+    if (!finite_val(sum)) my_flags |= kFlagNonfiniteOut;
+    if (mn < 0.0f) my_flags |= kFlagNegativeOut;
+    Fsurf[f] = -s_k[1] * (u1 - T0) / z[1];
+  }
+  __syncthreads();
+  stage_up<false>(tile, T_out, f0, rows, w, ws);
+  if (my_flags) atomicOr(flags, my_flags);
+}
+
+int launch_q_up(int num_faces, int nz, const float* z, float dt, const float* Qn,
+                const float* Qnp1, const float* T_in, float* T_out, const float* ti,
+                const float* rhoc, const float* emiss, const float* Fgeotherm, float* Fsurf,
+                unsigned* flags, cudaStream_t s) {
+  const int nt = cond_up_threads(nz);
+  const size_t sm = cond_up_smem(nz, nt);
+  FGB_CUDA_TRY(cudaFuncSetAttribute(conduction_q_up_kernel,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  const unsigned grid = (unsigned)((num_faces + nt - 1) / nt);
+  conduction_q_up_kernel<<<grid, nt, sm, s>>>(num_faces, nz, z, dt, Qn, Qnp1, T_in, T_out, ti,
+                                              rhoc, emiss, Fgeotherm, Fsurf, flags);
+  FGB_LAUNCH_CHECK("conduction_q_up_kernel");
+  return FGB_OK;
+}
+
 // One step of the prescribed-surface-temperature problem (conductionT.c).
 template <class R, int NZMAX>
 __global__ void __launch_bounds__(kMaxThreads)
@@ -438,6 +667,14 @@ int dispatch_q(int num_faces, int nz, const R* z, R dt, const R* Qn, const R* Qn
   if (st) return st;
   if (num_faces == 0) return FGB_OK;
   cudaStream_t s = as_stream(stream);
+  if (sizeof(R) == sizeof(float) && cond_up_threads(nz) > 0)
+    return launch_q_up(num_faces, nz, reinterpret_cast<const float*>(z), (float)dt,
+                       reinterpret_cast<const float*>(Qn), reinterpret_cast<const float*>(Qnp1),
+                       reinterpret_cast<const float*>(T_in), reinterpret_cast<float*>(T_out),
+                       reinterpret_cast<const float*>(ti), reinterpret_cast<const float*>(rhoc),
+                       reinterpret_cast<const float*>(emiss),
+                       reinterpret_cast<const float*>(Fgeotherm), reinterpret_cast<float*>(Fsurf),
+                       flags, s);
   if (nz <= 47) return launch_q<R, 47>(num_faces, nz, z, dt, Qn, Qnp1, T_in, T_out, ti, rhoc, emiss, Fgeotherm, Fsurf, flags, s);
   if (nz <= 63) return launch_q<R, 63>(num_faces, nz, z, dt, Qn, Qnp1, T_in, T_out, ti, rhoc, emiss, Fgeotherm, Fsurf, flags, s);
   if (nz <= 127) return launch_q<R, 127>(num_faces, nz, z, dt, Qn, Qnp1, T_in, T_out, ti, rhoc, emiss, Fgeotherm, Fsurf, flags, s);

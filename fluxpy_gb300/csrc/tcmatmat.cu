@@ -208,7 +208,9 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
 // columns per CTA (a multiple of the MMA M = 128), CH = reduction rows per
 // stage.  Phase A computes 128 rows of Z per CTA, so that each gathered X
 // row feeds twice the flops; phase B runs 128-row tiles for the plain BF16
-// product (the re-tiled panel) and the 64-row tiles for the split one.
+// product (the re-tiled panel) and the 64-row tiles for the split one;
+// 256-row tiles (MMA N = 256, two CTAs per SM: 256 TMEM columns each) are
+// the plain product's widest layout.
 // Split mode keeps SEGS x 32 compensated sums per thread (32 for 64-row
 // tiles or slices, 64 for 128-row ones).
 // CTAS = CTAs per SM the shape is built for.  The plain products run four
@@ -226,7 +228,7 @@ struct TcCfg {
   static constexpr int NR = NR_;
   static constexpr int NC = 128;
   static constexpr int CH = 32;
-  static constexpr int CTAS = SPLIT ? (NR == 64 ? 2 : 1) : 4;
+  static constexpr int CTAS = SPLIT ? (NR == 64 ? 2 : 1) : (NR >= 256 ? 2 : 4);
   // threads per CTA: the split products on 128-row tiles / slices run 16
   // warps, so that each thread keeps 32 compensated sums (as on 64-row
   // tiles with 8 warps), one CTA per SM
@@ -659,14 +661,15 @@ tc_gather_gemm(TcArgs a) {
   }
 }
 
-// 128-row panel from the 64-row FP32 one: old panel row r (tile t) with
-// new_row[r] >= 0 lands in half (t & 1) of new row new_row[r], as BF16; the
-// new panel is zeroed by the caller (a new row gets at most one old row per
-// half: a source appears once per 64-row tile).  One warp per old row.
-// lo (optional): the split operand's low part, bf16(w - bf16(w)).
+// Wider panel from the 64-row FP32 one: old panel row r (64-row tile t)
+// with new_row[r] >= 0 lands in part part[r] (t mod width / 64) of new row
+// new_row[r], as BF16; the new panel (width weights per row) is zeroed by
+// the caller (a new row gets at most one old row per part: a source appears
+// once per 64-row tile).  One warp per old row.  lo (optional): the split
+// operand's low part, bf16(w - bf16(w)).
 __global__ void retile_panel_kernel(const float* __restrict__ panel64, long long num_rows,
                                     const long long* __restrict__ new_row,
-                                    const unsigned char* __restrict__ half,
+                                    const unsigned char* __restrict__ part, int width,
                                     __nv_bfloat16* __restrict__ panel128,
                                     __nv_bfloat16* __restrict__ lo128) {
   const int lane = threadIdx.x & 31;
@@ -676,7 +679,7 @@ __global__ void retile_panel_kernel(const float* __restrict__ panel64, long long
     const long long nr = new_row[r];
     if (nr < 0) continue;
     const float2 w = reinterpret_cast<const float2*>(panel64 + r * 64)[lane];
-    const long long o = nr * 128 + half[r] * 64 + 2 * lane;
+    const long long o = nr * width + part[r] * 64 + 2 * lane;
     const __nv_bfloat16 hx = __float2bfloat16(w.x), hy = __float2bfloat16(w.y);
     panel128[o] = hx;
     panel128[o + 1] = hy;
@@ -1210,7 +1213,11 @@ int fgb_tc_phase_b(const struct fgb_op_desc* d, const void* w_hi, const void* w_
   if (tr == 128)
     return split ? fgb::launch_tc<fgb::kModeB, true, 128>(a, d->num_tiles, st)
                  : fgb::launch_tc<fgb::kModeB, false, 128>(a, d->num_tiles, st);
-  if (tr != 64) { fgb::set_error("tile_rows must be 64 or 128"); return FGB_BAD_ARG; }
+  if (tr == 256) {
+    if (split) { fgb::set_error("split products take 64- or 128-row tiles"); return FGB_BAD_ARG; }
+    return fgb::launch_tc<fgb::kModeB, false, 256>(a, d->num_tiles, st);
+  }
+  if (tr != 64) { fgb::set_error("tile_rows must be 64, 128 or 256"); return FGB_BAD_ARG; }
   return split ? fgb::launch_tc<fgb::kModeB, true, 64>(a, d->num_tiles, st)
                : fgb::launch_tc<fgb::kModeB, false, 64>(a, d->num_tiles, st);
 }
@@ -1244,7 +1251,21 @@ int fgb_retile_panel_bf16(const float* panel64, long long num_rows, const long l
   if (num_rows == 0) return FGB_OK;
   fgb::retile_panel_kernel<<<fgb::grid_for(num_rows * 32, 256, 152LL * 64), 256, 0,
                              fgb::as_stream(stream)>>>(
-      panel64, num_rows, new_row, half, static_cast<__nv_bfloat16*>(panel128), nullptr);
+      panel64, num_rows, new_row, half, 128, static_cast<__nv_bfloat16*>(panel128), nullptr);
+  FGB_LAUNCH_CHECK("retile_panel_kernel");
+  return FGB_OK;
+}
+
+int fgb_retile_panel_bf16_n(const float* panel64, long long num_rows, const long long* new_row,
+                            const unsigned char* part, int width, void* out, void* stream) {
+  if (num_rows < 0 || !panel64 || !out || (width != 128 && width != 256)) {
+    fgb::set_error("bad arguments (width must be 128 or 256)");
+    return FGB_BAD_ARG;
+  }
+  if (num_rows == 0) return FGB_OK;
+  fgb::retile_panel_kernel<<<fgb::grid_for(num_rows * 32, 256, 152LL * 64), 256, 0,
+                             fgb::as_stream(stream)>>>(
+      panel64, num_rows, new_row, part, width, static_cast<__nv_bfloat16*>(out), nullptr);
   FGB_LAUNCH_CHECK("retile_panel_kernel");
   return FGB_OK;
 }
@@ -1256,7 +1277,7 @@ int fgb_retile_panel_split_bf16(const float* panel64, long long num_rows,
   if (num_rows == 0) return FGB_OK;
   fgb::retile_panel_kernel<<<fgb::grid_for(num_rows * 32, 256, 152LL * 64), 256, 0,
                              fgb::as_stream(stream)>>>(
-      panel64, num_rows, new_row, half, static_cast<__nv_bfloat16*>(hi128),
+      panel64, num_rows, new_row, half, 128, static_cast<__nv_bfloat16*>(hi128),
       static_cast<__nv_bfloat16*>(lo128));
   FGB_LAUNCH_CHECK("retile_panel_kernel");
   return FGB_OK;

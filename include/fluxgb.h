@@ -79,7 +79,10 @@ int fgb_conduction_q_f64(int num_faces, int nz, const double* z, double dt,
                          double* T_out, const double* ti, const double* rhoc,
                          const double* emiss, const double* Fgeotherm, double* Fsurf,
                          unsigned* flags, void* stream);
-/* Same in FP32 (same algorithm; used by the FP32 time-stepping driver). */
+/* Same in FP32 (used by the FP32 time-stepping driver): the same equations,
+ * eliminated from the bottom up, so that the predictor-corrector redos of
+ * the radiative boundary re-solve only the surface row (the same solution in
+ * exact arithmetic; results within FP32 rounding of the FP64 entry point). */
 int fgb_conduction_q_f32(int num_faces, int nz, const float* z, float dt, const float* Qn,
                          const float* Qnp1, const float* T_in, float* T_out,
                          const float* ti, const float* rhoc, const float* emiss,
@@ -406,7 +409,8 @@ struct fgb_op_desc {
   long long num_work;   /* a_woff[num_items] */
   long long panel_rows; /* t_p0[num_tiles] */
   int tile_rows;        /* rows per phase-B tile: 64 (every kernel), or 128
-                           (tensor-core BF16 phase B only); 0 means 64 */
+                           or 256 (tensor-core BF16 phase B only; 256: plain
+                           products); 0 means 64 */
   int slice_rows;       /* rows per tensor-core phase-A work slice (a_woff
                            counts slices of this height): 128, or 64 for the
                            split products of fgb_tc_phase_a_bf16; 0 means 128 */
@@ -504,6 +508,13 @@ int fgb_tc_phase_b_tma(const struct fgb_op_desc* d, const void* w_hi, const void
  * flops. */
 int fgb_retile_panel_bf16(const float* panel64, long long num_rows, const long long* new_row,
                           const unsigned char* half, void* panel128, void* stream);
+/* The same for tiles of `width` rows (128 or 256): old row r goes to part
+ * part[r] (its 64-row tile's position in the wider tile) of new row
+ * new_row[r]; out (width BF16 weights per row) must be zeroed.  A descriptor
+ * with tile_rows = 256 gives fgb_tc_phase_b's plain product 256 output rows
+ * per CTA (MMA N = 256). */
+int fgb_retile_panel_bf16_n(const float* panel64, long long num_rows, const long long* new_row,
+                            const unsigned char* part, int width, void* out, void* stream);
 /* The same for split products: hi128 = bf16(w), lo128 = bf16(w - hi), both
  * zeroed by the caller (fgb_tc_phase_b takes them with tile_rows = 128). */
 int fgb_retile_panel_split_bf16(const float* panel64, long long num_rows,

@@ -370,6 +370,54 @@ def test_phase_b_128_row_tiles_match_64(terrain_op, K):
     assert FF.stats["panel_rows_128"] > 0
 
 
+@pytest.mark.parametrize("K", [256, 520])
+def test_phase_b_256_row_tiles_match_64(terrain_op, K):
+    """The plain BF16 phase B on the 256-row panel (rows of the four 64-row
+    tiles 4t .. 4t + 3 that gather the same source merged; MMA N = 256)
+    against the 64-row panel: same products, summed in another order; the
+    256-row layout has at most as many rows as the 128-row one."""
+    import ctypes as C
+    from fluxpy_gb300 import _lib
+    sm, FF = terrain_op
+    N = sm.num_faces
+    nz = FF._num_zrows
+    tc = FF.tc_operands256()
+    g = torch.Generator(device="cuda").manual_seed(K + 7)
+    S = torch.rand((nz + N, K), device="cuda", generator=g).to(torch.bfloat16)
+    add = torch.rand((N, K), device="cuda", generator=g)
+    fl = _lib.ptr(FF.device_flags())
+    st = _lib.stream_handle()
+    Y64 = torch.full((N, K), float("nan"), device="cuda")
+    Y256 = torch.full((N, K), float("nan"), device="cuda")
+    _lib.call("fgb_tc_phase_b", C.byref(FF._desc), _lib.ptr(FF.tc_operands64()["w_hi"]), None,
+              _lib.ptr(S[nz:]), None, _lib.ptr(S[:nz]), None, _lib.ptr(Y64), K, _lib.ptr(add),
+              0.5, fl, st)
+    assert FF._desc256.tile_rows == 256
+    _lib.call("fgb_tc_phase_b", C.byref(FF._desc256), _lib.ptr(tc["w256"]), None,
+              _lib.ptr(S[nz:]), None, _lib.ptr(S[:nz]), None, _lib.ptr(Y256), K, _lib.ptr(add),
+              0.5, fl, st)
+    FF.check_device_flags()
+    assert torch.isfinite(Y256).all()
+    ref = (Y64 - add).abs().max().item()
+    assert (Y256 - Y64).abs().max().item() <= 1e-5 * ref
+    assert 0 < FF.stats["panel_rows_256"] <= FF.stats["panel_rows_128"] + 64 * FF._desc256.num_tiles
+    # the product through the plan that uses it (phase A writes Z into
+    # S[:nz], then the 256-row phase B runs on S)
+    plan = FF.product_plan()
+    old = dict(plan)
+    try:
+        plan["plain"] = "b256"
+        Y = torch.empty_like(Y64)
+        FF.bf16_product(S[nz:], None, S[:nz], Y, add=add, alpha=0.5)
+        _lib.call("fgb_tc_phase_b", C.byref(FF._desc256), _lib.ptr(tc["w256"]), None,
+                  _lib.ptr(S[nz:]), None, _lib.ptr(S[:nz]), None, _lib.ptr(Y256), K,
+                  _lib.ptr(add), 0.5, fl, st)
+        FF.check_device_flags()
+        assert torch.equal(Y, Y256)
+    finally:
+        plan.update(old)
+
+
 @pytest.mark.parametrize("split", [False, True])
 def test_phase_b_separate_sources_match_stacked(terrain_op, split):
     """fgb_tc_phase_b with Z and X in separate buffers (a row select per

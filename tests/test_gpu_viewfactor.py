@@ -27,10 +27,15 @@ def test_matches_reference_c(golden):
     rel = np.abs(F - ref) / np.abs(ref)
     # the nine edge-pair terms of the closed form are much larger than their
     # sum (most for parallel edges), so two FP64 evaluations in different
-    # operation orders agree to ~1e-8 relative, not to the last bit
+    # operation orders agree to ~1e-8 relative, not to the last bit; for two
+    # nearly coplanar triangles that share an edge (normals 0.14 degrees
+    # apart, F = 4.3e-7) the sum cancels to 7 digits below its terms and the
+    # two evaluations differ by 4e-11 absolute (1e-4 relative), below what
+    # brute-force quadrature of that singular pair can resolve
+    bound = np.maximum(1e-7 * np.abs(ref), 1e-10)
     for kind in np.unique(golden["kind"]):
         sel = golden["kind"] == kind
-        assert rel[sel].max() < 1e-7, (kind, rel[sel].max())
+        assert np.all(np.abs(F - ref)[sel] <= bound[sel]), (kind, rel[sel].max())
     assert np.median(rel) < 1e-11
 
 

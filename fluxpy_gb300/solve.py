@@ -104,7 +104,7 @@ def _rho_vec(rho, E_d):
 
 # ---------------------------------------------------- reference solver --
 def solve_radiosity(FF, E, rho=1, albedo_placement='right', method='jacobi', tol=None,
-                    max_iter=100000, rtol=1e-5):
+                    max_iter=100000, rtol=1e-5, out=None):
     """Solve B = E + F (rho B) (right) or B = E + rho F B (left)
     (src/flux/solve.py:4-22).  Host arrays in, host arrays out; device
     tensors in, device tensors out.
@@ -114,9 +114,15 @@ def solve_radiosity(FF, E, rho=1, albedo_placement='right', method='jacobi', tol
     (N, K)): every column is solved to a relative residual ``rtol`` by
     ``solve_radiosity_batched``; the returned niter is the number of outer
     iterations.  Host input (numpy or a pinned CPU tensor) is copied to the
-    device and the result back to the host."""
+    device and the result back to the host; ``out`` (batched methods only:
+    an array or tensor of E's shape) receives B instead of a new array, so
+    that a caller who solves repeatedly from pinned host memory keeps the
+    device-to-host copy at full speed without pinning a new buffer per
+    call."""
     if method in ('batched-fp32', 'batched-bf16'):
-        return _solve_batched_public(FF, E, rho, albedo_placement, method, rtol)
+        return _solve_batched_public(FF, E, rho, albedo_placement, method, rtol, out)
+    if out is not None:
+        raise ValueError("out is supported by the batched methods only")
     on_dev = isinstance(E, torch.Tensor)
     E_np = None if on_dev else np.asarray(E)
     dtype = np.dtype(E_np.dtype if E_np is not None else
@@ -146,7 +152,7 @@ def solve_radiosity(FF, E, rho=1, albedo_placement='right', method='jacobi', tol
     return B.cpu().numpy().astype(dtype, copy=False), niter
 
 
-def _solve_batched_public(FF, E, rho, placement, method, rtol):
+def _solve_batched_public(FF, E, rho, placement, method, rtol, out=None):
     if placement != 'right':
         raise ValueError("batched solves use right albedo placement")
     dev = _lib.require_cuda()
@@ -164,6 +170,12 @@ def _solve_batched_public(FF, E, rho, placement, method, rtol):
                                 stats=st)
     if vec:
         B = B.reshape(-1)
+    if out is not None:
+        if tuple(out.shape) != tuple(B.shape):
+            raise ValueError(f"out has shape {tuple(out.shape)}, B has {tuple(B.shape)}")
+        dst = out if isinstance(out, torch.Tensor) else torch.from_numpy(out)
+        dst.copy_(B)
+        return out, st["outer"]
     if host_in:
         if isinstance(E, torch.Tensor):
             out = torch.empty(B.shape, dtype=torch.float32, pin_memory=E.is_pinned())

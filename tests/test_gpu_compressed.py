@@ -178,6 +178,40 @@ def test_batched_solvers_reach_rtol():
         assert rel <= bound, (prec, eng, res, incr, rel, st)
 
 
+def test_public_batched_solve_host_buffers():
+    """solve_radiosity(..., method='batched-bf16' / 'batched-fp32') with host
+    inputs: numpy in, numpy out; a pinned tensor in, a pinned tensor out;
+    out= receives B; all equal to the device-resident batched solve."""
+    sm = _terrain_case(32, seed=5)
+    FF = CompressedFormFactorMatrix(sm, tol=1e-5, min_size=4096, dtype=np.float32,
+                                    RootBlock=FormFactorOctreeBlock)
+    dirs = terrain.random_sun_directions(16, seed=3)
+    E = sm.get_direct_irradiance_batch(1365.0, dirs, out_dtype=torch.float32)
+    for method, prec in (("batched-bf16", "bf16-refine"), ("batched-fp32", "fp32")):
+        Bd = solve_radiosity_batched(FF, E, 0.12, rtol=1e-5, precision=prec).cpu()
+        Bn, niter = solve_radiosity(FF, E.cpu().numpy(), 0.12, method=method)
+        assert isinstance(Bn, np.ndarray) and niter >= 1
+        assert np.array_equal(Bn, Bd.numpy())
+        Ep = torch.empty(E.shape, dtype=torch.float32, pin_memory=True)
+        Ep.copy_(E.cpu())
+        Bt, _ = solve_radiosity(FF, Ep, 0.12, method=method)
+        assert isinstance(Bt, torch.Tensor) and not Bt.is_cuda and Bt.is_pinned()
+        assert torch.equal(Bt, Bd)
+        out = torch.full(E.shape, float("nan"), pin_memory=True)
+        Bo, _ = solve_radiosity(FF, Ep, 0.12, method=method, out=out)
+        assert Bo is out and torch.equal(out, Bd)
+        outn = np.full(tuple(E.shape), np.nan, np.float32)
+        Bo, _ = solve_radiosity(FF, E.cpu().numpy(), 0.12, method=method, out=outn)
+        assert Bo is outn and np.array_equal(outn, Bd.numpy())
+        # one column as a vector
+        b, _ = solve_radiosity(FF, E[:, 3].cpu().numpy(), 0.12, method=method)
+        assert b.shape == (sm.num_faces,)
+    with pytest.raises(ValueError, match="shape"):
+        solve_radiosity(FF, Ep, 0.12, method="batched-bf16", out=torch.empty(3, 3))
+    with pytest.raises(ValueError, match="batched methods only"):
+        solve_radiosity(FF, E[:, 0].cpu().numpy(), 0.12, out=np.empty(sm.num_faces))
+
+
 @pytest.fixture(scope="module")
 def terrain_op():
     sm = _terrain_case(64)

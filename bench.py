@@ -1099,10 +1099,19 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
     plain_plan = FF.product_plan()["plain"]
     plain_rows = {"b128": 128, "b256": 256}.get(plain_plan, 64)
 
+    split_plan = FF.product_plan()["split"]
+    split_rows = 128 if split_plan.endswith("b128") else 64
+
     def tc_b(split, rows=None):
-        # plain products run on the layout the autotuner chose (128- or
-        # 256-row tiles), split ones on the 64-row panel (as the solver does)
-        rows = plain_rows if rows is None else rows
+        # the layouts the autotuner chose, as the solver runs them: plain
+        # products on 128- or 256-row tiles, split ones on 64- or 128-row
+        # tiles
+        rows = (split_rows if split else plain_rows) if rows is None else rows
+        if split and rows == 128:
+            _lib.call("fgb_tc_phase_b", C.byref(FF._desc128), _lib.ptr(tc["w128"]),
+                      _lib.ptr(FF._split128_lo()), _lib.ptr(xh), _lib.ptr(xl), _lib.ptr(zh),
+                      _lib.ptr(zl), _lib.ptr(Y), K, _lib.ptr(Ek), 1.0, _lib.ptr(flags), st())
+            return
         if rows in (128, 256) and not split:
             dsc, w = ((FF._desc128, tc["w128"]) if rows == 128 else
                       (FF._desc256, FF.tc_operands256()["w256"]))
@@ -1123,11 +1132,16 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
         _lib.call("fgb_matmat_f32", desc, _lib.ptr(panel_f), _lib.ptr(vpanel_f), _lib.ptr(X32),
                   _lib.ptr(Z32), _lib.ptr(Y), K, None, 1.0, int(FF._needs_zero_z), phases, st())
 
+    a_rows64 = split_plan.startswith("a64")
     ms = {"phaseA_tc": t_events(lambda: tc_a(False)), "phaseB_tc": t_events(lambda: tc_b(False)),
-          "phaseA_tc_split": t_events(lambda: tc_a(True)),
+          "phaseA_tc_split": t_events(lambda: tc_a(True, rows64=a_rows64)),
           "phaseB_tc_split": t_events(lambda: tc_b(True))}
+    ms_split_other = t_events(lambda: tc_b(True, rows=192 - split_rows), 3)
+    if split_rows == 64:
+        FF.tc_operands().pop("w128_lo", None)    # built for this comparison only
+        torch.cuda.empty_cache()
     ms_tma = t_events(tc_b_tma, 3)
-    ms_a128 = t_events(lambda: tc_a(True, rows64=False), 3)
+    ms_a_other = t_events(lambda: tc_a(True, rows64=not a_rows64), 3)
     ms_b64 = t_events(lambda: tc_b(False, rows=64), 3)
     ms_bwide = {r: t_events(lambda: tc_b(False, rows=r), 3) for r in (128, 256)
                 if r != plain_rows and (r == 128 or "w256" in FF.tc_operands())}
@@ -1155,7 +1169,9 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
         "phaseA_tc_split": (4 * V_ + 4 * K * N + 4 * K * zrows, 6.0 * V_ * K,
                             6.0 * int(FF._vpanel_size) * K),
         "phaseB_tc_split": (4 * U_ + 8 * nnz + 4 * K * (zrows + N) + 8 * K * N,
-                            6.0 * (U_ + nnz) * K, 6.0 * int(FF._panel_rows) * 64 * K),
+                            6.0 * (U_ + nnz) * K,
+                            6.0 * int(FF.stats.get(f"panel_rows_{split_rows}", FF._panel_rows))
+                            * split_rows * K),
         "phaseA_f32": (4 * V_ + 4 * K * N + 4 * K * zrows, 2.0 * V_ * K,
                        2.0 * int(FF._vpanel_size) * K),
         "phaseB_f32": (4 * U_ + 8 * nnz + 4 * K * (zrows + N) + 8 * K * N, 2.0 * (U_ + nnz) * K,
@@ -1201,7 +1217,10 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
                         "phaseB_tc_tile_rows": plain_rows,
                         "phaseB_tc_64row_tiles": ms_b64,
                         **{f"phaseB_tc_{r}row_tiles": v for r, v in ms_bwide.items()},
-                        "phaseA_tc_split_128row_slices": ms_a128,
+                        "phaseB_tc_split_tile_rows": split_rows,
+                        f"phaseB_tc_split_{192 - split_rows}row_tiles": ms_split_other,
+                        "phaseA_tc_split_slice_rows": 64 if a_rows64 else 128,
+                        f"phaseA_tc_split_{128 if a_rows64 else 64}row_slices": ms_a_other,
                         "per_step_ms": per_step,
                         "tflops_algorithmic": {k: work[k][1] / (ms[k] * 1e-3) / 1e12 for k in ms},
                         "tflops_executed": {k: work[k][2] / (ms[k] * 1e-3) / 1e12 for k in ms}}

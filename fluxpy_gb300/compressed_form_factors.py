@@ -1423,10 +1423,10 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
 
     def tc_split128(self):
         """hi and lo parts of the 128-row phase-B panel for split products
-        on 128-row tiles (16-warp CTAs, one per SM).  Measured slower than
-        the 64-row split product at two CTAs per SM (146 vs 119 ms at 522k
-        facets and 1,024 columns), so the solver does not use them; built on
-        request, not kept."""
+        on 128-row tiles (8 warps and two CTAs per SM, the drained windows
+        summed in plain FP32).  At 522k facets and 1,024 columns the split
+        phase B took 71 ms on them against 106 ms on the 64-row tiles, with
+        the same product error; autotune_products chooses between them."""
         panel, _ = self.panels("fp32")
         return self._build_tc128(panel, split=True)
 
@@ -1465,8 +1465,9 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
     def split_product(self, X, Y, add=None, alpha=1.0, work=None):
         """Y = add + alpha F X for FP32 X (N x K, K % 8 == 0) on the tensor
         cores with split-BF16 operands (hi.hi + lo.hi + hi.lo; the tensor
-        core's FP32 accumulators are drained every two chunks into
-        compensated register sums).  Each product term is exact and the
+        core's FP32 accumulators are drained every 256 reduction rows into
+        register sums, compensated on 64-row tiles).  Each product term is
+        exact and the
         split operands carry ~17 significant bits, so the result behaves
         like FP32 arithmetic with 7 fewer bits.  work: optional dict of
         scratch tensors (reused)."""
@@ -1493,7 +1494,7 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         _lib.call("fgb_split_bf16", _lib.ptr(X), _lib.ptr(xh), _lib.ptr(xl), N * K, st)
         if self._num_zrows > 0:
             # phase A writes the hi / lo BF16 parts of Z directly: 64-row work
-            # slices (two CTAs per SM) or 128-row ones (16-warp CTAs)
+            # slices or 128-row ones (two CTAs per SM either way)
             dA = self._desc_tc if plan.startswith("a128") else self._desc_tc64
             _lib.call("fgb_tc_phase_a_bf16", C.byref(dA), _lib.ptr(tc["vt_hi"]),
                       _lib.ptr(tc["vt_lo"]), _lib.ptr(xh), _lib.ptr(xl), _lib.ptr(zh),

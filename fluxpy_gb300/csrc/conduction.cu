@@ -366,26 +366,43 @@ __host__ __device__ inline size_t cond_up_smem(int nz, int nt) {
   return (base + 15) / 16 * 16 + (sizeof(UpRow) + sizeof(DownRow)) * (size_t)(nz + 1);
 }
 
-// Row-major global rows [f0, f0 + rows) x w <-> the tile, when the tile's
-// stride is w (w odd) and both sides are 16-byte aligned: a contiguous copy
-// in 16-byte pieces (the last few floats one by one); otherwise stage().
+// A warp's own rows [f0, f0 + rows) x w (rows <= 32) <-> its part of the
+// tile: a contiguous copy in 16-byte pieces (the last few floats one by
+// one) when the tile's stride is w (w odd) and the global rows are 16-byte
+// aligned; otherwise element by element.  Only the warp's lanes take part,
+// so no CTA barrier is needed around it.
+// Loads go through cp.async (global to shared without a register round
+// trip): the caller waits for them (cp.async.wait_all) before its barrier.
 template <bool IN>
-__device__ void stage_up(float* tile, float* T, long long f0, int rows, int w, int ws) {
+__device__ void stage_warp(float* tile, float* T, long long f0, int rows, int w, int ws,
+                           int lane) {
   float* g = T + f0 * w;
-  if (ws != w || (reinterpret_cast<uintptr_t>(g) & 15) != 0) {
-    stage<float, IN>(tile, T, f0, rows, w, ws);
+  const int n = rows * w;
+  if (ws == w && (reinterpret_cast<uintptr_t>(g) & 15) == 0 &&
+      (reinterpret_cast<uintptr_t>(tile) & 15) == 0) {
+    const int n4 = n >> 2;
+    float4* t4 = reinterpret_cast<float4*>(tile);
+    float4* g4 = reinterpret_cast<float4*>(g);
+    for (int i = lane; i < n4; i += 32) {
+      if (IN) {
+        const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(t4 + i));
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(g4 + i)
+                     : "memory");
+      } else {
+        g4[i] = t4[i];
+      }
+    }
+    if (IN) asm volatile("cp.async.commit_group;\n" ::: "memory");
+    for (int i = 4 * n4 + lane; i < n; i += 32) {
+      if (IN) tile[i] = g[i];
+      else g[i] = tile[i];
+    }
     return;
   }
-  const int n = rows * w, n4 = n >> 2, nt = blockDim.x;
-  float4* t4 = reinterpret_cast<float4*>(tile);
-  float4* g4 = reinterpret_cast<float4*>(g);
-  for (int i = threadIdx.x; i < n4; i += nt) {
-    if (IN) t4[i] = g4[i];
-    else g4[i] = t4[i];
-  }
-  for (int i = 4 * n4 + threadIdx.x; i < n; i += nt) {
-    if (IN) tile[i] = g[i];
-    else g[i] = tile[i];
+  for (int q = lane; q < n; q += 32) {
+    const int r = q / w, c = q - r * w;
+    if (IN) tile[r * ws + c] = g[q];
+    else g[q] = tile[r * ws + c];
   }
 }
 
@@ -425,12 +442,18 @@ conduction_q_up_kernel(int num_faces, int nz, const float* __restrict__ z, float
   UpRow* s_up = reinterpret_cast<UpRow*>(smem_raw + (base + 15) / 16 * 16);
   DownRow* s_dn = reinterpret_cast<DownRow*>(s_up + w);
 
-  grid_coeffs_q<float>(nz, z, dt, ti, rhoc, s_k, s_alpha, s_gamma, s_a, s_b, s_c, &s_misc[0]);
-  __syncthreads();
+  // each warp stages its own 32 facets' profiles first (their loads are in
+  // flight while the coefficients and the elimination are formed)
+  const int t = threadIdx.x, lane = t & 31;
   const long long f0 = (long long)blockIdx.x * nt;
   const int rows = (int)min((long long)nt, (long long)num_faces - f0);
-  // profiles first (their loads are in flight during the recurrence below)
-  stage_up<true>(tile, const_cast<float*>(T_in), f0, rows, w, ws);
+  const int wrow0 = t & ~31;
+  const int wrows = max(0, min(32, rows - wrow0));
+  float* wtile = tile + wrow0 * ws;
+  stage_warp<true>(wtile, const_cast<float*>(T_in), f0 + wrow0, wrows, w, ws, lane);
+  grid_coeffs_q<float>(nz, z, dt, ti, rhoc, s_k, s_alpha, s_gamma, s_a, s_b, s_c, &s_misc[0]);
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+  __syncthreads();
   // the rows' own coefficients, one row per thread (fields apart from the
   // e and rb that thread 0 writes below)
   for (int j = threadIdx.x + 2; j <= nz; j += nt) {
@@ -463,7 +486,6 @@ conduction_q_up_kernel(int num_faces, int nz, const float* __restrict__ z, float
   }
   __syncthreads();
 
-  const int t = threadIdx.x;
   unsigned my_flags = 0;
   if (t < rows) {
     const long long f = f0 + t;
@@ -541,8 +563,9 @@ conduction_q_up_kernel(int num_faces, int nz, const float* __restrict__ z, float
     if (mn < 0.0f) my_flags |= kFlagNegativeOut;
     Fsurf[f] = -s_k[1] * (u1 - T0) / z[1];
   }
-  __syncthreads();
-  stage_up<false>(tile, T_out, f0, rows, w, ws);
+  // the warp writes its own rows back
+  __syncwarp();
+  stage_warp<false>(wtile, T_out, f0 + wrow0, wrows, w, ws, lane);
   if (my_flags) atomicOr(flags, my_flags);
 }
 

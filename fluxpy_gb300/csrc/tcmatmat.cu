@@ -53,10 +53,12 @@ constexpr int kTcRows = 64;        // rows of a phase-B tile
 constexpr int kTcThreads = 256;
 // split mode: the tensor core's FP32 accumulation loses up to ~2^-23 of the
 // running sum per MMA, which over thousands of reduction steps exceeds the
-// split operands' 2^-16 accuracy; every kTcWin chunks (12 MMAs) the window's
-// accumulators are drained into registers and summed there with Kahan
-// compensation
-constexpr int kTcWin = 2;
+// split operands' 2^-16 accuracy; every kTcWin chunks (256 reduction rows,
+// 48 MMAs) the window's accumulators are drained into registers and summed
+// there with Kahan compensation.  At 522k facets and 1,024 columns windows
+// of 2, 4 and 8 chunks gave the same product error (6e-6 of max |F x|
+// against FP64) and took 135, 130 and 127 ms for the split product.
+constexpr int kTcWin = 8;
 constexpr unsigned long long kWaitNs = 2000000000ull;           // 2 s
 
 enum { kModeA = 0, kModeB = 1 };
@@ -211,8 +213,8 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
 // product (the re-tiled panel) and the 64-row tiles for the split one;
 // 256-row tiles (MMA N = 256, two CTAs per SM: 256 TMEM columns each) are
 // the plain product's widest layout.
-// Split mode keeps SEGS x 32 compensated sums per thread (32 for 64-row
-// tiles or slices, 64 for 128-row ones).
+// Split mode keeps SEGS x 32 sums per thread (32 for 64-row tiles or
+// slices, compensated; 64 for 128-row ones, plain FP32).
 // CTAS = CTAs per SM the shape is built for.  The plain products run four
 // (NC = 128, CH = 32, a 3-stage ring of 16 KiB stages): each CTA's loop
 // waits, per chunk, for its copies and for the previous chunk's MMAs, and
@@ -221,18 +223,22 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
 // phase B and 31 ms for phase A, against 53 and 51 ms for one CTA per SM
 // with NC = 256, CH = 64 and a 4-stage ring (the median phase-A group has
 // 62 columns: one or two chunks per work item).  The split products run two
-// CTAs per SM on 64-row tiles / slices (~120 registers per thread) and one
-// on 128-row slices (~225: 64 compensated sums per thread).
+// CTAs per SM: on 64-row tiles / slices with 32 compensated sums per thread
+// (~120 registers), on 128-row ones with 64 plain FP32 sums (128).
 template <int MODE, bool SPLIT, int NR_ = (MODE == kModeA ? 128 : 64)>
 struct TcCfg {
   static constexpr int NR = NR_;
   static constexpr int NC = 128;
   static constexpr int CH = 32;
-  static constexpr int CTAS = SPLIT ? (NR == 64 ? 2 : 1) : (NR >= 256 ? 2 : 4);
-  // threads per CTA: the split products on 128-row tiles / slices run 16
-  // warps, so that each thread keeps 32 compensated sums (as on 64-row
-  // tiles with 8 warps), one CTA per SM
-  static constexpr int THREADS = (SPLIT && NR == 128) ? 512 : 256;
+  // the split products on 128-row tiles / slices sum their drained windows
+  // (256 reduction rows each) in plain FP32: 64 sums per thread leave no
+  // room for compensation at two CTAs of 8 warps per SM.  (With Kahan sums
+  // they needed 16 warps and one CTA per SM: split phase B 146 ms against
+  // 71 ms now at 522k facets and 1,024 columns, with the same product
+  // error.)  The 64-row shapes keep Kahan-compensated sums.
+  static constexpr bool KAHAN = !(SPLIT && NR == 128);
+  static constexpr int CTAS = SPLIT ? 2 : (NR >= 256 ? 2 : 4);
+  static constexpr int THREADS = 256;
   static constexpr int NQ = THREADS / 128;           // warps per TMEM lane quarter
   // phase B: chunks ahead at which a thread loads the source indices of its
   // gathered rows (the index load would otherwise stall the copies of the
@@ -470,9 +476,12 @@ tc_gather_gemm(TcArgs a) {
   // 32 (pc % (NR / 32)) .. + 31)
   const int quarter = warp & 3, pc0 = warp >> 2;
   constexpr int NV = SPLIT ? Cfg::PPW * 32 : 1;       // compensated sums per thread
-  float racc[NV], rcmp[NV];
+  constexpr int NVC = Cfg::KAHAN ? NV : 1;
+  float racc[NV], rcmp[NVC];
 #pragma unroll
-  for (int i = 0; i < NV; i++) { racc[i] = 0.f; rcmp[i] = 0.f; }
+  for (int i = 0; i < NV; i++) racc[i] = 0.f;
+#pragma unroll
+  for (int i = 0; i < NVC; i++) rcmp[i] = 0.f;
   auto piece_col = [&](int pc) {         // TMEM column of piece pc (in a set)
     return (pc / (NR / 32)) * NR + (pc % (NR / 32)) * 32;
   };
@@ -484,7 +493,10 @@ tc_gather_gemm(TcArgs a) {
         tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + set * (Cfg::HALVES * NR) +
                       piece_col(pc0 + Cfg::NQ * k), v);
 #pragma unroll
-        for (int i = 0; i < 32; i++) kahan_add(racc[k * 32 + i], rcmp[k * 32 + i], v[i]);
+        for (int i = 0; i < 32; i++) {
+          if constexpr (Cfg::KAHAN) kahan_add(racc[k * 32 + i], rcmp[k * 32 + i], v[i]);
+          else racc[k * 32 + i] = __fadd_rn(racc[k * 32 + i], v[i]);
+        }
       }
       tc_fence_before();
     }
@@ -773,6 +785,8 @@ bool misaligned(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) !=
 //   warp 1      MMA issuer (lane 0): waits "full", issues, commits "empty"
 //   warps 4..7  epilogue (TMEM lanes 32 (w - 4) ..); in split mode they also
 //               drain each chunk's accumulator set into compensated sums
+//               (a 64-row window; the cp.async kernel drains every kTcWin
+//               32-row chunks)
 // Split mode: NC = 128 columns (one accumulator half, two TMEM sets that
 // alternate by chunk), hi and lo maps for both operands.
 template <bool SPLIT>

@@ -280,7 +280,8 @@ def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_
     (mma.sync kernels).
     residual: how bf16-refine evaluates F (rho B): 'split-bf16' (tensor
     cores, split-BF16 operands hi.hi + lo.hi + hi.lo, FP32 accumulation
-    drained into compensated sums; ~17-bit arithmetic, the convergence test
+    drained every 256 reduction rows into register sums; ~17-bit
+    arithmetic, the convergence test
     keeps a margin for it, _SPLIT_MARGIN) or 'fp32' (FP32 CUDA-core kernels).
     incremental: with 'split-bf16', only the first residual is evaluated in
     full; later ones are updated as R <- R - D + F_bf16 (rho D) with the last

@@ -496,8 +496,10 @@ int fgb_tc_phase_b(const struct fgb_op_desc* d, const void* w_hi, const void* w_
 /* Phase B with the sources stacked in one (num_zrows + N) x K tensor S = [Z; X]
  * (and S_lo for split products), rows gathered by TMA (tile::gather4, four
  * 128-byte lines per request) in a warp-specialised kernel.  Same results as
- * fgb_tc_phase_b; slower on GB300 for these 128-byte row pieces than the
- * cp.async gathers (per-request cost), kept as the TMA variant. */
+ * fgb_tc_phase_b for plain products (split ones drain their FP32 windows
+ * after 64 rows instead of 256: equal to FP32 rounding); slower on GB300 for
+ * these 128-byte row pieces than the cp.async gathers (per-request cost),
+ * kept as the TMA variant. */
 int fgb_tc_phase_b_tma(const struct fgb_op_desc* d, const void* w_hi, const void* w_lo,
                        const void* S_hi, const void* S_lo, float* Y, int K, const float* add,
                        float alpha, unsigned* flags, void* stream);

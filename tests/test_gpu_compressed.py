@@ -285,8 +285,9 @@ def test_split_bf16_product_accuracy(terrain_op, K):
 def test_tma_gather_phase_b_matches_cp_async(terrain_op, K):
     """The TMA variant of phase B (sources stacked as [Z; X], rows gathered
     by tile::gather4 in a warp-specialised kernel) against the cp.async
-    kernel: same MMA order and accumulation windows, identical results,
-    plain and split."""
+    kernel: the same MMA order, identical plain results; the split products
+    drain their accumulators after different windows (64 rows in the TMA
+    variant, 256 in the cp.async kernel), so they agree to FP32 rounding."""
     import ctypes as C
     from fluxpy_gb300 import _lib
     sm, FF = terrain_op
@@ -319,7 +320,12 @@ def test_tma_gather_phase_b_matches_cp_async(terrain_op, K):
                   _lib.ptr(add), -0.25, fl, st)
         FF.check_device_flags()
         assert torch.isfinite(Y_tma).all()
-        assert torch.equal(Y_tma, Y_cp), split
+        if split:
+            # one or two roundings of Y itself (|Y| ~ 1, |alpha F x| ~ 0.1)
+            ref = Y_cp.abs().max().item()
+            assert (Y_tma - Y_cp).abs().max().item() <= 1e-6 * ref
+        else:
+            assert torch.equal(Y_tma, Y_cp)
 
 
 @pytest.mark.parametrize("slice_rows", [128, 64])

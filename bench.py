@@ -60,6 +60,9 @@ def parse():
     p.add_argument("--no-extras", action="store_true", help="skip FP32/e2e/error/CPU legs")
     p.add_argument("--plain-tiles", default="auto", choices=["auto", "64", "128", "256"],
                    help="phase-B tile rows of the plain BF16 product (auto: autotuned)")
+    p.add_argument("--split-plan", default="auto",
+                   choices=["auto", "a64-b64", "a128-b64", "a64-b128", "a128-b128"],
+                   help="phase-A slice / phase-B tile rows of the split product (auto: autotuned)")
     p.add_argument("--facets", type=int, default=522242,
                    help="facets of the conduction workload")
     p.add_argument("--conduction-spinup", type=int, default=300,
@@ -787,6 +790,8 @@ def main():
     tune = FF.autotune_products(args.rhs)
     if args.plain_tiles != "auto":
         FF.product_plan()["plain"] = "b" + args.plain_tiles
+    if args.split_plan != "auto":
+        FF.product_plan()["split"] = args.split_plan
     nf = sm.num_faces
     dirs = replica_directions(terrain, args.rhs, rank)
     E = sm.get_direct_irradiance_batch(F0, dirs, out_dtype=torch.float32)

@@ -44,7 +44,7 @@ __global__ void colmax_absdiff_kernel(const float* __restrict__ Y, const float* 
   __syncthreads();
   for (long long i = blockIdx.x; i < N; i += gridDim.x) {
     for (int c = threadIdx.x; c < K; c += blockDim.x) {
-      float d = fabsf(Y[i * K + c] - B[i * K + c]);
+      float d = fabsf(B ? Y[i * K + c] - B[i * K + c] : Y[i * K + c]);
       if (d != d) d = INFINITY;  // NaN never converges
       unsigned u = __float_as_uint(d);
       if (u > s_max[c]) s_max[c] = u;

@@ -225,10 +225,13 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
 // 62 columns: one or two chunks per work item).  The split products run two
 // CTAs per SM: on 64-row tiles / slices with 32 compensated sums per thread
 // (~120 registers), on 128-row ones with 64 plain FP32 sums (128).
+// right-hand-side columns per CTA of the plain phase A (128 or 256)
+constexpr int kPhaseANC = 128;
+
 template <int MODE, bool SPLIT, int NR_ = (MODE == kModeA ? 128 : 64)>
 struct TcCfg {
   static constexpr int NR = NR_;
-  static constexpr int NC = 128;
+  static constexpr int NC = (MODE == kModeA && !SPLIT) ? kPhaseANC : 128;
   static constexpr int CH = 32;
   // the split products on 128-row tiles / slices sum their drained windows
   // (256 reduction rows each) in plain FP32: 64 sums per thread leave no
@@ -237,7 +240,7 @@ struct TcCfg {
   // 71 ms now at 522k facets and 1,024 columns, with the same product
   // error.)  The 64-row shapes keep Kahan-compensated sums.
   static constexpr bool KAHAN = !(SPLIT && NR == 128);
-  static constexpr int CTAS = SPLIT ? 2 : (NR >= 256 ? 2 : 4);
+  static constexpr int CTAS = SPLIT ? 2 : ((NR >= 256 || NC >= 256) ? 2 : 4);
   static constexpr int THREADS = 256;
   static constexpr int NQ = THREADS / 128;           // warps per TMEM lane quarter
   // phase B: chunks ahead at which a thread loads the source indices of its

@@ -332,10 +332,11 @@ def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_
         r = _to_device(rho, dev, torch.float32)
         rho_d = r if E_is_permuted else FF.permute(r)
         rho_d = rho_d.contiguous()
-    emax = Ep.abs().amax(0)
-    thresh = (rtol * emax).cpu().numpy().astype(np.float32)
-    thresh[thresh == 0] = 0.0
     colmax = torch.zeros(K, dtype=torch.int32, device=dev)
+    _lib.call("fgb_colmax_absdiff", _lib.ptr(Ep), None, N, K, _lib.ptr(colmax), stream)
+    emax_np = _colmax(colmax)            # max |E| per column
+    thresh = (np.float32(rtol) * emax_np).astype(np.float32)
+    thresh[thresh == 0] = 0.0
     Z32 = (torch.empty((max(FF._num_zrows, 1), K), dtype=torch.float32, device=dev) if fp32_z
            else None)
     X32 = torch.empty_like(Ep)
@@ -364,7 +365,7 @@ def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_
         # BF16 sources stacked as [Z; X] (one tensor: TMA gathers in phase B)
         Sb, Zb, Xb = FF.stacked_sources(K, dev)
         work = {"s_hi": Sb}
-        emax_h = np.maximum(emax.cpu().numpy(), 1e-30)
+        emax_h = np.maximum(emax_np, 1e-30)
         if residual == "split-bf16":
             # the computed residual may be smaller than the exact one by the
             # split product's error bound: check against a reduced threshold
@@ -384,7 +385,10 @@ def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_
                 FF.bf16_product(Xb, Z32, Zb, Y, add=R, alpha=1.0, engine=engine)
                 st["bf16_matmats"] += 1
                 R, Y = Y, R
-                res = R.abs().amax(0).cpu().numpy()
+                colmax.zero_()
+                _lib.call("fgb_colmax_absdiff", _lib.ptr(R), None, N, K, _lib.ptr(colmax),
+                          stream)
+                res = _colmax(colmax)
                 FF.check_device_flags()
             else:
                 # residual with the FP32 operator
@@ -409,14 +413,17 @@ def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_
                     break
                 rhs, sweeps = R, inner
             # correction: D <- rhs + F_bf16 (rho D), `sweeps` sweeps from D = rhs
-            D.copy_(rhs)
-            for _ in range(sweeps):
-                _lib.call("fgb_scale_rows_bf16", _lib.ptr(D), _lib.ptr(rho_d), rho_s, _lib.ptr(Xb),
-                          N, K, stream)
+            # (the first sweep reads rhs itself)
+            if sweeps == 0:
+                D.copy_(rhs)
+            for s_ in range(sweeps):
+                src = rhs if s_ == 0 else D
+                _lib.call("fgb_scale_rows_bf16", _lib.ptr(src), _lib.ptr(rho_d), rho_s,
+                          _lib.ptr(Xb), N, K, stream)
                 FF.bf16_product(Xb, Z32, Zb, D, add=rhs, alpha=1.0, engine=engine)
                 st["bf16_matmats"] += 1
             if it == 1:
-                B.copy_(D)
+                B, D = D, B
             else:
                 _lib.call("fgb_axpy_cols", _lib.ptr(B), _lib.ptr(D), None, N, K, stream)
         else:

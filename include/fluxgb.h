@@ -628,6 +628,7 @@ int fgb_scale_rows_f32(const float* B, const float* rho, float rho_scalar, float
                        int K, void* stream);
 int fgb_scale_rows_bf16(const float* B, const float* rho, float rho_scalar, void* X, long long N,
                         int K, void* stream);
+/* colmax[c] = max(colmax[c], max_i |Y - B|) per column (B may be NULL: |Y|). */
 int fgb_colmax_absdiff(const float* Y, const float* B, long long N, int K, unsigned* colmax,
                        void* stream);
 int fgb_residual(const float* Y, const float* B, const float* E, float* R, long long N, int K,

@@ -345,6 +345,7 @@ class fgb_op_desc(C.Structure):
         ("max_group_tiles", C.c_int), ("g_kzp", C.c_void_p), ("g_vtoff", C.c_void_p),
         ("a_woff", C.c_void_p), ("num_work", C.c_longlong), ("panel_rows", C.c_longlong),
         ("tile_rows", C.c_int), ("slice_rows", C.c_int), ("a_witem", C.c_void_p),
+        ("tile_order", C.c_void_p),
     ]
 
 
@@ -355,6 +356,28 @@ ITEM_COLS = 2048
 PANEL_ALIGN = 64
 # Z rows computed per CTA by the tensor-core phase A
 TC_A_ROWS = 128
+
+
+def _hilbert_index(x, y, order=16):
+    """Index along the Hilbert curve of integer points (x, y) in
+    [0, 2^order)^2 (the classic quadrant-by-quadrant construction)."""
+    x = np.array(x, np.int64, copy=True)
+    y = np.array(y, np.int64, copy=True)
+    d = np.zeros_like(x)
+    s = 1 << (order - 1)
+    while s > 0:
+        rx = ((x & s) > 0).astype(np.int64)
+        ry = ((y & s) > 0).astype(np.int64)
+        d += s * s * ((3 * rx) ^ ry)
+        m = ry == 0
+        flip = m & (rx == 1)
+        x[flip] = s - 1 - x[flip]
+        y[flip] = s - 1 - y[flip]
+        t = x[m].copy()
+        x[m] = y[m]
+        y[m] = t
+        s >>= 1
+    return d
 
 
 def _transpose_exact_csr(tcsr, ex_m, ex_n, chunk_nnz=200_000_000):
@@ -1355,10 +1378,31 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         desc.num_tiles = nt2
         desc.panel_rows = total2
         desc.tile_rows = width
-        setattr(self, f"_dev{width}", dict(t_p0=t2, src=src2))
+        order = self._hilbert_tile_order(width, nt2, dev)
+        desc.tile_order = order.data_ptr()
+        setattr(self, f"_dev{width}", dict(t_p0=t2, src=src2, tile_order=order))
         setattr(self, f"_desc{width}", desc)
         self.stats[f"panel_rows_{width}"] = total2
         return w128, lo128
+
+    def _hilbert_tile_order(self, width, ntiles, dev):
+        """The order in which the tensor-core phase B takes its tiles of
+        `width` rows: along a Hilbert curve through the tiles' centroids,
+        projected on the two axes of largest extent (neighbouring tiles
+        gather many of the same source rows; at 522k facets this ran 1 %
+        faster than cluster order, a random order 12 % slower)."""
+        N = self.num_faces
+        P = np.asarray(self.shape_model.P, np.float64)[self._tree.perm]
+        tile = np.arange(N) // width
+        cnt = np.maximum(np.bincount(tile, minlength=ntiles), 1)
+        cent = np.stack([np.bincount(tile, weights=P[:, a], minlength=ntiles) / cnt
+                         for a in range(3)], 1)
+        ext = cent.max(0) - cent.min(0)
+        ax = np.argsort(-ext, kind="stable")[:2]
+        q = ((cent[:, ax] - cent[:, ax].min(0)) / np.maximum(ext[ax], 1e-300) * 65535.0)
+        key = _hilbert_index(q[:, 0].astype(np.int64), q[:, 1].astype(np.int64))
+        order = np.argsort(key, kind="stable").astype(np.int32)
+        return torch.as_tensor(order, device=dev)
 
     def tc_operands256(self):
         """The 256-row phase-B panel ('w256', BF16) of the plain product's

@@ -197,6 +197,8 @@ struct TcArgs {
   // null otherwise
   const __nv_bfloat16* s_hi;
   const __nv_bfloat16* s_lo;
+  // phase B: the tile of work unit u is tile_order[u] (null: u)
+  const int* tile_order;
 };
 
 __device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
@@ -320,9 +322,10 @@ tc_gather_gemm(TcArgs a) {
   long long xrow0 = 0;                // phase A: X row of reduction row 0
   bool excl = true;
   if (MODE == kModeB) {
-    r_first = a.t_p0[unit];
-    r_end = a.t_p0[unit + 1];
-    out_row0 = unit * NR;
+    const long long tile = a.tile_order ? (long long)a.tile_order[unit] : unit;
+    r_first = a.t_p0[tile];
+    r_end = a.t_p0[tile + 1];
+    out_row0 = tile * NR;
     out_rows = (int)min((long long)NR, a.N - out_row0);
     if (((r_end - r_first) % 64) != 0) {
       // not a whole number of chunks: flagged, and the tile is left empty
@@ -1212,6 +1215,7 @@ int fgb_tc_phase_b(const struct fgb_op_desc* d, const void* w_hi, const void* w_
   if (d->num_tiles <= 0) return FGB_OK;
   fgb::TcArgs a{};
   a.t_p0 = d->t_p0; a.src = d->src; a.N = d->N; a.num_zrows = d->num_zrows;
+  a.tile_order = d->tile_order;
 
   a.w_hi = static_cast<const __nv_bfloat16*>(w_hi);
   a.w_lo = static_cast<const __nv_bfloat16*>(w_lo);

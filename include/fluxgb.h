@@ -418,6 +418,10 @@ struct fgb_op_desc {
                            tensor-core phase-A work slice (the i with
                            a_woff[i] <= slice < a_woff[i+1]); null: found by
                            binary search over a_woff */
+  const int* tile_order; /* optional, num_tiles entries (tensor-core phase B):
+                           the order in which the CTAs take the tiles (a
+                           permutation of 0 .. num_tiles - 1); null: in
+                           order */
 };
 /*
  * y = F x (or y = add + alpha F x), vectors in cluster order.  Replaces

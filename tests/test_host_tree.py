@@ -155,3 +155,19 @@ def test_host_tree_equals_recursive_restatement(name, P, ndim, parts, tol, min_s
         cols = list(op.get_col_inds_for_row(int(f)))
         assert all(np.array_equal(c, tree.ref_indices(op._cols[b])) for c, b in zip(cols, want))
         assert np.array_equal(np.sort(np.concatenate(cols)), np.arange(P.shape[0]))
+
+
+def test_hilbert_index_visits_the_grid_along_the_curve():
+    """The Hilbert index of the tile order: order-2 curve visits the 4 x 4
+    grid cell by cell (each step to an edge neighbour), order-4 curve is a
+    bijection onto 0 .. 255 with unit steps."""
+    from fluxpy_gb300.compressed_form_factors import _hilbert_index
+    x = np.array([0, 1, 1, 0, 0, 0, 1, 1, 2, 2, 3, 3, 3, 2, 2, 3])
+    y = np.array([0, 0, 1, 1, 2, 3, 3, 2, 2, 3, 3, 2, 1, 1, 0, 0])
+    assert np.array_equal(_hilbert_index(x, y, order=2), np.arange(16))
+    gx, gy = np.meshgrid(np.arange(16), np.arange(16), indexing="ij")
+    d = _hilbert_index(gx.ravel(), gy.ravel(), order=4)
+    assert np.array_equal(np.sort(d), np.arange(256))
+    o = np.argsort(d)
+    steps = np.abs(np.diff(gx.ravel()[o])) + np.abs(np.diff(gy.ravel()[o]))
+    assert np.all(steps == 1)

@@ -107,12 +107,10 @@ __device__ void grid_coeffs_t(int nz, const R* z, R dt, const R* ti, const R* rh
 constexpr int kMaxThreads = 128;
 constexpr size_t kSmemBudget = 227 * 1024;  // the per-CTA opt-in maximum
 
-// Shared layout, all of element type R: 7 coefficient arrays of nz+1 (k,
-// alpha, gamma, a, b, c, misc), then the staged temperature tile, nt rows
-// of stride ws = (nz+1)|1 (odd, so that the threads of a warp reading
-// element i of their own rows hit distinct banks).  The sweep's own arrays
-// (u, gam) are per-thread local arrays: the shared layout stays small, so
-// that many CTAs (warps) share an SM and hide the sweep's dependent chain.
+// The staged temperature tile: nt rows of stride ws = (nz+1)|1 (odd, so
+// that the threads of a warp reading element i of their own rows hit
+// distinct banks), after 7 coefficient arrays of nz+1 (k, alpha, gamma, a,
+// b, c, misc).
 __host__ __device__ inline int tile_stride(int nz) { return (nz + 1) | 1; }
 
 // Shared layout: the coefficients, the tile (nt rows of stride ws), the
@@ -250,7 +248,7 @@ __device__ bool thomas_cn(int nz, R* Trow, R r1, R b1, R rhs_bottom, const Layer
 }
 
 // One step of the radiative-flux boundary problem for every facet.
-template <class R, int NZMAX>
+template <class R>
 __global__ void __launch_bounds__(kMaxThreads, 1)
 conduction_q_kernel(int num_faces, int nz, const R* __restrict__ z, R dt,
                     const R* __restrict__ Qn, const R* __restrict__ Qnp1,
@@ -585,7 +583,7 @@ int launch_q_up(int num_faces, int nz, const float* z, float dt, const float* Qn
 }
 
 // One step of the prescribed-surface-temperature problem (conductionT.c).
-template <class R, int NZMAX>
+template <class R>
 __global__ void __launch_bounds__(kMaxThreads)
 conduction_t_kernel(int num_faces, int nz, const R* __restrict__ z, R dt,
                     const R* __restrict__ Tsurf, const R* __restrict__ Tsurfp1,
@@ -641,13 +639,13 @@ conduction_t_kernel(int num_faces, int nz, const R* __restrict__ z, R dt,
   if (my_flags) atomicOr(flags, my_flags);
 }
 
-template <class R, int NZMAX>
+template <class R>
 int launch_q(int num_faces, int nz, const R* z, R dt, const R* Qn, const R* Qnp1,
              const R* T_in, R* T_out, const R* ti, const R* rhoc, const R* emiss,
              const R* Fgeotherm, R* Fsurf, unsigned* flags, cudaStream_t s) {
   const int nt = cond_threads<R>(nz);
   const size_t sm = cond_smem<R>(nz, nt);
-  auto k = conduction_q_kernel<R, NZMAX>;
+  auto k = conduction_q_kernel<R>;
   FGB_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   const unsigned grid = (unsigned)((num_faces + nt - 1) / nt);
   k<<<grid, nt, sm, s>>>(num_faces, nz, z, dt, Qn, Qnp1, T_in, T_out, ti, rhoc, emiss,
@@ -656,13 +654,13 @@ int launch_q(int num_faces, int nz, const R* z, R dt, const R* Qn, const R* Qnp1
   return FGB_OK;
 }
 
-template <class R, int NZMAX>
+template <class R>
 int launch_t(int num_faces, int nz, const R* z, R dt, const R* Ts, const R* Tsp1,
              const R* T_in, R* T_out, const R* ti, const R* rhoc, const R* Fgeotherm,
              R* Fsurf, unsigned* flags, cudaStream_t s) {
   const int nt = cond_threads<R>(nz);
   const size_t sm = cond_smem<R>(nz, nt);
-  auto k = conduction_t_kernel<R, NZMAX>;
+  auto k = conduction_t_kernel<R>;
   FGB_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   const unsigned grid = (unsigned)((num_faces + nt - 1) / nt);
   k<<<grid, nt, sm, s>>>(num_faces, nz, z, dt, Ts, Tsp1, T_in, T_out, ti, rhoc, Fgeotherm,
@@ -698,10 +696,7 @@ int dispatch_q(int num_faces, int nz, const R* z, R dt, const R* Qn, const R* Qn
                        reinterpret_cast<const float*>(emiss),
                        reinterpret_cast<const float*>(Fgeotherm), reinterpret_cast<float*>(Fsurf),
                        flags, s);
-  if (nz <= 47) return launch_q<R, 47>(num_faces, nz, z, dt, Qn, Qnp1, T_in, T_out, ti, rhoc, emiss, Fgeotherm, Fsurf, flags, s);
-  if (nz <= 63) return launch_q<R, 63>(num_faces, nz, z, dt, Qn, Qnp1, T_in, T_out, ti, rhoc, emiss, Fgeotherm, Fsurf, flags, s);
-  if (nz <= 127) return launch_q<R, 127>(num_faces, nz, z, dt, Qn, Qnp1, T_in, T_out, ti, rhoc, emiss, Fgeotherm, Fsurf, flags, s);
-  return launch_q<R, 255>(num_faces, nz, z, dt, Qn, Qnp1, T_in, T_out, ti, rhoc, emiss, Fgeotherm, Fsurf, flags, s);
+  return launch_q<R>(num_faces, nz, z, dt, Qn, Qnp1, T_in, T_out, ti, rhoc, emiss, Fgeotherm, Fsurf, flags, s);
 }
 
 template <class R>
@@ -712,10 +707,7 @@ int dispatch_t(int num_faces, int nz, const R* z, R dt, const R* Ts, const R* Ts
   if (st) return st;
   if (num_faces == 0) return FGB_OK;
   cudaStream_t s = as_stream(stream);
-  if (nz <= 47) return launch_t<R, 47>(num_faces, nz, z, dt, Ts, Tsp1, T_in, T_out, ti, rhoc, Fgeotherm, Fsurf, flags, s);
-  if (nz <= 63) return launch_t<R, 63>(num_faces, nz, z, dt, Ts, Tsp1, T_in, T_out, ti, rhoc, Fgeotherm, Fsurf, flags, s);
-  if (nz <= 127) return launch_t<R, 127>(num_faces, nz, z, dt, Ts, Tsp1, T_in, T_out, ti, rhoc, Fgeotherm, Fsurf, flags, s);
-  return launch_t<R, 255>(num_faces, nz, z, dt, Ts, Tsp1, T_in, T_out, ti, rhoc, Fgeotherm, Fsurf, flags, s);
+  return launch_t<R>(num_faces, nz, z, dt, Ts, Tsp1, T_in, T_out, ti, rhoc, Fgeotherm, Fsurf, flags, s);
 }
 
 }  // namespace

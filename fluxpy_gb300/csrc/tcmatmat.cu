@@ -1203,7 +1203,8 @@ int fgb_tc_phase_b(const struct fgb_op_desc* d, const void* w_hi, const void* w_
   if (!d || !flags) { fgb::set_error("null operator or flags"); return FGB_BAD_ARG; }
   if (K < 8 || (K % 8) != 0) { fgb::set_error("K must be a positive multiple of 8"); return FGB_BAD_ARG; }
   const bool split = w_lo != nullptr;
-  if (split != (X_lo != nullptr) || split != (Z_lo != nullptr)) {
+  // (an operator without low-rank blocks has no Z: its pointers may be null)
+  if (split != (X_lo != nullptr) || (d->num_zrows > 0 && split != (Z_lo != nullptr))) {
     fgb::set_error("split operands must come in pairs");
     return FGB_BAD_ARG;
   }

@@ -119,6 +119,31 @@ def test_compressed_lowrank_error_vs_exact():
     assert (Yb[:, :4].double() - Y64).abs().max().item() / ref < 2e-2
 
 
+def test_batched_steady_state_matches_reference_golden(ffref):
+    """compute_steady_state_temp with method='batched-bf16' (BF16+refine
+    solves, split-BF16 tensor-core infrared product) on the compressed
+    operator of the crater, against the reference's own T for three sun
+    directions (tests/golden/ffref.npz)."""
+    sm = gshape.EmbreeTrimeshShapeModel(ffref["crater_V"], ffref["crater_F"])
+    FF = CompressedFormFactorMatrix(sm, tol=1e-5, min_size=1024, dtype=np.float32,
+                                    RootBlock=FormFactorOctreeBlock)
+    E2 = ffref["crater_E2"]
+    T2 = compute_steady_state_temp(FF, E2, 0.12, 0.95, method="batched-bf16")
+    assert T2.shape == ffref["crater_T2"].shape
+    # (measured on GB300: 1.6e-4 K; the solves stop at 1e-5 relative)
+    assert np.max(np.abs(T2 - ffref["crater_T2"])) < 1e-3
+    # the same with the FP32 batched method (CUDA-core infrared product)
+    T3 = compute_steady_state_temp(FF, E2, 0.12, 0.95, method="batched-fp32")
+    assert np.max(np.abs(T3 - ffref["crater_T2"])) < 1e-3
+    # an operator without low-rank blocks (tol = 0: no Z rows) through the
+    # same tensor-core path
+    FF0 = CompressedFormFactorMatrix(sm, tol=0, min_size=1024, dtype=np.float32,
+                                     RootBlock=FormFactorOctreeBlock)
+    assert FF0._num_zrows == 0
+    T0 = compute_steady_state_temp(FF0, E2, 0.12, 0.95, method="batched-bf16")
+    assert np.max(np.abs(T0 - ffref["crater_T2"])) < 1e-3
+
+
 def test_solve_matches_reference_golden(ffref):
     sm = gshape.EmbreeTrimeshShapeModel(ffref["crater_V"], ffref["crater_F"])
     FF = get_form_factor_matrix(sm)

@@ -1532,9 +1532,12 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
         sl = buf("s_lo", (nz + N, K), torch.bfloat16)
         zh, xh = sh[:nz], sh[nz:]
         zl, xl = sl[:nz], sl[nz:]
-        tc = self.tc_operands(split=True)
-        flags = _lib.ptr(self.device_flags())
         plan = self.product_plan()["split"]
+        # the operands this plan reads (the 64-row parts only for b64 tiles)
+        tc = self.tc_operands()
+        if "vt_lo" not in tc or (not plan.endswith("b128") and "w_lo" not in tc):
+            tc = self.tc_operands(split=True)
+        flags = _lib.ptr(self.device_flags())
         _lib.call("fgb_split_bf16", _lib.ptr(X), _lib.ptr(xh), _lib.ptr(xl), N * K, st)
         if self._num_zrows > 0:
             # phase A writes the hi / lo BF16 parts of Z directly: 64-row work
@@ -1630,8 +1633,13 @@ class CompressedFormFactorMatrix(scipy.sparse.linalg.LinearOperator):
                 for k, v in table.items() if any(t is not None for t in v.values())}
         plan.update(old)
         plan.update(best)
+        # give back the memory of the layouts not chosen (built again on
+        # request)
         if not plan["split"].endswith("b128"):
-            tc.pop("w128_lo", None)      # not used: give the memory back
+            tc.pop("w128_lo", None)
+        elif plan["plain"] != "b64":
+            tc.pop("w_hi", None)         # the 64-row BF16 parts (2 x 20 GB at 522k)
+            tc.pop("w_lo", None)
         if plan["plain"] != "b256":
             tc.pop("w256", None)
         del X, Y, Sb, Zb, Xb, work

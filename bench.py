@@ -823,12 +823,16 @@ def main():
     torch.cuda.nvtx.range_push("timed_steps")
     ev0.record(stream)
     stats = []
+    marks = []
     for _ in range(args.steps):
         B, st = step()
         stats.append(st)
+        marks.append(torch.cuda.Event(enable_timing=True))
+        marks[-1].record(stream)
     ev1.record(stream)
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_pop()
+    step_ms = [a.elapsed_time(b) for a, b in zip([ev0] + marks[:-1], marks)]
     launches = _lib.launch_count() - launches0
     clk = clocks.stop()
     ms_total = job_time_ms(ev0.elapsed_time(ev1), dist, dev)
@@ -850,6 +854,7 @@ def main():
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16",
         "data": "synthetic", "config": _config(args, nf), "clocks": clk,
         "gpu_launches": int(launches),
+        "ms_each_step": [round(t, 2) for t in step_ms],
         "solver": {"outer": [s["outer"] for s in stats], "bf16_matmats": stats[-1]["bf16_matmats"],
                    "split_bf16_matmats": stats[-1].get("split_matmats", 0),
                    "fp32_matmats": stats[-1]["fp32_matmats"], "chunks": stats[-1].get("chunks", 1),
@@ -1086,7 +1091,10 @@ def measure_extras(args, FF, sm, E, Ep, B, stats, dev):
     torch.cuda.synchronize()
     t_e2e = (time.perf_counter() - t0) / reps
     out["e2e"] = {"value": K / t_e2e, "unit": "solves/s", "h2d_bytes_per_step": N * K * 4,
-                  "d2h_bytes_per_step": N * K * 4, "ms_per_step": t_e2e * 1e3}
+                  "d2h_bytes_per_step": N * K * 4, "ms_per_step": t_e2e * 1e3,
+                  "note": "solve_radiosity(FF, E_host, 0.12, method='batched-bf16', out=B_host),"
+                          " pinned host buffers; B is copied to B_host on a side stream while"
+                          " the last residual check runs"}
     del E_host, B_host, Bh
     torch.cuda.empty_cache()
     # ---- dominant kernels, timed alone with CUDA events, on the column

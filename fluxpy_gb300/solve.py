@@ -118,7 +118,9 @@ def solve_radiosity(FF, E, rho=1, albedo_placement='right', method='jacobi', tol
     an array or tensor of E's shape) receives B instead of a new array, so
     that a caller who solves repeatedly from pinned host memory keeps the
     device-to-host copy at full speed without pinning a new buffer per
-    call."""
+    call.  With 'batched-bf16' and a pinned float32 destination (``out``, or
+    the pinned result made for a pinned E) the copy of the accepted B runs
+    during the residual check that accepts it."""
     if method in ('batched-fp32', 'batched-bf16'):
         return _solve_batched_public(FF, E, rho, albedo_placement, method, rtol, out)
     if out is not None:
@@ -157,6 +159,14 @@ def _solve_batched_public(FF, E, rho, placement, method, rtol, out=None):
         raise ValueError("batched solves use right albedo placement")
     dev = _lib.require_cuda()
     host_in = not (isinstance(E, torch.Tensor) and E.is_cuda)
+    dst = None
+    if out is not None:
+        dst = out if isinstance(out, torch.Tensor) else torch.from_numpy(out)
+        eshape = tuple(E.shape) if isinstance(E, torch.Tensor) else np.shape(E)
+        if tuple(dst.shape) != eshape:
+            raise ValueError(f"out has shape {tuple(dst.shape)}, B has {eshape}")
+    elif host_in and isinstance(E, torch.Tensor):
+        dst = torch.empty(E.shape, dtype=torch.float32, pin_memory=E.is_pinned())
     if isinstance(E, torch.Tensor):
         E_d = E.to(dev, torch.float32, non_blocking=True)
     else:
@@ -164,23 +174,21 @@ def _solve_batched_public(FF, E, rho, placement, method, rtol, out=None):
     vec = E_d.ndim == 1
     if vec:
         E_d = E_d.reshape(-1, 1)
+    # a pinned float32 destination receives B from the solver itself, the
+    # copy overlapping the last residual check
+    early = (dst is not None and not vec and method == "batched-bf16" and not dst.is_cuda
+             and dst.dtype == torch.float32 and dst.is_contiguous() and dst.is_pinned())
     st = {}
     B = solve_radiosity_batched(FF, E_d, rho, rtol=rtol,
                                 precision="fp32" if method == "batched-fp32" else "bf16-refine",
-                                stats=st)
+                                stats=st, host_out=dst if early else None)
     if vec:
         B = B.reshape(-1)
-    if out is not None:
-        if tuple(out.shape) != tuple(B.shape):
-            raise ValueError(f"out has shape {tuple(out.shape)}, B has {tuple(B.shape)}")
-        dst = out if isinstance(out, torch.Tensor) else torch.from_numpy(out)
-        dst.copy_(B)
-        return out, st["outer"]
+    if dst is not None:
+        if not st.get("host_out"):
+            dst.copy_(B)
+        return (out if out is not None else dst), st["outer"]
     if host_in:
-        if isinstance(E, torch.Tensor):
-            out = torch.empty(B.shape, dtype=torch.float32, pin_memory=E.is_pinned())
-            out.copy_(B)
-            return out, st["outer"]
         return B.cpu().numpy(), st["outer"]
     return B, st["outer"]
 
@@ -231,6 +239,66 @@ def _colmax(t):
     return t.view(torch.int32).cpu().numpy().view(np.float32)
 
 
+_COPY_STREAMS = {}
+
+
+class _EarlyCopy:
+    """Device-to-host copy of each candidate solution, on a side stream.
+
+    The refinement updates B before the residual check that accepts it (the
+    incremental residual update, one BF16 product).  ``offer(B)`` puts B into
+    facet order on the solver's stream and copies it to the pinned host
+    buffer ``dst`` on a side stream, so the copy runs during that check.
+    ``fence()`` makes the solver's stream wait for the copy in flight (the
+    facet-order buffer it reads may then be released) and withdraws the
+    offer; the solver calls it before it changes B.  When the check accepts the
+    offered B, ``result()`` waits for the copy and returns B in facet order
+    (the same gather as ``unpermute``)."""
+
+    def __init__(self, FF, dst: torch.Tensor):
+        self.FF, self.dst = FF, dst
+        dev = torch.cuda.current_device()
+        if dev not in _COPY_STREAMS:
+            _COPY_STREAMS[dev] = torch.cuda.Stream()
+        self.stream = _COPY_STREAMS[dev]
+        self.Bu = None
+        self.src = None
+        self.done = None
+        self.copies = 0
+
+    def fence(self):
+        if self.done is not None:
+            torch.cuda.current_stream().wait_event(self.done)
+            self.done = None
+            self.src = None
+
+    def offer(self, Bp: torch.Tensor):
+        self.fence()
+        main = torch.cuda.current_stream()
+        # allocated and written on the solver's stream, read by the side
+        # stream; released only after the solver's stream waited for it
+        self.Bu = self.FF.unpermute(Bp)
+        ready = torch.cuda.Event()
+        ready.record(main)
+        self.stream.wait_event(ready)
+        with torch.cuda.stream(self.stream):
+            self.dst.copy_(self.Bu, non_blocking=True)
+        self.done = torch.cuda.Event()
+        self.done.record(self.stream)
+        self.src = Bp
+        self.copies += 1
+
+    def result(self, Bp: torch.Tensor):
+        """B in facet order with ``dst`` filled, or None if the last offer
+        was not ``Bp``."""
+        if self.src is not Bp or self.done is None:
+            self.fence()
+            return None
+        self.done.synchronize()
+        torch.cuda.current_stream().wait_event(self.done)
+        return self.Bu
+
+
 # Split-BF16 residual: the operands' hi + lo parts carry ~17 significant
 # bits (|v - hi - lo| <= 2^-18 |v|), so the product behaves like FP32
 # arithmetic with 7 fewer bits: measured within 1e-5 of max |F x| against
@@ -261,7 +329,7 @@ def _auto_chunk(FF, N, K, fp32_z=True):
 def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_iter=200,
                             inner=1, E_is_permuted=False, return_permuted=False, stats=None,
                             chunk=None, inner0=2, engine="tc", residual="split-bf16",
-                            incremental=True):
+                            incremental=True, host_out=None):
     """Right-placement radiosity solve for K sun directions at once.
 
     FF: CompressedFormFactorMatrix; E: (N, K) device tensor (facet order, or
@@ -286,6 +354,11 @@ def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_
     incremental: with 'split-bf16', only the first residual is evaluated in
     full; later ones are updated as R <- R - D + F_bf16 (rho D) with the last
     (small) correction D, one BF16 product instead of a split one.
+    host_out: a pinned host tensor of E's shape (bf16-refine, facet order,
+    one column block, K a multiple of 8): every updated B is copied into it
+    on a side stream while its residual is checked, so the copy of the
+    accepted B overlaps the last check; on return it holds B
+    (``stats['host_out']`` is True).
     Returns B (N, K) fp32; fills `stats` (iterations, matmats, residuals).
     """
     dev = E.device
@@ -359,6 +432,13 @@ def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_
         else:
             raise NoConvergence("FP32 Jacobi did not converge")
     elif precision == "bf16-refine":
+        early = None
+        if host_out is not None and not return_permuted:
+            if (tuple(host_out.shape) != (N, K) or host_out.dtype != torch.float32
+                    or not host_out.is_contiguous() or not host_out.is_pinned()):
+                raise ValueError("host_out must be a contiguous pinned float32 tensor of "
+                                 f"shape {(N, K)}")
+            early = _EarlyCopy(FF, host_out)
         B = torch.empty_like(Ep)
         R = torch.empty_like(Ep)
         D = torch.empty_like(Ep)
@@ -425,9 +505,21 @@ def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_
             if it == 1:
                 B, D = D, B
             else:
+                if early is not None:
+                    early.fence()
                 _lib.call("fgb_axpy_cols", _lib.ptr(B), _lib.ptr(D), None, N, K, stream)
+                if early is not None:
+                    early.offer(B)
         else:
+            if early is not None:
+                early.fence()
             raise NoConvergence("refinement did not converge")
+        if early is not None:
+            Bu = early.result(B)
+            st["host_out"] = Bu is not None
+            st["host_out_copies"] = early.copies
+            if Bu is not None:
+                return Bu
     else:
         raise ValueError(precision)
     if return_permuted:

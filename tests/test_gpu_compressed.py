@@ -231,6 +231,29 @@ def test_public_batched_solve_host_buffers():
         # one column as a vector
         b, _ = solve_radiosity(FF, E[:, 3].cpu().numpy(), 0.12, method=method)
         assert b.shape == (sm.num_faces,)
+    # the side-stream copy of each candidate B: the host buffer and the
+    # returned B equal a solve without it, also when some copies are of
+    # candidates that the next check rejects (one first sweep, no correction
+    # sweeps and rho = 0.5: more outer iterations)
+    copies = []
+    for inner0, inner, rho in ((2, 1, 0.12), (1, 0, 0.5)):
+        st0, st1 = {}, {}
+        Bd = solve_radiosity_batched(FF, E, rho, inner0=inner0, inner=inner, stats=st0)
+        hb = torch.full(E.shape, float("nan"), pin_memory=True)
+        B1 = solve_radiosity_batched(FF, E, rho, inner0=inner0, inner=inner, stats=st1,
+                                     host_out=hb)
+        torch.cuda.synchronize()
+        assert st1["outer"] == st0["outer"] and torch.equal(B1, Bd)
+        # a copy is offered after each correction; the one of the accepted B
+        # fills the buffer (none when the first residual check accepts)
+        assert st1["host_out_copies"] == st1["outer"] - 1
+        assert st1["host_out"] == (st1["outer"] >= 2)
+        if st1["host_out"]:
+            assert torch.equal(hb, Bd.cpu())
+        copies.append(st1["host_out_copies"])
+    assert max(copies) >= 2
+    with pytest.raises(ValueError, match="host_out"):
+        solve_radiosity_batched(FF, E, 0.12, host_out=torch.empty(E.shape))
     with pytest.raises(ValueError, match="shape"):
         solve_radiosity(FF, Ep, 0.12, method="batched-bf16", out=torch.empty(3, 3))
     with pytest.raises(ValueError, match="batched methods only"):

@@ -89,10 +89,10 @@ def _device_operator(FF, dev, dtype):
     raise TypeError(f"unsupported form factor operator: {type(FF)}")
 
 
-def _to_device(x, dev, dtype):
+def _to_device(x, dev, dtype: torch.dtype):
     if isinstance(x, torch.Tensor):
         return x.to(dev, dtype)
-    return torch.as_tensor(np.asarray(x, dtype=dtype), device=dev)
+    return torch.as_tensor(np.asarray(x), device=dev).to(dtype)
 
 
 def _rho_vec(rho, E_d):
@@ -185,7 +185,7 @@ def _solve_batched_public(FF, E, rho, placement, method, rtol, out=None):
     if vec:
         B = B.reshape(-1)
     if dst is not None:
-        if not st.get("host_out"):
+        if not early:
             dst.copy_(B)
         return (out if out is not None else dst), st["outer"]
     if host_in:
@@ -309,6 +309,9 @@ class _EarlyCopy:
 _SPLIT_MARGIN = 0.3
 
 
+_MAX_BLOCK_COLUMNS = 8192
+
+
 def _auto_chunk(FF, N, K, fp32_z=True):
     free, _ = torch.cuda.mem_get_info()
     # memory held by the caching allocator but not in use is available too
@@ -318,7 +321,9 @@ def _auto_chunk(FF, N, K, fp32_z=True):
     # (+ the unpermuted result); a fixed reserve for the allocator's slack
     per_col = N * (7 * 4 + 2 * 2) + max(FF._num_zrows, 1) * (8 if fp32_z else 4)
     c = int(0.85 * max(free - (6 << 30), 0) / per_col) // 8 * 8
-    c = max(8, min(K, c))
+    # the per-column reductions (colmax, residual) keep one word per column
+    # in shared memory: at most _MAX_BLOCK_COLUMNS columns per block
+    c = max(8, min(K, c, _MAX_BLOCK_COLUMNS))
     if c < K:
         # equal chunks (a narrow last chunk runs the products at low width)
         n = -(-K // c)
@@ -354,15 +359,47 @@ def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_
     incremental: with 'split-bf16', only the first residual is evaluated in
     full; later ones are updated as R <- R - D + F_bf16 (rho D) with the last
     (small) correction D, one BF16 product instead of a split one.
-    host_out: a pinned host tensor of E's shape (bf16-refine, facet order,
-    one column block, K a multiple of 8): every updated B is copied into it
-    on a side stream while its residual is checked, so the copy of the
-    accepted B overlaps the last check; on return it holds B
-    (``stats['host_out']`` is True).
+    chunk: columns per block (default: what fits in free device memory);
+    the columns are independent, and blocks hold at most 8,192 of them.
+    K = 0 returns an empty (N, 0) result.
+    host_out: a contiguous pinned float32 host tensor of E's shape that
+    holds B on return (facet order; not with return_permuted).  For
+    bf16-refine in one column block with K a multiple of 8, every updated B
+    is copied into it on a side stream while its residual is checked, so the
+    copy of the accepted B overlaps the last check
+    (``stats['host_out_overlapped']``); otherwise B is copied after the solve.
     Returns B (N, K) fp32; fills `stats` (iterations, matmats, residuals).
     """
+    if host_out is None:
+        return _solve_batched(FF, E, rho, rtol, precision, max_iter, inner, E_is_permuted,
+                              return_permuted, stats, chunk, inner0, engine, residual,
+                              incremental)
+    if return_permuted:
+        raise ValueError("host_out receives B in facet order: not with return_permuted")
+    if (not isinstance(host_out, torch.Tensor) or host_out.is_cuda
+            or tuple(host_out.shape) != tuple(E.shape) or host_out.dtype != torch.float32
+            or not host_out.is_contiguous() or not host_out.is_pinned()):
+        raise ValueError("host_out must be a contiguous pinned float32 host tensor of shape "
+                         f"{tuple(E.shape)}")
+    st = stats if stats is not None else {}
+    B = _solve_batched(FF, E, rho, rtol, precision, max_iter, inner, E_is_permuted, False, st,
+                       chunk, inner0, engine, residual, incremental, host_out)
+    if not st.get("host_out_overlapped"):
+        host_out.copy_(B)
+    return B
+
+
+def _solve_batched(FF, E, rho, rtol, precision, max_iter, inner, E_is_permuted,
+                   return_permuted, stats, chunk, inner0, engine, residual, incremental,
+                   host_out=None):
     dev = E.device
     N, K0 = E.shape
+    if K0 == 0:
+        if stats is not None:
+            stats.update(outer=0, fp32_matmats=0, bf16_matmats=0)
+        return torch.empty((N, 0), dtype=torch.float32, device=dev)
+    if chunk is not None:
+        chunk = max(1, min(int(chunk), _MAX_BLOCK_COLUMNS))
     # the tensor-core products write Z directly in BF16; FP32 Z is needed by
     # the CUDA-core / mma.sync products only
     fp32_z = precision == "fp32" or residual == "fp32" or engine != "tc"
@@ -375,11 +412,10 @@ def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_
         agg = {}
         for c0 in range(0, K0, chunk):
             st = {}
-            parts.append(solve_radiosity_batched(FF, E[:, c0:c0 + chunk].contiguous(), rho, rtol,
-                                                 precision, max_iter, inner, E_is_permuted,
-                                                 return_permuted, st, chunk=chunk,
-                                                 inner0=inner0, engine=engine,
-                                                 residual=residual, incremental=incremental))
+            parts.append(_solve_batched(FF, E[:, c0:c0 + chunk].contiguous(), rho, rtol,
+                                        precision, max_iter, inner, E_is_permuted,
+                                        return_permuted, st, chunk, inner0, engine, residual,
+                                        incremental))
             for k_, v_ in st.items():
                 if isinstance(v_, (int, float)) and k_ != "residual":
                     agg[k_] = agg.get(k_, 0) + v_
@@ -390,9 +426,11 @@ def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_
     if precision == "bf16-refine" and K0 % 8:
         pad = 8 - K0 % 8
         E = torch.cat([E, torch.zeros((N, pad), dtype=E.dtype, device=dev)], 1)
-        B = solve_radiosity_batched(FF, E, rho, rtol, precision, max_iter, inner, E_is_permuted,
-                                    return_permuted, stats, chunk=chunk, inner0=inner0,
-                                    engine=engine, residual=residual, incremental=incremental)
+        # one block of the padded width (a narrower chunk would split it and
+        # pad each part again)
+        B = _solve_batched(FF, E, rho, rtol, precision, max_iter, inner, E_is_permuted,
+                           return_permuted, stats, K0 + pad, inner0, engine, residual,
+                           incremental)
         return B[:, :K0].contiguous()
     K = K0
     stream = _lib.stream_handle()
@@ -432,13 +470,7 @@ def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_
         else:
             raise NoConvergence("FP32 Jacobi did not converge")
     elif precision == "bf16-refine":
-        early = None
-        if host_out is not None and not return_permuted:
-            if (tuple(host_out.shape) != (N, K) or host_out.dtype != torch.float32
-                    or not host_out.is_contiguous() or not host_out.is_pinned()):
-                raise ValueError("host_out must be a contiguous pinned float32 tensor of "
-                                 f"shape {(N, K)}")
-            early = _EarlyCopy(FF, host_out)
+        early = _EarlyCopy(FF, host_out) if host_out is not None else None
         B = torch.empty_like(Ep)
         R = torch.empty_like(Ep)
         D = torch.empty_like(Ep)
@@ -516,7 +548,7 @@ def solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision="bf16-refine", max_
             raise NoConvergence("refinement did not converge")
         if early is not None:
             Bu = early.result(B)
-            st["host_out"] = Bu is not None
+            st["host_out_overlapped"] = Bu is not None
             st["host_out_copies"] = early.copies
             if Bu is not None:
                 return Bu

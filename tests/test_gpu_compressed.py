@@ -166,6 +166,30 @@ def test_solve_matches_reference_golden(ffref):
         solve_radiosity(FF, E, 0.12, "right", "cg")
 
 
+def test_solve_per_facet_albedo_matches_oracle(ffref):
+    """solve_radiosity with one albedo per facet (numpy array), right and
+    left placement, on the crater's exact form factors: the oracle's Jacobi
+    iteration count and solution (src/flux/solve.py:36-45 multiplies
+    rho * B elementwise)."""
+    from oracle import solve as osolve
+    sm = gshape.EmbreeTrimeshShapeModel(ffref["crater_V"], ffref["crater_F"])
+    FF = get_form_factor_matrix(sm)
+    E = ffref["crater_E"]
+    rho = np.random.default_rng(8).uniform(0.05, 0.4, sm.num_faces)
+    for placement in ("right", "left"):
+        B, niter = solve_radiosity(FF, E, rho, placement, "jacobi")
+        Bo, no = osolve.solve_radiosity(FF, E, rho, placement)
+        # (the stopping test sits at FP64 resolution: a product summed in
+        # another order may end one iteration earlier or later)
+        assert abs(niter - no) <= 1
+        assert np.allclose(B, Bo, rtol=1e-9, atol=1e-9 * abs(Bo).max())
+    # the compressed operator (tol = 0) through the same path
+    FFc = CompressedFormFactorMatrix(sm, tol=0, min_size=4096)
+    Bc, nc = solve_radiosity(FFc, E, rho)
+    Bo, no = osolve.solve_radiosity(FF, E, rho)
+    assert abs(nc - no) <= 1 and np.allclose(Bc, Bo, rtol=1e-9, atol=1e-9 * abs(Bo).max())
+
+
 def test_solve_with_compressed_operator_and_kernel_matrix(ffref):
     sm = gshape.EmbreeTrimeshShapeModel(ffref["crater_V"], ffref["crater_F"])
     FF = CompressedFormFactorMatrix(sm, tol=0, min_size=4096)
@@ -201,6 +225,60 @@ def test_batched_solvers_reach_rtol():
         R = Ep - (Bp[:, :8] - FBp)
         rel = (R.abs().amax(0) / Ep.abs().amax(0).clamp_min(1e-30)).max().item()
         assert rel <= bound, (prec, eng, res, incr, rel, st)
+
+
+def test_batched_solve_edge_cases():
+    """Batched solves with a per-facet albedo, a column count that is not a
+    multiple of 8 (padded internally), a zero column (a sun below the
+    horizon) and columns solved in chunks: every column reaches rtol in FP64
+    arithmetic, the zero column stays exactly zero, and the chunked solve
+    agrees with the one-block solve."""
+    sm = _terrain_case(32, seed=7)
+    FF = CompressedFormFactorMatrix(sm, tol=1e-5, min_size=4096, dtype=np.float32,
+                                    RootBlock=FormFactorOctreeBlock)
+    dirs = terrain.random_sun_directions(20, seed=4)
+    E20 = sm.get_direct_irradiance_batch(1365.0, dirs, out_dtype=torch.float32)
+    E = torch.cat([E20[:, :9], torch.zeros_like(E20[:, :1]), E20[:, 9:]], 1).contiguous()
+    assert E.shape[1] == 21
+    rho = np.random.default_rng(11).uniform(0.05, 0.3, sm.num_faces)
+    rho_p = FF.permute(torch.as_tensor(rho, device=E.device)).reshape(-1, 1)
+    Ep = FF.permute(E.double())
+    emax = Ep.abs().amax(0)
+    nz = emax > 0
+
+    def rel_residual(B):
+        Bp = FF.permute(B.double())
+        R = Ep - (Bp - FF.matmat_permuted((rho_p * Bp).contiguous(), "fp64"))
+        return (R.abs().amax(0)[nz] / emax[nz]).max().item()
+
+    for prec, bound in (("bf16-refine", 1e-5), ("fp32", 2e-5)):
+        st, stc = {}, {}
+        B = solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision=prec, stats=st)
+        assert B.shape == E.shape and B.dtype == torch.float32
+        assert rel_residual(B) <= bound, (prec, st)
+        assert torch.count_nonzero(B[:, 9]).item() == 0
+        Bc = solve_radiosity_batched(FF, E, rho, rtol=1e-5, precision=prec, stats=stc, chunk=8)
+        assert stc["chunks"] == 3
+        assert rel_residual(Bc) <= bound, (prec, stc)
+        assert torch.count_nonzero(Bc[:, 9]).item() == 0
+        diff = ((Bc - B).abs().amax(0)[nz] / B.abs().amax(0)[nz]).max().item()
+        assert diff <= 4 * bound, (prec, diff)
+        if prec == "bf16-refine":
+            B_bf16 = B
+    # more columns than one block takes (8,192): equal blocks of 4,104
+    Ew = E.repeat(1, 391)[:, :8200].contiguous()
+    stw = {}
+    Bw = solve_radiosity_batched(FF, Ew, rho, rtol=1e-5, stats=stw)
+    assert stw["chunks"] == 2 and Bw.shape == Ew.shape
+    assert torch.count_nonzero(Bw[:, 9::21]).item() == 0
+    Bw3 = Bw[:, :8190].reshape(-1, 390, 21)
+    den = B_bf16.abs().amax(0).clamp_min(1e-30)
+    diff = ((Bw3 - B_bf16[:, None, :]).abs().amax(0) / den).amax(0)[nz].max().item()
+    assert diff <= 4e-5, diff
+    # no columns
+    st0 = {}
+    B0 = solve_radiosity_batched(FF, E[:, :0], rho, stats=st0)
+    assert B0.shape == (sm.num_faces, 0) and st0["outer"] == 0
 
 
 def test_public_batched_solve_host_buffers():
@@ -247,11 +325,22 @@ def test_public_batched_solve_host_buffers():
         # a copy is offered after each correction; the one of the accepted B
         # fills the buffer (none when the first residual check accepts)
         assert st1["host_out_copies"] == st1["outer"] - 1
-        assert st1["host_out"] == (st1["outer"] >= 2)
-        if st1["host_out"]:
-            assert torch.equal(hb, Bd.cpu())
+        assert st1["host_out_overlapped"] == (st1["outer"] >= 2)
+        assert torch.equal(hb, Bd.cpu())
         copies.append(st1["host_out_copies"])
     assert max(copies) >= 2
+    # paths without the side-stream copy (FP32, column blocks) fill it after
+    # the solve
+    for kw in ({"precision": "fp32"}, {"chunk": 8}):
+        st2 = {}
+        Bd = solve_radiosity_batched(FF, E, 0.12, **kw)
+        hb = torch.full(E.shape, float("nan"), pin_memory=True)
+        B2 = solve_radiosity_batched(FF, E, 0.12, stats=st2, host_out=hb, **kw)
+        assert not st2.get("host_out_overlapped") and torch.equal(B2, Bd)
+        assert torch.equal(hb, Bd.cpu())
+    with pytest.raises(ValueError, match="return_permuted"):
+        solve_radiosity_batched(FF, E, 0.12, return_permuted=True,
+                                host_out=torch.empty(E.shape, pin_memory=True))
     with pytest.raises(ValueError, match="host_out"):
         solve_radiosity_batched(FF, E, 0.12, host_out=torch.empty(E.shape))
     with pytest.raises(ValueError, match="shape"):

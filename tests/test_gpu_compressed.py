@@ -188,6 +188,11 @@ def test_solve_per_facet_albedo_matches_oracle(ffref):
     Bc, nc = solve_radiosity(FFc, E, rho)
     Bo, no = osolve.solve_radiosity(FF, E, rho)
     assert abs(nc - no) <= 1 and np.allclose(Bc, Bo, rtol=1e-9, atol=1e-9 * abs(Bo).max())
+    # and the steady-state temperature of one direction (model.py:8-42
+    # takes rho per facet through the same solve)
+    T = compute_steady_state_temp(FF, E, rho, 0.95)
+    To = osolve.steady_state_temp(FF, E, rho, 0.95)
+    assert np.max(np.abs(T - To)) < 1e-6
 
 
 def test_solve_with_compressed_operator_and_kernel_matrix(ffref):

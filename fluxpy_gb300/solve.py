@@ -19,9 +19,6 @@ relative residual ``rtol``.
 """
 from __future__ import annotations
 
-import ctypes as C
-import time
-
 import numpy as np
 import scipy.sparse
 import torch

@@ -50,3 +50,89 @@ def test_column_blocks_follow_free_memory(free_memory):
     # nothing free: blocks of 8 columns, never fewer
     free_memory["free"] = 1 << 30
     assert solve._auto_chunk(FF, N, 1024, False) == 8
+
+
+def test_early_copy_ordering(monkeypatch):
+    """The side-stream copy of candidate solutions (no GPU: streams and
+    events are replaced by a log).  Each offer gathers B into facet order on
+    the solver's stream, the side stream waits for that before it copies,
+    the solver's stream waits for the copy before the gathered buffer is
+    released or B changes, and only the offer of the final B is returned."""
+    import contextlib
+
+    log = []
+
+    class Event:
+        count = 0
+
+        def __init__(self):
+            Event.count += 1
+            self.id = Event.count
+
+        def record(self, s):
+            log.append(("record", s.name, self.id))
+
+        def synchronize(self):
+            log.append(("sync", self.id))
+
+    class Stream:
+        def __init__(self, name="side"):
+            self.name = name
+
+        def wait_event(self, ev):
+            log.append(("wait", self.name, ev.id))
+
+    main = Stream("main")
+    cur = [main]
+
+    @contextlib.contextmanager
+    def on(s):
+        prev, cur[0] = cur[0], s
+        try:
+            yield
+        finally:
+            cur[0] = prev
+
+    monkeypatch.setattr(torch.cuda, "Stream", lambda *a, **k: Stream("side"))
+    monkeypatch.setattr(torch.cuda, "Event", Event)
+    monkeypatch.setattr(torch.cuda, "current_stream", lambda *a: cur[0])
+    monkeypatch.setattr(torch.cuda, "stream", on)
+    monkeypatch.setattr(torch.cuda, "current_device", lambda: 0)
+    monkeypatch.setattr(solve, "_COPY_STREAMS", {})
+    perm = torch.tensor([2, 0, 1, 3])
+
+    class Operator:
+        def unpermute(self, xp):
+            log.append(("gather", cur[0].name))
+            return xp.index_select(0, perm)
+
+    dst = torch.full((4, 2), float("nan"))
+    ec = solve._EarlyCopy(Operator(), dst)
+    B = torch.arange(8.0).reshape(4, 2)
+    ec.offer(B)
+    assert torch.equal(dst, B.index_select(0, perm)) and ec.copies == 1
+    # gathered on the solver's stream; the side stream waits for it, then
+    # records the end of its copy
+    assert log == [("gather", "main"), ("record", "main", 1), ("wait", "side", 1),
+                   ("record", "side", 2)]
+    # the solver changes B: its stream waits for the copy first
+    log.clear()
+    ec.fence()
+    assert log == [("wait", "main", 2)]
+    B += 1
+    ec.offer(B)
+    ec.offer(B)       # a second offer waits for the first copy before the gather
+    assert log[1:3] == [("gather", "main"), ("record", "main", 3)]
+    i = log.index(("record", "side", 4))
+    assert log[i + 1:i + 3] == [("wait", "main", 4), ("gather", "main")]
+    assert ec.copies == 3
+    # a check that accepts another tensor gets nothing back; the copy in
+    # flight is waited for
+    log.clear()
+    assert ec.result(B.clone()) is None and log == [("wait", "main", 6)]
+    # the accepted B: the host waits for its copy and gets the gathered B
+    ec.offer(B)
+    log.clear()
+    Bu = ec.result(B)
+    assert log == [("sync", 8), ("wait", "main", 8)]
+    assert torch.equal(Bu, B.index_select(0, perm)) and torch.equal(dst, Bu)

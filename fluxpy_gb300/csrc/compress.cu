@@ -438,6 +438,7 @@ int fgb_aca_scratch_floats(int rmax, long long mmax, long long nmax, long long* 
     fgb::set_error("bad ACA sizes (rmax in [1,128], block sides in [1, 2^31))");
     return FGB_BAD_ARG;
   }
+  if (!per_cta) { fgb::set_error("null output"); return FGB_BAD_ARG; }
   *per_cta = (long long)rmax * (mmax + nmax) + 2 * (mmax + nmax);
   return FGB_OK;
 }

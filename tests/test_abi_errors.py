@@ -76,3 +76,37 @@ def test_conduction_checks_grid(lib):
                      f"got {nz}")
         # no facets: nothing to do
         assert f(0, 10, P, 1.0, P, P, P, P, P, P, P, P, P, None, None) == _lib.FGB_OK
+
+
+def test_scene_and_compression_entry_points_check_arguments(lib):
+    flags = C.c_uint(0)
+    pf = C.byref(flags)
+    _rejects(lib, lib.fgb_facet_geometry_f64(None, -1, None, 4, None, None, None, pf, None),
+             "negative sizes")
+    assert lib.fgb_facet_geometry_f64(None, 0, None, 0, None, None, None, pf, None) == _lib.FGB_OK
+    h = C.c_void_p()
+    _rejects(lib, lib.fgb_bvh_build_f64(None, 3, None, -1, 0, C.byref(h), pf, None),
+             "bad arguments")
+    _rejects(lib, lib.fgb_bvh_build_f64(None, 3, None, 1, 0, None, pf, None), "bad arguments")
+    # an empty scene: a handle with no primitives, no device memory
+    assert lib.fgb_bvh_build_f64(None, 0, None, 0, 0, C.byref(h), pf, None) == _lib.FGB_OK
+    n, nbytes = C.c_longlong(-1), C.c_longlong(-1)
+    assert lib.fgb_bvh_info(h, C.byref(n), C.byref(nbytes)) == _lib.FGB_OK
+    assert n.value == 0 and nbytes.value == 0
+    assert lib.fgb_bvh_free(h) == _lib.FGB_OK
+    _rejects(lib, lib.fgb_bvh_info(None, C.byref(n), None), "null bvh")
+    _rejects(lib, lib.fgb_visibility_f64(None, None, 4, None, 2, None, 2, 1, 0, None, None, pf,
+                                         None), "null BVH")
+    _rejects(lib, lib.fgb_ff_triangles_f64(None, None, -1, None, pf, None), "n must be >= 0")
+    _rejects(lib, lib.fgb_ff_triangles_f64(None, None, 3, None, pf, None), "null pointer")
+    assert lib.fgb_ff_triangles_f64(None, None, 0, None, pf, None) == _lib.FGB_OK
+    # ACA scratch: ranks up to 128, block sides below 2^31, an output word
+    per = C.c_longlong(0)
+    for r, m, n_ in ((0, 64, 64), (129, 64, 64), (8, 0, 64), (8, 64, 1 << 31)):
+        _rejects(lib, lib.fgb_aca_scratch_floats(r, m, n_, C.byref(per)), "bad ACA sizes")
+    _rejects(lib, lib.fgb_aca_scratch_floats(8, 64, 32, None), "null output")
+    assert lib.fgb_aca_scratch_floats(8, 64, 32, C.byref(per)) == _lib.FGB_OK
+    assert per.value == 8 * (64 + 32) + 2 * (64 + 32)
+    _rejects(lib, lib.fgb_split_bf16(None, None, None, -1, None), "bad arguments")
+    _rejects(lib, lib.fgb_retile_panel_bf16_n(0x10000, 4, None, None, 64, 0x20000, None),
+             "128 or 256")

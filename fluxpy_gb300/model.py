@@ -53,6 +53,17 @@ def _per_facet(v, like):
     return t.reshape(-1, 1)
 
 
+def _elementwise(v, like):
+    """A scalar as a float; a per-facet array (numpy or tensor) as a tensor
+    on ``like``'s device and dtype, for elementwise products with it (the
+    reference multiplies numpy arrays, model.py:61-67, 223)."""
+    if np.isscalar(v) or np.ndim(v) == 0:
+        return float(v)
+    if isinstance(v, torch.Tensor):
+        return v.to(like.device, like.dtype)
+    return torch.as_tensor(np.asarray(v), device=like.device).to(like.dtype)
+
+
 def _tensor_core_operator(FF):
     from .compressed_form_factors import CompressedFormFactorMatrix
     return isinstance(FF, CompressedFormFactorMatrix)
@@ -116,8 +127,14 @@ def compute_steady_state_temp(FF, E, rho, emiss, Fsurf=0., clamp=True,
 
 def update_incoming_radiances(FF, E, rho, emiss, Qrefl, QIR, Tsurf, clamp=True):
     """Lagged reflected and infrared fluxes for one time step
-    (model.py:44-69; eqs. 17-18 of the radiosity paper)."""
+    (model.py:44-69; eqs. 17-18 of the radiosity paper).  rho and emiss are
+    scalars or per-facet arrays; a per-facet rho scales F (E + Qrefl)
+    facet by facet.  (The reference's ``rho * FF @ (E + Qrefl)`` is
+    ``(rho * FF) @ (E + Qrefl)``: the same for a scalar rho, but a
+    vector-matrix product, and then a single number, for a per-facet
+    array.)"""
     if isinstance(E, torch.Tensor):
+        rho, emiss = _elementwise(rho, E), _elementwise(emiss, E)
         Qrefl_np1 = rho * _apply(FF, E + Qrefl)
         if clamp:
             Qrefl_np1 = torch.clamp_min(Qrefl_np1, 0)
@@ -125,7 +142,10 @@ def update_incoming_radiances(FF, E, rho, emiss, Qrefl, QIR, Tsurf, clamp=True):
         if clamp:
             QIR_np1 = torch.clamp_min(QIR_np1, 0)
         return Qrefl_np1, QIR_np1
-    Qrefl_np1 = rho * FF @ (E + Qrefl)
+    if np.isscalar(rho) or np.ndim(rho) == 0:
+        Qrefl_np1 = rho * FF @ (E + Qrefl)
+    else:
+        Qrefl_np1 = np.asarray(rho) * (FF @ (E + Qrefl))
     if clamp:
         Qrefl_np1 = np.maximum(0, Qrefl_np1)
     QIR_np1 = FF @ (emiss * sigSB * Tsurf**4 + (1 - emiss) * QIR)
@@ -200,6 +220,7 @@ class ThermalModel:
             z, T0, ti, rhoc, emiss, Fgeotherm, Q0, Tsurf, bcond='Q')
         self._dev = _lib.require_cuda()
         self._Tsurf = torch.as_tensor(Tsurf, device=self._dev)
+        self._rho_d = _elementwise(rho, self._Tsurf)
         self._emiss_d = self._pcc_thermal_model_1d.emiss_device
         self._iter_count = 0
         self._Qrefl = None
@@ -235,10 +256,10 @@ class ThermalModel:
         dt = self._t[i] - self._t[i - 1]
         first = i == 1
         Qrefl, QIR = update_incoming_radiances(
-            self._FF, E, self._rho, self._emiss_d,
+            self._FF, E, self._rho_d, self._emiss_d,
             Qrefl=torch.zeros_like(E) if first else self._Qrefl,
             QIR=torch.zeros_like(E) if first else self._QIR, Tsurf=self._Tsurf)
-        Q = (1 - self._rho) * (E + Qrefl) + self._emiss_d * QIR
+        Q = (1 - self._rho_d) * (E + Qrefl) + self._emiss_d * QIR
         pcc = self._pcc_thermal_model_1d
         pcc.step(dt, Q)
         self._Qrefl, self._QIR = Qrefl, QIR

@@ -30,6 +30,9 @@ Sections:
            iteration counts and 2 solutions,
            into cpuarm.npz, with the time per solve of the reference's solve
            and of the oracle's on this machine.
+  thermal  the helpers at the end of src/flux/thermal.pyx (setgrid,
+           flux_noatm, analytT_; plain Python, run from the source text) on
+           fixed inputs, into thermal_helpers.npz.
   ffref    form-factor matrices and steady-state solves computed by the
            reference's Python code (src/flux/form_factors.py,
            compressed_form_factors.py, solve.py, model.py), imported from the
@@ -355,8 +358,38 @@ def make_cpuarm():
           f"reference {t_ref / len(cols) * 1e3:.1f} ms/solve, oracle {t_orc / len(cols) * 1e3:.1f}")
 
 
+def thermal_helper_cases():
+    """Inputs of the thermal.pyx helper goldens (shared with the test)."""
+    grids = [(20, 1.08, 0.5), (40, 1.0817, 1.0), (60, 1.05, 1.0), (10, 1.0, 0.3),
+             (5, 0.9, 2.0), (2, 1.2, 0.1), (3, 1.5, 0.2)]
+    ha = np.linspace(-np.pi, np.pi, 13)
+    flux = [(R, decl, lat, h, slope, az)
+            for R in (1.0, 1.52) for decl in (-0.4, 0.0, 0.2)
+            for lat in (-1.2, -0.3, 0.05, 0.5, 1.4) for h in ha
+            for slope in (0.0, 0.3) for az in (0.0, 2.0)]
+    analyt = dict(z=np.linspace(0.0, 0.5, 7), T0=250.0, rhoc=1.2e6, ti=100.0, P=86400.0,
+                  dt=3600.0)
+    return grids, np.array(flux), analyt
+
+
+def make_thermal():
+    """setgrid, flux_noatm and analytT_ as the reference defines them at the
+    end of src/flux/thermal.pyx (plain Python after the Cython class, so
+    they run here without building the extension)."""
+    src = (REF / "src" / "flux" / "thermal.pyx").read_text()
+    ns = {"np": np}
+    exec(compile(src[src.index("\ndef setgrid("):], "thermal.pyx", "exec"), ns)
+    grids, flux, analyt = thermal_helper_cases()
+    z = [ns["setgrid"](*g) for g in grids]
+    F = np.array([ns["flux_noatm"](*row) for row in flux])
+    T = ns["analytT_"](**analyt)
+    np.savez_compressed(HERE / "thermal_helpers.npz", setgrid=np.concatenate(z),
+                        setgrid_len=np.array([len(a) for a in z]), flux_noatm=F, analytT=T)
+    print("thermal:", len(z), "grids,", F.size, "fluxes, analytT", T.shape)
+
+
 SECTIONS = {"pcc": make_pcc, "spheres": make_spheres, "ffref": make_ffref, "tree": make_tree,
-            "vf": make_vf, "cpuarm": make_cpuarm}
+            "vf": make_vf, "cpuarm": make_cpuarm, "thermal": make_thermal}
 
 if __name__ == "__main__":
     todo = sys.argv[1:] or list(SECTIONS)

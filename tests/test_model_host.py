@@ -55,3 +55,33 @@ def test_elementwise_conversion():
     assert model._elementwise(0.5, x) == 0.5 and isinstance(model._elementwise(np.float32(2), x), float)
     v = model._elementwise(np.arange(4, dtype=np.float32), x)
     assert v.dtype == torch.float64 and v.tolist() == [0.0, 1.0, 2.0, 3.0]
+
+
+def test_thermal_model_checks_inputs_before_device_use():
+    """ThermalModel's argument checks (model.py:110-172): sun positions,
+    every required keyword in the reference's order, shapes and types."""
+    from types import SimpleNamespace
+    nf, nt = 6, 4
+    sm = SimpleNamespace(num_faces=nf)
+    t = np.linspace(0.0, 3600.0, nt)
+    D = np.tile([0.0, 0.0, 1.0], (nt, 1))
+    F0 = np.full(nt, 1365.0)
+    z = np.array([0.0, 0.01, 0.03, 0.05])
+    full = dict(z=z, T0=200.0, ti=100.0, rhoc=1e6, emiss=0.95, Fgeotherm=0.005)
+    with pytest.raises(ValueError, match="N x 3 ndarray"):
+        model.ThermalModel(None, t, D[:, :2], F0, 0.12, shape_model=sm, **full)
+    with pytest.raises(ValueError, match="equal or multiple"):
+        model.ThermalModel(None, t, D[:3], F0, 0.12, shape_model=sm, **full)
+    names = ["z", "T0", "ti", "rhoc", "emiss", "Fgeotherm"]
+    for i, name in enumerate(names):
+        kw = {k: full[k] for k in names[:i]}
+        with pytest.raises(ValueError, match=f'keyword argument "{name}"'):
+            model.ThermalModel(None, t, D, F0, 0.12, shape_model=sm, **kw)
+    with pytest.raises(ValueError, match="invalid shape"):
+        model.ThermalModel(None, t, D, F0, 0.12, shape_model=sm,
+                           **{**full, "emiss": np.full(nf + 1, 0.9)})
+    with pytest.raises(ValueError, match="invalid shape"):
+        model.ThermalModel(None, t, D, F0, 0.12, shape_model=sm,
+                           **{**full, "T0": np.full((nf, z.size + 1), 200.0)})
+    with pytest.raises(TypeError, match="bad type"):
+        model.ThermalModel(None, t, D, F0, 0.12, shape_model=sm, **{**full, "ti": [100.0] * 4})

@@ -136,3 +136,32 @@ def test_early_copy_ordering(monkeypatch):
     Bu = ec.result(B)
     assert log == [("sync", 8), ("wait", "main", 8)]
     assert torch.equal(Bu, B.index_select(0, perm)) and torch.equal(dst, Bu)
+
+
+def test_argument_checks_before_device_use():
+    """The reference's argument errors (compressed_form_factors.py:737-738,
+    879-885; solve.py:9-22) come before any device work."""
+    import numpy as np
+    from fluxpy_gb300.compressed_form_factors import (CompressedFormFactorMatrix,
+                                                      CompressedKernelMatrix)
+    with pytest.raises(RuntimeError, match="tol should be a nonnegative float"):
+        CompressedFormFactorMatrix(None, tol=-1e-5)
+    with pytest.raises(RuntimeError, match="invalid max_depth type"):
+        CompressedFormFactorMatrix(None, max_depth=2.0)
+    with pytest.raises(RuntimeError, match="invalid max_depth value"):
+        CompressedFormFactorMatrix(None, max_depth=0)
+    with pytest.raises(RuntimeError, match="max_depth not specified"):
+        CompressedFormFactorMatrix(None, force_max_depth=True)
+    with pytest.raises(ValueError, match="need 0 < rho <= 1"):
+        CompressedKernelMatrix(None, 0.0)
+    with pytest.raises(ValueError, match="need 0 < rho <= 1"):
+        CompressedKernelMatrix(None, 1.5)
+    with pytest.raises(ValueError, match='albedo_placement must be "left" or "right"'):
+        CompressedKernelMatrix(None, 0.5, "middle")
+    E = np.ones(4)
+    with pytest.raises(Exception, match='albedo_placement must be "left" or "right"'):
+        solve.solve_radiosity(None, E, 0.12, "middle")
+    with pytest.raises(ValueError, match="batched methods only"):
+        solve.solve_radiosity(None, E, 0.12, out=np.empty(4))
+    with pytest.raises(ValueError, match="right albedo placement"):
+        solve.solve_radiosity(None, E[:, None], 0.12, "left", method="batched-bf16")
